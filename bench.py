@@ -1,0 +1,311 @@
+#!/usr/bin/env python3
+"""Benchmark of the wavefront render path's traversal on the LBVH microbench
+workload: 1,000,000 triangles (centroids uniform in the unit cube, lognormal
+edges), 4,194,304 incoherent rays (origins uniform in the cube, directions
+uniform on the sphere), closest-hit queries, FP32, 30-bit Morton LBVH.
+
+One step = one closest-hit pass over the 4M rays with rays and BVH resident in
+HBM. The L2 is flushed (a 256 MB write) before every timed step.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gr|reference]
+
+Prints one JSON line (rank 0). `--impl reference` times the reference's
+traversal semantics (pathtracer_kernel.h:175-233, restated on the CPU because
+the reference has no CPU traversal) on the host cores, on a bounded sample.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "gpu-renderer_gb300"))
+
+import numpy as np  # noqa: E402
+
+N_TRIS = 1_000_000
+N_RAYS = 4_194_304
+METRIC = "incoherent closest-hit Mrays/s (1M-triangle LBVH, 4M rays)"
+UNIT = "Mrays/s"
+WORKLOAD = "lbvh-traversal-microbench: 1M tris, 4M incoherent rays, closest hit"
+# Algorithmic bytes per ray, from the reference traversal's node/triangle visit
+# counts on this ray set (CPU oracle, 262,144-ray sample): V_node = 348.44,
+# V_tri = 4.63; B_ray = 32 (ray) + 16 (hit) + 32 V_node + 36 V_tri.
+V_NODE_REF = 348.44
+V_TRI_REF = 4.63
+BYTES_PER_RAY = 32 + 16 + 32 * V_NODE_REF + 36 * V_TRI_REF
+FALLBACK_HBM_GBS = 6800.0
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples taken while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, ValueError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def cpu_reference(steps, warmup, sample_rays=262144):
+    """The reference traversal (closest hit, right-first, FP64 Moller-Trumbore)
+    restated on the CPU, all host threads, on a bounded sample of the rays."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    from gr import scenes
+    verts = scenes.triangle_soup(N_TRIS)
+    rays = scenes.incoherent_rays(N_RAYS)
+    stride = max(1, N_RAYS // sample_rays)
+    sample = np.ascontiguousarray(rays[::stride][:sample_rays])
+    bvh = pyoracle.lbvh(verts)
+    threads = pyoracle.threads()
+    for _ in range(warmup):
+        pyoracle.trace_ref(bvh["ref_nodes"], verts, sample[:4096], nthreads=threads)
+    times = []
+    st = None
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        _, st = pyoracle.trace_ref(bvh["ref_nodes"], verts, sample, stats=True, nthreads=threads)
+        times.append(time.perf_counter() - t0)
+    value = sample.shape[0] * len(times) / sum(times) / 1e6
+    return {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "%d of the %d incoherent rays (every %dth), reference traversal semantics "
+                      "(pathtracer_kernel.h:175-233) restated in C++, %d threads" % (
+                          sample.shape[0], N_RAYS, stride, threads),
+            "v_node": float(st[:, 0].mean()), "v_tri": float(st[:, 1].mean()),
+            "seconds_per_step": sum(times) / len(times)}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    cb = cpu_reference(max(args.steps, 1), max(args.warmup, 0) and 1)
+    out = {
+        "impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": cb["seconds_per_step"] * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "sample": cb["sample"]},
+        "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+
+
+def l2_flush(buf):
+    buf.zero_()
+
+
+def run_gpu(args):
+    import torch
+    import gr
+    from gr import scenes
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    verts = scenes.triangle_soup(N_TRIS)
+    rays = scenes.incoherent_rays(N_RAYS)
+    ctx = gr.Context(local)
+    bvh = gr.BVH(ctx)
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    d_verts = torch.from_numpy(verts).to(dev)
+    d_rays = torch.from_numpy(rays).to(dev)
+    d_hits = torch.empty((N_RAYS, 4), dtype=torch.float32, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    # BVH build (timed separately, reported as an extra)
+    build_ms = []
+    for i in range(3 + 5):
+        l2_flush(flush)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        bvh.build_device(d_verts, N_TRIS, stream=sp)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if i >= 3:
+            build_ms.append(e0.elapsed_time(e1))
+
+    def step(buf_rays, buf_hits, n, any_hit=False):
+        bvh.trace_device(buf_rays, n, buf_hits, any_hit=any_hit, stream=sp)
+
+    for _ in range(max(args.warmup, 3)):
+        step(d_rays, d_hits, N_RAYS)
+    torch.cuda.synchronize()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    ev = []
+    for _ in range(args.steps):
+        l2_flush(flush)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        step(d_rays, d_hits, N_RAYS)
+        e1.record(stream)
+        ev.append((e0, e1))
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    kernel_ms = [a.elapsed_time(b) for a, b in ev]
+    total_s = sum(kernel_ms) / 1e3
+
+    # secondary queries on the same scene: coherent closest hit and shadow any-hit
+    extras = {}
+    for name, gen, anyh in (("coherent_closest", scenes.coherent_rays, False),
+                            ("shadow_anyhit", scenes.shadow_rays, True)):
+        r2 = gen() if name == "coherent_closest" else gen(N_RAYS)
+        d_r2 = torch.from_numpy(r2).to(dev)
+        for _ in range(3):
+            step(d_r2, d_hits, r2.shape[0], anyh)
+        ms = []
+        for _ in range(max(3, min(args.steps, 10))):
+            l2_flush(flush)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            step(d_r2, d_hits, r2.shape[0], anyh)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        extras[name + "_mrays_s"] = r2.shape[0] / (statistics.median(ms) / 1e3) / 1e6
+        del d_r2
+    clock_info = clocks.stop()
+
+    # end to end through the C ABI with host buffers (pinned), copies inside
+    h_rays = torch.from_numpy(rays).pin_memory()
+    h_hits = torch.empty((N_RAYS, 4), dtype=torch.float32).pin_memory()
+    L = gr.load()
+    for _ in range(2):
+        ctx.check(L.gr_trace_host(bvh.h, gr._P(h_rays.data_ptr()), N_RAYS, gr._P(h_hits.data_ptr()), 0))
+    e2e_t = []
+    for _ in range(max(3, min(args.steps, 10))):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ctx.check(L.gr_trace_host(bvh.h, gr._P(h_rays.data_ptr()), N_RAYS, gr._P(h_hits.data_ptr()), 0))
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_value = N_RAYS * len(e2e_t) / sum(e2e_t) / 1e6
+
+    # whole-job value: max time over ranks, rays over all ranks
+    t_max = total_s
+    if ws > 1:
+        t = torch.tensor([total_s], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_max = float(t.item())
+    value = ws * N_RAYS * args.steps / t_max / 1e6
+
+    if rank == 0:
+        peak, peak_kind = measured_peaks()
+        avg_ms = sum(kernel_ms) / len(kernel_ms)
+        achieved = BYTES_PER_RAY * N_RAYS / (avg_ms / 1e3) / 1e9
+        traffic = None
+        tp = os.path.join(ROOT, "profiles", "trace_closest_traffic.json")
+        if os.path.exists(tp):
+            with open(tp) as f:
+                traffic = json.load(f).get("bytes_per_launch")
+        cb = cpu_reference(1, 0)
+        out = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_max * 1e3 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "triangles": N_TRIS, "rays": N_RAYS, "query": "closest hit",
+                       "l2": "flushed (256 MB write) before every timed step", "parallelism": "replicas"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
+                         "kernel": "k_trace<closest>", "bytes_per_ray": BYTES_PER_RAY},
+            "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": N_RAYS * 32,
+                    "d2h_bytes_per_step": N_RAYS * 16, "api": "gr_trace_host (pinned host rays and hits)"},
+            "gpu_launches": args.steps,
+            "clocks": clock_info,
+            "extra": dict(extras, bvh_build_ms=statistics.median(build_ms),
+                          bvh_build_mtris_s=N_TRIS / (statistics.median(build_ms) / 1e3) / 1e6,
+                          kernel_ms_median=statistics.median(kernel_ms)),
+        }
+        print(json.dumps(out), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gr", choices=["gr", "reference"])
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,246 @@
+// C ABI: context, BVH and traversal entry points (include/gr.h).
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "gr_internal.h"
+
+namespace gr {
+
+cudaError_t DevBuf::ensure(size_t want) {
+    if (want <= bytes && p) return cudaSuccess;
+    release();
+    cudaError_t e = cudaMalloc(&p, want ? want : 256);
+    if (e != cudaSuccess) {
+        p = nullptr;
+        bytes = 0;
+        return e;
+    }
+    bytes = want;
+    return cudaSuccess;
+}
+
+void DevBuf::release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+}
+
+}  // namespace gr
+
+namespace {
+
+gr_status fail(gr_ctx* ctx, gr_status st, const char* what) {
+    if (ctx) ctx->last_error = what;
+    return st;
+}
+
+gr_status cuda_fail(gr_ctx* ctx, cudaError_t e, const char* where) {
+    cudaGetLastError();  // clear a sticky launch error so the context stays usable
+    if (ctx) {
+        ctx->last_error = std::string(where) + ": " + cudaGetErrorString(e);
+    }
+    return e == cudaErrorMemoryAllocation ? GR_ERR_OOM_BUDGET : GR_ERR_CUDA;
+}
+
+#define GR_CUDA(ctx, call)                                   \
+    do {                                                     \
+        cudaError_t e__ = (call);                            \
+        if (e__ != cudaSuccess) return cuda_fail(ctx, e__, #call); \
+    } while (0)
+
+cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+gr_status check_device_errors(gr_bvh* bvh, uint32_t err) {
+    if (err & gr::ERR_TIMEOUT) return fail(bvh->ctx, GR_ERR_TIMEOUT, "device wait timed out");
+    if (err & gr::ERR_STACK) return fail(bvh->ctx, GR_ERR_OVERFLOW, "traversal stack overflow");
+    if (err & gr::ERR_QUEUE) return fail(bvh->ctx, GR_ERR_OVERFLOW, "queue capacity exceeded");
+    if (err & gr::ERR_RANGE) return fail(bvh->ctx, GR_ERR_INVALID, "out-of-range index skipped on device");
+    return GR_OK;
+}
+
+gr::BvhDevice device_view(gr_bvh* bvh) {
+    gr::BvhDevice v;
+    v.nodes = (const gr::Node*)bvh->buf.nodes.p;
+    v.tris = (const gr::Tri*)bvh->buf.tris.p;
+    v.meta = (const gr::BvhMeta*)bvh->buf.meta.p;
+    v.n = bvh->n;
+    return v;
+}
+
+gr_status read_meta(gr_bvh* bvh, gr::BvhMeta* m) {
+    GR_CUDA(bvh->ctx, cudaMemcpy(m, bvh->buf.meta.p, sizeof(gr::BvhMeta), cudaMemcpyDeviceToHost));
+    return GR_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gr_version(void) { return 100; }
+
+const char* gr_status_string(int st) {
+    switch (st) {
+        case GR_OK: return "ok";
+        case GR_ERR_INVALID: return "invalid argument";
+        case GR_ERR_CUDA: return "CUDA error";
+        case GR_ERR_OOM_BUDGET: return "out of memory or over budget";
+        case GR_ERR_PARSE: return "parse error";
+        case GR_ERR_TIMEOUT: return "device wait timed out";
+        case GR_ERR_OVERFLOW: return "device capacity exceeded";
+        default: return "unknown status";
+    }
+}
+
+gr_status gr_context_create(int device, gr_ctx** out) {
+    if (!out) return GR_ERR_INVALID;
+    *out = nullptr;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count) {
+        cudaGetLastError();
+        return GR_ERR_CUDA;
+    }
+    gr_ctx* ctx = new (std::nothrow) gr_ctx();
+    if (!ctx) return GR_ERR_OOM_BUDGET;
+    ctx->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = ctx->counter.ensure(256);
+    if (e == cudaSuccess) e = cudaMemset(ctx->counter.p, 0, 256);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        delete ctx;
+        return GR_ERR_CUDA;
+    }
+    *out = ctx;
+    return GR_OK;
+}
+
+gr_status gr_context_destroy(gr_ctx* ctx) {
+    if (!ctx) return GR_ERR_INVALID;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    ctx->counter.release();
+    ctx->stage_in.release();
+    ctx->stage_out.release();
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return GR_OK;
+}
+
+const char* gr_last_error(const gr_ctx* ctx) { return ctx ? ctx->last_error.c_str() : "no context"; }
+
+gr_status gr_bvh_create(gr_ctx* ctx, gr_bvh** out) {
+    if (!ctx || !out) return GR_ERR_INVALID;
+    gr_bvh* b = new (std::nothrow) gr_bvh();
+    if (!b) return fail(ctx, GR_ERR_OOM_BUDGET, "host allocation failed");
+    b->ctx = ctx;
+    *out = b;
+    return GR_OK;
+}
+
+gr_status gr_bvh_destroy(gr_bvh* bvh) {
+    if (!bvh) return GR_ERR_INVALID;
+    cudaSetDevice(bvh->ctx->device);
+    cudaStreamSynchronize(bvh->ctx->stream);
+    delete bvh;
+    return GR_OK;
+}
+
+uint32_t gr_bvh_size(const gr_bvh* bvh) { return bvh ? bvh->n : 0; }
+
+gr_status gr_bvh_build(gr_bvh* bvh, const float* d_verts, uint32_t n, void* stream) {
+    if (!bvh) return GR_ERR_INVALID;
+    if (n > gr::kMaxTriangles) return fail(bvh->ctx, GR_ERR_INVALID, "too many triangles");
+    if (n > 0 && !d_verts) return fail(bvh->ctx, GR_ERR_INVALID, "null vertex pointer");
+    GR_CUDA(bvh->ctx, cudaSetDevice(bvh->ctx->device));
+    bvh->built = false;
+    GR_CUDA(bvh->ctx, gr::lbvh_build(bvh->buf, d_verts, n, bvh->ctx->num_sms, as_stream(stream)));
+    bvh->n = n;
+    bvh->built = true;
+    return GR_OK;
+}
+
+gr_status gr_bvh_build_host(gr_bvh* bvh, const float* h_verts, uint32_t n) {
+    if (!bvh) return GR_ERR_INVALID;
+    if (n > 0 && !h_verts) return fail(bvh->ctx, GR_ERR_INVALID, "null vertex pointer");
+    GR_CUDA(bvh->ctx, cudaSetDevice(bvh->ctx->device));
+    cudaStream_t s = bvh->ctx->stream;
+    gr::DevBuf& staging = bvh->ctx->stage_in;
+    GR_CUDA(bvh->ctx, staging.ensure(36ull * (n ? n : 1)));
+    if (n) GR_CUDA(bvh->ctx, cudaMemcpyAsync(staging.p, h_verts, 36ull * n, cudaMemcpyHostToDevice, s));
+    gr_status st = gr_bvh_build(bvh, (const float*)staging.p, n, s);
+    if (st != GR_OK) return st;
+    GR_CUDA(bvh->ctx, cudaStreamSynchronize(s));
+    gr::BvhMeta m;
+    st = read_meta(bvh, &m);
+    if (st != GR_OK) return st;
+    return check_device_errors(bvh, m.err);
+}
+
+gr_status gr_bvh_export(gr_bvh* bvh, uint32_t* h_sorted_prim, uint32_t* h_sorted_code, uint32_t* h_ref_nodes,
+                        uint32_t* h_nodes, float* h_tris, uint32_t* h_root) {
+    if (!bvh || !bvh->built) return GR_ERR_INVALID;
+    GR_CUDA(bvh->ctx, cudaSetDevice(bvh->ctx->device));
+    GR_CUDA(bvh->ctx, cudaDeviceSynchronize());
+    gr::BvhMeta m;
+    gr_status st = read_meta(bvh, &m);
+    if (st != GR_OK) return st;
+    st = check_device_errors(bvh, m.err);
+    if (st != GR_OK) return st;
+    const uint32_t n = bvh->n;
+    if (h_root) *h_root = m.root;
+    if (n == 0) return GR_OK;
+    if (h_sorted_prim) GR_CUDA(bvh->ctx, cudaMemcpy(h_sorted_prim, bvh->buf.prim.p, 4ull * n, cudaMemcpyDeviceToHost));
+    if (h_sorted_code) GR_CUDA(bvh->ctx, cudaMemcpy(h_sorted_code, bvh->buf.code.p, 4ull * n, cudaMemcpyDeviceToHost));
+    if (h_nodes)
+        GR_CUDA(bvh->ctx, cudaMemcpy(h_nodes, bvh->buf.nodes.p, sizeof(gr::Node) * (n > 1 ? n - 1 : 1),
+                                     cudaMemcpyDeviceToHost));
+    if (h_tris) GR_CUDA(bvh->ctx, cudaMemcpy(h_tris, bvh->buf.tris.p, sizeof(gr::Tri) * n, cudaMemcpyDeviceToHost));
+    if (h_ref_nodes) {
+        gr::DevBuf out;
+        const size_t bytes = 32ull * (2ull * n - 1);
+        GR_CUDA(bvh->ctx, out.ensure(bytes));
+        GR_CUDA(bvh->ctx, gr::lbvh_export_ref(bvh->buf, n, (uint32_t*)out.p, bvh->ctx->stream));
+        GR_CUDA(bvh->ctx, cudaMemcpyAsync(h_ref_nodes, out.p, bytes, cudaMemcpyDeviceToHost, bvh->ctx->stream));
+        GR_CUDA(bvh->ctx, cudaStreamSynchronize(bvh->ctx->stream));
+    }
+    return GR_OK;
+}
+
+gr_status gr_trace(gr_bvh* bvh, const gr_ray* d_rays, uint64_t n, gr_hit* d_hits, int any_hit, void* stream) {
+    if (!bvh || !bvh->built) return GR_ERR_INVALID;
+    if (n > 0 && (!d_rays || !d_hits)) return fail(bvh->ctx, GR_ERR_INVALID, "null ray or hit pointer");
+    gr_ctx* ctx = bvh->ctx;
+    GR_CUDA(ctx, cudaSetDevice(ctx->device));
+    unsigned long long* counter = (unsigned long long*)ctx->counter.p;
+    uint32_t* err = (uint32_t*)((char*)ctx->counter.p + 64);
+    GR_CUDA(ctx, gr::trace_launch(device_view(bvh), d_rays, n, d_hits, any_hit, counter, err, ctx->num_sms,
+                                  as_stream(stream)));
+    return GR_OK;
+}
+
+gr_status gr_trace_host(gr_bvh* bvh, const gr_ray* h_rays, uint64_t n, gr_hit* h_hits, int any_hit) {
+    if (!bvh || !bvh->built) return GR_ERR_INVALID;
+    if (n > 0 && (!h_rays || !h_hits)) return fail(bvh->ctx, GR_ERR_INVALID, "null ray or hit pointer");
+    gr_ctx* ctx = bvh->ctx;
+    GR_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (n == 0) return GR_OK;
+    cudaStream_t s = ctx->stream;
+    gr::DevBuf& dr = ctx->stage_in;
+    gr::DevBuf& dh = ctx->stage_out;
+    GR_CUDA(ctx, dr.ensure(sizeof(gr_ray) * n));
+    GR_CUDA(ctx, dh.ensure(sizeof(gr_hit) * n));
+    GR_CUDA(ctx, cudaMemcpyAsync(dr.p, h_rays, sizeof(gr_ray) * n, cudaMemcpyHostToDevice, s));
+    gr_status st = gr_trace(bvh, (const gr_ray*)dr.p, n, (gr_hit*)dh.p, any_hit, s);
+    if (st != GR_OK) return st;
+    GR_CUDA(ctx, cudaMemcpyAsync(h_hits, dh.p, sizeof(gr_hit) * n, cudaMemcpyDeviceToHost, s));
+    GR_CUDA(ctx, cudaStreamSynchronize(s));
+    uint32_t err = 0;
+    GR_CUDA(ctx, cudaMemcpy(&err, (char*)ctx->counter.p + 64, 4, cudaMemcpyDeviceToHost));
+    return check_device_errors(bvh, err);
+}
+
+}  // extern "C"

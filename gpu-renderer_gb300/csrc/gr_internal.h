@@ -1,0 +1,112 @@
+// Internal declarations shared by the host C++ and the CUDA translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "gr.h"
+
+namespace gr {
+
+// Device-side error word bits (kernels never trap; they set a bit and return).
+enum : uint32_t {
+    ERR_TIMEOUT = 1u << 0,   // a bounded spin gave up
+    ERR_STACK = 1u << 1,     // traversal stack overflow
+    ERR_QUEUE = 1u << 2,     // queue capacity exceeded
+    ERR_RANGE = 1u << 3,     // an index out of range was seen and skipped
+};
+
+// Bounded spin limit for decoupled look-back waits (each iteration is an L2
+// load, so this is far more than any predecessor tile can take).
+constexpr uint32_t kSpinLimit = 1u << 22;
+
+// Largest triangle count a BVH accepts: look-back words pack a 30-bit count.
+constexpr uint32_t kMaxTriangles = (1u << 30) - 1;
+
+// Traversal-node layout, 64 bytes (four 16-byte words):
+//   q0 = (c0.lo.x, c0.hi.x, c0.lo.y, c0.hi.y)
+//   q1 = (c1.lo.x, c1.hi.x, c1.lo.y, c1.hi.y)
+//   q2 = (c0.lo.z, c0.hi.z, c1.lo.z, c1.hi.z)
+//   q3 = (child0, child1, parent, 0) as int32; child < 0 is leaf ~p, where p
+//        is the sorted position of a triangle in the leaf-order triangle array.
+// Node index = the gap between sorted positions g and g+1 that the node splits.
+struct Node {
+    float4 q0, q1, q2;
+    int4 q3;
+};
+static_assert(sizeof(Node) == 64, "node layout");
+
+// Leaf-order triangle: three 16-byte words (v0, prim bits), (v1, 0), (v2, 0).
+struct Tri {
+    float4 a, b, c;
+};
+static_assert(sizeof(Tri) == 48, "triangle layout");
+
+constexpr uint32_t kNoNode = 0xFFFFFFFFu;
+
+// Device buffer owned by an object; grows on demand, never shrinks.
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t want);
+    void release();
+    ~DevBuf() { release(); }
+};
+
+struct BvhMeta;
+
+// What a traversal kernel needs; the root index is read on the device from the
+// BVH header so no host synchronisation sits between build and trace.
+struct BvhDevice {
+    const Node* nodes;
+    const Tri* tris;
+    const BvhMeta* meta;  // meta->root is kNoNode when the BVH is empty
+    uint32_t n;
+};
+
+// Build scratch + outputs, sliced from a few allocations.
+struct BvhBuffers {
+    DevBuf nodes, tris, code, prim;  // outputs kept for traversal / export
+    DevBuf scratch;                  // transient build state
+    DevBuf meta;                     // small device header (root, unique count, error word)
+};
+
+// Host-visible layout of the small per-BVH device header.
+struct BvhMeta {
+    uint32_t root;
+    uint32_t unique;
+    uint32_t err;
+    uint32_t pad;
+    float cbox[6];  // centroid bounds used for the Morton codes
+    float pad2[2];
+};
+
+// lbvh.cu
+cudaError_t lbvh_build(BvhBuffers& b, const float* d_verts, uint32_t n, int num_sms, cudaStream_t s);
+cudaError_t lbvh_export_ref(const BvhBuffers& b, uint32_t n, uint32_t* d_ref_nodes, cudaStream_t s);
+
+// trace.cu
+cudaError_t trace_launch(const BvhDevice& bvh, const gr_ray* d_rays, uint64_t n, gr_hit* d_hits, int any_hit,
+                         unsigned long long* d_counter, uint32_t* d_err, int num_sms, cudaStream_t s);
+
+}  // namespace gr
+
+// Context and object definitions (host side).
+struct gr_ctx {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    std::string last_error;
+    gr::DevBuf counter;  // traversal work counter (offset 0) + error word (offset 64)
+    gr::DevBuf stage_in, stage_out;  // device staging for the host-memory entry points
+};
+
+struct gr_bvh {
+    gr_ctx* ctx = nullptr;
+    // not copyable: owns device memory
+    uint32_t n = 0;
+    bool built = false;
+    gr::BvhBuffers buf;
+};

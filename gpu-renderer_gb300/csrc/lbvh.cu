@@ -1,0 +1,718 @@
+// GPU LBVH build: Morton codes -> onesweep radix sort -> equal-code runs ->
+// Karras radix tree over unique codes + midpoint subtrees inside runs ->
+// bottom-up atomic refit. Produces the same tree as the reference's host
+// LBVH_build (src/renderer/bvh.h:186-221) with ties kept in input order.
+//
+// Every float operation that feeds a Morton code is written with an explicit
+// round-to-nearest intrinsic so nvcc cannot contract it into an FMA: the codes
+// must equal the reference host computation (bvh.h:193-204) bit for bit.
+#include <algorithm>
+
+#include "gr_internal.h"
+
+namespace gr {
+namespace {
+
+constexpr int kBlock = 256;
+
+// ---- small device helpers ---------------------------------------------------
+
+__device__ __forceinline__ uint32_t ld_acquire(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release(uint32_t* p, uint32_t v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ uint32_t lanemask_lt() {
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+struct Box3 {
+    float lo[3], hi[3];
+};
+
+__device__ __forceinline__ Box3 tri_box(const float* __restrict__ v, uint64_t i) {
+    const float* p = v + 9ull * i;
+    float a[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) a[k] = __ldg(p + k);
+    Box3 b;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        b.lo[k] = fminf(fminf(a[k], a[3 + k]), a[6 + k]);
+        b.hi[k] = fmaxf(fmaxf(a[k], a[3 + k]), a[6 + k]);
+    }
+    return b;
+}
+
+// Standard 10-bit spread: bit i moves to bit 3i.
+__device__ __forceinline__ uint32_t spread10(uint32_t x) {
+    x &= 0x3FFu;
+    x = (x | (x << 16)) & 0x030000FFu;
+    x = (x | (x << 8)) & 0x0300F00Fu;
+    x = (x | (x << 4)) & 0x030C30C3u;
+    x = (x | (x << 2)) & 0x09249249u;
+    return x;
+}
+
+// Block-wide exclusive scan of one uint32 per thread (blockDim.x <= 1024).
+template <int THREADS>
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* s_warp, uint32_t* total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_warp[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        constexpr int W = THREADS / 32;
+        uint32_t w = lane < W ? s_warp[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xFFFFFFFFu, w, o);
+            if (lane >= o) w += y;
+        }
+        if (lane < W) s_warp[lane] = w;  // inclusive warp totals
+    }
+    __syncthreads();
+    uint32_t base = warp > 0 ? s_warp[warp - 1] : 0;
+    *total = s_warp[THREADS / 32 - 1];
+    __syncthreads();
+    return base + x - v;
+}
+
+// ---- 1. centroid bounds -------------------------------------------------------
+
+__global__ void __launch_bounds__(kBlock) k_centroid_partials(const float* __restrict__ verts, uint32_t n,
+                                                              float* __restrict__ partial) {
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (uint32_t i = blockIdx.x * kBlock + threadIdx.x; i < n; i += gridDim.x * kBlock) {
+        Box3 b = tri_box(verts, i);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            float c = __fmul_rn(__fadd_rn(b.lo[k], b.hi[k]), 0.5f);  // AABB::centroid
+            lo[k] = fminf(lo[k], c);
+            hi[k] = fmaxf(hi[k], c);
+        }
+    }
+    __shared__ float s[6][kBlock / 32];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        for (int o = 16; o > 0; o >>= 1) {
+            lo[k] = fminf(lo[k], __shfl_xor_sync(0xFFFFFFFFu, lo[k], o));
+            hi[k] = fmaxf(hi[k], __shfl_xor_sync(0xFFFFFFFFu, hi[k], o));
+        }
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) {
+        for (int k = 0; k < 3; ++k) { s[k][warp] = lo[k]; s[3 + k][warp] = hi[k]; }
+    }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        const int k = threadIdx.x;
+        float r = s[k][0];
+        for (int w = 1; w < kBlock / 32; ++w) r = k < 3 ? fminf(r, s[k][w]) : fmaxf(r, s[k][w]);
+        partial[6 * blockIdx.x + k] = r;
+    }
+}
+
+__global__ void k_centroid_final(const float* __restrict__ partial, int nparts, BvhMeta* meta) {
+    if (threadIdx.x < 6) {
+        const int k = threadIdx.x;
+        float r = k < 3 ? INFINITY : -INFINITY;
+        for (int p = 0; p < nparts; ++p) r = k < 3 ? fminf(r, partial[6 * p + k]) : fmaxf(r, partial[6 * p + k]);
+        meta->cbox[k] = r;
+    }
+}
+
+// ---- 2. Morton codes + the four digit histograms ------------------------------
+
+__global__ void __launch_bounds__(kBlock) k_morton_hist(const float* __restrict__ verts, uint32_t n,
+                                                        const BvhMeta* __restrict__ meta, uint32_t* __restrict__ keys,
+                                                        uint32_t* __restrict__ vals, uint32_t* __restrict__ hist) {
+    __shared__ uint32_t s_hist[4 * 256];
+    for (int i = threadIdx.x; i < 4 * 256; i += kBlock) s_hist[i] = 0;
+    __syncthreads();
+    float blo[3], bhi[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) { blo[k] = meta->cbox[k]; bhi[k] = meta->cbox[3 + k]; }
+    for (uint32_t i = blockIdx.x * kBlock + threadIdx.x; i < n; i += gridDim.x * kBlock) {
+        Box3 b = tri_box(verts, i);
+        uint32_t cell[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            float c = __fmul_rn(__fadd_rn(b.lo[k], b.hi[k]), 0.5f);
+            float q = __fmul_rn(__fdiv_rn(__fsub_rn(c, blo[k]), __fsub_rn(bhi[k], blo[k])), 1024.0f);
+            uint32_t x = __float2uint_rz(q);  // truncation; NaN -> 0
+            cell[k] = x > 1023u ? 1023u : x;  // 1024 -> 1023 (bvh.h:15)
+        }
+        uint32_t code = (spread10(cell[2]) << 2) | (spread10(cell[1]) << 1) | spread10(cell[0]);
+        keys[i] = code;
+        vals[i] = i;
+        atomicAdd(&s_hist[code & 0xFF], 1u);
+        atomicAdd(&s_hist[256 + ((code >> 8) & 0xFF)], 1u);
+        atomicAdd(&s_hist[512 + ((code >> 16) & 0xFF)], 1u);
+        atomicAdd(&s_hist[768 + (code >> 24)], 1u);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 4 * 256; i += kBlock)
+        if (s_hist[i]) atomicAdd(&hist[i], s_hist[i]);
+}
+
+__global__ void __launch_bounds__(256) k_hist_scan(const uint32_t* __restrict__ hist, uint32_t* __restrict__ offs) {
+    __shared__ uint32_t s_warp[8];
+    uint32_t total;
+    const uint32_t v = hist[256 * blockIdx.x + threadIdx.x];
+    offs[256 * blockIdx.x + threadIdx.x] = block_exclusive_scan<256>(v, s_warp, &total);
+}
+
+// ---- 3. onesweep radix pass ------------------------------------------------------
+// One pass sorts by one 8-bit digit. Tiles of 4096 keys are ranked in shared
+// memory (warp multi-split with match_any, stable in input order), the tile's
+// per-digit counts are published and prefixed with decoupled look-back, and
+// keys are written out grouped by digit.
+
+constexpr int kOsThreads = 512;
+constexpr int kOsItems = 8;
+constexpr int kOsTile = kOsThreads * kOsItems;
+constexpr int kOsWarps = kOsThreads / 32;
+constexpr uint32_t kFlagAgg = 1u << 30, kFlagInc = 2u << 30, kCountMask = (1u << 30) - 1;
+constexpr size_t kOsSmem = sizeof(uint32_t) * (kOsWarps * 256 + 256 + 256 + 2 * kOsTile + 8 + 1);
+
+__global__ void __launch_bounds__(kOsThreads) k_onesweep(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
+                                                         uint32_t* __restrict__ kout, uint32_t* __restrict__ vout,
+                                                         uint32_t n, int pass, const uint32_t* __restrict__ offs,
+                                                         uint32_t* __restrict__ status, uint32_t* __restrict__ tile_ctr,
+                                                         uint32_t* __restrict__ err) {
+    extern __shared__ uint32_t smem[];
+    uint32_t* s_wcnt = smem;                       // [warps][256]
+    uint32_t* s_dstart = s_wcnt + kOsWarps * 256;  // [256] tile-local digit starts
+    uint32_t* s_gbase = s_dstart + 256;            // [256] global digit bases
+    uint32_t* s_keys = s_gbase + 256;              // [tile]
+    uint32_t* s_vals = s_keys + kOsTile;           // [tile]
+    uint32_t* s_warp = s_vals + kOsTile;           // [8] scan scratch
+    uint32_t* s_tile = s_warp + 8;
+
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int shift = 8 * pass;
+    if (threadIdx.x == 0) *s_tile = atomicAdd(tile_ctr + pass, 1u);
+    for (int i = threadIdx.x; i < kOsWarps * 256; i += kOsThreads) s_wcnt[i] = 0;
+    __syncthreads();
+    const uint32_t tile = *s_tile;
+    const uint64_t base = (uint64_t)tile * kOsTile;
+
+    uint32_t key[kOsItems], val[kOsItems], rank[kOsItems], dig[kOsItems];
+#pragma unroll
+    for (int j = 0; j < kOsItems; ++j) {
+        const uint64_t idx = base + warp * (32 * kOsItems) + j * 32 + lane;
+        const bool ok = idx < n;
+        key[j] = ok ? kin[idx] : 0u;
+        val[j] = ok ? vin[idx] : 0u;
+        dig[j] = ok ? ((key[j] >> shift) & 0xFFu) : 256u;
+    }
+    const uint32_t ltmask = lanemask_lt();
+    uint32_t* wc = s_wcnt + warp * 256;
+#pragma unroll
+    for (int j = 0; j < kOsItems; ++j) {
+        const uint32_t d = dig[j];
+        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
+        const uint32_t lt = __popc(peers & ltmask);
+        const uint32_t before = d < 256u ? wc[d] : 0u;
+        __syncwarp();
+        if (d < 256u && lt == 0) wc[d] = before + __popc(peers);
+        __syncwarp();
+        rank[j] = before + lt;
+    }
+    __syncthreads();
+
+    uint32_t cnt = 0;
+    if (threadIdx.x < 256) {
+        const int d = threadIdx.x;
+        uint32_t run = 0;
+        for (int w = 0; w < kOsWarps; ++w) {
+            const uint32_t t = s_wcnt[w * 256 + d];
+            s_wcnt[w * 256 + d] = run;
+            run += t;
+        }
+        cnt = run;
+    }
+    __syncthreads();
+    uint32_t tot;
+    const uint32_t dstart = block_exclusive_scan<kOsThreads>(threadIdx.x < 256 ? cnt : 0u, s_warp, &tot);
+    if (threadIdx.x < 256) {
+        const int d = threadIdx.x;
+        s_dstart[d] = dstart;
+        uint32_t* st = status + (size_t)tile * 256 + d;
+        uint32_t excl = 0;
+        if (tile == 0) {
+            st_release(st, kFlagInc | cnt);
+        } else {
+            st_release(st, kFlagAgg | cnt);
+            int64_t t = (int64_t)tile - 1;
+            uint32_t spins = 0;
+            while (t >= 0) {
+                const uint32_t v = ld_acquire(status + (size_t)t * 256 + d);
+                const uint32_t flag = v & ~kCountMask;
+                if (flag == 0) {
+                    if (++spins > kSpinLimit) {
+                        atomicOr(err, ERR_TIMEOUT);
+                        break;
+                    }
+                    continue;
+                }
+                excl += v & kCountMask;
+                if (flag == kFlagInc) break;
+                --t;
+            }
+            st_release(st, kFlagInc | ((excl + cnt) & kCountMask));
+        }
+        s_gbase[d] = offs[256 * pass + d] + excl;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < kOsItems; ++j) {
+        const uint32_t d = dig[j];
+        if (d < 256u) {
+            const uint32_t r = s_dstart[d] + s_wcnt[warp * 256 + d] + rank[j];
+            s_keys[r] = key[j];
+            s_vals[r] = val[j];
+        }
+    }
+    __syncthreads();
+    const uint64_t left = (uint64_t)n - base;
+    const uint32_t valid = left < (uint64_t)kOsTile ? (uint32_t)left : (uint32_t)kOsTile;
+    for (uint32_t i = threadIdx.x; i < valid; i += kOsThreads) {
+        const uint32_t k = s_keys[i];
+        const uint32_t d = (k >> shift) & 0xFFu;
+        const uint32_t pos = s_gbase[d] + (i - s_dstart[d]);
+        if (pos < n) {
+            kout[pos] = k;
+            vout[pos] = s_vals[i];
+        } else {
+            atomicOr(err, ERR_RANGE);
+        }
+    }
+}
+
+// ---- 4. equal-code runs (single-pass scan with decoupled look-back) ------------
+
+constexpr int kRunThreads = 256;
+constexpr int kRunItems = 16;
+constexpr int kRunTile = kRunThreads * kRunItems;
+
+__global__ void __launch_bounds__(kRunThreads) k_runs(const uint32_t* __restrict__ code, uint32_t n,
+                                                      uint32_t* __restrict__ ucode, uint32_t* __restrict__ run_start,
+                                                      uint32_t* __restrict__ uidx, uint32_t* __restrict__ status,
+                                                      uint32_t* __restrict__ tile_ctr, BvhMeta* meta,
+                                                      uint32_t* __restrict__ err) {
+    __shared__ uint32_t s_warp[kRunThreads / 32];
+    __shared__ uint32_t s_tile, s_excl;
+    if (threadIdx.x == 0) s_tile = atomicAdd(tile_ctr, 1u);
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    const uint64_t first = (uint64_t)tile * kRunTile + (uint64_t)threadIdx.x * kRunItems;
+    uint32_t heads = 0;
+    bool head[kRunItems];
+#pragma unroll
+    for (int j = 0; j < kRunItems; ++j) {
+        const uint64_t i = first + j;
+        head[j] = i < n && (i == 0 || code[i] != code[i - 1]);
+        heads += head[j];
+    }
+    uint32_t tot;
+    const uint32_t off = block_exclusive_scan<kRunThreads>(heads, s_warp, &tot);
+    if (threadIdx.x == 0) {
+        uint32_t* st = status + tile;
+        uint32_t excl = 0;
+        if (tile == 0) {
+            st_release(st, kFlagInc | tot);
+        } else {
+            st_release(st, kFlagAgg | tot);
+            int64_t t = (int64_t)tile - 1;
+            uint32_t spins = 0;
+            while (t >= 0) {
+                const uint32_t v = ld_acquire(status + t);
+                const uint32_t flag = v & ~kCountMask;
+                if (flag == 0) {
+                    if (++spins > kSpinLimit) { atomicOr(err, ERR_TIMEOUT); break; }
+                    continue;
+                }
+                excl += v & kCountMask;
+                if (flag == kFlagInc) break;
+                --t;
+            }
+            st_release(st, kFlagInc | ((excl + tot) & kCountMask));
+        }
+        s_excl = excl;
+        const uint64_t tiles = ((uint64_t)n + kRunTile - 1) / kRunTile;
+        if (tile + 1 == tiles) {
+            meta->unique = excl + tot;
+            run_start[excl + tot] = n;  // sentinel: run u spans [run_start[u], run_start[u+1])
+        }
+    }
+    __syncthreads();
+    uint32_t u = s_excl + off;  // number of heads before this thread's first item
+#pragma unroll
+    for (int j = 0; j < kRunItems; ++j) {
+        const uint64_t i = first + j;
+        if (i < n) {
+            if (head[j]) {
+                ucode[u] = code[i];
+                run_start[u] = (uint32_t)i;
+                ++u;
+            }
+            uidx[i] = u - 1;
+        }
+    }
+}
+
+// ---- 5. hierarchy ------------------------------------------------------------------
+
+__device__ __forceinline__ int delta(const uint32_t* __restrict__ uc, int i, int j, int m) {
+    if (j < 0 || j >= m) return -1;
+    return __clz(uc[i] ^ uc[j]);  // unique codes: never equal for i != j
+}
+
+// Root (or leaf) code of the midpoint subtree of run u.
+__device__ __forceinline__ int32_t run_root(const uint32_t* __restrict__ run_start, uint32_t u) {
+    const uint32_t s = run_start[u], len = run_start[u + 1] - s;
+    return len == 1 ? ~(int32_t)s : (int32_t)(s + (len >> 1) - 1);
+}
+
+// Karras (HPG 2012) split finding over the unique codes. Each unique internal
+// node k records its split gamma and whether its children are unique leaves.
+__global__ void __launch_bounds__(kBlock) k_karras(const uint32_t* __restrict__ ucode,
+                                                   const uint32_t* __restrict__ run_start, const BvhMeta* __restrict__ meta,
+                                                   uint32_t* __restrict__ kgamma, uint32_t* __restrict__ gap_of) {
+    const int m = (int)meta->unique;
+    for (int i = blockIdx.x * kBlock + threadIdx.x; i < m - 1; i += gridDim.x * kBlock) {
+        const int d = (delta(ucode, i, i + 1, m) - delta(ucode, i, i - 1, m)) >= 0 ? 1 : -1;
+        const int dmin = delta(ucode, i, i - d, m);
+        int lmax = 2;
+        while (delta(ucode, i, i + lmax * d, m) > dmin) lmax <<= 1;
+        int l = 0;
+        for (int t = lmax >> 1; t >= 1; t >>= 1)
+            if (delta(ucode, i, i + (l + t) * d, m) > dmin) l += t;
+        const int j = i + l * d;
+        const int dnode = delta(ucode, i, j, m);
+        int s = 0;
+        for (int div = 2;; div <<= 1) {
+            const int t = (l + div - 1) / div;
+            if (delta(ucode, i, i + (s + t) * d, m) > dnode) s += t;
+            if (t == 1) break;
+        }
+        const int gamma = i + s * d + min(d, 0);
+        const int lo = min(i, j), hi = max(i, j);
+        // bit 31: left child is a unique leaf; bit 30: right child is a unique leaf
+        kgamma[i] = (uint32_t)gamma | (lo == gamma ? 0x80000000u : 0u) | (hi == gamma + 1 ? 0x40000000u : 0u);
+        gap_of[i] = run_start[gamma + 1] - 1;
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) k_link(const uint32_t* __restrict__ kgamma, const uint32_t* __restrict__ gap_of,
+                                                 const uint32_t* __restrict__ run_start, BvhMeta* meta, Node* nodes,
+                                                 uint32_t* __restrict__ parent_leaf) {
+    const int m = (int)meta->unique;
+    for (int k = blockIdx.x * kBlock + threadIdx.x; k < m - 1; k += gridDim.x * kBlock) {
+        const uint32_t g = kgamma[k];
+        const uint32_t gamma = g & 0x3FFFFFFFu;
+        const uint32_t G = gap_of[k];
+        const int32_t left = (g & 0x80000000u) ? run_root(run_start, gamma) : (int32_t)gap_of[gamma];
+        const int32_t right = (g & 0x40000000u) ? run_root(run_start, gamma + 1) : (int32_t)gap_of[gamma + 1];
+        nodes[G].q3.x = left;
+        nodes[G].q3.y = right;
+        if (left >= 0) nodes[left].q3.z = (int32_t)G; else parent_leaf[~left] = G;
+        if (right >= 0) nodes[right].q3.z = (int32_t)G; else parent_leaf[~right] = G;
+        if (k == 0) {
+            nodes[G].q3.z = (int32_t)kNoNode;
+            meta->root = G;
+        }
+    }
+}
+
+// Internal nodes inside equal-code runs: the run [s, e) is split at its
+// midpoint recursively (bvh.h:162-165). Each gap g inside a run finds its node
+// by descending from the run's root.
+__global__ void __launch_bounds__(kBlock) k_run_nodes(const uint32_t* __restrict__ code, uint32_t n,
+                                                      const uint32_t* __restrict__ uidx,
+                                                      const uint32_t* __restrict__ run_start, BvhMeta* meta, Node* nodes,
+                                                      uint32_t* __restrict__ parent_leaf, uint32_t* __restrict__ err) {
+    for (uint32_t g = blockIdx.x * kBlock + threadIdx.x; g + 1 < n; g += gridDim.x * kBlock) {
+        if (code[g] != code[g + 1]) continue;
+        const uint32_t u = uidx[g];
+        uint32_t a = run_start[u], b = run_start[u + 1] - 1;  // inclusive leaf range
+        uint32_t G = a + ((b - a + 1) >> 1) - 1;
+        if (G == g && meta->unique == 1) {
+            nodes[G].q3.z = (int32_t)kNoNode;
+            meta->root = G;
+        }
+        int guard = 0;
+        while (G != g) {
+            if (g < G) b = G; else a = G + 1;
+            G = a + ((b - a + 1) >> 1) - 1;
+            if (++guard > 64) { atomicOr(err, ERR_RANGE); break; }
+        }
+        const int32_t left = (a == G) ? ~(int32_t)a : (int32_t)(a + ((G - a + 1) >> 1) - 1);
+        const int32_t right = (G + 1 == b) ? ~(int32_t)b : (int32_t)(G + 1 + ((b - G) >> 1) - 1);
+        nodes[G].q3.x = left;
+        nodes[G].q3.y = right;
+        if (left >= 0) nodes[left].q3.z = (int32_t)G; else parent_leaf[~left] = G;
+        if (right >= 0) nodes[right].q3.z = (int32_t)G; else parent_leaf[~right] = G;
+    }
+}
+
+// ---- 6. refit + leaf-order triangles ---------------------------------------------
+
+__device__ __forceinline__ void put_child_box(Node* nd, int slot, const Box3& b) {
+    float4* q = reinterpret_cast<float4*>(nd);
+    q[slot] = make_float4(b.lo[0], b.hi[0], b.lo[1], b.hi[1]);
+    reinterpret_cast<float2*>(&nd->q2)[slot] = make_float2(b.lo[2], b.hi[2]);
+}
+
+__device__ __forceinline__ Box3 get_child_box_l2(const Node* nd, int slot) {
+    const float4 xy = __ldcg(reinterpret_cast<const float4*>(nd) + slot);
+    const float2 z = __ldcg(reinterpret_cast<const float2*>(&nd->q2) + slot);
+    Box3 b;
+    b.lo[0] = xy.x; b.hi[0] = xy.y; b.lo[1] = xy.z; b.hi[1] = xy.w; b.lo[2] = z.x; b.hi[2] = z.y;
+    return b;
+}
+
+__global__ void __launch_bounds__(kBlock) k_refit(const float* __restrict__ verts, uint32_t n,
+                                                  const uint32_t* __restrict__ prim, const uint32_t* __restrict__ parent_leaf,
+                                                  Node* nodes, Tri* __restrict__ tris, uint32_t* __restrict__ counters,
+                                                  uint32_t* __restrict__ err) {
+    for (uint32_t p = blockIdx.x * kBlock + threadIdx.x; p < n; p += gridDim.x * kBlock) {
+        const uint32_t id = prim[p];
+        const float* v = verts + 9ull * id;
+        float a[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) a[k] = __ldg(v + k);
+        Tri t;
+        t.a = make_float4(a[0], a[1], a[2], __uint_as_float(id));
+        t.b = make_float4(a[3], a[4], a[5], 0.0f);
+        t.c = make_float4(a[6], a[7], a[8], 0.0f);
+        tris[p] = t;
+        Box3 box;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            box.lo[k] = fminf(fminf(a[k], a[3 + k]), a[6 + k]);
+            box.hi[k] = fmaxf(fmaxf(a[k], a[3 + k]), a[6 + k]);
+        }
+        if (n == 1) {
+            // one triangle: a single node whose two children are the same leaf
+            Node nd;
+            nd.q0 = make_float4(box.lo[0], box.hi[0], box.lo[1], box.hi[1]);
+            nd.q1 = nd.q0;
+            nd.q2 = make_float4(box.lo[2], box.hi[2], box.lo[2], box.hi[2]);
+            nd.q3 = make_int4(~0, ~0, (int32_t)kNoNode, 0);
+            nodes[0] = nd;
+            continue;
+        }
+        int32_t me = ~(int32_t)p;
+        uint32_t node = parent_leaf[p];
+        int guard = 0;
+        while (node != kNoNode) {
+            Node* nd = nodes + node;
+            const int slot = (nd->q3.x == me) ? 0 : 1;
+            put_child_box(nd, slot, box);
+            __threadfence();
+            if (atomicAdd(&counters[node], 1u) == 0) break;  // sibling not done yet
+            __threadfence();
+            const Box3 sib = get_child_box_l2(nd, slot ^ 1);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                box.lo[k] = fminf(box.lo[k], sib.lo[k]);
+                box.hi[k] = fmaxf(box.hi[k], sib.hi[k]);
+            }
+            me = (int32_t)node;
+            node = (uint32_t)__ldcg(&nd->q3.z);
+            if (++guard > 128) { atomicOr(err, ERR_RANGE); break; }
+        }
+    }
+}
+
+// ---- 7. reference-layout export (parity only) -------------------------------------
+// Preorder index of a node covering leaves [first, ...] = 2*first + number of
+// left turns on the path from the root.
+
+__global__ void __launch_bounds__(kBlock) k_export_ref(const Node* __restrict__ nodes, const Tri* __restrict__ tris,
+                                                       const uint32_t* __restrict__ parent_leaf, uint32_t n,
+                                                       uint32_t* __restrict__ out) {
+    const uint64_t total = 2ull * n - 1;
+    for (uint64_t x = blockIdx.x * (uint64_t)kBlock + threadIdx.x; x < total; x += (uint64_t)gridDim.x * kBlock) {
+        uint32_t w[8];
+        uint32_t first, parent;
+        int32_t me;
+        if (x < n) {  // leaf at sorted position x
+            const uint32_t p = (uint32_t)x;
+            const Tri t = tris[p];
+            const float a[9] = {t.a.x, t.a.y, t.a.z, t.b.x, t.b.y, t.b.z, t.c.x, t.c.y, t.c.z};
+            for (int k = 0; k < 3; ++k) {
+                w[k] = __float_as_uint(fminf(fminf(a[k], a[3 + k]), a[6 + k]));
+                w[3 + k] = __float_as_uint(fmaxf(fmaxf(a[k], a[3 + k]), a[6 + k]));
+            }
+            w[6] = __float_as_uint(t.a.w);
+            w[7] = 1;
+            first = p;
+            me = ~(int32_t)p;
+            parent = n == 1 ? kNoNode : parent_leaf[p];
+        } else {  // internal node at gap G
+            const uint32_t G = (uint32_t)(x - n);
+            const Node nd = nodes[G];
+            w[0] = __float_as_uint(fminf(nd.q0.x, nd.q1.x));
+            w[1] = __float_as_uint(fminf(nd.q0.z, nd.q1.z));
+            w[2] = __float_as_uint(fminf(nd.q2.x, nd.q2.z));
+            w[3] = __float_as_uint(fmaxf(nd.q0.y, nd.q1.y));
+            w[4] = __float_as_uint(fmaxf(nd.q0.w, nd.q1.w));
+            w[5] = __float_as_uint(fmaxf(nd.q2.y, nd.q2.w));
+            int32_t c = nd.q3.x;
+            int guard = 0;
+            while (c >= 0 && ++guard < 128) c = nodes[c].q3.x;
+            first = (uint32_t)~c;
+            w[7] = 0;
+            me = (int32_t)G;
+            parent = (uint32_t)nd.q3.z;
+            w[6] = 0;  // filled below once the preorder index is known
+        }
+        uint32_t left_turns = 0;
+        int guard = 0;
+        while (parent != kNoNode && ++guard < 128) {
+            const int4 q = nodes[parent].q3;
+            if (q.x == me) ++left_turns;
+            me = (int32_t)parent;
+            parent = (uint32_t)q.z;
+        }
+        const uint32_t pre = 2 * first + left_turns;
+        if (x >= n) {
+            const uint32_t G = (uint32_t)(x - n);
+            w[6] = pre + 2 * (G - first + 1);
+        }
+        uint4* o = reinterpret_cast<uint4*>(out + 8ull * pre);
+        o[0] = make_uint4(w[0], w[1], w[2], w[3]);
+        o[1] = make_uint4(w[4], w[5], w[6], w[7]);
+    }
+}
+
+size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+struct Scratch {
+    uint32_t *keys_alt, *vals_alt, *uidx, *ucode, *run_start, *kgamma, *gap_of, *parent_leaf, *counters;
+    uint32_t *hist, *offs, *os_status, *run_status, *tile_ctr, *err;
+    float* partial;
+    size_t zero_bytes;  // bytes from hist up to the end of the zeroed region
+    void* zero_base;
+};
+
+constexpr int kPartials = 1024;
+
+size_t scratch_layout(uint32_t n, char* base, Scratch* s) {
+    const uint64_t os_tiles = ((uint64_t)n + kOsTile - 1) / kOsTile;
+    const uint64_t run_tiles = ((uint64_t)n + kRunTile - 1) / kRunTile;
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        char* p = base ? base + off : nullptr;
+        off += align256(bytes);
+        return p;
+    };
+    const size_t w = 4ull * n;
+    s->keys_alt = (uint32_t*)take(w);
+    s->vals_alt = (uint32_t*)take(w);
+    s->uidx = (uint32_t*)take(w);
+    s->ucode = (uint32_t*)take(w);
+    s->run_start = (uint32_t*)take(w + 4);
+    s->kgamma = (uint32_t*)take(w);
+    s->gap_of = (uint32_t*)take(w);
+    s->parent_leaf = (uint32_t*)take(w);
+    s->partial = (float*)take(sizeof(float) * 6 * kPartials);
+    // everything from here on is zeroed before each build
+    const size_t zstart = off;
+    s->counters = (uint32_t*)take(w);
+    s->hist = (uint32_t*)take(4 * 256 * 4);
+    s->offs = (uint32_t*)take(4 * 256 * 4);
+    s->os_status = (uint32_t*)take(4ull * os_tiles * 256 * 4);
+    s->run_status = (uint32_t*)take(run_tiles * 4);
+    s->tile_ctr = (uint32_t*)take(16 * 4);
+    s->err = (uint32_t*)take(4);
+    s->zero_base = base ? base + zstart : nullptr;
+    s->zero_bytes = off - zstart;
+    return off;
+}
+
+}  // namespace
+
+cudaError_t lbvh_build(BvhBuffers& b, const float* d_verts, uint32_t n, int num_sms, cudaStream_t st) {
+    cudaError_t e;
+    if ((e = b.meta.ensure(sizeof(BvhMeta))) != cudaSuccess) return e;
+    BvhMeta* meta = (BvhMeta*)b.meta.p;
+    if ((e = cudaMemsetAsync(meta, 0, sizeof(BvhMeta), st)) != cudaSuccess) return e;
+    if (n == 0) {
+        const uint32_t none = kNoNode;
+        return cudaMemcpyAsync(&meta->root, &none, 4, cudaMemcpyHostToDevice, st);
+    }
+    const size_t nn = n > 1 ? n - 1 : 1;
+    if ((e = b.nodes.ensure(nn * sizeof(Node))) != cudaSuccess) return e;
+    if ((e = b.tris.ensure((size_t)n * sizeof(Tri))) != cudaSuccess) return e;
+    if ((e = b.code.ensure(4ull * n)) != cudaSuccess) return e;
+    if ((e = b.prim.ensure(4ull * n)) != cudaSuccess) return e;
+    Scratch s;
+    const size_t need = scratch_layout(n, nullptr, &s);
+    if ((e = b.scratch.ensure(need)) != cudaSuccess) return e;
+    scratch_layout(n, (char*)b.scratch.p, &s);
+    if ((e = cudaMemsetAsync(s.zero_base, 0, s.zero_bytes, st)) != cudaSuccess) return e;
+    Node* nodes = (Node*)b.nodes.p;
+    uint32_t* code = (uint32_t*)b.code.p;
+    uint32_t* prim = (uint32_t*)b.prim.p;
+
+    const int grid = (int)std::min<uint64_t>(((uint64_t)n + kBlock - 1) / kBlock, (uint64_t)num_sms * 8);
+    const int parts = std::min(grid, kPartials);
+    k_centroid_partials<<<parts, kBlock, 0, st>>>(d_verts, n, s.partial);
+    k_centroid_final<<<1, 32, 0, st>>>(s.partial, parts, meta);
+    k_morton_hist<<<std::min(grid, num_sms * 2), kBlock, 0, st>>>(d_verts, n, meta, code, prim, s.hist);
+    k_hist_scan<<<4, 256, 0, st>>>(s.hist, s.offs);
+
+    if ((e = cudaFuncSetAttribute(k_onesweep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kOsSmem)) !=
+        cudaSuccess)
+        return e;
+    const uint32_t os_tiles = (n + kOsTile - 1) / kOsTile;
+    uint32_t* kin = code;
+    uint32_t* vin = prim;
+    uint32_t* kout = s.keys_alt;
+    uint32_t* vout = s.vals_alt;
+    for (int pass = 0; pass < 4; ++pass) {
+        k_onesweep<<<os_tiles, kOsThreads, kOsSmem, st>>>(kin, vin, kout, vout, n, pass, s.offs,
+                                                          s.os_status + (size_t)pass * os_tiles * 256, s.tile_ctr, s.err);
+        std::swap(kin, kout);
+        std::swap(vin, vout);
+    }
+    // four passes: the sorted data is back in code/prim
+
+    const uint32_t run_tiles = (n + kRunTile - 1) / kRunTile;
+    k_runs<<<run_tiles, kRunThreads, 0, st>>>(code, n, s.ucode, s.run_start, s.uidx, s.run_status, s.tile_ctr + 4,
+                                              meta, s.err);
+    k_karras<<<grid, kBlock, 0, st>>>(s.ucode, s.run_start, meta, s.kgamma, s.gap_of);
+    k_link<<<grid, kBlock, 0, st>>>(s.kgamma, s.gap_of, s.run_start, meta, nodes, s.parent_leaf);
+    k_run_nodes<<<grid, kBlock, 0, st>>>(code, n, s.uidx, s.run_start, meta, nodes, s.parent_leaf, s.err);
+    k_refit<<<grid, kBlock, 0, st>>>(d_verts, n, prim, s.parent_leaf, nodes, (Tri*)b.tris.p, s.counters, s.err);
+    // fold the build's error word into the header the host reads
+    if ((e = cudaMemcpyAsync(&meta->err, s.err, 4, cudaMemcpyDeviceToDevice, st)) != cudaSuccess) return e;
+    return cudaGetLastError();
+}
+
+cudaError_t lbvh_export_ref(const BvhBuffers& b, uint32_t n, uint32_t* d_ref_nodes, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    Scratch s;
+    scratch_layout(n, (char*)b.scratch.p, &s);
+    const uint64_t total = 2ull * n - 1;
+    const int grid = (int)std::min<uint64_t>((total + kBlock - 1) / kBlock, 4096);
+    k_export_ref<<<grid, kBlock, 0, st>>>((const Node*)b.nodes.p, (const Tri*)b.tris.p, s.parent_leaf, n, d_ref_nodes);
+    return cudaGetLastError();
+}
+
+}  // namespace gr

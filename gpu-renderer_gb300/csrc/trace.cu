@@ -1,0 +1,228 @@
+// Closest-hit and any-hit traversal of the binary LBVH.
+//
+// Replaces trace_kernel / trace_shadow_kernel (src/renderer/pathtracer_kernel.h
+// :175-308). Differences by design:
+//   - persistent warps: a fixed grid of warps pulls 32 rays at a time from a
+//     global counter until the queue is drained;
+//   - child boxes live in the parent node and are fetched as 16-byte vector
+//     loads; both children are tested at once and the nearer is visited first;
+//   - a short per-thread stack in shared memory, spilling to local memory only
+//     past kShortStack entries;
+//   - the FP32 watertight triangle test (Woop, Benthin, Wald, JCGT 2013) on
+//     leaf-order triangle copies instead of the reference's FP64
+//     Moller-Trumbore through 408-byte Triangle records.
+// Every float operation is an explicit round-to-nearest intrinsic so the
+// result is reproducible by the host oracle bit for bit.
+#include <algorithm>
+
+#include "gr_internal.h"
+
+namespace gr {
+namespace {
+
+constexpr int kTraceThreads = 128;
+constexpr int kShortStack = 12;
+constexpr int kStackMax = 64;
+
+struct RayW {
+    float ox, oy, oz, tmin, tmax;
+    float sx, sy, sz;
+    int kx, ky, kz;
+    float ix, iy, iz;     // reciprocal direction (near-zero components clamped)
+    float nox, noy, noz;  // -origin * reciprocal direction
+};
+
+__device__ __forceinline__ float pick(float x, float y, float z, int k) { return k == 0 ? x : (k == 1 ? y : z); }
+
+__device__ __forceinline__ RayW prepare(const float4 r0, const float4 r1) {
+    RayW p;
+    p.ox = r0.x; p.oy = r0.y; p.oz = r0.z;
+    const float dx = r0.w, dy = r1.x, dz = r1.y;
+    p.tmin = r1.z;
+    p.tmax = r1.w;
+    const float ax = fabsf(dx), ay = fabsf(dy), az = fabsf(dz);
+    int kz = 0;
+    float m = ax;
+    if (ay > m) { kz = 1; m = ay; }
+    if (az > m) kz = 2;
+    int kx = kz == 2 ? 0 : kz + 1;
+    int ky = kx == 2 ? 0 : kx + 1;
+    const float dkz = pick(dx, dy, dz, kz);
+    if (dkz < 0.0f) { const int t = kx; kx = ky; ky = t; }
+    p.kx = kx; p.ky = ky; p.kz = kz;
+    p.sx = __fdiv_rn(pick(dx, dy, dz, kx), dkz);
+    p.sy = __fdiv_rn(pick(dx, dy, dz, ky), dkz);
+    p.sz = __frcp_rn(dkz);
+    const float eps = 0x1p-80f;
+    const float cx = fabsf(dx) > eps ? dx : copysignf(eps, dx);
+    const float cy = fabsf(dy) > eps ? dy : copysignf(eps, dy);
+    const float cz = fabsf(dz) > eps ? dz : copysignf(eps, dz);
+    p.ix = __frcp_rn(cx); p.iy = __frcp_rn(cy); p.iz = __frcp_rn(cz);
+    p.nox = -__fmul_rn(p.ox, p.ix); p.noy = -__fmul_rn(p.oy, p.iy); p.noz = -__fmul_rn(p.oz, p.iz);
+    return p;
+}
+
+__device__ __forceinline__ bool slab(const RayW& p, float lox, float hix, float loy, float hiy, float loz, float hiz,
+                                     float tbest, float& tn) {
+    const float x0 = __fmaf_rn(lox, p.ix, p.nox), x1 = __fmaf_rn(hix, p.ix, p.nox);
+    const float y0 = __fmaf_rn(loy, p.iy, p.noy), y1 = __fmaf_rn(hiy, p.iy, p.noy);
+    const float z0 = __fmaf_rn(loz, p.iz, p.noz), z1 = __fmaf_rn(hiz, p.iz, p.noz);
+    const float tnear = fmaxf(fmaxf(fminf(x0, x1), fminf(y0, y1)), fmaxf(fminf(z0, z1), p.tmin));
+    const float tfar = fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fminf(fmaxf(z0, z1), tbest));
+    tn = tnear;
+    return tnear <= tfar;
+}
+
+__device__ __forceinline__ bool tri_test(const RayW& p, const float4 a, const float4 b, const float4 c, float tbest,
+                                         float& t, float& u, float& v) {
+    const float Ax0 = __fsub_rn(a.x, p.ox), Ay0 = __fsub_rn(a.y, p.oy), Az0 = __fsub_rn(a.z, p.oz);
+    const float Bx0 = __fsub_rn(b.x, p.ox), By0 = __fsub_rn(b.y, p.oy), Bz0 = __fsub_rn(b.z, p.oz);
+    const float Cx0 = __fsub_rn(c.x, p.ox), Cy0 = __fsub_rn(c.y, p.oy), Cz0 = __fsub_rn(c.z, p.oz);
+    const float Akz = pick(Ax0, Ay0, Az0, p.kz), Bkz = pick(Bx0, By0, Bz0, p.kz), Ckz = pick(Cx0, Cy0, Cz0, p.kz);
+    const float Ax = __fmaf_rn(-p.sx, Akz, pick(Ax0, Ay0, Az0, p.kx));
+    const float Ay = __fmaf_rn(-p.sy, Akz, pick(Ax0, Ay0, Az0, p.ky));
+    const float Bx = __fmaf_rn(-p.sx, Bkz, pick(Bx0, By0, Bz0, p.kx));
+    const float By = __fmaf_rn(-p.sy, Bkz, pick(Bx0, By0, Bz0, p.ky));
+    const float Cx = __fmaf_rn(-p.sx, Ckz, pick(Cx0, Cy0, Cz0, p.kx));
+    const float Cy = __fmaf_rn(-p.sy, Ckz, pick(Cx0, Cy0, Cz0, p.ky));
+    const float U = __fsub_rn(__fmul_rn(Cx, By), __fmul_rn(Cy, Bx));
+    const float V = __fsub_rn(__fmul_rn(Ax, Cy), __fmul_rn(Ay, Cx));
+    const float W = __fsub_rn(__fmul_rn(Bx, Ay), __fmul_rn(By, Ax));
+    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
+    const float det = __fadd_rn(__fadd_rn(U, V), W);
+    if (det == 0.0f) return false;
+    const float Az = __fmul_rn(p.sz, Akz), Bz = __fmul_rn(p.sz, Bkz), Cz = __fmul_rn(p.sz, Ckz);
+    const float T = __fmaf_rn(U, Az, __fmaf_rn(V, Bz, __fmul_rn(W, Cz)));
+    const float rcp = __frcp_rn(det);
+    const float tt = __fmul_rn(T, rcp);
+    if (!(tt >= p.tmin && tt <= tbest)) return false;
+    t = tt;
+    u = __fmul_rn(V, rcp);
+    v = __fmul_rn(W, rcp);
+    return true;
+}
+
+template <bool ANY>
+__device__ __forceinline__ float4 trace_ray(const Node* __restrict__ nodes, const Tri* __restrict__ tris, uint32_t root,
+                                            const RayW& p, int2 (*s_stack)[kTraceThreads], uint32_t* err) {
+    int2 l_stack[kStackMax - kShortStack];
+    float best_t = p.tmax, bu = 0.0f, bv = 0.0f;
+    uint32_t best_prim = 0xFFFFFFFFu;
+    int sp = 0;
+    int32_t node = (int32_t)root;
+    bool done = root == kNoNode;
+    const int tid = threadIdx.x;
+    while (!done) {
+        const float4* q = reinterpret_cast<const float4*>(nodes + node);
+        const float4 q0 = __ldg(q), q1 = __ldg(q + 1), q2 = __ldg(q + 2);
+        const int4 q3 = __ldg(reinterpret_cast<const int4*>(q + 3));
+        float tn0, tn1;
+        const bool h0 = slab(p, q0.x, q0.y, q0.z, q0.w, q2.x, q2.y, best_t, tn0);
+        const bool h1 = slab(p, q1.x, q1.y, q1.z, q1.w, q2.z, q2.w, best_t, tn1);
+        const bool swap = h0 && h1 && tn1 < tn0;
+        const int32_t cn = swap ? q3.y : q3.x, cf = swap ? q3.x : q3.y;
+        const float tnf = swap ? tn0 : tn1;
+        const bool hn = swap ? h1 : h0, hf = swap ? h0 : h1;
+        int32_t next = -1;
+        bool have = false;
+#pragma unroll
+        for (int s = 0; s < 2; ++s) {
+            const bool h = s == 0 ? hn : hf;
+            const int32_t c = s == 0 ? cn : cf;
+            if (!h) continue;
+            if (c < 0) {
+                const Tri* tr = tris + (uint32_t)(~c);
+                const float4 a = __ldg(&tr->a), b = __ldg(&tr->b), cc = __ldg(&tr->c);
+                float t, u, v;
+                if (tri_test(p, a, b, cc, best_t, t, u, v)) {
+                    const uint32_t prim = __float_as_uint(a.w);
+                    if (ANY) {
+                        best_t = t; bu = u; bv = v; best_prim = prim;
+                        done = true;
+                        break;
+                    }
+                    if (t < best_t || prim < best_prim) {
+                        best_t = t; bu = u; bv = v; best_prim = prim;
+                    }
+                }
+            } else if (!have) {
+                next = c;
+                have = true;
+            } else {
+                if (sp < kShortStack) {
+                    s_stack[sp][tid] = make_int2(c, __float_as_int(tnf));
+                } else if (sp < kStackMax) {
+                    l_stack[sp - kShortStack] = make_int2(c, __float_as_int(tnf));
+                } else {
+                    atomicOr(err, ERR_STACK);
+                    done = true;
+                    break;
+                }
+                ++sp;
+            }
+        }
+        if (done) break;
+        if (!have) {
+            for (;;) {
+                if (sp == 0) { done = true; break; }
+                --sp;
+                const int2 e = sp < kShortStack ? s_stack[sp][tid] : l_stack[sp - kShortStack];
+                if (ANY || __int_as_float(e.y) <= best_t) { next = e.x; break; }
+            }
+        }
+        node = next;
+    }
+    if (best_prim == 0xFFFFFFFFu) return make_float4(p.tmax, __int_as_float(-1), 0.0f, 0.0f);
+    return make_float4(best_t, __uint_as_float(best_prim), bu, bv);
+}
+
+template <bool ANY>
+__global__ void __launch_bounds__(kTraceThreads) k_trace(const Node* __restrict__ nodes, const Tri* __restrict__ tris,
+                                                         const BvhMeta* __restrict__ meta, const float4* __restrict__ rays, uint64_t n,
+                                                         float4* __restrict__ hits, unsigned long long* counter,
+                                                         uint32_t* err) {
+    __shared__ int2 s_stack[kShortStack][kTraceThreads];
+    const int lane = threadIdx.x & 31;
+    const uint32_t root = meta->root;
+    for (;;) {
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(counter, 32ull);
+        base = __shfl_sync(0xFFFFFFFFu, base, 0);
+        if (base >= n) break;
+        const uint64_t i = base + lane;
+        if (i < n) {
+            const float4 r0 = __ldg(rays + 2 * i), r1 = __ldg(rays + 2 * i + 1);
+            const RayW p = prepare(r0, r1);
+            hits[i] = trace_ray<ANY>(nodes, tris, root, p, s_stack, err);
+        }
+    }
+}
+
+}  // namespace
+
+cudaError_t trace_launch(const BvhDevice& bvh, const gr_ray* d_rays, uint64_t n, gr_hit* d_hits, int any_hit,
+                         unsigned long long* d_counter, uint32_t* d_err, int num_sms, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return e;
+    static int occ[2] = {0, 0};
+    int& o = occ[any_hit ? 1 : 0];
+    if (o == 0) {
+        e = any_hit ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_trace<true>, kTraceThreads, 0)
+                    : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_trace<false>, kTraceThreads, 0);
+        if (e != cudaSuccess) return e;
+        if (o < 1) o = 1;
+    }
+    const uint64_t warps_needed = (n + 31) / 32;
+    const uint64_t blocks_needed = (warps_needed + kTraceThreads / 32 - 1) / (kTraceThreads / 32);
+    const int grid = (int)std::min<uint64_t>((uint64_t)num_sms * o, blocks_needed);
+    const float4* r = reinterpret_cast<const float4*>(d_rays);
+    float4* h = reinterpret_cast<float4*>(d_hits);
+    if (any_hit)
+        k_trace<true><<<grid, kTraceThreads, 0, s>>>(bvh.nodes, bvh.tris, bvh.meta, r, n, h, d_counter, d_err);
+    else
+        k_trace<false><<<grid, kTraceThreads, 0, s>>>(bvh.nodes, bvh.tris, bvh.meta, r, n, h, d_counter, d_err);
+    return cudaGetLastError();
+}
+
+}  // namespace gr

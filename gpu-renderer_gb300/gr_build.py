@@ -1,0 +1,94 @@
+"""Builds libgr.so (CUDA kernels for sm_103a + host C++ + the C ABI) in-tree.
+
+Usage: python gpu-renderer_gb300/gr_build.py [--force]
+Objects go to gpu-renderer_gb300/_build/, the library to gpu-renderer_gb300/lib/.
+"""
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+OBJ = os.path.join(HERE, "_build")
+LIB = os.path.join(HERE, "lib")
+CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+NVCC = os.path.join(CUDA_HOME, "bin", "nvcc") if os.path.exists(os.path.join(CUDA_HOME, "bin", "nvcc")) else "nvcc"
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+INCLUDES = ["-I", os.path.join(ROOT, "include"), "-I", CSRC]
+NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"] + ARCH
+CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-Wextra", "-Wno-unused-parameter",
+             "-I", os.path.join(CUDA_HOME, "include")]
+
+
+def _sources():
+    out = []
+    for name in sorted(os.listdir(CSRC)):
+        if name.endswith(".cu") or name.endswith(".cpp"):
+            out.append(os.path.join(CSRC, name))
+    return out
+
+
+def _headers():
+    hs = [os.path.join(ROOT, "include", h) for h in os.listdir(os.path.join(ROOT, "include"))]
+    hs += [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".h", ".cuh"))]
+    return hs
+
+
+def _stale(target, deps):
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def _compile(src, force):
+    obj = os.path.join(OBJ, os.path.basename(src) + ".o")
+    if not force and not _stale(obj, [src] + _headers()):
+        return obj
+    if src.endswith(".cu"):
+        cmd = [NVCC] + NVCC_FLAGS + INCLUDES + ["-c", src, "-o", obj]
+    else:
+        cmd = ["g++"] + CXX_FLAGS + INCLUDES + ["-c", src, "-o", obj]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("compile failed: %s\n%s\n%s" % (" ".join(cmd), r.stdout, r.stderr))
+    return obj
+
+
+def build(force=False, verbose=False):
+    os.makedirs(OBJ, exist_ok=True)
+    os.makedirs(LIB, exist_ok=True)
+    srcs = _sources()
+    with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
+        objs = list(ex.map(lambda s: _compile(s, force), srcs))
+    lib = os.path.join(LIB, "libgr.so")
+    if force or _stale(lib, objs):
+        cmd = [NVCC] + ARCH + ["-shared", "-cudart", "static", "-o", lib] + objs
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("link failed: %s\n%s\n%s" % (" ".join(cmd), r.stdout, r.stderr))
+    if verbose:
+        print("built", lib)
+    return lib
+
+
+def build_oracle():
+    """Builds the CPU oracle (test infrastructure) and, where the reference
+    sources are present, the reference's own host LBVH next to it."""
+    odir = os.path.join(ROOT, "oracle")
+    r = subprocess.run(["make", "-s", "-C", odir, "-j4"], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("oracle build failed:\n%s\n%s" % (r.stdout, r.stderr))
+    ref = os.path.join(odir, "ref", "build_ref.sh")
+    if os.path.isdir("/root/reference/src") and shutil.which("bash"):
+        r = subprocess.run(["bash", ref], capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("reference build failed:\n%s\n%s" % (r.stdout, r.stderr))
+
+
+if __name__ == "__main__":
+    build(force="--force" in sys.argv, verbose=True)
+    build_oracle()

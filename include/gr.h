@@ -1,0 +1,115 @@
+/*
+ * gr — GB300-native wavefront path tracer: the C ABI.
+ *
+ * This is the drop-in boundary for slongle/GPU-Renderer's render path. The
+ * reference has no C ABI (everything links into one executable); each entry
+ * point below names the in-process reference interface it replaces.
+ *
+ * Conventions
+ *   - every call returns a gr_status; nothing here calls exit() or aborts
+ *     (the reference's CUDA_CHECK exits, src/utility/buffer.h:3-12);
+ *   - `stream` arguments are cudaStream_t passed as void* (NULL = legacy
+ *     default stream); calls that take a stream are stream-ordered and do not
+ *     synchronise the device;
+ *   - pointers named d_* are device pointers, h_* are host pointers;
+ *   - one gr_ctx per host thread; objects created from a context are used from
+ *     that context's thread only.
+ */
+#ifndef GR_H_
+#define GR_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum gr_status {
+    GR_OK = 0,
+    GR_ERR_INVALID = 1,     /* bad argument or object state */
+    GR_ERR_CUDA = 2,        /* a CUDA runtime call failed; see gr_last_error */
+    GR_ERR_OOM_BUDGET = 3,  /* allocation failed or exceeds the memory budget */
+    GR_ERR_PARSE = 4,       /* scene file could not be parsed */
+    GR_ERR_TIMEOUT = 5,     /* a bounded device-side wait gave up */
+    GR_ERR_OVERFLOW = 6     /* a device-side capacity (stack, queue) was exceeded */
+} gr_status;
+
+/* Ray and hit records, byte-compatible with the reference's Ray and Hit
+ * (src/renderer/ray.h:5-19). A miss has prim == -1. */
+typedef struct gr_ray {
+    float o[3];
+    float d[3];
+    float tmin, tmax;
+} gr_ray;
+
+typedef struct gr_hit {
+    float t;      /* distance in units of |d|; tmax when prim == -1 */
+    int32_t prim; /* triangle index in the input order, -1 on a miss */
+    float u, v;   /* barycentric weights of vertex 1 and vertex 2 */
+} gr_hit;
+
+typedef struct gr_ctx gr_ctx;
+typedef struct gr_bvh gr_bvh;
+
+/* ---- context ------------------------------------------------------------ */
+
+/* Binds `device` and creates a context (streams, memory pool). */
+gr_status gr_context_create(int device, gr_ctx** out);
+gr_status gr_context_destroy(gr_ctx* ctx);
+/* Text of the last error recorded on `ctx` (never NULL). */
+const char* gr_last_error(const gr_ctx* ctx);
+/* Static description of a status code. */
+const char* gr_status_string(int status);
+/* Library version as an integer: major*10000 + minor*100 + patch. */
+int gr_version(void);
+
+/* ---- acceleration structure ----------------------------------------------
+ * Replaces LBVH_build (src/renderer/bvh.h:186-221), which runs single-threaded
+ * on the host. The GPU build computes 30-bit Morton codes of triangle
+ * centroids, sorts them with a stable onesweep radix sort, builds the Karras
+ * radix tree over unique codes with midpoint splits inside equal-code runs
+ * (the reference's rule, bvh.h:161-176) and refits boxes bottom-up. */
+
+gr_status gr_bvh_create(gr_ctx* ctx, gr_bvh** out);
+gr_status gr_bvh_destroy(gr_bvh* bvh);
+
+/* Builds over `n` triangles given as 9 floats each (p0.xyz, p1.xyz, p2.xyz)
+ * in device memory. The BVH keeps no pointer to d_verts. */
+gr_status gr_bvh_build(gr_bvh* bvh, const float* d_verts, uint32_t n, void* stream);
+
+/* Same, from host memory (copies in, builds, waits). */
+gr_status gr_bvh_build_host(gr_bvh* bvh, const float* h_verts, uint32_t n);
+
+/* Number of triangles the BVH was built over. */
+uint32_t gr_bvh_size(const gr_bvh* bvh);
+
+/* Copies the build to host buffers for parity checks (waits for the device):
+ *   h_sorted_prim, h_sorted_code : n words — triangle ids and Morton codes in
+ *                                  sorted order (the reference's MortonInfo)
+ *   h_ref_nodes                  : 8 words x (2n-1) — the reference's
+ *                                  BVHLinearNode array in DFS preorder
+ *                                  (box min.xyz, max.xyz, tri/right index, leaf)
+ *   h_nodes                      : 16 words x max(n-1,1) — the traversal layout
+ *   h_tris                       : 12 floats x n — triangles in leaf order
+ *   h_root                       : root node index
+ * Any pointer may be NULL. */
+gr_status gr_bvh_export(gr_bvh* bvh, uint32_t* h_sorted_prim, uint32_t* h_sorted_code, uint32_t* h_ref_nodes,
+                        uint32_t* h_nodes, float* h_tris, uint32_t* h_root);
+
+/* ---- traversal -------------------------------------------------------------
+ * Replaces trace / trace_shadow (src/renderer/pathtracer_kernel.h:235-246 and
+ * :310-321) on a queue of rays: closest hit (any_hit = 0) or first hit found
+ * (any_hit = 1). FP32 watertight triangle test; closest-hit ties at equal t go
+ * to the smaller prim id. */
+
+gr_status gr_trace(gr_bvh* bvh, const gr_ray* d_rays, uint64_t n, gr_hit* d_hits, int any_hit, void* stream);
+
+/* Host-memory variant: copies rays in, traces, copies hits out, waits. */
+gr_status gr_trace_host(gr_bvh* bvh, const gr_ray* h_rays, uint64_t n, gr_hit* h_hits, int any_hit);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GR_H_ */

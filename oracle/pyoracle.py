@@ -1,0 +1,126 @@
+"""ctypes wrapper of the CPU oracle (oracle/build/liboracle.so).
+
+Test infrastructure: imported only by tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py. The product (libgr.so) never uses it.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "build", "liboracle.so")
+REF_LIB = os.path.join(HERE, "_ref", "libref_lbvh.so")
+_P = ctypes.c_void_p
+_lib = None
+_ref = None
+
+
+def build():
+    r = subprocess.run(["make", "-s", "-C", HERE, "-j4"], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + r.stdout + r.stderr)
+
+
+def load():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        _lib = ctypes.CDLL(LIB)
+    return _lib
+
+
+def ref_available():
+    return os.path.exists(REF_LIB)
+
+
+def load_ref():
+    global _ref
+    if _ref is None:
+        _ref = ctypes.CDLL(REF_LIB)
+    return _ref
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(_P)
+
+
+def threads():
+    return os.cpu_count() or 1
+
+
+def morton(verts):
+    v = np.ascontiguousarray(verts, np.float32).reshape(-1, 9)
+    codes = np.zeros(v.shape[0], np.uint32)
+    cbox = np.zeros(6, np.float32)
+    load().or_morton(_p(v), v.shape[0], _p(codes), _p(cbox))
+    return codes, cbox
+
+
+def lbvh(verts):
+    v = np.ascontiguousarray(verts, np.float32).reshape(-1, 9)
+    n = v.shape[0]
+    out = {
+        "sorted_prim": np.zeros(n, np.uint32), "sorted_code": np.zeros(n, np.uint32),
+        "ref_nodes": np.zeros(max(2 * n - 1, 0) * 8, np.uint32),
+        "nodes": np.zeros(max(n - 1, 1) * 16, np.uint32), "tris": np.zeros(12 * n, np.float32),
+    }
+    root = ctypes.c_uint32()
+    load().or_lbvh_build(_p(v), n, _p(out["sorted_prim"]), _p(out["sorted_code"]), _p(out["ref_nodes"]),
+                         _p(out["nodes"]), _p(out["tris"]), ctypes.byref(root))
+    out["root"] = root.value
+    return out
+
+
+def trace(bvh, rays, any_hit=False, stats=False, nthreads=None):
+    r = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
+    m = r.shape[0]
+    hits = np.zeros((m, 4), np.float32)
+    st = np.zeros((m, 2), np.uint32) if stats else None
+    load().or_trace(_p(bvh["nodes"]), _p(bvh["tris"]), ctypes.c_uint32(bvh["root"]), _p(r), ctypes.c_uint64(m),
+                    int(any_hit), _p(hits), _p(st), nthreads or threads())
+    return (hits, st) if stats else hits
+
+
+def trace_brute(verts, rays, any_hit=False, nthreads=None):
+    v = np.ascontiguousarray(verts, np.float32).reshape(-1, 9)
+    r = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
+    hits = np.zeros((r.shape[0], 4), np.float32)
+    load().or_trace_brute(_p(v), v.shape[0], _p(r), ctypes.c_uint64(r.shape[0]), int(any_hit), _p(hits),
+                          nthreads or threads())
+    return hits
+
+
+def trace_ref(ref_nodes, verts, rays, any_hit=False, stats=False, nthreads=None):
+    v = np.ascontiguousarray(verts, np.float32).reshape(-1, 9)
+    r = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
+    m = r.shape[0]
+    hits = np.zeros((m, 4), np.float32)
+    st = np.zeros((m, 2), np.uint32) if stats else None
+    load().or_trace_ref(_p(ref_nodes), _p(v), v.shape[0], _p(r), ctypes.c_uint64(m), int(any_hit), _p(hits),
+                        _p(st), nthreads or threads())
+    return (hits, st) if stats else hits
+
+
+def fp64_check(ref_nodes, verts, rays, prim, rel_gap=1e-6, bary_margin=1e-6, nthreads=None):
+    v = np.ascontiguousarray(verts, np.float32).reshape(-1, 9)
+    r = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
+    p = np.ascontiguousarray(prim, np.int32)
+    m = r.shape[0]
+    t64 = np.zeros(m, np.float64)
+    amb = np.zeros(m, np.uint8)
+    load().or_fp64_check(_p(ref_nodes), _p(v), v.shape[0], _p(r), ctypes.c_uint64(m), _p(p), _p(t64), _p(amb),
+                         ctypes.c_double(rel_gap), ctypes.c_double(bary_margin), nthreads or threads())
+    return t64, amb.astype(bool)
+
+
+def ref_lbvh(verts):
+    """The reference's own host LBVH_build (bvh.h), compiled from its sources."""
+    v = np.ascontiguousarray(verts, np.float32).reshape(-1, 9)
+    n = v.shape[0]
+    nodes = np.zeros(max(2 * n - 1, 0) * 8, np.uint32)
+    codes = np.zeros(n, np.uint32)
+    load_ref().ref_lbvh_build(_p(v), n, _p(nodes), _p(codes))
+    return nodes, codes

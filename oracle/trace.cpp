@@ -1,0 +1,459 @@
+// CPU oracle: ray traversal. Test infrastructure only (see oracle.h).
+//
+// Three traversals live here:
+//   1. or_trace       — the product's FP32 watertight traversal, restated from
+//                       its specification (not from the CUDA source) so that
+//                       hit ids, t, u, v can be compared bit for bit.
+//   2. or_trace_ref   — the reference's traversal (pathtracer_kernel.h:175-308)
+//                       over its own node layout with its mixed-precision
+//                       Moller-Trumbore test (:119-152) and slab test (:154-173).
+//   3. or_fp64_check  — an FP64 distance oracle with an ambiguity classifier.
+// Compiled with -ffp-contract=off: every a*b+c below rounds twice unless it
+// is written as fmaf().
+#include "oracle.h"
+
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <thread>
+#include <vector>
+
+namespace {
+
+template <class F>
+void parallel_rays(uint64_t nrays, int threads, F&& fn) {
+    if (threads <= 1 || nrays < 4096) {
+        fn(0, nrays);
+        return;
+    }
+    std::atomic<uint64_t> next{0};
+    const uint64_t chunk = 1024;
+    std::vector<std::thread> pool;
+    for (int t = 0; t < threads; ++t) {
+        pool.emplace_back([&] {
+            for (;;) {
+                uint64_t b = next.fetch_add(chunk);
+                if (b >= nrays) break;
+                fn(b, std::min(nrays, b + chunk));
+            }
+        });
+    }
+    for (auto& th : pool) th.join();
+}
+
+inline float f_of(uint32_t w) { float f; std::memcpy(&f, &w, 4); return f; }
+inline uint32_t w_of(float f) { uint32_t w; std::memcpy(&w, &f, 4); return w; }
+
+// ---------------------------------------------------------------------------
+// Product traversal specification
+// ---------------------------------------------------------------------------
+struct RayPre {
+    float o[3], d[3], tmin, tmax;
+    int kx, ky, kz;
+    float sx, sy, sz;
+    float idir[3], ood[3];
+};
+
+inline void prepare(const float* r, RayPre& p) {
+    for (int k = 0; k < 3; ++k) { p.o[k] = r[k]; p.d[k] = r[3 + k]; }
+    p.tmin = r[6];
+    p.tmax = r[7];
+    // watertight set-up (Woop, Benthin, Wald, JCGT 2013): kz = dominant axis,
+    // ties resolved toward the lower axis index
+    float ax = std::fabs(p.d[0]), ay = std::fabs(p.d[1]), az = std::fabs(p.d[2]);
+    int kz = 0;
+    float m = ax;
+    if (ay > m) { kz = 1; m = ay; }
+    if (az > m) { kz = 2; }
+    int kx = kz + 1; if (kx == 3) kx = 0;
+    int ky = kx + 1; if (ky == 3) ky = 0;
+    if (p.d[kz] < 0.0f) { int t = kx; kx = ky; ky = t; }
+    p.kx = kx; p.ky = ky; p.kz = kz;
+    p.sx = p.d[kx] / p.d[kz];
+    p.sy = p.d[ky] / p.d[kz];
+    p.sz = 1.0f / p.d[kz];
+    // slab set-up: near-zero components become +-2^-80 so no product is inf*0
+    const float eps = 0x1p-80f;
+    for (int k = 0; k < 3; ++k) {
+        float dk = std::fabs(p.d[k]) > eps ? p.d[k] : std::copysign(eps, p.d[k]);
+        p.idir[k] = 1.0f / dk;
+        p.ood[k] = p.o[k] * p.idir[k];
+    }
+}
+
+// Child-box slab test; returns entry distance through *tn.
+inline bool slab(const RayPre& p, float lox, float hix, float loy, float hiy, float loz, float hiz, float tbest,
+                 float* tn) {
+    float x0 = std::fmaf(lox, p.idir[0], -p.ood[0]), x1 = std::fmaf(hix, p.idir[0], -p.ood[0]);
+    float y0 = std::fmaf(loy, p.idir[1], -p.ood[1]), y1 = std::fmaf(hiy, p.idir[1], -p.ood[1]);
+    float z0 = std::fmaf(loz, p.idir[2], -p.ood[2]), z1 = std::fmaf(hiz, p.idir[2], -p.ood[2]);
+    float tnear = std::fmax(std::fmax(std::fmin(x0, x1), std::fmin(y0, y1)), std::fmax(std::fmin(z0, z1), p.tmin));
+    float tfar = std::fmin(std::fmin(std::fmax(x0, x1), std::fmax(y0, y1)), std::fmin(std::fmax(z0, z1), tbest));
+    *tn = tnear;
+    return tnear <= tfar;
+}
+
+// Watertight FP32 test. Edge functions are plain products and differences so a
+// shared edge evaluates to exactly opposite values in both triangles.
+inline bool tri_test(const RayPre& p, const float* v0, const float* v1, const float* v2, float tbest, float* t_out,
+                     float* u_out, float* v_out) {
+    float A[3], B[3], C[3];
+    for (int k = 0; k < 3; ++k) { A[k] = v0[k] - p.o[k]; B[k] = v1[k] - p.o[k]; C[k] = v2[k] - p.o[k]; }
+    float Ax = std::fmaf(-p.sx, A[p.kz], A[p.kx]), Ay = std::fmaf(-p.sy, A[p.kz], A[p.ky]);
+    float Bx = std::fmaf(-p.sx, B[p.kz], B[p.kx]), By = std::fmaf(-p.sy, B[p.kz], B[p.ky]);
+    float Cx = std::fmaf(-p.sx, C[p.kz], C[p.kx]), Cy = std::fmaf(-p.sy, C[p.kz], C[p.ky]);
+    float U = Cx * By - Cy * Bx;
+    float V = Ax * Cy - Ay * Cx;
+    float W = Bx * Ay - By * Ax;
+    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
+    float det = (U + V) + W;
+    if (det == 0.0f) return false;
+    float Az = p.sz * A[p.kz], Bz = p.sz * B[p.kz], Cz = p.sz * C[p.kz];
+    float T = std::fmaf(U, Az, std::fmaf(V, Bz, W * Cz));
+    float rcp = 1.0f / det;
+    float t = T * rcp;
+    if (!(t >= p.tmin && t <= tbest)) return false;
+    *t_out = t;
+    *u_out = V * rcp;
+    *v_out = W * rcp;
+    return true;
+}
+
+struct Best {
+    float t, u, v;
+    uint32_t prim;  // 0xFFFFFFFF = none
+};
+
+// Closest-hit acceptance: smaller t wins, equal t goes to the smaller prim id,
+// which makes the result independent of the order triangles are visited in.
+inline void consider(const RayPre& p, const float* tri, Best& b) {
+    float t, u, v;
+    if (!tri_test(p, tri, tri + 4, tri + 8, b.t, &t, &u, &v)) return;
+    uint32_t prim = w_of(tri[3]);
+    if (t < b.t || prim < b.prim) {
+        b.t = t; b.u = u; b.v = v; b.prim = prim;
+    }
+}
+
+void trace_one(const uint32_t* nodes, const float* tris, uint32_t root, const float* ray, int any, float* hit,
+               uint32_t* st) {
+    RayPre p;
+    prepare(ray, p);
+    Best b{p.tmax, 0.0f, 0.0f, 0xFFFFFFFFu};
+    uint32_t visits = 0, tests = 0;
+    struct Entry { int32_t node; float tn; };
+    Entry stack[128];
+    int sp = 0;
+    int32_t node = (int32_t)root;
+    bool done = (root == 0xFFFFFFFFu);
+    while (!done) {
+        const uint32_t* w = nodes + 16ull * (uint32_t)node;
+        const float* f = reinterpret_cast<const float*>(w);
+        ++visits;
+        float tn0, tn1;
+        bool h0 = slab(p, f[0], f[1], f[2], f[3], f[8], f[9], b.t, &tn0);
+        bool h1 = slab(p, f[4], f[5], f[6], f[7], f[10], f[11], b.t, &tn1);
+        int32_t c[2] = {(int32_t)w[12], (int32_t)w[13]};
+        float tn[2] = {tn0, tn1};
+        bool h[2] = {h0, h1};
+        int first = (h0 && h1 && tn1 < tn0) ? 1 : 0;
+        int32_t next = -1;
+        bool have_next = false;
+        for (int s = 0; s < 2 && !done; ++s) {
+            int k = s == 0 ? first : 1 - first;
+            if (!h[k]) continue;
+            if (c[k] < 0) {
+                const float* tri = tris + 12ull * (uint32_t)(~c[k]);
+                ++tests;
+                if (any) {
+                    float t, u, v;
+                    if (tri_test(p, tri, tri + 4, tri + 8, b.t, &t, &u, &v)) {
+                        b.t = t; b.u = u; b.v = v; b.prim = w_of(tri[3]);
+                        done = true;
+                    }
+                } else {
+                    consider(p, tri, b);
+                }
+            } else if (!have_next) {
+                next = c[k];
+                have_next = true;
+            } else {
+                stack[sp].node = c[k];
+                stack[sp].tn = tn[k];
+                ++sp;
+            }
+        }
+        if (done) break;
+        if (!have_next) {
+            for (;;) {
+                if (sp == 0) { done = true; break; }
+                --sp;
+                if (any || stack[sp].tn <= b.t) { next = stack[sp].node; have_next = true; break; }
+            }
+        }
+        node = next;
+    }
+    if (b.prim == 0xFFFFFFFFu) {
+        hit[0] = p.tmax;  // t of a miss is left at tMax; prim -1; u = v = 0
+        uint32_t m = 0xFFFFFFFFu;
+        std::memcpy(hit + 1, &m, 4);
+        hit[2] = 0.0f; hit[3] = 0.0f;
+    } else {
+        hit[0] = b.t;
+        std::memcpy(hit + 1, &b.prim, 4);
+        hit[2] = b.u; hit[3] = b.v;
+    }
+    if (st) { st[0] = visits; st[1] = tests; }
+}
+
+// ---------------------------------------------------------------------------
+// Reference traversal (pathtracer_kernel.h)
+// ---------------------------------------------------------------------------
+struct V3 { float x, y, z; };
+inline V3 sub(V3 a, V3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline V3 cross(V3 a, V3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+inline float dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+
+// triangle_intersect (:119-152): float cross/dot, double determinant chain,
+// inclusive edges and inclusive [tMin, tMax]
+inline bool ref_tri(const float* tv, V3 o, V3 D, float tmin, float tmax, float* th, float* uh, float* vh) {
+    V3 p0{tv[0], tv[1], tv[2]}, p1{tv[3], tv[4], tv[5]}, p2{tv[6], tv[7], tv[8]};
+    V3 E1 = sub(p1, p0), E2 = sub(p2, p0);
+    V3 P = cross(D, E2);
+    double det = dot(P, E1);
+    if (det == 0) return false;
+    double invDet = 1.0 / det;
+    V3 T = sub(o, p0);
+    double u = dot(P, T) * invDet;
+    if (u < 0.0 || u > 1.0) return false;
+    V3 Q = cross(T, E1);
+    double v = dot(Q, D) * invDet;
+    if (v < 0.0 || u + v > 1.0) return false;
+    double t = dot(Q, E2) * invDet;
+    if (t < tmin || t > tmax) return false;
+    *th = (float)t; *uh = (float)u; *vh = (float)v;
+    return true;
+}
+
+// aabb_intersect (:154-173); device min/max on floats are fminf/fmaxf
+inline bool ref_box(const float* lo, const float* hi, V3 o, V3 inv, const int neg[3], float rtmin, float rtmax) {
+    const float* sel[2] = {lo, hi};
+    float tMin = (sel[neg[0]][0] - o.x) * inv.x;
+    float tMax = (sel[1 - neg[0]][0] - o.x) * inv.x;
+    float tyMin = (sel[neg[1]][1] - o.y) * inv.y;
+    float tyMax = (sel[1 - neg[1]][1] - o.y) * inv.y;
+    if (tMin > tyMax || tyMin > tMax) return false;
+    tMin = std::fmax(tMin, tyMin);
+    tMax = std::fmin(tMax, tyMax);
+    float tzMin = (sel[neg[2]][2] - o.z) * inv.z;
+    float tzMax = (sel[1 - neg[2]][2] - o.z) * inv.z;
+    if (tMin > tzMax || tzMin > tMax) return false;
+    tMin = std::fmax(tMin, tzMin);
+    tMax = std::fmin(tMax, tzMax);
+    return (tMin < rtmax) && (tMax > rtmin);
+}
+
+void trace_ref_one(const uint32_t* nodes, const float* verts, const float* ray, int any, float* hit, uint32_t* st) {
+    V3 o{ray[0], ray[1], ray[2]}, d{ray[3], ray[4], ray[5]};
+    float tmin = ray[6], tmax = ray[7];
+    V3 inv{1 / d.x, 1 / d.y, 1 / d.z};
+    int neg[3] = {inv.x < 0, inv.y < 0, inv.z < 0};
+    float ht = 0, hu = 0, hv = 0;
+    int32_t hid = -1;
+    int cur = 0, sp = 0;
+    int stack[64];
+    uint32_t visits = 0, tests = 0;
+    for (;;) {
+        const uint32_t* w = nodes + 8ull * cur;
+        const float* f = reinterpret_cast<const float*>(w);
+        ++visits;
+        if (ref_box(f, f + 3, o, inv, neg, tmin, tmax)) {
+            if (w[7]) {
+                ++tests;
+                float t, u, v;
+                if (ref_tri(verts + 9ull * w[6], o, d, tmin, tmax, &t, &u, &v)) {
+                    ht = t; hu = u; hv = v;
+                    tmax = t;
+                    hid = (int32_t)w[6];
+                    if (any) break;
+                }
+                if (sp == 0) break;
+                cur = stack[--sp];
+            } else {
+                if (sp >= 64) break;  // the reference's stack holds 64 entries
+                stack[sp++] = cur + 1;
+                cur = (int)w[6];
+            }
+        } else {
+            if (sp == 0) break;
+            cur = stack[--sp];
+        }
+    }
+    // the reference leaves t/u/v unset on a miss; the oracle reports zeros
+    hit[0] = hid < 0 ? 0.0f : ht;
+    std::memcpy(hit + 1, &hid, 4);
+    hit[2] = hid < 0 ? 0.0f : hu;
+    hit[3] = hid < 0 ? 0.0f : hv;
+    if (st) { st[0] = visits; st[1] = tests; }
+}
+
+// ---------------------------------------------------------------------------
+// FP64 oracle
+// ---------------------------------------------------------------------------
+struct D3 { double x, y, z; };
+inline D3 dsub(D3 a, D3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline D3 dcross(D3 a, D3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+inline double ddot(D3 a, D3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+
+// Double-precision Moller-Trumbore with a barycentric tolerance; returns t and
+// the smallest barycentric coordinate.
+inline bool tri64(const float* tv, D3 o, D3 d, double tol, double* t, double* minbary) {
+    D3 p0{tv[0], tv[1], tv[2]}, p1{tv[3], tv[4], tv[5]}, p2{tv[6], tv[7], tv[8]};
+    D3 e1 = dsub(p1, p0), e2 = dsub(p2, p0);
+    D3 P = dcross(d, e2);
+    double det = ddot(P, e1);
+    if (det == 0) return false;
+    double inv = 1.0 / det;
+    D3 T = dsub(o, p0);
+    double u = ddot(P, T) * inv;
+    D3 Q = dcross(T, e1);
+    double v = ddot(Q, d) * inv;
+    double w = 1.0 - u - v;
+    double mb = std::fmin(u, std::fmin(v, w));
+    if (mb < -tol) return false;
+    *t = ddot(Q, e2) * inv;
+    *minbary = mb;
+    return true;
+}
+
+}  // namespace
+
+extern "C" void or_trace(const uint32_t* nodes, const float* tris, uint32_t root, const float* rays, uint64_t nrays,
+                         int any_hit, float* hits, uint32_t* stats, int threads) {
+    parallel_rays(nrays, threads, [&](uint64_t b, uint64_t e) {
+        for (uint64_t i = b; i < e; ++i)
+            trace_one(nodes, tris, root, rays + 8 * i, any_hit, hits + 4 * i, stats ? stats + 2 * i : nullptr);
+    });
+}
+
+extern "C" void or_trace_brute(const float* verts, uint32_t n, const float* rays, uint64_t nrays, int any_hit,
+                               float* hits, int threads) {
+    parallel_rays(nrays, threads, [&](uint64_t b, uint64_t e) {
+        float tri[12];
+        for (uint64_t i = b; i < e; ++i) {
+            RayPre p;
+            prepare(rays + 8 * i, p);
+            Best best{p.tmax, 0.0f, 0.0f, 0xFFFFFFFFu};
+            for (uint32_t j = 0; j < n; ++j) {
+                const float* v = verts + 9ull * j;
+                tri[0] = v[0]; tri[1] = v[1]; tri[2] = v[2]; std::memcpy(tri + 3, &j, 4);
+                tri[4] = v[3]; tri[5] = v[4]; tri[6] = v[5];
+                tri[8] = v[6]; tri[9] = v[7]; tri[10] = v[8];
+                if (any_hit) {
+                    float t, u, vv;
+                    if (tri_test(p, tri, tri + 4, tri + 8, p.tmax, &t, &u, &vv)) {
+                        best = {t, u, vv, j};
+                        break;
+                    }
+                } else {
+                    consider(p, tri, best);
+                }
+            }
+            float* h = hits + 4 * i;
+            if (best.prim == 0xFFFFFFFFu) {
+                h[0] = p.tmax; uint32_t m = 0xFFFFFFFFu; std::memcpy(h + 1, &m, 4); h[2] = h[3] = 0.0f;
+            } else {
+                h[0] = best.t; std::memcpy(h + 1, &best.prim, 4); h[2] = best.u; h[3] = best.v;
+            }
+        }
+    });
+}
+
+extern "C" void or_trace_ref(const uint32_t* ref_nodes, const float* verts, uint32_t n, const float* rays,
+                             uint64_t nrays, int any_hit, float* hits, uint32_t* stats, int threads) {
+    if (n == 0) {
+        for (uint64_t i = 0; i < nrays; ++i) {
+            int32_t m = -1;
+            hits[4 * i] = 0.0f; std::memcpy(hits + 4 * i + 1, &m, 4); hits[4 * i + 2] = hits[4 * i + 3] = 0.0f;
+            if (stats) stats[2 * i] = stats[2 * i + 1] = 0;
+        }
+        return;
+    }
+    parallel_rays(nrays, threads, [&](uint64_t b, uint64_t e) {
+        for (uint64_t i = b; i < e; ++i)
+            trace_ref_one(ref_nodes, verts, rays + 8 * i, any_hit, hits + 4 * i, stats ? stats + 2 * i : nullptr);
+    });
+}
+
+extern "C" void or_fp64_check(const uint32_t* ref_nodes, const float* verts, uint32_t n, const float* rays,
+                              uint64_t nrays, const int32_t* prim, double* t64, uint8_t* ambiguous, double rel_gap,
+                              double bary_margin, int threads) {
+    parallel_rays(nrays, threads, [&](uint64_t b, uint64_t e) {
+        std::vector<int> stack;
+        stack.reserve(128);
+        for (uint64_t i = b; i < e; ++i) {
+            const float* r = rays + 8 * i;
+            D3 o{r[0], r[1], r[2]}, d{r[3], r[4], r[5]};
+            double tmin = r[6], tmax = r[7];
+            // distance to the reported triangle
+            double tp = std::numeric_limits<double>::quiet_NaN();
+            if (prim[i] >= 0 && (uint32_t)prim[i] < n) {
+                double t, mb;
+                if (tri64(verts + 9ull * prim[i], o, d, 1e30, &t, &mb)) tp = t;
+            }
+            t64[i] = tp;
+            // all candidates within tolerance: closest and runner-up distances
+            double best = std::numeric_limits<double>::infinity(), second = best, best_mb = 1.0;
+            if (n > 0) {
+                stack.clear();
+                stack.push_back(0);
+                while (!stack.empty()) {
+                    int cur = stack.back();
+                    stack.pop_back();
+                    const uint32_t* w = ref_nodes + 8ull * cur;
+                    const float* f = reinterpret_cast<const float*>(w);
+                    // padded FP64 slab test (conservative)
+                    double t0 = -std::numeric_limits<double>::infinity(), t1 = -t0;
+                    const double pad = 1e-6;
+                    double dd[3] = {d.x, d.y, d.z}, oo[3] = {o.x, o.y, o.z};
+                    bool in = true;
+                    for (int k = 0; k < 3 && in; ++k) {
+                        double lo = f[k], hi = f[3 + k];
+                        double ext = pad * (1.0 + std::fabs(lo) + std::fabs(hi));
+                        lo -= ext; hi += ext;
+                        if (dd[k] == 0.0) {
+                            if (oo[k] < lo || oo[k] > hi) in = false;
+                            continue;
+                        }
+                        double a = (lo - oo[k]) / dd[k], c = (hi - oo[k]) / dd[k];
+                        if (a > c) std::swap(a, c);
+                        t0 = std::fmax(t0, a);
+                        t1 = std::fmin(t1, c);
+                    }
+                    if (!in || t0 > t1 || t1 < tmin * (1 - 1e-6) - 1e-9 || t0 > tmax * (1 + 1e-6) + 1e-9) continue;
+                    if (t0 > second * (1 + 1e-6) + 1e-9) continue;
+                    if (w[7]) {
+                        double t, mb;
+                        if (tri64(verts + 9ull * w[6], o, d, bary_margin, &t, &mb)) {
+                            if (t < tmin * (1 - 1e-7) - 1e-12 || t > tmax * (1 + 1e-7) + 1e-12) continue;
+                            if (t < best) { second = best; best = t; best_mb = mb; }
+                            else if (t < second) second = t;
+                        }
+                    } else {
+                        stack.push_back(cur + 1);
+                        stack.push_back((int)w[6]);
+                    }
+                }
+            }
+            bool amb = false;
+            if (best < std::numeric_limits<double>::infinity()) {
+                if (best_mb < bary_margin) amb = true;
+                if (second - best <= rel_gap * std::fmax(std::fabs(best), 1e-30)) amb = true;
+                if (std::fabs(best - tmin) <= rel_gap * std::fmax(std::fabs(best), 1e-30)) amb = true;
+                if (std::fabs(best - tmax) <= rel_gap * std::fmax(std::fabs(best), 1e-30)) amb = true;
+            }
+            ambiguous[i] = amb ? 1 : 0;
+        }
+    });
+}
