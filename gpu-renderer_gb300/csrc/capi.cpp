@@ -27,6 +27,22 @@ void DevBuf::release() {
     bytes = 0;
 }
 
+void context_free(gr_ctx* ctx) {
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    ctx->counter.release();
+    ctx->stage_in.release();
+    ctx->stage_out.release();
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+void ctx_retain(gr_ctx* ctx) { ++ctx->refs; }
+
+void ctx_release(gr_ctx* ctx) {
+    if (--ctx->refs == 0 && ctx->destroyed) context_free(ctx);
+}
+
 }  // namespace gr
 
 namespace {
@@ -119,14 +135,9 @@ gr_status gr_context_create(int device, gr_ctx** out) {
 }
 
 gr_status gr_context_destroy(gr_ctx* ctx) {
-    if (!ctx) return GR_ERR_INVALID;
-    cudaSetDevice(ctx->device);
-    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-    ctx->counter.release();
-    ctx->stage_in.release();
-    ctx->stage_out.release();
-    if (ctx->stream) cudaStreamDestroy(ctx->stream);
-    delete ctx;
+    if (!ctx || ctx->destroyed) return GR_ERR_INVALID;
+    ctx->destroyed = true;
+    if (ctx->refs == 0) gr::context_free(ctx);
     return GR_OK;
 }
 
@@ -137,15 +148,18 @@ gr_status gr_bvh_create(gr_ctx* ctx, gr_bvh** out) {
     gr_bvh* b = new (std::nothrow) gr_bvh();
     if (!b) return fail(ctx, GR_ERR_OOM_BUDGET, "host allocation failed");
     b->ctx = ctx;
+    gr::ctx_retain(ctx);
     *out = b;
     return GR_OK;
 }
 
 gr_status gr_bvh_destroy(gr_bvh* bvh) {
     if (!bvh) return GR_ERR_INVALID;
-    cudaSetDevice(bvh->ctx->device);
-    cudaStreamSynchronize(bvh->ctx->stream);
+    gr_ctx* ctx = bvh->ctx;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
     delete bvh;
+    gr::ctx_release(ctx);
     return GR_OK;
 }
 

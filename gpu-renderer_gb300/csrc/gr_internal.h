@@ -94,7 +94,11 @@ cudaError_t trace_launch(const BvhDevice& bvh, const gr_ray* d_rays, uint64_t n,
 }  // namespace gr
 
 // Context and object definitions (host side).
+// A context is freed when it has been destroyed and no object created from it
+// is alive any more, so objects may outlive a gr_context_destroy call.
 struct gr_ctx {
+    int refs = 0;
+    bool destroyed = false;
     int device = 0;
     int num_sms = 0;
     cudaStream_t stream = nullptr;
@@ -102,6 +106,13 @@ struct gr_ctx {
     gr::DevBuf counter;  // traversal work counter (offset 0) + error word (offset 64)
     gr::DevBuf stage_in, stage_out;  // device staging for the host-memory entry points
 };
+
+namespace gr {
+// reference counting of contexts by the objects created from them
+void ctx_retain(gr_ctx* ctx);
+void ctx_release(gr_ctx* ctx);
+void context_free(gr_ctx* ctx);
+}  // namespace gr
 
 struct gr_bvh {
     gr_ctx* ctx = nullptr;

@@ -428,6 +428,7 @@ __global__ void __launch_bounds__(kBlock) k_link(const uint32_t* __restrict__ kg
         const int32_t right = (g & 0x40000000u) ? run_root(run_start, gamma + 1) : (int32_t)gap_of[gamma + 1];
         nodes[G].q3.x = left;
         nodes[G].q3.y = right;
+        nodes[G].q3.w = 0;
         if (left >= 0) nodes[left].q3.z = (int32_t)G; else parent_leaf[~left] = G;
         if (right >= 0) nodes[right].q3.z = (int32_t)G; else parent_leaf[~right] = G;
         if (k == 0) {
@@ -463,6 +464,7 @@ __global__ void __launch_bounds__(kBlock) k_run_nodes(const uint32_t* __restrict
         const int32_t right = (G + 1 == b) ? ~(int32_t)b : (int32_t)(G + 1 + ((b - G) >> 1) - 1);
         nodes[G].q3.x = left;
         nodes[G].q3.y = right;
+        nodes[G].q3.w = 0;
         if (left >= 0) nodes[left].q3.z = (int32_t)G; else parent_leaf[~left] = G;
         if (right >= 0) nodes[right].q3.z = (int32_t)G; else parent_leaf[~right] = G;
     }
