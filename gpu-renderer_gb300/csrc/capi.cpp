@@ -258,3 +258,24 @@ gr_status gr_trace_host(gr_bvh* bvh, const gr_ray* h_rays, uint64_t n, gr_hit* h
 }
 
 }  // extern "C"
+
+extern "C" gr_status gr_bvh_build_noalloc(gr_ctx* ctx, const float* d_verts, uint32_t n, void* d_nodes, void* d_tris,
+                                          uint32_t* d_sorted_prim, uint32_t* d_sorted_code, void* d_header,
+                                          void* stream) {
+    if (!ctx) return GR_ERR_INVALID;
+    const uint32_t limit = gr::lbvh_static_max_triangles();
+    if (n > limit) {
+        ctx->last_error = "gr_bvh_build_noalloc: " + std::to_string(n) +
+                          " triangles exceed the fixed scratch limit of " + std::to_string(limit) +
+                          "; use gr_bvh_build";
+        return GR_ERR_INVALID;
+    }
+    if (!d_header || (n > 0 && (!d_verts || !d_nodes || !d_tris || !d_sorted_prim || !d_sorted_code))) {
+        ctx->last_error = "gr_bvh_build_noalloc: null pointer";
+        return GR_ERR_INVALID;
+    }
+    GR_CUDA(ctx, cudaSetDevice(ctx->device));
+    GR_CUDA(ctx, gr::lbvh_build_static(d_verts, n, (gr::Node*)d_nodes, (gr::Tri*)d_tris, d_sorted_code, d_sorted_prim,
+                                       (gr::BvhMeta*)d_header, ctx->device, ctx->num_sms, as_stream(stream)));
+    return GR_OK;
+}

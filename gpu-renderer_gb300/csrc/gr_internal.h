@@ -86,6 +86,10 @@ struct BvhMeta {
 // lbvh.cu
 cudaError_t lbvh_build(BvhBuffers& b, const float* d_verts, uint32_t n, int num_sms, cudaStream_t s);
 cudaError_t lbvh_export_ref(const BvhBuffers& b, uint32_t n, uint32_t* d_ref_nodes, cudaStream_t s);
+// build whose scratch is a file-scope device array (no allocation); see lbvh.cu
+uint32_t lbvh_static_max_triangles();
+cudaError_t lbvh_build_static(const float* d_verts, uint32_t n, Node* nodes, Tri* tris, uint32_t* code,
+                              uint32_t* prim, BvhMeta* meta, int device, int num_sms, cudaStream_t s);
 
 // trace.cu
 cudaError_t trace_launch(const BvhDevice& bvh, const gr_ray* d_rays, uint64_t n, gr_hit* d_hits, int any_hit,

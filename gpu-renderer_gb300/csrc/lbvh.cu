@@ -7,6 +7,7 @@
 // round-to-nearest intrinsic so nvcc cannot contract it into an FMA: the codes
 // must equal the reference host computation (bvh.h:193-204) bit for bit.
 #include <algorithm>
+#include <mutex>
 
 #include "gr_internal.h"
 
@@ -714,6 +715,104 @@ cudaError_t lbvh_export_ref(const BvhBuffers& b, uint32_t n, uint32_t* d_ref_nod
     const uint64_t total = 2ull * n - 1;
     const int grid = (int)std::min<uint64_t>((total + kBlock - 1) / kBlock, 4096);
     k_export_ref<<<grid, kBlock, 0, st>>>((const Node*)b.nodes.p, (const Tri*)b.tris.p, s.parent_leaf, n, d_ref_nodes);
+    return cudaGetLastError();
+}
+
+}  // namespace gr
+
+// ---- build without allocation ------------------------------------------------------
+// Some callers cannot call cudaMalloc: code that runs while a stream is being
+// captured into a CUDA graph, plug-ins whose host application owns every byte
+// of device memory, and latency-critical loops where cudaMalloc / cudaFree
+// would synchronise the device. For them the build's scratch (sort buffers,
+// run arrays, parent links, refit counters, look-back words) lives in one
+// file-scope device array, sized for kStaticMaxTriangles triangles; the caller
+// passes the input soup and every output buffer.
+//
+// Every call shares this one array and it keeps the last call's contents: the
+// part that must start at zero is cleared at the start of each call, and two
+// calls that overlap on the GPU (different streams, no ordering between them)
+// race on it.
+
+namespace gr {
+namespace {
+
+constexpr uint32_t kStaticMaxTriangles = 1u << 17;  // 131,072 triangles
+
+// Upper bound of scratch_layout(kStaticMaxTriangles): nine per-triangle word
+// arrays (+1 word), the centroid partials, histograms, look-back words, tile
+// counters and the error word, each rounded up to 256 bytes.
+constexpr size_t kStaticScratchBytes =
+    9 * (((size_t)kStaticMaxTriangles * 4 + 4 + 255) & ~size_t(255)) + ((6 * 1024 * 4 + 255) & ~size_t(255)) +
+    2 * 4096 + 4 * ((kStaticMaxTriangles + 4095) / 4096) * 256 * 4 + ((kStaticMaxTriangles + 4095) / 4096) * 4 +
+    16 * 256;
+
+static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_static_mu;
+void* g_static_ptr[kMaxDevices] = {};
+
+// Device address of g_static_scratch on the current device. The array's name
+// in host code is only a host-side stand-in, so the address is looked up once
+// per device (with that device current) and cached.
+cudaError_t static_scratch(int device, void** out) {
+    if (device < 0 || device >= kMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_static_mu);
+    if (!g_static_ptr[device]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+        if (e != cudaSuccess) return e;
+        g_static_ptr[device] = p;
+    }
+    *out = g_static_ptr[device];
+    return cudaSuccess;
+}
+
+}  // namespace
+
+uint32_t lbvh_static_max_triangles() { return kStaticMaxTriangles; }
+
+cudaError_t lbvh_build_static(const float* d_verts, uint32_t n, Node* nodes, Tri* tris, uint32_t* code,
+                              uint32_t* prim, BvhMeta* meta, int device, int num_sms, cudaStream_t st) {
+    cudaError_t e;
+    void* base = nullptr;
+    if ((e = static_scratch(device, &base)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(meta, 0, sizeof(BvhMeta), st)) != cudaSuccess) return e;
+    if (n == 0) return cudaMemsetAsync(&meta->root, 0xFF, 4, st);
+    Scratch s;
+    if (scratch_layout(n, nullptr, &s) > kStaticScratchBytes) return cudaErrorInvalidValue;
+    scratch_layout(n, (char*)base, &s);
+    if ((e = cudaMemsetAsync(s.zero_base, 0, s.zero_bytes, st)) != cudaSuccess) return e;
+
+    const int grid = (int)std::min<uint64_t>(((uint64_t)n + kBlock - 1) / kBlock, (uint64_t)num_sms * 8);
+    const int parts = std::min(grid, kPartials);
+    k_centroid_partials<<<parts, kBlock, 0, st>>>(d_verts, n, s.partial);
+    k_centroid_final<<<1, 32, 0, st>>>(s.partial, parts, meta);
+    k_morton_hist<<<std::min(grid, num_sms * 2), kBlock, 0, st>>>(d_verts, n, meta, code, prim, s.hist);
+    k_hist_scan<<<4, 256, 0, st>>>(s.hist, s.offs);
+    if ((e = cudaFuncSetAttribute(k_onesweep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kOsSmem)) !=
+        cudaSuccess)
+        return e;
+    const uint32_t os_tiles = (n + kOsTile - 1) / kOsTile;
+    uint32_t* kin = code;
+    uint32_t* vin = prim;
+    uint32_t* kout = s.keys_alt;
+    uint32_t* vout = s.vals_alt;
+    for (int pass = 0; pass < 4; ++pass) {
+        k_onesweep<<<os_tiles, kOsThreads, kOsSmem, st>>>(kin, vin, kout, vout, n, pass, s.offs,
+                                                          s.os_status + (size_t)pass * os_tiles * 256, s.tile_ctr, s.err);
+        std::swap(kin, kout);
+        std::swap(vin, vout);
+    }
+    const uint32_t run_tiles = (n + kRunTile - 1) / kRunTile;
+    k_runs<<<run_tiles, kRunThreads, 0, st>>>(code, n, s.ucode, s.run_start, s.uidx, s.run_status, s.tile_ctr + 4,
+                                              meta, s.err);
+    k_karras<<<grid, kBlock, 0, st>>>(s.ucode, s.run_start, meta, s.kgamma, s.gap_of);
+    k_link<<<grid, kBlock, 0, st>>>(s.kgamma, s.gap_of, s.run_start, meta, nodes, s.parent_leaf);
+    k_run_nodes<<<grid, kBlock, 0, st>>>(code, n, s.uidx, s.run_start, meta, nodes, s.parent_leaf, s.err);
+    k_refit<<<grid, kBlock, 0, st>>>(d_verts, n, prim, s.parent_leaf, nodes, tris, s.counters, s.err);
+    if ((e = cudaMemcpyAsync(&meta->err, s.err, 4, cudaMemcpyDeviceToDevice, st)) != cudaSuccess) return e;
     return cudaGetLastError();
 }
 

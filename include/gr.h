@@ -84,6 +84,28 @@ gr_status gr_bvh_build_host(gr_bvh* bvh, const float* h_verts, uint32_t n);
 /* Number of triangles the BVH was built over. */
 uint32_t gr_bvh_size(const gr_bvh* bvh);
 
+/* Build without any device allocation. This entry point has no counterpart in
+ * the reference. It is for callers that cannot call cudaMalloc: code running
+ * while a stream is captured into a CUDA graph, plug-ins whose host
+ * application owns all device memory, and latency-critical loops where
+ * cudaMalloc / cudaFree would synchronise the device.
+ *
+ * The caller passes the input soup and every output buffer (device memory):
+ *   d_nodes        64 bytes x max(n-1, 1)  traversal nodes (layout of gr_bvh_export's h_nodes)
+ *   d_tris         48 bytes x n            triangles in leaf order (gr_bvh_export's h_tris)
+ *   d_sorted_prim  4 bytes x n             triangle ids in Morton order
+ *   d_sorted_code  4 bytes x n             Morton codes in sorted order
+ *   d_header       64 bytes                uint32 root index at byte 0, device error bits at byte 8
+ * The build's scratch is one fixed device array inside the library, sized for
+ * at most 131,072 triangles (about 4.8 MB, held on every GPU that loads the
+ * library until the process exits); a larger n returns GR_ERR_INVALID. The
+ * first call on a device looks up that array's device address, so make the
+ * first call on each device before any stream capture. All calls share the
+ * array: it is cleared where it must start at zero, and calls that overlap on
+ * the GPU race on it. Stream-ordered; does not wait for the device. */
+gr_status gr_bvh_build_noalloc(gr_ctx* ctx, const float* d_verts, uint32_t n, void* d_nodes, void* d_tris,
+                               uint32_t* d_sorted_prim, uint32_t* d_sorted_code, void* d_header, void* stream);
+
 /* Copies the build to host buffers for parity checks (waits for the device):
  *   h_sorted_prim, h_sorted_code : n words — triangle ids and Morton codes in
  *                                  sorted order (the reference's MortonInfo)
