@@ -169,15 +169,16 @@ def run_gpu(args):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     dev = torch.device("cuda", local)
-    verts = scenes.triangle_soup(N_TRIS)
-    rays = scenes.incoherent_rays(N_RAYS)
+    n_tris, n_rays = args.tris, args.rays
+    verts = scenes.triangle_soup(n_tris)
+    rays = scenes.incoherent_rays(n_rays)
     ctx = gr.Context(local)
     bvh = gr.BVH(ctx)
     stream = torch.cuda.current_stream()
     sp = stream.cuda_stream
     d_verts = torch.from_numpy(verts).to(dev)
     d_rays = torch.from_numpy(rays).to(dev)
-    d_hits = torch.empty((N_RAYS, 4), dtype=torch.float32, device=dev)
+    d_hits = torch.empty((max(n_rays, N_RAYS), 4), dtype=torch.float32, device=dev)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
 
     # BVH build (timed separately, reported as an extra)
@@ -186,7 +187,7 @@ def run_gpu(args):
         l2_flush(flush)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        bvh.build_device(d_verts, N_TRIS, stream=sp)
+        bvh.build_device(d_verts, n_tris, stream=sp)
         e1.record(stream)
         torch.cuda.synchronize()
         if i >= 3:
@@ -196,7 +197,7 @@ def run_gpu(args):
         bvh.trace_device(buf_rays, n, buf_hits, any_hit=any_hit, stream=sp)
 
     for _ in range(max(args.warmup, 3)):
-        step(d_rays, d_hits, N_RAYS)
+        step(d_rays, d_hits, n_rays)
     torch.cuda.synchronize()
 
     clocks = ClockSampler(local)
@@ -209,7 +210,7 @@ def run_gpu(args):
         l2_flush(flush)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        step(d_rays, d_hits, N_RAYS)
+        step(d_rays, d_hits, n_rays)
         e1.record(stream)
         ev.append((e0, e1))
     torch.cuda.synchronize()
@@ -217,6 +218,14 @@ def run_gpu(args):
         torch.distributed.barrier()
     kernel_ms = [a.elapsed_time(b) for a, b in ev]
     total_s = sum(kernel_ms) / 1e3
+
+    if args.quick:
+        clocks.stop()
+        if rank == 0:
+            print(json.dumps({"quick": True, "tris": n_tris, "rays": n_rays,
+                              "kernel_ms_median": statistics.median(kernel_ms),
+                              "mrays_s": n_rays / (statistics.median(kernel_ms) / 1e3) / 1e6}), flush=True)
+        return
 
     # secondary queries on the same scene: coherent closest hit and shadow any-hit
     extras = {}
@@ -300,6 +309,10 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gr", choices=["gr", "reference"])
+    ap.add_argument("--tris", type=int, default=N_TRIS, help="triangle count (profiling cases)")
+    ap.add_argument("--rays", type=int, default=N_RAYS, help="ray count (profiling cases)")
+    ap.add_argument("--quick", action="store_true",
+                    help="time the main query only (no extras, e2e or CPU baseline); for profiling")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
