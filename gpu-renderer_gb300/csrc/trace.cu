@@ -102,79 +102,89 @@ __device__ __forceinline__ bool tri_test(const RayW& p, const float4 a, const fl
     return true;
 }
 
-template <bool ANY>
-__device__ __forceinline__ float4 trace_ray(const Node* __restrict__ nodes, const Tri* __restrict__ tris, uint32_t root,
-                                            const RayW& p, int2 (*s_stack)[kTraceThreads], uint32_t* err) {
-    int2 l_stack[kStackMax - kShortStack];
-    float best_t = p.tmax, bu = 0.0f, bv = 0.0f;
-    uint32_t best_prim = 0xFFFFFFFFu;
-    int sp = 0;
-    int32_t node = (int32_t)root;
-    bool done = root == kNoNode;
-    const int tid = threadIdx.x;
-    while (!done) {
-        const float4* q = reinterpret_cast<const float4*>(nodes + node);
-        const float4 q0 = __ldg(q), q1 = __ldg(q + 1), q2 = __ldg(q + 2);
-        const int4 q3 = __ldg(reinterpret_cast<const int4*>(q + 3));
-        float tn0, tn1;
-        const bool h0 = slab(p, q0.x, q0.y, q0.z, q0.w, q2.x, q2.y, best_t, tn0);
-        const bool h1 = slab(p, q1.x, q1.y, q1.z, q1.w, q2.z, q2.w, best_t, tn1);
-        const bool swap = h0 && h1 && tn1 < tn0;
-        const int32_t cn = swap ? q3.y : q3.x, cf = swap ? q3.x : q3.y;
-        const float tnf = swap ? tn0 : tn1;
-        const bool hn = swap ? h1 : h0, hf = swap ? h0 : h1;
-        int32_t next = -1;
-        bool have = false;
-#pragma unroll
-        for (int s = 0; s < 2; ++s) {
-            const bool h = s == 0 ? hn : hf;
-            const int32_t c = s == 0 ? cn : cf;
-            if (!h) continue;
-            if (c < 0) {
-                const Tri* tr = tris + (uint32_t)(~c);
-                const float4 a = __ldg(&tr->a), b = __ldg(&tr->b), cc = __ldg(&tr->c);
-                float t, u, v;
-                if (tri_test(p, a, b, cc, best_t, t, u, v)) {
-                    const uint32_t prim = __float_as_uint(a.w);
-                    if (ANY) {
-                        best_t = t; bu = u; bv = v; best_prim = prim;
-                        done = true;
-                        break;
-                    }
-                    if (t < best_t || prim < best_prim) {
-                        best_t = t; bu = u; bv = v; best_prim = prim;
-                    }
-                }
-            } else if (!have) {
-                next = c;
-                have = true;
-            } else {
-                if (sp < kShortStack) {
-                    s_stack[sp][tid] = make_int2(c, __float_as_int(tnf));
-                } else if (sp < kStackMax) {
-                    l_stack[sp - kShortStack] = make_int2(c, __float_as_int(tnf));
-                } else {
-                    atomicOr(err, ERR_STACK);
-                    done = true;
-                    break;
-                }
-                ++sp;
-            }
-        }
-        if (done) break;
-        if (!have) {
-            for (;;) {
-                if (sp == 0) { done = true; break; }
-                --sp;
-                const int2 e = sp < kShortStack ? s_stack[sp][tid] : l_stack[sp - kShortStack];
-                if (ANY || __int_as_float(e.y) <= best_t) { next = e.x; break; }
-            }
-        }
-        node = next;
-    }
-    if (best_prim == 0xFFFFFFFFu) return make_float4(p.tmax, __int_as_float(-1), 0.0f, 0.0f);
-    return make_float4(best_t, __uint_as_float(best_prim), bu, bv);
+__device__ __forceinline__ uint32_t lanemask_lt() {
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
 }
+
+// Per-lane traversal state. A lane owns one ray at a time; when its ray
+// finishes the lane goes idle and is refilled with a new ray once enough lanes
+// of the warp are idle, so long-tailed rays do not hold a whole warp.
+struct Lane {
+    RayW p;
+    float best_t, bu, bv;
+    uint32_t best_prim;
+    uint64_t ray;
+    int32_t node;
+    int sp;
+};
+
+// Processes one node for the lane; returns true when the ray is finished.
+template <bool ANY>
+__device__ __forceinline__ bool trace_step(const Node* __restrict__ nodes, const Tri* __restrict__ tris, Lane& L,
+                                           int2 (*s_stack)[kTraceThreads], int2* l_stack, uint32_t* err) {
+    const int tid = threadIdx.x;
+    const float4* q = reinterpret_cast<const float4*>(nodes + L.node);
+    const float4 q0 = __ldg(q), q1 = __ldg(q + 1), q2 = __ldg(q + 2);
+    const int4 q3 = __ldg(reinterpret_cast<const int4*>(q + 3));
+    float tn0, tn1;
+    const bool h0 = slab(L.p, q0.x, q0.y, q0.z, q0.w, q2.x, q2.y, L.best_t, tn0);
+    const bool h1 = slab(L.p, q1.x, q1.y, q1.z, q1.w, q2.z, q2.w, L.best_t, tn1);
+    const bool swap = h0 && h1 && tn1 < tn0;
+    const int32_t cn = swap ? q3.y : q3.x, cf = swap ? q3.x : q3.y;
+    const float tnf = swap ? tn0 : tn1;
+    const bool hn = swap ? h1 : h0, hf = swap ? h0 : h1;
+    int32_t next = -1;
+    bool have = false;
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+        const bool h = s == 0 ? hn : hf;
+        const int32_t c = s == 0 ? cn : cf;
+        if (!h) continue;
+        if (c < 0) {
+            const Tri* tr = tris + (uint32_t)(~c);
+            const float4 a = __ldg(&tr->a), b = __ldg(&tr->b), cc = __ldg(&tr->c);
+            float t, u, v;
+            if (tri_test(L.p, a, b, cc, L.best_t, t, u, v)) {
+                const uint32_t prim = __float_as_uint(a.w);
+                if (ANY) {
+                    L.best_t = t; L.bu = u; L.bv = v; L.best_prim = prim;
+                    return true;
+                }
+                if (t < L.best_t || prim < L.best_prim) {
+                    L.best_t = t; L.bu = u; L.bv = v; L.best_prim = prim;
+                }
+            }
+        } else if (!have) {
+            next = c;
+            have = true;
+        } else {
+            if (L.sp < kShortStack) {
+                s_stack[L.sp][tid] = make_int2(c, __float_as_int(tnf));
+            } else if (L.sp < kStackMax) {
+                l_stack[L.sp - kShortStack] = make_int2(c, __float_as_int(tnf));
+            } else {
+                atomicOr(err, ERR_STACK);
+                return true;
+            }
+            ++L.sp;
+        }
+    }
+    if (!have) {
+        for (;;) {
+            if (L.sp == 0) return true;
+            --L.sp;
+            const int2 e = L.sp < kShortStack ? s_stack[L.sp][tid] : l_stack[L.sp - kShortStack];
+            if (ANY || __int_as_float(e.y) <= L.best_t) { next = e.x; break; }
+        }
+    }
+    L.node = next;
+    return false;
+}
+
+// Refill when at least this many lanes of a warp are idle.
+constexpr int kRefillLanes = 8;
 
 template <bool ANY>
 __global__ void __launch_bounds__(kTraceThreads) k_trace(const Node* __restrict__ nodes, const Tri* __restrict__ tris,
@@ -182,18 +192,49 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace(const Node* __restrict_
                                                          float4* __restrict__ hits, unsigned long long* counter,
                                                          uint32_t* err) {
     __shared__ int2 s_stack[kShortStack][kTraceThreads];
+    int2 l_stack[kStackMax - kShortStack];
     const int lane = threadIdx.x & 31;
+    const uint32_t ltmask = lanemask_lt();
     const uint32_t root = meta->root;
+    Lane L;
+    bool active = false;
+    bool exhausted = false;
     for (;;) {
-        unsigned long long base = 0;
-        if (lane == 0) base = atomicAdd(counter, 32ull);
-        base = __shfl_sync(0xFFFFFFFFu, base, 0);
-        if (base >= n) break;
-        const uint64_t i = base + lane;
-        if (i < n) {
-            const float4 r0 = __ldg(rays + 2 * i), r1 = __ldg(rays + 2 * i + 1);
-            const RayW p = prepare(r0, r1);
-            hits[i] = trace_ray<ANY>(nodes, tris, root, p, s_stack, err);
+        const uint32_t idle = __ballot_sync(0xFFFFFFFFu, !active);
+        const int nidle = __popc(idle);
+        if (!exhausted && (nidle >= kRefillLanes || nidle == 32)) {
+            unsigned long long base = 0;
+            if (lane == 0) base = atomicAdd(counter, (unsigned long long)nidle);
+            base = __shfl_sync(0xFFFFFFFFu, base, 0);
+            if (base + nidle >= n) exhausted = true;
+            if (!active) {
+                const uint64_t i = base + __popc(idle & ltmask);
+                if (i < n) {
+                    const float4 r0 = __ldg(rays + 2 * i), r1 = __ldg(rays + 2 * i + 1);
+                    L.p = prepare(r0, r1);
+                    L.best_t = L.p.tmax;
+                    L.bu = 0.0f;
+                    L.bv = 0.0f;
+                    L.best_prim = 0xFFFFFFFFu;
+                    L.ray = i;
+                    L.node = (int32_t)root;
+                    L.sp = 0;
+                    active = true;
+                    if (root == kNoNode) {
+                        hits[i] = make_float4(L.p.tmax, __int_as_float(-1), 0.0f, 0.0f);
+                        active = false;
+                    }
+                }
+            }
+        }
+        if (__ballot_sync(0xFFFFFFFFu, active) == 0) {
+            if (exhausted) break;
+            continue;
+        }
+        if (active && trace_step<ANY>(nodes, tris, L, s_stack, l_stack, err)) {
+            hits[L.ray] = L.best_prim == 0xFFFFFFFFu ? make_float4(L.p.tmax, __int_as_float(-1), 0.0f, 0.0f)
+                                                     : make_float4(L.best_t, __uint_as_float(L.best_prim), L.bu, L.bv);
+            active = false;
         }
     }
 }
