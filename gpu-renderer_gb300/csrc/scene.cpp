@@ -1,0 +1,319 @@
+// Scene records and the render entry points of the C ABI (include/gr.h).
+//
+// gr_scene_create replaces Scene::Scene + Scene::createDeviceData
+// (slongle/GPU-Renderer src/renderer/scene.cpp:4-51): meshes are flattened to
+// one triangle list, emissive triangles become the light list, and the LBVH is
+// built on the GPU instead of on the host. The reference stores a 408-byte
+// Triangle record per triangle (embedding its mesh view and material); here
+// the device holds the flat vertex soup, optional per-corner normals, and a
+// 4-byte material index per triangle.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "render.h"
+
+namespace {
+
+gr_status fail(gr_ctx* ctx, gr_status st, const std::string& what) {
+    if (ctx) ctx->last_error = what;
+    return st;
+}
+
+gr_status cuda_fail(gr_ctx* ctx, cudaError_t e, const char* where) {
+    cudaGetLastError();
+    if (ctx) ctx->last_error = std::string(where) + ": " + cudaGetErrorString(e);
+    return e == cudaErrorMemoryAllocation ? GR_ERR_OOM_BUDGET : GR_ERR_CUDA;
+}
+
+#define SC_CUDA(ctx, call)                                                \
+    do {                                                                  \
+        cudaError_t e__ = (call);                                         \
+        if (e__ != cudaSuccess) return cuda_fail(ctx, e__, #call);        \
+    } while (0)
+
+bool emissive(const gr_material& m) { return m.emission[0] != 0.0f || m.emission[1] != 0.0f || m.emission[2] != 0.0f; }
+
+size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+// Slices one allocation into the path-state arrays for `cap` paths.
+size_t path_layout(uint32_t cap, char* base, gr::Paths* ps) {
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        char* p = base ? base + off : nullptr;
+        off += align256(bytes);
+        return p;
+    };
+    const size_t c = cap;
+    ps->ray = (float4*)take(32 * c);
+    ps->hit = (float4*)take(16 * c);
+    ps->thr = (float4*)take(16 * c);
+    ps->acc = (float4*)take(16 * c);
+    ps->flags = (uint32_t*)take(4 * c);
+    ps->rng = (unsigned long long*)take(8 * c);
+    ps->qa = (uint32_t*)take(4 * c);
+    ps->qb = (uint32_t*)take(4 * c);
+    ps->sray = (float4*)take(32 * c);
+    ps->scon = (float4*)take(16 * c);
+    ps->cnt = (uint32_t*)take(sizeof(uint32_t) * (2 * gr::kMaxDepth + 8));
+    ps->work = (unsigned long long*)take(sizeof(unsigned long long) * (2 * gr::kMaxDepth + 4));
+    ps->hdr = (gr::WaveHeader*)take(sizeof(gr::WaveHeader));
+    ps->capacity = cap;
+    return off;
+}
+
+gr::SceneDev scene_view(gr_scene* sc) {
+    gr::SceneDev d{};
+    d.verts = (const float*)sc->verts.p;
+    d.normals = (const float4*)sc->normals.p;
+    d.tri_mat = (const uint32_t*)sc->tri_mat.p;
+    d.mats = (const gr::DevMaterial*)sc->mats.p;
+    d.lights = (const uint32_t*)sc->lights.p;
+    d.num_lights = sc->num_lights;
+    d.num_tris = sc->num_tris;
+    d.nodes = (const gr::Node*)sc->bvh->buf.nodes.p;
+    d.tris = (const gr::Tri*)sc->bvh->buf.tris.p;
+    d.meta = (const gr::BvhMeta*)sc->bvh->buf.meta.p;
+    d.cam = sc->cam;
+    d.env_r = sc->env[0];
+    d.env_g = sc->env[1];
+    d.env_b = sc->env[2];
+    d.has_env = sc->has_env;
+    return d;
+}
+
+}  // namespace
+
+extern "C" {
+
+gr_status gr_scene_create(gr_ctx* ctx, const gr_mesh* meshes, uint32_t num_meshes, const gr_material* materials,
+                          uint32_t num_materials, const gr_camera* camera, const gr_environment* env,
+                          gr_scene** out) {
+    if (!ctx || !out || !camera || (num_meshes && !meshes) || (num_materials && !materials))
+        return fail(ctx, GR_ERR_INVALID, "gr_scene_create: null argument");
+    *out = nullptr;
+    if (camera->width == 0 || camera->height == 0 || !(camera->fov_deg > 0.0f && camera->fov_deg < 180.0f))
+        return fail(ctx, GR_ERR_INVALID, "gr_scene_create: bad camera");
+    uint64_t ntri = 0;
+    bool any_normals = false;
+    for (uint32_t i = 0; i < num_meshes; ++i) {
+        const gr_mesh& m = meshes[i];
+        if (m.num_triangles && (!m.positions || !m.indices))
+            return fail(ctx, GR_ERR_INVALID, "gr_scene_create: mesh without positions or indices");
+        if (m.material >= num_materials) return fail(ctx, GR_ERR_INVALID, "gr_scene_create: material out of range");
+        for (uint64_t k = 0; k < 3ull * m.num_triangles; ++k)
+            if (m.indices[k] >= m.num_vertices) return fail(ctx, GR_ERR_INVALID, "gr_scene_create: index out of range");
+        ntri += m.num_triangles;
+        any_normals |= m.normals != nullptr;
+    }
+    if (ntri > gr::kMaxTriangles) return fail(ctx, GR_ERR_INVALID, "gr_scene_create: too many triangles");
+    for (uint32_t i = 0; i < num_materials; ++i) {
+        const int t = materials[i].type;
+        if (t != GR_MAT_DIFFUSE && t != GR_MAT_DIELECTRIC && t != GR_MAT_CONDUCTOR)
+            return fail(ctx, GR_ERR_INVALID, "gr_scene_create: unknown material type");
+    }
+
+    std::vector<float> soup(9 * ntri);
+    std::vector<float> nrm(any_normals ? 12 * ntri : 0, 0.0f);
+    std::vector<uint32_t> tmat(ntri);
+    std::vector<uint32_t> lights;
+    uint64_t t = 0;
+    for (uint32_t i = 0; i < num_meshes; ++i) {
+        const gr_mesh& m = meshes[i];
+        const bool light = emissive(materials[m.material]);
+        for (uint32_t j = 0; j < m.num_triangles; ++j, ++t) {
+            for (int c = 0; c < 3; ++c) {
+                const uint32_t vi = m.indices[3ull * j + c];
+                std::memcpy(&soup[9 * t + 3 * c], m.positions + 3ull * vi, 12);
+                if (m.normals) std::memcpy(&nrm[12 * t + 4 * c], m.normals + 3ull * vi, 12);
+            }
+            tmat[t] = m.material | (m.normals ? 0x80000000u : 0u);
+            if (light) lights.push_back((uint32_t)t);
+        }
+    }
+    std::vector<gr::DevMaterial> dm(num_materials ? num_materials : 1);
+    for (uint32_t i = 0; i < num_materials; ++i) {
+        const gr_material& s = materials[i];
+        gr::DevMaterial& d = dm[i];
+        d.type = s.type;
+        d.cr = s.color[0]; d.cg = s.color[1]; d.cb = s.color[2];
+        d.er = s.emission[0]; d.eg = s.emission[1]; d.eb = s.emission[2];
+        d.ax = s.alpha_u; d.ay = s.alpha_v;
+        d.eir = s.eta_i[0]; d.eig = s.eta_i[1]; d.eib = s.eta_i[2];
+        d.etr = s.eta_t[0]; d.etg = s.eta_t[1]; d.etb = s.eta_t[2];
+        d.kr = s.k[0]; d.kg = s.k[1]; d.kb = s.k[2];
+        d.ior = s.ior;
+        d.emissive = emissive(s) ? 1u : 0u;
+    }
+
+    gr_scene* sc = new (std::nothrow) gr_scene();
+    if (!sc) return fail(ctx, GR_ERR_OOM_BUDGET, "host allocation failed");
+    sc->ctx = ctx;
+    gr::ctx_retain(ctx);
+    auto cleanup = [&](gr_status st) {
+        gr_scene_destroy(sc);
+        return st;
+    };
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e != cudaSuccess) return cleanup(cuda_fail(ctx, e, "cudaSetDevice"));
+    sc->num_tris = (uint32_t)ntri;
+    sc->num_lights = (uint32_t)lights.size();
+    struct Up {
+        gr::DevBuf* buf;
+        const void* src;
+        size_t bytes;
+    } ups[] = {
+        {&sc->verts, soup.data(), soup.size() * 4},
+        {&sc->normals, nrm.data(), nrm.size() * 4},
+        {&sc->tri_mat, tmat.data(), tmat.size() * 4},
+        {&sc->mats, dm.data(), dm.size() * sizeof(gr::DevMaterial)},
+        {&sc->lights, lights.data(), lights.size() * 4},
+    };
+    for (auto& u : ups) {
+        if (u.bytes == 0) continue;
+        if ((e = u.buf->ensure(u.bytes)) != cudaSuccess) return cleanup(cuda_fail(ctx, e, "scene upload alloc"));
+        if ((e = cudaMemcpy(u.buf->p, u.src, u.bytes, cudaMemcpyHostToDevice)) != cudaSuccess)
+            return cleanup(cuda_fail(ctx, e, "scene upload"));
+    }
+    gr_status st = gr_bvh_create(ctx, &sc->bvh);
+    if (st != GR_OK) return cleanup(st);
+    st = gr_bvh_build(sc->bvh, (const float*)sc->verts.p, (uint32_t)ntri, ctx->stream);
+    if (st != GR_OK) return cleanup(st);
+    if ((e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess) return cleanup(cuda_fail(ctx, e, "bvh build"));
+
+    // camera (Camera::setup, camera.h:21-38; degToRad, fwd.h:28-31)
+    const float* M = camera->to_world;
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 4; ++c) sc->cam.m[4 * r + c] = M[4 * r + c];
+    const float fov = camera->fov_deg / 180.0f * 3.14159265358979323846f;
+    sc->cam.tan_half = std::tan(fov * 0.5f);
+    sc->cam.aspect = (float)camera->width / (float)camera->height;
+    sc->cam.width = camera->width;
+    sc->cam.height = camera->height;
+    if (env && env->enabled) {
+        sc->has_env = 1;
+        std::memcpy(sc->env, env->radiance, 12);
+    }
+    const size_t npix = (size_t)camera->width * camera->height;
+    if ((e = sc->fb.ensure(24 * npix)) != cudaSuccess) return cleanup(cuda_fail(ctx, e, "framebuffer"));
+    if ((e = sc->fb_count.ensure(4 * npix)) != cudaSuccess) return cleanup(cuda_fail(ctx, e, "framebuffer"));
+    if ((e = cudaMemset(sc->fb.p, 0, 24 * npix)) != cudaSuccess) return cleanup(cuda_fail(ctx, e, "framebuffer"));
+    if ((e = cudaMemset(sc->fb_count.p, 0, 4 * npix)) != cudaSuccess) return cleanup(cuda_fail(ctx, e, "framebuffer"));
+    *out = sc;
+    return GR_OK;
+}
+
+gr_status gr_scene_destroy(gr_scene* sc) {
+    if (!sc) return GR_ERR_INVALID;
+    gr_ctx* ctx = sc->ctx;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    if (sc->bvh) gr_bvh_destroy(sc->bvh);
+    delete sc;
+    gr::ctx_release(ctx);
+    return GR_OK;
+}
+
+gr_status gr_scene_info(const gr_scene* sc, uint32_t* width, uint32_t* height, uint32_t* triangles, uint32_t* lights) {
+    if (!sc) return GR_ERR_INVALID;
+    if (width) *width = sc->cam.width;
+    if (height) *height = sc->cam.height;
+    if (triangles) *triangles = sc->num_tris;
+    if (lights) *lights = sc->num_lights;
+    return GR_OK;
+}
+
+gr_status gr_render(gr_scene* sc, const gr_render_opts* opts, float* h_rgb, gr_render_stats* stats) {
+    if (!sc || !opts) return GR_ERR_INVALID;
+    gr_ctx* ctx = sc->ctx;
+    if (opts->max_depth > (uint32_t)gr::kMaxDepth)
+        return fail(ctx, GR_ERR_INVALID, "gr_render: max_depth above " + std::to_string(gr::kMaxDepth));
+    const auto t0 = std::chrono::steady_clock::now();
+    SC_CUDA(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->stream;
+    const uint32_t npix = sc->cam.width * sc->cam.height;
+    const uint64_t want_paths = opts->wave_paths ? opts->wave_paths : (1u << 22);
+    uint32_t per_wave = (uint32_t)std::max<uint64_t>(1, want_paths / npix);
+    if (opts->spp) per_wave = std::min(per_wave, opts->spp);
+    const uint64_t cap64 = (uint64_t)per_wave * npix;
+    if (cap64 > 0xFFFFFFFFull / 2) return fail(ctx, GR_ERR_INVALID, "gr_render: wave too large");
+    const uint32_t cap = (uint32_t)cap64;
+    gr::Paths ps;
+    if (cap > sc->path_capacity) {
+        const size_t bytes = path_layout(cap, nullptr, &ps);
+        SC_CUDA(ctx, sc->path_mem.ensure(bytes));
+        sc->path_capacity = cap;
+    }
+    path_layout(sc->path_capacity, (char*)sc->path_mem.p, &ps);
+    gr::WaveHeader hdr{};
+    hdr.sample_base = sc->samples_done;
+    hdr.max_wave = per_wave;
+    hdr.remaining = opts->spp;
+    hdr.wave_samples = std::min(per_wave, opts->spp);
+    SC_CUDA(ctx, cudaMemcpyAsync(ps.hdr, &hdr, sizeof(hdr), cudaMemcpyHostToDevice, s));
+    SC_CUDA(ctx, cudaMemsetAsync(ps.cnt + 2 * gr::kMaxDepth + 4, 0, 4, s));
+    gr::RenderParams rp;
+    rp.max_depth = opts->max_depth;
+    rp.rr_depth = opts->rr_depth;
+    rp.flags = opts->flags;
+    rp.seed = opts->seed;
+    rp.npix = npix;
+    const uint32_t waves = opts->spp ? (opts->spp + per_wave - 1) / per_wave : 0;
+    const gr::SceneDev view = scene_view(sc);
+    SC_CUDA(ctx, gr::render_waves(view, ps, rp, (double*)sc->fb.p, (uint32_t*)sc->fb_count.p, waves, ctx->num_sms, s));
+    SC_CUDA(ctx, cudaMemcpyAsync(&hdr, ps.hdr, sizeof(hdr), cudaMemcpyDeviceToHost, s));
+    uint32_t err = 0;
+    SC_CUDA(ctx, cudaMemcpyAsync(&err, ps.cnt + 2 * gr::kMaxDepth + 4, 4, cudaMemcpyDeviceToHost, s));
+    SC_CUDA(ctx, cudaStreamSynchronize(s));
+    sc->samples_done += opts->spp;
+    if (h_rgb) {
+        std::vector<double> sum(3ull * npix);
+        std::vector<uint32_t> cnt(npix);
+        SC_CUDA(ctx, cudaMemcpy(sum.data(), sc->fb.p, 24ull * npix, cudaMemcpyDeviceToHost));
+        SC_CUDA(ctx, cudaMemcpy(cnt.data(), sc->fb_count.p, 4ull * npix, cudaMemcpyDeviceToHost));
+        for (uint32_t p = 0; p < npix; ++p) {
+            const double inv = cnt[p] ? 1.0 / cnt[p] : 0.0;
+            for (int c = 0; c < 3; ++c) h_rgb[3ull * p + c] = (float)(sum[3ull * p + c] * inv);
+        }
+    }
+    if (stats) {
+        stats->ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        stats->closest_rays = hdr.closest_rays;
+        stats->shadow_rays = hdr.shadow_rays;
+        stats->samples = (uint64_t)opts->spp * npix;
+        stats->waves = waves;
+        stats->device_errors = err;
+    }
+    if (err & gr::ERR_STACK) return fail(ctx, GR_ERR_OVERFLOW, "gr_render: traversal stack overflow");
+    if (err) return fail(ctx, GR_ERR_CUDA, "gr_render: device error bits set");
+    return GR_OK;
+}
+
+gr_status gr_scene_accumulation(gr_scene* sc, double* h_sum_rgb, uint32_t* h_count) {
+    if (!sc) return GR_ERR_INVALID;
+    gr_ctx* ctx = sc->ctx;
+    SC_CUDA(ctx, cudaSetDevice(ctx->device));
+    SC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    const size_t npix = (size_t)sc->cam.width * sc->cam.height;
+    if (h_sum_rgb) SC_CUDA(ctx, cudaMemcpy(h_sum_rgb, sc->fb.p, 24 * npix, cudaMemcpyDeviceToHost));
+    if (h_count) SC_CUDA(ctx, cudaMemcpy(h_count, sc->fb_count.p, 4 * npix, cudaMemcpyDeviceToHost));
+    return GR_OK;
+}
+
+gr_status gr_scene_reset(gr_scene* sc) {
+    if (!sc) return GR_ERR_INVALID;
+    gr_ctx* ctx = sc->ctx;
+    SC_CUDA(ctx, cudaSetDevice(ctx->device));
+    const size_t npix = (size_t)sc->cam.width * sc->cam.height;
+    SC_CUDA(ctx, cudaMemsetAsync(sc->fb.p, 0, 24 * npix, ctx->stream));
+    SC_CUDA(ctx, cudaMemsetAsync(sc->fb_count.p, 0, 4 * npix, ctx->stream));
+    SC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    sc->samples_done = 0;
+    return GR_OK;
+}
+
+}  // extern "C"

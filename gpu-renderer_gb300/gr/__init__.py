@@ -156,3 +156,176 @@ class BVH:
             self.close()
         except Exception:
             pass
+
+
+# ---- scene records (include/gr.h) --------------------------------------------------
+
+class Material(ctypes.Structure):
+    _fields_ = [("type", ctypes.c_int32), ("color", ctypes.c_float * 3), ("emission", ctypes.c_float * 3),
+                ("alpha_u", ctypes.c_float), ("alpha_v", ctypes.c_float), ("eta_i", ctypes.c_float * 3),
+                ("eta_t", ctypes.c_float * 3), ("k", ctypes.c_float * 3), ("ior", ctypes.c_float)]
+
+
+class Mesh(ctypes.Structure):
+    _fields_ = [("positions", _P), ("num_vertices", ctypes.c_uint32), ("normals", _P), ("indices", _P),
+                ("num_triangles", ctypes.c_uint32), ("material", ctypes.c_uint32)]
+
+
+class Camera(ctypes.Structure):
+    _fields_ = [("to_world", ctypes.c_float * 16), ("fov_deg", ctypes.c_float), ("width", ctypes.c_uint32),
+                ("height", ctypes.c_uint32)]
+
+
+class Environment(ctypes.Structure):
+    _fields_ = [("radiance", ctypes.c_float * 3), ("enabled", ctypes.c_int32)]
+
+
+class RenderOpts(ctypes.Structure):
+    _fields_ = [("spp", ctypes.c_uint32), ("max_depth", ctypes.c_uint32), ("seed", ctypes.c_uint64),
+                ("rr_depth", ctypes.c_int32), ("flags", ctypes.c_uint32), ("wave_paths", ctypes.c_uint32)]
+
+
+class RenderStats(ctypes.Structure):
+    _fields_ = [("ms", ctypes.c_double), ("closest_rays", ctypes.c_uint64), ("shadow_rays", ctypes.c_uint64),
+                ("samples", ctypes.c_uint64), ("waves", ctypes.c_uint32), ("device_errors", ctypes.c_uint32)]
+
+
+MAT_DIFFUSE, MAT_DIELECTRIC, MAT_CONDUCTOR = 0, 1, 2
+RENDER_REFERENCE_COMPAT = 1
+
+_SCENE_SIGS = {
+    "gr_scene_create": ([_P, _P, ctypes.c_uint32, _P, ctypes.c_uint32, _P, _P, ctypes.POINTER(_P)], ctypes.c_int),
+    "gr_scene_destroy": ([_P], ctypes.c_int),
+    "gr_scene_info": ([_P, _P, _P, _P, _P], ctypes.c_int),
+    "gr_render": ([_P, ctypes.POINTER(RenderOpts), _P, ctypes.POINTER(RenderStats)], ctypes.c_int),
+    "gr_scene_accumulation": ([_P, _P, _P], ctypes.c_int),
+    "gr_scene_reset": ([_P], ctypes.c_int),
+}
+
+
+def _declare(sigs):
+    L = load()
+    for name, (args, res) in sigs.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = res
+    return L
+
+
+def material_record(m):
+    """dict -> Material. Keys: type, color, emission, alpha (or alpha_u/alpha_v),
+    eta_i, eta_t, k, ior."""
+    r = Material()
+    r.type = int(m.get("type", MAT_DIFFUSE))
+    r.color[:] = [float(x) for x in m.get("color", (0.5, 0.5, 0.5))]
+    r.emission[:] = [float(x) for x in m.get("emission", (0.0, 0.0, 0.0))]
+    a = m.get("alpha", 0.1)
+    r.alpha_u = float(m.get("alpha_u", a))
+    r.alpha_v = float(m.get("alpha_v", a))
+    r.eta_i[:] = [float(x) for x in m.get("eta_i", (1.0, 1.0, 1.0))]
+    r.eta_t[:] = [float(x) for x in m.get("eta_t", (0.200438, 0.924033, 1.10221))]
+    r.k[:] = [float(x) for x in m.get("k", (3.91295, 2.45285, 2.14219))]
+    r.ior = float(m.get("ior", 1.5))
+    return r
+
+
+class Scene:
+    """A scene on the GPU (gr_scene): meshes, materials, camera, environment.
+
+    `desc` is a gr.scenes.SceneDesc (meshes as numpy arrays)."""
+
+    def __init__(self, ctx, desc):
+        L = _declare(_SCENE_SIGS)
+        self.ctx = ctx
+        self.desc = desc
+        self._keep = []
+        meshes = (Mesh * max(len(desc.meshes), 1))()
+        for i, m in enumerate(desc.meshes):
+            pos = np.ascontiguousarray(m.positions, np.float32)
+            idx = np.ascontiguousarray(m.indices, np.uint32)
+            nrm = None if m.normals is None else np.ascontiguousarray(m.normals, np.float32)
+            self._keep += [pos, idx, nrm]
+            meshes[i].positions = pos.ctypes.data
+            meshes[i].num_vertices = pos.shape[0]
+            meshes[i].normals = None if nrm is None else nrm.ctypes.data
+            meshes[i].indices = idx.ctypes.data
+            meshes[i].num_triangles = idx.shape[0]
+            meshes[i].material = m.material
+        mats = (Material * max(len(desc.materials), 1))(*[material_record(m) for m in desc.materials])
+        cam = Camera()
+        cam.to_world[:] = [float(x) for x in np.asarray(desc.camera["to_world"], np.float32).reshape(16)]
+        cam.fov_deg = float(desc.camera["fov"])
+        cam.width = int(desc.camera["width"])
+        cam.height = int(desc.camera["height"])
+        env = Environment()
+        if desc.env is not None:
+            env.radiance[:] = [float(x) for x in desc.env]
+            env.enabled = 1
+        h = _P()
+        ctx.check(L.gr_scene_create(ctx.h, meshes, len(desc.meshes), mats, len(desc.materials), ctypes.byref(cam),
+                                    ctypes.byref(env), ctypes.byref(h)), "gr_scene_create")
+        self.h = h
+        self._keep = []
+        self.width, self.height = cam.width, cam.height
+
+    def render(self, spp, max_depth=8, seed=0, rr_depth=3, flags=0, wave_paths=0, want_image=True):
+        L = _declare(_SCENE_SIGS)
+        o = RenderOpts(spp, max_depth, seed, rr_depth, flags, wave_paths)
+        st = RenderStats()
+        img = np.zeros((self.height, self.width, 3), np.float32) if want_image else None
+        self.ctx.check(L.gr_render(self.h, ctypes.byref(o), _ptr(img), ctypes.byref(st)), "gr_render")
+        return img, st
+
+    def accumulation(self):
+        L = _declare(_SCENE_SIGS)
+        s = np.zeros((self.height, self.width, 3), np.float64)
+        c = np.zeros((self.height, self.width), np.uint32)
+        self.ctx.check(L.gr_scene_accumulation(self.h, _ptr(s), _ptr(c)), "gr_scene_accumulation")
+        return s, c
+
+    def reset(self):
+        self.ctx.check(_declare(_SCENE_SIGS).gr_scene_reset(self.h), "gr_scene_reset")
+
+    def info(self):
+        v = [ctypes.c_uint32() for _ in range(4)]
+        self.ctx.check(_declare(_SCENE_SIGS).gr_scene_info(self.h, *[ctypes.byref(x) for x in v]), "gr_scene_info")
+        return {"width": v[0].value, "height": v[1].value, "triangles": v[2].value, "lights": v[3].value}
+
+    def close(self):
+        if getattr(self, "h", None):
+            _declare(_SCENE_SIGS).gr_scene_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class PathTracer:
+    """The reference's PathTracer interface (src/renderer/pathtracer.h:16-46)
+    over a gr scene: render(num) adds `num` samples per pixel, output() writes
+    the image, reset() clears the accumulation."""
+
+    def __init__(self, scene, max_path_length=33, seed=0, rr_depth=3, flags=0):
+        self.scene = scene
+        self.max_path_length = max_path_length
+        self.seed = seed
+        self.rr_depth = rr_depth
+        self.flags = flags
+        self.sample_num = 0
+
+    def render(self, num=1):
+        img, st = self.scene.render(num, self.max_path_length, self.seed, self.rr_depth, self.flags)
+        self.sample_num += num
+        self.image = img
+        return img, st
+
+    def output(self, filename):
+        from . import imageio
+        imageio.write_image(filename, self.image)
+
+    def reset(self):
+        self.scene.reset()
+        self.sample_num = 0

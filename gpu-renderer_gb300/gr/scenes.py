@@ -81,3 +81,225 @@ def coherent_rays(w=2048, h=2048, fov_deg=40.0, eye=(0.5, 0.5, -1.0), target=(0.
     R[:, 6] = 0.0
     R[:, 7] = 1e34
     return R
+
+
+# ---- scene descriptions for the render configurations -----------------------------
+
+class MeshDesc:
+    def __init__(self, positions, indices, material, normals=None):
+        self.positions = np.ascontiguousarray(positions, np.float32).reshape(-1, 3)
+        self.indices = np.ascontiguousarray(indices, np.uint32).reshape(-1, 3)
+        self.normals = None if normals is None else np.ascontiguousarray(normals, np.float32).reshape(-1, 3)
+        self.material = int(material)
+
+
+class SceneDesc:
+    """Meshes + materials (dicts for gr.material_record) + camera + constant
+    environment radiance (None for no environment)."""
+
+    def __init__(self, meshes, materials, camera, env=None):
+        self.meshes = meshes
+        self.materials = materials
+        self.camera = camera
+        self.env = env
+
+    @property
+    def num_triangles(self):
+        return sum(m.indices.shape[0] for m in self.meshes)
+
+    def flatten(self):
+        """Triangle soup, per-corner normals, material words, in the order the
+        library flattens them (mesh order, then triangle order)."""
+        n = self.num_triangles
+        soup = np.zeros((n, 9), np.float32)
+        nrm = np.zeros((n, 12), np.float32)
+        tmat = np.zeros(n, np.uint32)
+        t = 0
+        for m in self.meshes:
+            k = m.indices.shape[0]
+            soup[t:t + k] = m.positions[m.indices].reshape(k, 9)
+            if m.normals is not None:
+                nn = m.normals[m.indices]  # (k, 3, 3)
+                nrm[t:t + k].reshape(k, 3, 4)[:, :, :3] = nn
+                tmat[t:t + k] = m.material | 0x80000000
+            else:
+                tmat[t:t + k] = m.material
+            t += k
+        any_n = any(m.normals is not None for m in self.meshes)
+        return soup, (nrm if any_n else None), tmat
+
+
+def look_at(origin, target, up):
+    """Camera-to-world matrix of the reference's LookAt (transform.cpp:220-249):
+    columns left, up, forward, origin; row-major 4x4 float32."""
+    o = np.asarray(origin, np.float32)
+    f = np.asarray(target, np.float32) - o
+    f = f / np.sqrt(np.float32(np.dot(f, f)))
+    left = np.cross(np.asarray(up, np.float32), f).astype(np.float32)
+    left = left / np.sqrt(np.float32(np.dot(left, left)))
+    u = np.cross(f, left).astype(np.float32)
+    M = np.eye(4, dtype=np.float32)
+    M[:3, 0] = left
+    M[:3, 1] = u
+    M[:3, 2] = f
+    M[:3, 3] = o
+    return M
+
+
+def quad(p0, p1, p2, p3):
+    """Two triangles (p0, p1, p2), (p0, p2, p3); geometric normal follows the
+    reference's cross(p0 - p2, p1 - p2) of the first triangle."""
+    P = np.array([p0, p1, p2, p3], np.float32)
+    return P, np.array([[0, 1, 2], [0, 2, 3]], np.uint32)
+
+
+def box_mesh(center, size, yaw):
+    """12-triangle axis box, rotated by `yaw` about +y."""
+    sx, sy, sz = size
+    c = np.array(center, np.float32)
+    corners = np.array([[x, y, z] for x in (-0.5, 0.5) for y in (0.0, 1.0) for z in (-0.5, 0.5)], np.float32)
+    corners *= np.array([sx, sy, sz], np.float32)
+    cy, syw = np.cos(yaw), np.sin(yaw)
+    R = np.array([[cy, 0, syw], [0, 1, 0], [-syw, 0, cy]], np.float32)
+    P = (corners @ R.T + c).astype(np.float32)
+    # corner index = 4*ix + 2*iy + iz
+    faces = [(0, 1, 3, 2), (4, 6, 7, 5), (0, 4, 5, 1), (2, 3, 7, 6), (0, 2, 6, 4), (1, 5, 7, 3)]
+    idx = []
+    for a, b, cc, d in faces:
+        idx += [[a, b, cc], [a, cc, d]]
+    return P, np.array(idx, np.uint32)
+
+
+def cornell_box(width=256, height=256, seed_salt=0):
+    """Config 1: procedural Cornell box. Five walls as 10 triangles (floor,
+    ceiling, back grey 0.75; left red 0.63/0.065/0.05; right green
+    0.14/0.45/0.09), a 2-triangle quad light of radiance 15 below the ceiling,
+    and two 12-triangle boxes rotated by a seeded yaw. Lambert everywhere;
+    pinhole camera with a 40 degree field of view."""
+    r = rng(1, seed_salt)
+    grey = {"type": 0, "color": (0.75, 0.75, 0.75)}
+    red = {"type": 0, "color": (0.63, 0.065, 0.05)}
+    green = {"type": 0, "color": (0.14, 0.45, 0.09)}
+    light = {"type": 0, "color": (0.75, 0.75, 0.75), "emission": (15.0, 15.0, 15.0)}
+    mats = [grey, red, green, light]
+    meshes = []
+    walls = [
+        (quad((-1, 0, -1), (1, 0, -1), (1, 0, 1), (-1, 0, 1)), 0),     # floor
+        (quad((-1, 2, -1), (-1, 2, 1), (1, 2, 1), (1, 2, -1)), 0),     # ceiling
+        (quad((-1, 0, -1), (-1, 2, -1), (1, 2, -1), (1, 0, -1)), 0),   # back
+        (quad((-1, 0, -1), (-1, 0, 1), (-1, 2, 1), (-1, 2, -1)), 1),   # left
+        (quad((1, 0, -1), (1, 2, -1), (1, 2, 1), (1, 0, 1)), 2),       # right
+    ]
+    for (P, I), mi in walls:
+        meshes.append(MeshDesc(P, I, mi))
+    # light quad facing down: cross(p0 - p2, p1 - p2) points to -y
+    LP, LI = quad((-0.25, 1.98, -0.25), (0.25, 1.98, -0.25), (0.25, 1.98, 0.25), (-0.25, 1.98, 0.25))
+    meshes.append(MeshDesc(LP, LI, 3))
+    yaw = r.random(2) * 2.0 * np.pi
+    for center, size, yw in (((-0.35, 0.0, -0.35), (0.6, 1.2, 0.6), yaw[0]),
+                             ((0.35, 0.0, 0.3), (0.6, 0.6, 0.6), yaw[1])):
+        P, I = box_mesh(center, size, yw)
+        meshes.append(MeshDesc(P, I, 0))
+    cam = {"to_world": look_at((0.0, 1.0, 3.8), (0.0, 1.0, 0.0), (0.0, 1.0, 0.0)), "fov": 40.0,
+           "width": width, "height": height}
+    return SceneDesc(meshes, mats, cam, env=None)
+
+
+def icosphere(level):
+    """Unit icosphere: 20 * 4^level triangles with shared vertices."""
+    t = (1.0 + 5.0 ** 0.5) / 2.0
+    V = np.array([[-1, t, 0], [1, t, 0], [-1, -t, 0], [1, -t, 0], [0, -1, t], [0, 1, t], [0, -1, -t], [0, 1, -t],
+                  [t, 0, -1], [t, 0, 1], [-t, 0, -1], [-t, 0, 1]], np.float64)
+    V /= np.linalg.norm(V, axis=1, keepdims=True)
+    F = np.array([[0, 11, 5], [0, 5, 1], [0, 1, 7], [0, 7, 10], [0, 10, 11], [1, 5, 9], [5, 11, 4], [11, 10, 2],
+                  [10, 7, 6], [7, 1, 8], [3, 9, 4], [3, 4, 2], [3, 2, 6], [3, 6, 8], [3, 8, 9], [4, 9, 5],
+                  [2, 4, 11], [6, 2, 10], [8, 6, 7], [9, 8, 1]], np.int64)
+    for _ in range(level):
+        e = np.concatenate([F[:, [0, 1]], F[:, [1, 2]], F[:, [2, 0]]])
+        e.sort(axis=1)
+        uniq, inv = np.unique(e, axis=0, return_inverse=True)
+        mid = V[uniq[:, 0]] + V[uniq[:, 1]]
+        mid /= np.linalg.norm(mid, axis=1, keepdims=True)
+        base = V.shape[0]
+        V = np.concatenate([V, mid])
+        nf = F.shape[0]
+        inv = inv.reshape(-1)
+        m01, m12, m20 = inv[:nf] + base, inv[nf:2 * nf] + base, inv[2 * nf:] + base
+        F = np.concatenate([np.stack([F[:, 0], m01, m20], 1), np.stack([F[:, 1], m12, m01], 1),
+                            np.stack([F[:, 2], m20, m12], 1), np.stack([m01, m12, m20], 1)])
+    return V, F
+
+
+def value_noise3(p, seed, octaves=3):
+    """Seeded 3-octave value noise on points p (N, 3): hashed lattice values in
+    [-1, 1], smoothstep-trilinear interpolation, frequency doubling and
+    amplitude halving per octave; result roughly in [-1, 1]."""
+    out = np.zeros(p.shape[0], np.float64)
+    amp, freq, norm = 1.0, 2.0, 0.0
+    for o in range(octaves):
+        q = p * freq
+        i0 = np.floor(q).astype(np.int64)
+        f = q - i0
+        f = f * f * (3.0 - 2.0 * f)
+        acc = np.zeros(p.shape[0])
+        for dx in (0, 1):
+            for dy in (0, 1):
+                for dz in (0, 1):
+                    h = (i0[:, 0] + dx) * 73856093 ^ (i0[:, 1] + dy) * 19349663 ^ (i0[:, 2] + dz) * 83492791
+                    h = (h ^ (seed * 2654435761 + o * 97531)) & 0xFFFFFFFF
+                    h = (h * 2246822519) & 0xFFFFFFFF
+                    h ^= h >> 13
+                    h = (h * 3266489917) & 0xFFFFFFFF
+                    h ^= h >> 16
+                    v = (h / 4294967295.0) * 2.0 - 1.0
+                    w = (f[:, 0] if dx else 1 - f[:, 0]) * (f[:, 1] if dy else 1 - f[:, 1]) * \
+                        (f[:, 2] if dz else 1 - f[:, 2])
+                    acc += w * v
+        out += amp * acc
+        norm += amp
+        amp *= 0.5
+        freq *= 2.0
+    return out / norm
+
+
+def displaced_sphere(level, radius, center, amplitude, seed):
+    """Icosphere radially displaced by value noise; vertex normals are
+    normalised sums of adjacent face normals."""
+    V, F = icosphere(level)
+    disp = 1.0 + amplitude * value_noise3(V, seed)
+    P = V * disp[:, None] * radius + np.asarray(center, np.float64)
+    fn = np.cross(P[F[:, 1]] - P[F[:, 0]], P[F[:, 2]] - P[F[:, 0]])
+    N = np.zeros_like(P)
+    for k in range(3):
+        np.add.at(N, F[:, k], fn)
+    N /= np.linalg.norm(N, axis=1, keepdims=True)
+    return P.astype(np.float32), F.astype(np.uint32), N.astype(np.float32)
+
+
+def glossy_scene(width=1024, height=768, level=8, glass_level=5, seed_salt=0):
+    """Config 3: four noise-displaced icospheres (level 8 = 1,310,720 triangles
+    each, amplitude 0.05) with GGX conductors of roughness 0.01 / 0.1 / 0.25 /
+    0.5 (Cu-like eta/k, the reference's defaults), one smooth dielectric sphere
+    (IOR 1.5, icosphere level 5 = 20,480 triangles), a 2-triangle ground plane,
+    a constant environment and one quad light."""
+    mats = [
+        {"type": 0, "color": (0.5, 0.5, 0.5)},                                   # ground
+        {"type": 0, "color": (0.5, 0.5, 0.5), "emission": (20.0, 20.0, 20.0)},   # light
+        {"type": 1, "color": (1.0, 1.0, 1.0), "ior": 1.5},                       # glass
+    ]
+    alphas = (0.01, 0.1, 0.25, 0.5)
+    for a in alphas:
+        mats.append({"type": 2, "color": (1.0, 1.0, 1.0), "alpha": a})
+    meshes = []
+    GP, GI = quad((-10, 0, -10), (-10, 0, 10), (10, 0, 10), (10, 0, -10))
+    meshes.append(MeshDesc(GP, GI, 0))
+    LP, LI = quad((-0.5, 3.0, -0.5), (0.5, 3.0, -0.5), (0.5, 3.0, 0.5), (-0.5, 3.0, 0.5))
+    meshes.append(MeshDesc(LP, LI, 1))
+    for i, x in enumerate((-1.65, -0.55, 0.55, 1.65)):
+        P, F, N = displaced_sphere(level, 0.5, (x, 0.55, 0.0), 0.05, seed=SEED_BASE + 3 + i + (seed_salt << 4))
+        meshes.append(MeshDesc(P, F, 3 + i, normals=N))
+    P, F, N = displaced_sphere(glass_level, 0.4, (0.0, 0.4, 1.1), 0.0, seed=1)
+    meshes.append(MeshDesc(P, F, 2, normals=N))
+    cam = {"to_world": look_at((0.0, 1.3, 4.6), (0.0, 0.5, 0.0), (0.0, 1.0, 0.0)), "fov": 40.0,
+           "width": width, "height": height}
+    return SceneDesc(meshes, mats, cam, env=(0.3, 0.35, 0.45))

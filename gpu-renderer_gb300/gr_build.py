@@ -19,6 +19,10 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc") if os.path.exists(os.path.join(CUD
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 INCLUDES = ["-I", os.path.join(ROOT, "include"), "-I", CSRC]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"] + ARCH
+# The integrator's shading math rounds every operation as written (no FMA
+# contraction), like the host oracle it is compared with; traversal code uses
+# explicit round-to-nearest intrinsics everywhere and is unaffected.
+PER_FILE_FLAGS = {"render.cu": ["--fmad=false"]}
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-Wextra", "-Wno-unused-parameter",
              "-I", os.path.join(CUDA_HOME, "include")]
 
@@ -49,7 +53,7 @@ def _compile(src, force):
     if not force and not _stale(obj, [src] + _headers()):
         return obj
     if src.endswith(".cu"):
-        cmd = [NVCC] + NVCC_FLAGS + INCLUDES + ["-c", src, "-o", obj]
+        cmd = [NVCC] + NVCC_FLAGS + PER_FILE_FLAGS.get(os.path.basename(src), []) + INCLUDES + ["-c", src, "-o", obj]
     else:
         cmd = ["g++"] + CXX_FLAGS + INCLUDES + ["-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)

@@ -130,6 +130,103 @@ gr_status gr_trace(gr_bvh* bvh, const gr_ray* d_rays, uint64_t n, gr_hit* d_hits
 /* Host-memory variant: copies rays in, traces, copies hits out, waits. */
 gr_status gr_trace_host(gr_bvh* bvh, const gr_ray* h_rays, uint64_t n, gr_hit* h_hits, int any_hit);
 
+/* ---- scene records ----------------------------------------------------------
+ * Mirror the reference's TriangleMesh / Material / Camera / EnvironmentLight
+ * (src/renderer/triangle.h:28-49, material.h:15-34, camera.h:7-132,
+ * environment.h:30-53) as plain structs. Textures are constant (one value per
+ * material), as the reference's 1x1 textures are. */
+
+typedef enum gr_material_type {
+    GR_MAT_DIFFUSE = 0,    /* Lambert (reference MATERIAL_DIFFUSE, "diffuse") */
+    GR_MAT_DIELECTRIC = 1, /* smooth Fresnel dielectric (MATERIAL_SPECULAR: "dielectric", "glass", "mirror") */
+    GR_MAT_CONDUCTOR = 2   /* GGX rough conductor (MATERIAL_ROUGH_CONDUCTOR: "roughconductor", "conductor") */
+} gr_material_type;
+
+typedef struct gr_material {
+    int32_t type;       /* gr_material_type */
+    float color[3];     /* reflectance (diffuse) or specular reflectance */
+    float emission[3];  /* area-light radiance; non-zero makes the material's triangles lights */
+    float alpha_u, alpha_v; /* GGX roughness (conductor) */
+    float eta_i[3], eta_t[3], k[3]; /* conductor Fresnel terms */
+    float ior;          /* dielectric index of refraction (interior / exterior) */
+} gr_material;
+
+typedef struct gr_mesh {
+    const float* positions;  /* 3 floats per vertex, world space */
+    uint32_t num_vertices;
+    const float* normals;    /* NULL, or 3 floats per vertex (shading normals) */
+    const uint32_t* indices; /* 3 vertex indices per triangle */
+    uint32_t num_triangles;
+    uint32_t material;       /* index into the material table */
+} gr_mesh;
+
+/* Pinhole camera in the reference's Mitsuba convention (camera.h:21-38):
+ * row-major camera-to-world matrix, horizontal field of view in degrees. */
+typedef struct gr_camera {
+    float to_world[16];
+    float fov_deg;
+    uint32_t width, height;
+} gr_camera;
+
+typedef struct gr_environment {
+    float radiance[3]; /* constant environment radiance (reference "constant" emitter) */
+    int32_t enabled;
+} gr_environment;
+
+/* Render options. The reference's PTOptions (pathtracer.h:7-14) fixes
+ * max_path_length at 33 and draws one sample per render() call. */
+typedef struct gr_render_opts {
+    uint32_t spp;        /* samples per pixel added by this call */
+    uint32_t max_depth;  /* shading steps per path (the reference's max_path_length) */
+    uint64_t seed;       /* RNG seed; a path's stream is keyed by (seed, pixel, sample index) */
+    int32_t rr_depth;    /* Russian roulette after this bounce (reference: 3); < 0 disables */
+    uint32_t flags;      /* GR_RENDER_* */
+    uint32_t wave_paths; /* paths in flight per wave (0 = library default) */
+} gr_render_opts;
+
+/* Reproduce the reference's integrator quirks for comparison with its
+ * images: the Russian-roulette rescale is not stored, roulette-killed paths
+ * see the environment at the next bounce, and the GGX pdf is D|cos h|/(4 wo.h)
+ * (pathtracer_kernel.h:738-748, microfacet.h:148-155). Default: corrected. */
+#define GR_RENDER_REFERENCE_COMPAT 1u
+
+typedef struct gr_render_stats {
+    double ms;             /* host wall time of the call */
+    uint64_t closest_rays; /* camera + scatter rays traced */
+    uint64_t shadow_rays;  /* NEE shadow rays traced */
+    uint64_t samples;      /* pixel samples added */
+    uint32_t waves;        /* path waves launched */
+    uint32_t device_errors;/* device error bits seen (0 = none) */
+} gr_render_stats;
+
+typedef struct gr_scene gr_scene;
+
+/* Replaces Scene::Scene + createDeviceData (scene.cpp:4-51): flattens the
+ * meshes into one triangle list (mesh order, then triangle order), collects
+ * emissive triangles as lights, uploads, and builds the LBVH on the GPU. */
+gr_status gr_scene_create(gr_ctx* ctx, const gr_mesh* meshes, uint32_t num_meshes, const gr_material* materials,
+                          uint32_t num_materials, const gr_camera* camera, const gr_environment* env,
+                          gr_scene** out);
+gr_status gr_scene_destroy(gr_scene* scene);
+gr_status gr_scene_info(const gr_scene* scene, uint32_t* width, uint32_t* height, uint32_t* triangles,
+                        uint32_t* lights);
+
+/* Replaces PathTracer::render(uint32 num) (pathtracer.cu:152-170): adds
+ * opts->spp samples per pixel to the scene's accumulation buffer with the
+ * wavefront integrator (camera rays, closest hit, NEE + MIS shading, shadow
+ * any-hit, Russian roulette) and, when h_rgb is not NULL, writes the running
+ * mean radiance (width x height x 3 floats, row 0 first) to host memory.
+ * Successive calls continue the sample sequence, as repeated render() calls do. */
+gr_status gr_render(gr_scene* scene, const gr_render_opts* opts, float* h_rgb, gr_render_stats* stats);
+
+/* The raw accumulation: per-pixel radiance sums (3 doubles) and sample counts.
+ * Either pointer may be NULL. Replaces FrameBuffer's m_buffer / m_sample_num. */
+gr_status gr_scene_accumulation(gr_scene* scene, double* h_sum_rgb, uint32_t* h_count);
+
+/* Clears the accumulation and restarts the sample sequence (PathTracer::reset,
+ * pathtracer.cu:195-200). */
+gr_status gr_scene_reset(gr_scene* scene);
+
 #ifdef __cplusplus
 }
 #endif

@@ -124,3 +124,49 @@ def ref_lbvh(verts):
     codes = np.zeros(n, np.uint32)
     load_ref().ref_lbvh_build(_p(v), n, _p(nodes), _p(codes))
     return nodes, codes
+
+
+class _OrMaterial(ctypes.Structure):
+    _fields_ = [("type", ctypes.c_int32), ("color", ctypes.c_float * 3), ("emission", ctypes.c_float * 3),
+                ("ax", ctypes.c_float), ("ay", ctypes.c_float), ("eta_i", ctypes.c_float * 3),
+                ("eta_t", ctypes.c_float * 3), ("k", ctypes.c_float * 3), ("ior", ctypes.c_float),
+                ("emissive", ctypes.c_uint32)]
+
+
+class _OrCamera(ctypes.Structure):
+    _fields_ = [("m", ctypes.c_float * 12), ("fov_deg", ctypes.c_float), ("width", ctypes.c_uint32),
+                ("height", ctypes.c_uint32)]
+
+
+def render(desc, spp, max_depth=8, seed=0, rr_depth=3, flags=0, sample_base=0, nthreads=None):
+    """The integrator restated on the CPU; returns (sum of radiance per pixel
+    as float64 (H, W, 3), spp). `desc` is a gr.scenes.SceneDesc."""
+    import gr
+    soup, nrm, tmat = desc.flatten()
+    mats = (_OrMaterial * max(len(desc.materials), 1))()
+    for i, m in enumerate(desc.materials):
+        r = gr.material_record(m)
+        o = mats[i]
+        o.type = r.type
+        o.color[:] = r.color[:]
+        o.emission[:] = r.emission[:]
+        o.ax, o.ay = r.alpha_u, r.alpha_v
+        o.eta_i[:] = r.eta_i[:]
+        o.eta_t[:] = r.eta_t[:]
+        o.k[:] = r.k[:]
+        o.ior = r.ior
+        o.emissive = 1 if any(x != 0.0 for x in r.emission) else 0
+    cam = _OrCamera()
+    M = np.asarray(desc.camera["to_world"], np.float32).reshape(4, 4)
+    cam.m[:] = [float(x) for x in M[:3].reshape(12)]
+    cam.fov_deg = float(desc.camera["fov"])
+    cam.width = int(desc.camera["width"])
+    cam.height = int(desc.camera["height"])
+    env = np.zeros(3, np.float32) if desc.env is None else np.asarray(desc.env, np.float32)
+    fb = np.zeros((cam.height, cam.width, 3), np.float64)
+    load().or_render(_p(soup), _p(nrm), _p(tmat), ctypes.c_uint32(soup.shape[0]), mats,
+                     ctypes.c_uint32(len(desc.materials)), ctypes.byref(cam), _p(env), int(desc.env is not None),
+                     ctypes.c_uint32(spp), ctypes.c_uint32(sample_base), ctypes.c_uint32(max_depth),
+                     ctypes.c_uint64(seed), ctypes.c_int32(rr_depth), ctypes.c_uint32(flags), _p(fb),
+                     nthreads or threads())
+    return fb

@@ -1,0 +1,89 @@
+"""GPU wavefront integrator against the CPU oracle (same seeds, same paths),
+plus properties of the accumulation: progressive renders, wave size and
+convergence."""
+import numpy as np
+import pytest
+
+import gr
+from gr import scenes as sc
+
+pytestmark = pytest.mark.gpu
+
+
+def mean_rel_err(a, b):
+    """Mean per-pixel relative error, with a floor of 1% of the image mean for
+    near-black pixels."""
+    floor = 0.01 * max(float(np.mean(np.abs(b))), 1e-6)
+    return float(np.mean(np.abs(a - b) / np.maximum(np.abs(b), floor)))
+
+
+# Tolerance for images rendered with identical seeds (GPU vs oracle).
+IMAGE_TOL = 1e-3
+
+
+def test_cornell_matches_oracle(ctx, oracle):
+    d = sc.cornell_box(64, 64)
+    s = gr.Scene(ctx, d)
+    img, st = s.render(16, max_depth=8, seed=7)
+    ref = oracle.render(d, 16, max_depth=8, seed=7) / 16.0
+    assert np.isfinite(img).all()
+    err = mean_rel_err(img, ref)
+    assert err < IMAGE_TOL, err
+    assert st.closest_rays >= 64 * 64 * 16 and st.shadow_rays > 0 and st.device_errors == 0
+
+
+@pytest.mark.parametrize("flags", [0, gr.RENDER_REFERENCE_COMPAT])
+def test_glossy_matches_oracle(ctx, oracle, flags):
+    d = sc.glossy_scene(96, 72, level=3, glass_level=2)
+    s = gr.Scene(ctx, d)
+    img, _ = s.render(8, max_depth=16, seed=3, rr_depth=3, flags=flags)
+    ref = oracle.render(d, 8, max_depth=16, seed=3, rr_depth=3, flags=flags) / 8.0
+    err = mean_rel_err(img, ref)
+    assert err < IMAGE_TOL, err
+
+
+def test_progressive_equals_single_call(ctx):
+    d = sc.cornell_box(48, 40)
+    a = gr.Scene(ctx, d)
+    a.render(3, max_depth=6, seed=11, want_image=False)
+    a.render(5, max_depth=6, seed=11, want_image=False)
+    b = gr.Scene(ctx, d)
+    b.render(8, max_depth=6, seed=11, want_image=False)
+    sa, ca = a.accumulation()
+    sb, cb = b.accumulation()
+    np.testing.assert_array_equal(ca, cb)
+    np.testing.assert_array_equal(sa, sb)
+
+
+def test_wave_size_does_not_change_the_image(ctx):
+    d = sc.cornell_box(40, 40)
+    a = gr.Scene(ctx, d)
+    a.render(6, max_depth=8, seed=5, wave_paths=40 * 40, want_image=False)  # one sample per wave
+    b = gr.Scene(ctx, d)
+    b.render(6, max_depth=8, seed=5, want_image=False)  # all six in one wave
+    np.testing.assert_array_equal(a.accumulation()[0], b.accumulation()[0])
+
+
+def test_reset_restarts_the_sequence(ctx):
+    d = sc.cornell_box(32, 32)
+    a = gr.Scene(ctx, d)
+    img1, _ = a.render(4, seed=2)
+    a.reset()
+    img2, _ = a.render(4, seed=2)
+    np.testing.assert_array_equal(img1, img2)
+
+
+def test_converged_rmse(ctx):
+    """RMSE against a 16,384-spp render falls like 1/sqrt(spp) and meets a
+    stated bound at 1,024 spp."""
+    d = sc.cornell_box(32, 32)
+    ref_scene = gr.Scene(ctx, d)
+    ref, _ = ref_scene.render(16384, max_depth=8, seed=1000)
+    errs = {}
+    for spp in (64, 1024):
+        s = gr.Scene(ctx, d)
+        img, _ = s.render(spp, max_depth=8, seed=spp)
+        errs[spp] = float(np.sqrt(np.mean((img - ref) ** 2)))
+    ratio = errs[64] / errs[1024]
+    assert 2.5 < ratio < 6.5, errs  # ideal 4
+    assert errs[1024] < 0.05 * float(ref.mean()) * 4, errs
