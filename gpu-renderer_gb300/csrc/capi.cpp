@@ -30,6 +30,8 @@ void DevBuf::release() {
 void context_free(gr_ctx* ctx) {
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->batch_pool && ctx->batch_pool_free) ctx->batch_pool_free(ctx->batch_pool);
+    ctx->batch_pool = nullptr;
     ctx->counter.release();
     ctx->stage_in.release();
     ctx->stage_out.release();

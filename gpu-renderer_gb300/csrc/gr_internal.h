@@ -109,6 +109,8 @@ struct gr_ctx {
     std::string last_error;
     gr::DevBuf counter;  // traversal work counter (offset 0) + error word (offset 64)
     gr::DevBuf stage_in, stage_out;  // device staging for the host-memory entry points
+    void* batch_pool = nullptr;          // wave pool of gr_render_batch (owned; freed with the context)
+    void (*batch_pool_free)(void*) = nullptr;
 };
 
 namespace gr {

@@ -16,6 +16,8 @@
 // the resolve adds paths to their pixel in sample order, so the image does not
 // depend on queue order, wave size, or what else is rendered alongside.
 #include <algorithm>
+#include <cstddef>
+#include <cstring>
 
 #include "render.h"
 #include "shading.cuh"
@@ -181,7 +183,7 @@ __device__ __forceinline__ float tri_area(const SceneDev& sc, uint32_t prim) {
     return sqrtf(dot(c, c)) * 0.5f;
 }
 
-__device__ __forceinline__ void add_acc(Paths& ps, uint32_t pid, V3 L) {
+__device__ __forceinline__ void add_acc(const Paths& ps, uint32_t pid, V3 L) {
     float4 a = ps.acc[pid];
     a.x += L.x;
     a.y += L.y;
@@ -189,18 +191,36 @@ __device__ __forceinline__ void add_acc(Paths& ps, uint32_t pid, V3 L) {
     ps.acc[pid] = a;
 }
 
+// ---- job lookup ---------------------------------------------------------------------
+// Jobs are packed in path-id order; the job of a path id is found by binary
+// search over the per-job path bases staged in shared memory.
+__device__ __forceinline__ uint32_t find_job(const uint32_t* s_base, uint32_t njobs, uint32_t x) {
+    uint32_t lo = 0, hi = njobs;  // s_base[lo] <= x < s_base[hi] (s_base[njobs] = total)
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (s_base[mid] <= x) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
 // ---- camera rays (generate_primary_rays_kernel, pathtracer_kernel.h:59-104) ------
-__global__ void __launch_bounds__(kShadeThreads) k_camera(SceneDev sc, Paths ps, RenderParams rp) {
+__global__ void __launch_bounds__(kShadeThreads) k_camera(Paths ps) {
+    __shared__ uint32_t s_base[kMaxJobs + 1];
     const WaveHeader h = *ps.hdr;
-    const uint32_t P = h.wave_samples * rp.npix;
+    for (uint32_t j = threadIdx.x; j < h.njobs; j += blockDim.x) s_base[j] = ps.jobs[j].path_base;
+    if (threadIdx.x == 0) s_base[h.njobs] = h.total_paths;
+    __syncthreads();
     const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t pid = blockIdx.x * blockDim.x + threadIdx.x; pid < P; pid += stride) {
-        const uint32_t pixel = pid % rp.npix;
-        const uint32_t s = h.sample_base + pid / rp.npix;
+    for (uint32_t pid = blockIdx.x * blockDim.x + threadIdx.x; pid < h.total_paths; pid += stride) {
+        const uint32_t j = find_job(s_base, h.njobs, pid);
+        const JobDev& J = ps.jobs[j];
+        const uint32_t local = pid - J.path_base;
+        const uint32_t pixel = local % J.npix;
+        const uint32_t s = J.sample_base + local / J.npix;
         const uint64_t inc = pcg_inc(pixel);
-        uint64_t st = pcg_seed(rp.seed + (uint64_t)s * 0x9E3779B97F4A7C15ull, inc);
+        uint64_t st = pcg_seed(J.seed + (uint64_t)s * 0x9E3779B97F4A7C15ull, inc);
         const float j0 = pcg_float(st, inc), j1 = pcg_float(st, inc);
-        const DevCamera& c = sc.cam;
+        const DevCamera& c = J.sc.cam;
         const float rx = (float)(pixel % c.width) + j0;
         const float ry = (float)(pixel / c.width) + j1;
         const V3 dc = normalize(v3((1.0f - 2.0f * rx / (float)c.width) * c.tan_half,
@@ -213,64 +233,72 @@ __global__ void __launch_bounds__(kShadeThreads) k_camera(SceneDev sc, Paths ps,
         ps.thr[pid] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
         ps.acc[pid] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         ps.flags[pid] = 0;
+        ps.job[pid] = j;
         ps.rng[pid] = st;
         ps.qa[pid] = pid;
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) ps.cnt[0] = P;
+    if (blockIdx.x == 0 && threadIdx.x == 0) ps.cnt[0] = h.total_paths;
 }
 
 // ---- traversal over queues ----------------------------------------------------------
 struct QueueSrc {
     const uint32_t* __restrict__ q;
-    const float4* __restrict__ ray;
-    float4* __restrict__ hit;
+    const Paths* ps;
     uint64_t n;
-    __device__ __forceinline__ void load(uint64_t i, float4& r0, float4& r1) const {
+    __device__ __forceinline__ uint32_t load(uint64_t i, float4& r0, float4& r1, const Node*& nd, const Tri*& tr) const {
         const uint32_t pid = q[i];
-        r0 = ray[2ull * pid];
-        r1 = ray[2ull * pid + 1];
+        r0 = ps->ray[2ull * pid];
+        r1 = ps->ray[2ull * pid + 1];
+        const SceneDev& sc = ps->jobs[ps->job[pid]].sc;
+        nd = sc.nodes;
+        tr = sc.tris;
+        return sc.meta->root;
     }
     __device__ __forceinline__ void finish(uint64_t i, const trav::Lane& L) const {
         const uint32_t pid = q[i];
-        hit[pid] = L.best_prim == 0xFFFFFFFFu ? make_float4(L.p.tmax, __int_as_float(-1), 0.0f, 0.0f)
-                                              : make_float4(L.best_t, __uint_as_float(L.best_prim), L.bu, L.bv);
+        ps->hit[pid] = L.best_prim == 0xFFFFFFFFu ? make_float4(L.p.tmax, __int_as_float(-1), 0.0f, 0.0f)
+                                                  : make_float4(L.best_t, __uint_as_float(L.best_prim), L.bu, L.bv);
     }
 };
 
-__global__ void __launch_bounds__(trav::kTraceThreads) k_trace_queue(SceneDev sc, Paths ps, int b) {
+__global__ void __launch_bounds__(trav::kTraceThreads) k_trace_queue(Paths ps, int b) {
     __shared__ int2 s_stack[trav::kShortStack][trav::kTraceThreads];
-    QueueSrc src{(b & 1) ? ps.qb : ps.qa, ps.ray, ps.hit, ps.cnt[b]};
-    trav::traverse_loop<false>(sc.nodes, sc.tris, sc.meta->root, src, ps.work + b, ps.cnt + kErrWord, s_stack);
+    if (b > (int)ps.hdr->max_depth) return;
+    QueueSrc src{(b & 1) ? ps.qb : ps.qa, &ps, ps.cnt[b]};
+    trav::traverse_loop<false>(src, ps.work + b, ps.cnt + kErrWord, s_stack);
 }
 
 // Shadow rays: an unoccluded ray adds its contribution to its path
 // (accumulate_light_sampling_contribution_kernel, pathtracer_kernel.h:642-664).
 struct ShadowSrc {
-    const float4* __restrict__ sray;
-    const float4* __restrict__ scon;
-    float4* acc;
+    const Paths* ps;
     uint64_t n;
-    __device__ __forceinline__ void load(uint64_t i, float4& r0, float4& r1) const {
-        r0 = sray[2 * i];
-        r1 = sray[2 * i + 1];
+    __device__ __forceinline__ uint32_t load(uint64_t i, float4& r0, float4& r1, const Node*& nd, const Tri*& tr) const {
+        r0 = ps->sray[2 * i];
+        r1 = ps->sray[2 * i + 1];
+        const uint32_t pid = __float_as_uint(ps->scon[i].w);
+        const SceneDev& sc = ps->jobs[ps->job[pid]].sc;
+        nd = sc.nodes;
+        tr = sc.tris;
+        return sc.meta->root;
     }
     __device__ __forceinline__ void finish(uint64_t i, const trav::Lane& L) const {
         if (L.best_prim != 0xFFFFFFFFu) return;
-        const float4 c = scon[i];
+        const float4 c = ps->scon[i];
         const uint32_t pid = __float_as_uint(c.w);
-        float4 a = acc[pid];
+        float4 a = ps->acc[pid];
         a.x += c.x;
         a.y += c.y;
         a.z += c.z;
-        acc[pid] = a;
+        ps->acc[pid] = a;
     }
 };
 
-__global__ void __launch_bounds__(trav::kTraceThreads) k_trace_shadow(SceneDev sc, Paths ps, int b) {
+__global__ void __launch_bounds__(trav::kTraceThreads) k_trace_shadow(Paths ps, int b) {
     __shared__ int2 s_stack[trav::kShortStack][trav::kTraceThreads];
-    ShadowSrc src{ps.sray, ps.scon, ps.acc, ps.cnt[kShadowBase + b]};
-    trav::traverse_loop<true>(sc.nodes, sc.tris, sc.meta->root, src, ps.work + kShadowBase + b, ps.cnt + kErrWord,
-                              s_stack);
+    if (b >= (int)ps.hdr->max_depth) return;
+    ShadowSrc src{&ps, ps.cnt[kShadowBase + b]};
+    trav::traverse_loop<true>(src, ps.work + kShadowBase + b, ps.cnt + kErrWord, s_stack);
 }
 
 // ---- shading --------------------------------------------------------------------------
@@ -278,12 +306,12 @@ __global__ void __launch_bounds__(trav::kTraceThreads) k_trace_shadow(SceneDev s
 // emission of a BSDF-sampled light hit, then Russian roulette:
 // accumulate_BSDF_sampling_contribution_kernel, pathtracer_kernel.h:684-749),
 // then shades the surviving hits (shade_hit_with_MIS_kernel, :488-628).
-// Step b == max_depth only finishes.
-__global__ void __launch_bounds__(kShadeThreads) k_shade(SceneDev sc, Paths ps, RenderParams rp, int b) {
+// Step b == the job's max_depth only finishes.
+__global__ void __launch_bounds__(kShadeThreads) k_shade(Paths ps, int b) {
+    if (b > (int)ps.hdr->max_depth) return;
     const uint32_t n = ps.cnt[b];
     const uint32_t* q = (b & 1) ? ps.qb : ps.qa;
     uint32_t* qn = (b & 1) ? ps.qa : ps.qb;
-    const bool compat = (rp.flags & GR_RENDER_REFERENCE_COMPAT) != 0;
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
         const uint32_t i = base + threadIdx.x;
@@ -294,7 +322,10 @@ __global__ void __launch_bounds__(kShadeThreads) k_shade(SceneDev sc, Paths ps, 
         uint32_t new_flags = 0;
         if (i < n) {
             pid = q[i];
-            const uint32_t pixel = pid % rp.npix;
+            const JobDev& J = ps.jobs[ps.job[pid]];
+            const SceneDev& sc = J.sc;
+            const bool compat = (J.flags & GR_RENDER_REFERENCE_COMPAT) != 0;
+            const uint32_t pixel = (pid - J.path_base) % J.npix;
             const uint64_t inc = pcg_inc(pixel);
             uint64_t st = ps.rng[pid];
             const float4 r0 = ps.ray[2ull * pid], r1 = ps.ray[2ull * pid + 1];
@@ -304,9 +335,9 @@ __global__ void __launch_bounds__(kShadeThreads) k_shade(SceneDev sc, Paths ps, 
             V3 thr = v3(th.x, th.y, th.z);
             const V3 rd = v3(r0.w, r1.x, r1.y);
             const int32_t prim = __float_as_int(hv.y);
-            bool alive = true;
+            bool alive = b <= (int)J.max_depth;
             bool as_miss = false;
-            if (b > 0) {
+            if (alive && b > 0) {
                 const float rr = pcg_float(st, inc);
                 if (prim >= 0 && !(flags & kFlagSpecular)) {
                     const DevMaterial* lm = sc.mats + (sc.tri_mat[prim] & 0x7FFFFFFFu);
@@ -320,7 +351,7 @@ __global__ void __launch_bounds__(kShadeThreads) k_shade(SceneDev sc, Paths ps, 
                         add_acc(ps, pid, thr * Le * w);
                     }
                 }
-                if (rp.rr_depth >= 0 && (int)(b - 1) > rp.rr_depth && maxc(thr) < 1.0f) {
+                if (J.rr_depth >= 0 && (int)(b - 1) > J.rr_depth && maxc(thr) < 1.0f) {
                     const float qk = fmaxf(0.05f, 1.0f - maxc(thr));
                     if (rr < qk) {
                         if (compat) as_miss = true; else alive = false;
@@ -329,7 +360,7 @@ __global__ void __launch_bounds__(kShadeThreads) k_shade(SceneDev sc, Paths ps, 
                     }
                 }
             }
-            if (alive && b < (int)rp.max_depth) {
+            if (alive && b < (int)J.max_depth) {
                 float s[8];
 #pragma unroll
                 for (int k = 0; k < 8; ++k) s[k] = pcg_float(st, inc);
@@ -407,41 +438,182 @@ __global__ void __launch_bounds__(kShadeThreads) k_shade(SceneDev sc, Paths ps, 
 }
 
 // ---- resolve: paths -> pixels in sample order ------------------------------------------
-__global__ void __launch_bounds__(kShadeThreads) k_resolve(Paths ps, RenderParams rp, double* fb, uint32_t* fbc) {
+__global__ void __launch_bounds__(kShadeThreads) k_resolve(Paths ps) {
+    __shared__ uint32_t s_base[kMaxJobs + 1];
     const WaveHeader h = *ps.hdr;
+    for (uint32_t j = threadIdx.x; j < h.njobs; j += blockDim.x) s_base[j] = ps.jobs[j].pix_base;
+    if (threadIdx.x == 0) s_base[h.njobs] = h.total_pix;
+    __syncthreads();
     const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t px = blockIdx.x * blockDim.x + threadIdx.x; px < rp.npix; px += stride) {
-        double r = fb[3ull * px], g = fb[3ull * px + 1], bl = fb[3ull * px + 2];
-        for (uint32_t s = 0; s < h.wave_samples; ++s) {
-            const float4 a = ps.acc[(size_t)s * rp.npix + px];
-            r += (double)a.x;
-            g += (double)a.y;
-            bl += (double)a.z;
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < h.total_pix; r += stride) {
+        const JobDev& J = ps.jobs[find_job(s_base, h.njobs, r)];
+        const uint32_t px = r - J.pix_base;
+        double* f = J.fb + 3ull * px;
+        double cr = f[0], cg = f[1], cb = f[2];
+        for (uint32_t s = 0; s < J.wave_samples; ++s) {
+            const float4 a = ps.acc[J.path_base + (size_t)s * J.npix + px];
+            cr += (double)a.x;
+            cg += (double)a.y;
+            cb += (double)a.z;
         }
-        fb[3ull * px] = r;
-        fb[3ull * px + 1] = g;
-        fb[3ull * px + 2] = bl;
-        fbc[px] += h.wave_samples;
+        f[0] = cr;
+        f[1] = cg;
+        f[2] = cb;
+        J.fbc[px] += J.wave_samples;
     }
 }
 
-__global__ void k_wave_end(Paths ps, RenderParams rp) {
+__global__ void k_wave_end(Paths ps) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     WaveHeader* h = ps.hdr;
     unsigned long long c = 0, sh = 0;
-    for (uint32_t b = 0; b <= rp.max_depth; ++b) c += ps.cnt[b];
-    for (uint32_t b = 0; b < rp.max_depth; ++b) sh += ps.cnt[kShadowBase + b];
+    for (uint32_t b = 0; b <= h->max_depth; ++b) c += ps.cnt[b];
+    for (uint32_t b = 0; b < h->max_depth; ++b) sh += ps.cnt[kShadowBase + b];
     h->closest_rays += c;
     h->shadow_rays += sh;
-    h->sample_base += h->wave_samples;
-    h->remaining -= h->wave_samples;
-    h->wave_samples = min(h->max_wave, h->remaining);
 }
+
+// One wave: clear counters, camera rays, kMaxWaveDepth x (trace, shade, shadow)
+// (steps past the wave's max_depth return at once), resolve, ray counts.
+cudaError_t issue_wave(const Paths& ps, uint32_t depth_steps, int tgrid, int sgrid, cudaStream_t s) {
+    cudaError_t e;
+    const size_t cnt_bytes = sizeof(uint32_t) * (2 * kMaxDepth + 4);
+    const size_t work_bytes = sizeof(unsigned long long) * (2 * kMaxDepth + 4);
+    if ((e = cudaMemsetAsync(ps.cnt, 0, cnt_bytes, s)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(ps.work, 0, work_bytes, s)) != cudaSuccess) return e;
+    k_camera<<<sgrid, kShadeThreads, 0, s>>>(ps);
+    for (int b = 0; b <= (int)depth_steps; ++b) {
+        k_trace_queue<<<tgrid, trav::kTraceThreads, 0, s>>>(ps, b);
+        k_shade<<<sgrid, kShadeThreads, 0, s>>>(ps, b);
+        if (b < (int)depth_steps) k_trace_shadow<<<tgrid, trav::kTraceThreads, 0, s>>>(ps, b);
+    }
+    k_resolve<<<sgrid, kShadeThreads, 0, s>>>(ps);
+    k_wave_end<<<1, 32, 0, s>>>(ps);
+    return cudaGetLastError();
+}
+
+uint64_t mix64(uint64_t h, uint64_t v) {
+    h ^= v + 0x9E3779B97F4A7C15ull + (h << 6) + (h >> 2);
+    return h;
+}
+
+size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+size_t path_layout(uint32_t cap, char* base, Paths* ps) {
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        char* p = base ? base + off : nullptr;
+        off += align256(bytes);
+        return p;
+    };
+    const size_t c = cap;
+    ps->ray = (float4*)take(32 * c);
+    ps->hit = (float4*)take(16 * c);
+    ps->thr = (float4*)take(16 * c);
+    ps->acc = (float4*)take(16 * c);
+    ps->flags = (uint32_t*)take(4 * c);
+    ps->job = (uint32_t*)take(4 * c);
+    ps->rng = (unsigned long long*)take(8 * c);
+    ps->qa = (uint32_t*)take(4 * c);
+    ps->qb = (uint32_t*)take(4 * c);
+    ps->sray = (float4*)take(32 * c);
+    ps->scon = (float4*)take(16 * c);
+    ps->cnt = (uint32_t*)take(sizeof(uint32_t) * (2 * kMaxDepth + 8));
+    ps->work = (unsigned long long*)take(sizeof(unsigned long long) * (2 * kMaxDepth + 4));
+    ps->hdr = (WaveHeader*)take(sizeof(WaveHeader));
+    ps->jobs = (JobDev*)take(sizeof(JobDev) * kMaxJobs);
+    ps->capacity = cap;
+    return off;
+}
+
+// The wave always runs this many bounce steps; steps past the wave's own
+// max_depth return immediately, so one captured graph serves every wave.
+constexpr uint32_t kGraphDepthSteps = 16;
 
 }  // namespace
 
-cudaError_t render_waves(const SceneDev& sc, Paths& ps, const RenderParams& rp, double* fb, uint32_t* fb_count,
-                         uint32_t waves, int num_sms, cudaStream_t s) {
+void WaveGraph::release() {
+    if (exec) cudaGraphExecDestroy(exec);
+    exec = nullptr;
+    key = 0;
+}
+
+void WavePool::release() {
+    graph.release();
+    for (int i = 0; i < kSlots; ++i)
+        if (ev[i]) {
+            cudaEventSynchronize(ev[i]);
+            cudaEventDestroy(ev[i]);
+            ev[i] = nullptr;
+        }
+    if (h_jobs) cudaFreeHost(h_jobs);
+    if (h_hdr) cudaFreeHost(h_hdr);
+    h_jobs = nullptr;
+    h_hdr = nullptr;
+    mem.release();
+    capacity = 0;
+}
+
+cudaError_t WavePool::ensure(uint32_t paths) {
+    cudaError_t e;
+    if (!h_jobs) {
+        if ((e = cudaMallocHost((void**)&h_jobs, sizeof(JobDev) * kMaxJobs * kSlots)) != cudaSuccess) return e;
+        if ((e = cudaMallocHost((void**)&h_hdr, sizeof(WaveHeader) * kSlots)) != cudaSuccess) return e;
+        for (int i = 0; i < kSlots; ++i)
+            if ((e = cudaEventCreateWithFlags(&ev[i], cudaEventDisableTiming)) != cudaSuccess) return e;
+    }
+    if (paths <= capacity && mem.p) return cudaSuccess;
+    graph.release();  // a captured wave points into the old path memory
+    Paths p;
+    const size_t bytes = path_layout(paths, nullptr, &p);
+    e = mem.ensure(bytes);
+    if (e != cudaSuccess) {
+        capacity = 0;
+        return e;
+    }
+    path_layout(paths, (char*)mem.p, &ps);
+    capacity = paths;
+    if ((e = cudaMemset(ps.hdr, 0, sizeof(WaveHeader))) != cudaSuccess) return e;
+    return cudaMemset(ps.cnt + kErrWord, 0, 4);
+}
+
+uint32_t pack_wave(std::vector<HostJob*>& jobs, uint32_t capacity, std::vector<JobDev>& out, uint32_t* total_paths,
+                   uint32_t* total_pix, uint32_t* max_depth) {
+    out.clear();
+    uint32_t paths = 0, pix = 0, depth = 0;
+    for (HostJob* j : jobs) {
+        if (out.size() >= kMaxJobs) break;
+        if (j->spp_done >= j->spp_total) continue;
+        const uint32_t free_paths = capacity - paths;
+        uint32_t take = std::min(j->spp_total - j->spp_done, free_paths / j->npix);
+        if (take == 0) continue;
+        JobDev d;
+        d.sc = j->sc;
+        d.fb = j->fb;
+        d.fbc = j->fbc;
+        d.path_base = paths;
+        d.npix = j->npix;
+        d.pix_base = pix;
+        d.wave_samples = take;
+        d.sample_base = j->sample_offset + j->spp_done;
+        d.max_depth = j->max_depth;
+        d.rr_depth = j->rr_depth;
+        d.flags = j->flags;
+        d.seed = j->seed;
+        out.push_back(d);
+        paths += take * j->npix;
+        pix += j->npix;
+        depth = std::max(depth, j->max_depth);
+        j->spp_done += take;
+    }
+    *total_paths = paths;
+    *total_pix = pix;
+    *max_depth = depth;
+    return (uint32_t)out.size();
+}
+
+cudaError_t run_wave(WavePool& pool, const JobDev* h_jobs, uint32_t njobs, uint32_t total_paths, uint32_t total_pix,
+                     uint32_t max_depth, int num_sms, cudaStream_t s, bool use_graph) {
     static int occ = 0;
     cudaError_t e;
     if (occ == 0) {
@@ -450,23 +622,54 @@ cudaError_t render_waves(const SceneDev& sc, Paths& ps, const RenderParams& rp, 
             return e;
         occ = std::max(occ, 1);
     }
+    if (njobs == 0 || njobs > kMaxJobs || total_paths > pool.capacity || max_depth > (uint32_t)kMaxDepth)
+        return cudaErrorInvalidValue;
+    const Paths& ps = pool.ps;
+    const int slot = pool.slot;
+    pool.slot = (pool.slot + 1) % WavePool::kSlots;
+    if ((e = cudaEventSynchronize(pool.ev[slot])) != cudaSuccess) return e;
+    JobDev* stage = pool.h_jobs + (size_t)slot * kMaxJobs;
+    std::memcpy(stage, h_jobs, sizeof(JobDev) * njobs);
+    WaveHeader& h = pool.h_hdr[slot];
+    h = WaveHeader{};
+    h.njobs = njobs;
+    h.total_paths = total_paths;
+    h.total_pix = total_pix;
+    h.max_depth = max_depth;
+    if ((e = cudaMemcpyAsync(ps.jobs, stage, sizeof(JobDev) * njobs, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+        return e;
+    // the header's running ray totals stay on the device; only the wave fields are written
+    if ((e = cudaMemcpyAsync(ps.hdr, &h, offsetof(WaveHeader, closest_rays), cudaMemcpyHostToDevice, s)) != cudaSuccess)
+        return e;
+    if ((e = cudaEventRecord(pool.ev[slot], s)) != cudaSuccess) return e;
     const int tgrid = num_sms * occ;
     const int sgrid = num_sms * 4;
-    const size_t cnt_bytes = sizeof(uint32_t) * (2 * kMaxDepth + 8);
-    const size_t work_bytes = sizeof(unsigned long long) * (2 * kMaxDepth + 4);
-    for (uint32_t w = 0; w < waves; ++w) {
-        if ((e = cudaMemsetAsync(ps.cnt, 0, cnt_bytes, s)) != cudaSuccess) return e;
-        if ((e = cudaMemsetAsync(ps.work, 0, work_bytes, s)) != cudaSuccess) return e;
-        k_camera<<<sgrid, kShadeThreads, 0, s>>>(sc, ps, rp);
-        for (int b = 0; b <= (int)rp.max_depth; ++b) {
-            k_trace_queue<<<tgrid, trav::kTraceThreads, 0, s>>>(sc, ps, b);
-            k_shade<<<sgrid, kShadeThreads, 0, s>>>(sc, ps, rp, b);
-            if (b < (int)rp.max_depth) k_trace_shadow<<<tgrid, trav::kTraceThreads, 0, s>>>(sc, ps, b);
+    const uint32_t steps = std::max(max_depth, kGraphDepthSteps);
+    if (!use_graph) return issue_wave(ps, max_depth, tgrid, sgrid, s);
+    uint64_t key = 0x51ED270B27A3C1F5ull;
+    const uint64_t words[] = {(uint64_t)(uintptr_t)ps.ray, ps.capacity, steps, (uint64_t)tgrid, (uint64_t)sgrid};
+    for (uint64_t w : words) key = mix64(key, w);
+    WaveGraph& g = pool.graph;
+    if (!g.exec || g.key != key) {
+        g.release();
+        cudaGraph_t graph = nullptr;
+        if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return e;
+        const cudaError_t ei = issue_wave(ps, steps, tgrid, sgrid, s);
+        e = cudaStreamEndCapture(s, &graph);
+        if (ei != cudaSuccess) {
+            if (graph) cudaGraphDestroy(graph);
+            return ei;
         }
-        k_resolve<<<sgrid, kShadeThreads, 0, s>>>(ps, rp, fb, fb_count);
-        k_wave_end<<<1, 32, 0, s>>>(ps, rp);
+        if (e != cudaSuccess) return e;
+        e = cudaGraphInstantiate(&g.exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) {
+            g.exec = nullptr;
+            return e;
+        }
+        g.key = key;
     }
-    return cudaGetLastError();
+    return cudaGraphLaunch(g.exec, s);
 }
 
 }  // namespace gr

@@ -29,6 +29,9 @@ struct DevCamera {
     uint32_t width, height;
 };
 
+// Camera::setup (camera.h:21-38) from the C-ABI record.
+DevCamera make_camera(const gr_camera& c);
+
 // Everything a shading or traversal kernel needs about one scene.
 struct SceneDev {
     const float* verts;       // 9 floats per triangle, scene order
@@ -46,25 +49,45 @@ struct SceneDev {
     int32_t has_env;
 };
 
-// Per-wave header in device memory, updated on the device between waves so a
-// wave's launch sequence is identical every time (graph friendly).
-struct WaveHeader {
-    uint32_t sample_base;   // first sample index of this wave
-    uint32_t wave_samples;  // samples per pixel in this wave
-    uint32_t remaining;     // samples per pixel still to do, this wave included
-    uint32_t max_wave;      // samples per pixel per full wave
-    unsigned long long closest_rays, shadow_rays;
+constexpr int kMaxDepth = 64;
+constexpr uint32_t kMaxJobs = 1024;  // jobs in one wave
+
+// One render job in a wave: a scene, its accumulation target, and the slice
+// of the wave's path ids that render its samples. Paths of a job are
+// pid = path_base + s * npix + pixel for s < wave_samples.
+struct JobDev {
+    SceneDev sc;
+    double* fb;          // 3 doubles per pixel (running sums)
+    uint32_t* fbc;       // samples per pixel
+    uint32_t path_base;  // first path id of the job in this wave
+    uint32_t npix;
+    uint32_t pix_base;   // first resolve slot of the job in this wave
+    uint32_t wave_samples;
+    uint32_t sample_base;  // sample index of the job's first sample in this wave
+    uint32_t max_depth;
+    int32_t rr_depth;
+    uint32_t flags;
+    uint64_t seed;
 };
 
-constexpr int kMaxDepth = 64;
+// Device-resident description of the current wave (written by the host
+// before each wave; the captured kernel sequence reads it).
+struct WaveHeader {
+    uint32_t njobs;
+    uint32_t total_paths;
+    uint32_t total_pix;
+    uint32_t max_depth;  // bounces the wave runs (max over its jobs)
+    unsigned long long closest_rays, shadow_rays;  // running totals
+};
 
-// Path state for one wave, indexed by path id pid = s * npix + pixel.
+// Path state for one wave, indexed by path id.
 struct Paths {
     float4* ray;    // 2 per path: (o.xyz, d.x), (d.y, d.z, tmin, tmax)
     float4* hit;    // (t, prim bits, u, v)
     float4* thr;    // (throughput rgb, pdf of the last BSDF sample)
     float4* acc;    // (radiance rgb, 0)
     uint32_t* flags;
+    uint32_t* job;  // job of each path
     unsigned long long* rng;
     uint32_t* qa;   // path-id queues, ping-pong by bounce
     uint32_t* qb;
@@ -73,19 +96,64 @@ struct Paths {
     uint32_t* cnt;  // [0, kMaxDepth]: closest queue sizes; [kMaxDepth+1, ...]: shadow queue sizes
     unsigned long long* work;  // dynamic-fetch counters, one per trace launch of a wave
     WaveHeader* hdr;
+    JobDev* jobs;   // kMaxJobs entries
     uint32_t capacity;
 };
 
-struct RenderParams {
+// A captured wave (CUDA graph), reused while its key (pointers, sizes) is
+// unchanged. The wave's contents (jobs, counts) live in device memory.
+struct WaveGraph {
+    cudaGraphExec_t exec = nullptr;
+    uint64_t key = 0;
+    void release();
+    ~WaveGraph() { release(); }
+};
+
+// Path memory, job staging and the captured wave of one renderer (a scene's
+// own gr_render, or a server).
+struct WavePool {
+    static constexpr int kSlots = 4;
+    DevBuf mem;
+    Paths ps{};
+    uint32_t capacity = 0;
+    WaveGraph graph;
+    // pinned staging for the per-wave job table and header, one slot per wave
+    // in flight; a slot is rewritten only after its event has completed
+    JobDev* h_jobs = nullptr;
+    WaveHeader* h_hdr = nullptr;
+    cudaEvent_t ev[kSlots] = {};
+    int slot = 0;
+    cudaError_t ensure(uint32_t paths);
+    void release();
+    ~WavePool() { release(); }
+};
+
+// Host-side view of one job for the wave scheduler.
+struct HostJob {
+    SceneDev sc;
+    double* fb;
+    uint32_t* fbc;
+    uint32_t npix;
+    uint32_t spp_total;
+    uint32_t spp_done;  // samples already scheduled
+    uint32_t sample_offset;  // sample index of this job's sample 0
     uint32_t max_depth;
     int32_t rr_depth;
     uint32_t flags;
     uint64_t seed;
-    uint32_t npix;
 };
 
-cudaError_t render_waves(const SceneDev& sc, Paths& ps, const RenderParams& rp, double* fb, uint32_t* fb_count,
-                         uint32_t waves, int num_sms, cudaStream_t s);
+// Runs one wave over `jobs` (already packed by the caller: path_base, pix_base,
+// wave_samples, sample_base filled in). Uses the pool's captured graph unless
+// use_graph is false.
+cudaError_t run_wave(WavePool& pool, const JobDev* h_jobs, uint32_t njobs, uint32_t total_paths, uint32_t total_pix,
+                     uint32_t max_depth, int num_sms, cudaStream_t s, bool use_graph);
+
+// Packs as many samples of `jobs` (in order) as fit into `capacity` paths;
+// returns the number of jobs in the wave (0 when nothing fits). Advances
+// spp_done of the scheduled jobs.
+uint32_t pack_wave(std::vector<HostJob*>& jobs, uint32_t capacity, std::vector<JobDev>& out, uint32_t* total_paths,
+                   uint32_t* total_pix, uint32_t* max_depth);
 
 }  // namespace gr
 
@@ -95,8 +163,7 @@ struct gr_scene {
     uint32_t num_tris = 0, num_lights = 0;
     gr::DevBuf verts, normals, tri_mat, mats, lights;
     gr::DevBuf fb, fb_count;
-    gr::DevBuf path_mem;
-    uint32_t path_capacity = 0;
+    gr::WavePool pool;
     uint32_t samples_done = 0;
     gr::DevCamera cam{};
     float env[3] = {0, 0, 0};

@@ -17,6 +17,24 @@
 
 #include "render.h"
 
+namespace gr {
+
+DevCamera make_camera(const gr_camera& camera) {
+    // Camera::setup (camera.h:21-38); degToRad (fwd.h:28-31)
+    DevCamera c{};
+    const float* M = camera.to_world;
+    for (int r = 0; r < 3; ++r)
+        for (int k = 0; k < 4; ++k) c.m[4 * r + k] = M[4 * r + k];
+    const float fov = camera.fov_deg / 180.0f * 3.14159265358979323846f;
+    c.tan_half = std::tan(fov * 0.5f);
+    c.aspect = (float)camera.width / (float)camera.height;
+    c.width = camera.width;
+    c.height = camera.height;
+    return c;
+}
+
+}  // namespace gr
+
 namespace {
 
 gr_status fail(gr_ctx* ctx, gr_status st, const std::string& what) {
@@ -37,34 +55,6 @@ gr_status cuda_fail(gr_ctx* ctx, cudaError_t e, const char* where) {
     } while (0)
 
 bool emissive(const gr_material& m) { return m.emission[0] != 0.0f || m.emission[1] != 0.0f || m.emission[2] != 0.0f; }
-
-size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
-
-// Slices one allocation into the path-state arrays for `cap` paths.
-size_t path_layout(uint32_t cap, char* base, gr::Paths* ps) {
-    size_t off = 0;
-    auto take = [&](size_t bytes) {
-        char* p = base ? base + off : nullptr;
-        off += align256(bytes);
-        return p;
-    };
-    const size_t c = cap;
-    ps->ray = (float4*)take(32 * c);
-    ps->hit = (float4*)take(16 * c);
-    ps->thr = (float4*)take(16 * c);
-    ps->acc = (float4*)take(16 * c);
-    ps->flags = (uint32_t*)take(4 * c);
-    ps->rng = (unsigned long long*)take(8 * c);
-    ps->qa = (uint32_t*)take(4 * c);
-    ps->qb = (uint32_t*)take(4 * c);
-    ps->sray = (float4*)take(32 * c);
-    ps->scon = (float4*)take(16 * c);
-    ps->cnt = (uint32_t*)take(sizeof(uint32_t) * (2 * gr::kMaxDepth + 8));
-    ps->work = (unsigned long long*)take(sizeof(unsigned long long) * (2 * gr::kMaxDepth + 4));
-    ps->hdr = (gr::WaveHeader*)take(sizeof(gr::WaveHeader));
-    ps->capacity = cap;
-    return off;
-}
 
 gr::SceneDev scene_view(gr_scene* sc) {
     gr::SceneDev d{};
@@ -185,15 +175,7 @@ gr_status gr_scene_create(gr_ctx* ctx, const gr_mesh* meshes, uint32_t num_meshe
     if (st != GR_OK) return cleanup(st);
     if ((e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess) return cleanup(cuda_fail(ctx, e, "bvh build"));
 
-    // camera (Camera::setup, camera.h:21-38; degToRad, fwd.h:28-31)
-    const float* M = camera->to_world;
-    for (int r = 0; r < 3; ++r)
-        for (int c = 0; c < 4; ++c) sc->cam.m[4 * r + c] = M[4 * r + c];
-    const float fov = camera->fov_deg / 180.0f * 3.14159265358979323846f;
-    sc->cam.tan_half = std::tan(fov * 0.5f);
-    sc->cam.aspect = (float)camera->width / (float)camera->height;
-    sc->cam.width = camera->width;
-    sc->cam.height = camera->height;
+    sc->cam = gr::make_camera(*camera);
     if (env && env->enabled) {
         sc->has_env = 1;
         std::memcpy(sc->env, env->radiance, 12);
@@ -212,6 +194,7 @@ gr_status gr_scene_destroy(gr_scene* sc) {
     gr_ctx* ctx = sc->ctx;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
+    sc->pool.release();
     if (sc->bvh) gr_bvh_destroy(sc->bvh);
     delete sc;
     gr::ctx_release(ctx);
@@ -241,33 +224,36 @@ gr_status gr_render(gr_scene* sc, const gr_render_opts* opts, float* h_rgb, gr_r
     if (opts->spp) per_wave = std::min(per_wave, opts->spp);
     const uint64_t cap64 = (uint64_t)per_wave * npix;
     if (cap64 > 0xFFFFFFFFull / 2) return fail(ctx, GR_ERR_INVALID, "gr_render: wave too large");
-    const uint32_t cap = (uint32_t)cap64;
-    gr::Paths ps;
-    if (cap > sc->path_capacity) {
-        const size_t bytes = path_layout(cap, nullptr, &ps);
-        SC_CUDA(ctx, sc->path_mem.ensure(bytes));
-        sc->path_capacity = cap;
+    SC_CUDA(ctx, sc->pool.ensure((uint32_t)cap64));
+    gr::WaveHeader before{};
+    SC_CUDA(ctx, cudaMemcpyAsync(&before, sc->pool.ps.hdr, sizeof(before), cudaMemcpyDeviceToHost, s));
+    gr::HostJob job;
+    job.sc = scene_view(sc);
+    job.fb = (double*)sc->fb.p;
+    job.fbc = (uint32_t*)sc->fb_count.p;
+    job.npix = npix;
+    job.spp_total = opts->spp;
+    job.spp_done = 0;
+    job.sample_offset = sc->samples_done;
+    job.max_depth = opts->max_depth;
+    job.rr_depth = opts->rr_depth;
+    job.flags = opts->flags;
+    job.seed = opts->seed;
+    std::vector<gr::HostJob*> jobs{&job};
+    std::vector<gr::JobDev> table;
+    uint32_t waves = 0;
+    for (;;) {
+        uint32_t paths = 0, pix = 0, depth = 0;
+        const uint32_t nj = gr::pack_wave(jobs, (uint32_t)cap64, table, &paths, &pix, &depth);
+        if (nj == 0) break;
+        SC_CUDA(ctx, gr::run_wave(sc->pool, table.data(), nj, paths, pix, depth, ctx->num_sms, s,
+                                  (opts->flags & GR_RENDER_NO_GRAPH) == 0));
+        ++waves;
     }
-    path_layout(sc->path_capacity, (char*)sc->path_mem.p, &ps);
-    gr::WaveHeader hdr{};
-    hdr.sample_base = sc->samples_done;
-    hdr.max_wave = per_wave;
-    hdr.remaining = opts->spp;
-    hdr.wave_samples = std::min(per_wave, opts->spp);
-    SC_CUDA(ctx, cudaMemcpyAsync(ps.hdr, &hdr, sizeof(hdr), cudaMemcpyHostToDevice, s));
-    SC_CUDA(ctx, cudaMemsetAsync(ps.cnt + 2 * gr::kMaxDepth + 4, 0, 4, s));
-    gr::RenderParams rp;
-    rp.max_depth = opts->max_depth;
-    rp.rr_depth = opts->rr_depth;
-    rp.flags = opts->flags;
-    rp.seed = opts->seed;
-    rp.npix = npix;
-    const uint32_t waves = opts->spp ? (opts->spp + per_wave - 1) / per_wave : 0;
-    const gr::SceneDev view = scene_view(sc);
-    SC_CUDA(ctx, gr::render_waves(view, ps, rp, (double*)sc->fb.p, (uint32_t*)sc->fb_count.p, waves, ctx->num_sms, s));
-    SC_CUDA(ctx, cudaMemcpyAsync(&hdr, ps.hdr, sizeof(hdr), cudaMemcpyDeviceToHost, s));
+    gr::WaveHeader after{};
     uint32_t err = 0;
-    SC_CUDA(ctx, cudaMemcpyAsync(&err, ps.cnt + 2 * gr::kMaxDepth + 4, 4, cudaMemcpyDeviceToHost, s));
+    SC_CUDA(ctx, cudaMemcpyAsync(&after, sc->pool.ps.hdr, sizeof(after), cudaMemcpyDeviceToHost, s));
+    SC_CUDA(ctx, cudaMemcpyAsync(&err, sc->pool.ps.cnt + 2 * gr::kMaxDepth + 4, 4, cudaMemcpyDeviceToHost, s));
     SC_CUDA(ctx, cudaStreamSynchronize(s));
     sc->samples_done += opts->spp;
     if (h_rgb) {
@@ -282,8 +268,8 @@ gr_status gr_render(gr_scene* sc, const gr_render_opts* opts, float* h_rgb, gr_r
     }
     if (stats) {
         stats->ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-        stats->closest_rays = hdr.closest_rays;
-        stats->shadow_rays = hdr.shadow_rays;
+        stats->closest_rays = after.closest_rays - before.closest_rays;
+        stats->shadow_rays = after.shadow_rays - before.shadow_rays;
         stats->samples = (uint64_t)opts->spp * npix;
         stats->waves = waves;
         stats->device_errors = err;

@@ -1,0 +1,493 @@
+// Batched rendering and the render server (include/gr.h). The reference has
+// no counterpart: it renders one scene, one sample per call.
+//
+// Both drive the same wave machinery as gr_render (render.cu): jobs are packed
+// into waves of at most `capacity` paths, each wave's job table is staged and
+// the captured wave is replayed. Because a path's result depends only on its
+// scene, pixel and sample, and each job's pixels are resolved in sample order,
+// a job's image is identical whatever else shares its waves.
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <new>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "render.h"
+
+namespace {
+
+gr_status cuda_status(cudaError_t e) { return e == cudaErrorMemoryAllocation ? GR_ERR_OOM_BUDGET : GR_ERR_CUDA; }
+
+gr::SceneDev view_of(gr_scene* sc) {
+    gr::SceneDev d{};
+    d.verts = (const float*)sc->verts.p;
+    d.normals = (const float4*)sc->normals.p;
+    d.tri_mat = (const uint32_t*)sc->tri_mat.p;
+    d.mats = (const gr::DevMaterial*)sc->mats.p;
+    d.lights = (const uint32_t*)sc->lights.p;
+    d.num_lights = sc->num_lights;
+    d.num_tris = sc->num_tris;
+    d.nodes = (const gr::Node*)sc->bvh->buf.nodes.p;
+    d.tris = (const gr::Tri*)sc->bvh->buf.tris.p;
+    d.meta = (const gr::BvhMeta*)sc->bvh->buf.meta.p;
+    d.cam = sc->cam;
+    d.env_r = sc->env[0];
+    d.env_g = sc->env[1];
+    d.env_b = sc->env[2];
+    d.has_env = sc->has_env;
+    return d;
+}
+
+uint32_t default_capacity(uint32_t wave_paths) { return wave_paths ? wave_paths : (1u << 22); }
+
+// Per-pixel mean of an accumulation (for the server's results).
+void mean_image(const double* sum, const uint32_t* cnt, uint32_t npix, float* out) {
+    for (uint32_t p = 0; p < npix; ++p) {
+        const double inv = cnt[p] ? 1.0 / cnt[p] : 0.0;
+        for (int c = 0; c < 3; ++c) out[3ull * p + c] = (float)(sum[3ull * p + c] * inv);
+    }
+}
+
+}  // namespace
+
+extern "C" uint64_t gr_scene_device_bytes(const gr_scene* sc) {
+    if (!sc) return 0;
+    uint64_t b = sc->verts.bytes + sc->normals.bytes + sc->tri_mat.bytes + sc->mats.bytes + sc->lights.bytes +
+                 sc->fb.bytes + sc->fb_count.bytes + sc->pool.mem.bytes;
+    if (sc->bvh) {
+        const gr::BvhBuffers& bb = sc->bvh->buf;
+        b += bb.nodes.bytes + bb.tris.bytes + bb.code.bytes + bb.prim.bytes + bb.scratch.bytes + bb.meta.bytes;
+    }
+    return b;
+}
+
+extern "C" gr_status gr_render_batch(gr_ctx* ctx, gr_scene* const* scenes, const gr_render_opts* opts, uint32_t n,
+                                     uint32_t wave_paths, gr_render_stats* stats) {
+    if (!ctx || (n && (!scenes || !opts))) return GR_ERR_INVALID;
+    const auto t0 = std::chrono::steady_clock::now();
+    std::vector<gr::HostJob> jobs(n);
+    std::vector<gr::HostJob*> order;
+    uint32_t max_npix = 1;
+    for (uint32_t i = 0; i < n; ++i) {
+        gr_scene* sc = scenes[i];
+        if (!sc || sc->ctx != ctx || opts[i].max_depth > (uint32_t)gr::kMaxDepth) {
+            ctx->last_error = "gr_render_batch: bad job " + std::to_string(i);
+            return GR_ERR_INVALID;
+        }
+        for (uint32_t k = 0; k < i; ++k)
+            if (scenes[k] == sc) {
+                ctx->last_error = "gr_render_batch: a scene appears twice";
+                return GR_ERR_INVALID;
+            }
+        gr::HostJob& j = jobs[i];
+        j.sc = view_of(sc);
+        j.fb = (double*)sc->fb.p;
+        j.fbc = (uint32_t*)sc->fb_count.p;
+        j.npix = sc->cam.width * sc->cam.height;
+        j.spp_total = opts[i].spp;
+        j.spp_done = 0;
+        j.sample_offset = sc->samples_done;
+        j.max_depth = opts[i].max_depth;
+        j.rr_depth = opts[i].rr_depth;
+        j.flags = opts[i].flags;
+        j.seed = opts[i].seed;
+        order.push_back(&j);
+        max_npix = std::max(max_npix, j.npix);
+    }
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e != cudaSuccess) return cuda_status(e);
+    const uint32_t cap = std::max(default_capacity(wave_paths), max_npix);
+    // one pool per context for batches, owned by the context
+    if (!ctx->batch_pool) {
+        ctx->batch_pool = new (std::nothrow) gr::WavePool();
+        if (!ctx->batch_pool) return GR_ERR_OOM_BUDGET;
+        ctx->batch_pool_free = [](void* p) { delete static_cast<gr::WavePool*>(p); };
+    }
+    gr::WavePool& pool = *static_cast<gr::WavePool*>(ctx->batch_pool);
+    if ((e = pool.ensure(cap)) != cudaSuccess) {
+        ctx->last_error = std::string("gr_render_batch: ") + cudaGetErrorString(e);
+        return cuda_status(e);
+    }
+    cudaStream_t s = ctx->stream;
+    gr::WaveHeader before{};
+    cudaMemcpyAsync(&before, pool.ps.hdr, sizeof(before), cudaMemcpyDeviceToHost, s);
+    std::vector<gr::JobDev> table;
+    uint32_t waves = 0;
+    const bool graph = !(n && (opts[0].flags & GR_RENDER_NO_GRAPH));
+    for (;;) {
+        uint32_t paths = 0, pix = 0, depth = 0;
+        const uint32_t nj = gr::pack_wave(order, pool.capacity, table, &paths, &pix, &depth);
+        if (nj == 0) break;
+        if ((e = gr::run_wave(pool, table.data(), nj, paths, pix, depth, ctx->num_sms, s, graph)) != cudaSuccess) {
+            ctx->last_error = std::string("gr_render_batch: ") + cudaGetErrorString(e);
+            cudaGetLastError();
+            return cuda_status(e);
+        }
+        ++waves;
+    }
+    gr::WaveHeader after{};
+    uint32_t err = 0;
+    cudaMemcpyAsync(&after, pool.ps.hdr, sizeof(after), cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(&err, pool.ps.cnt + 2 * gr::kMaxDepth + 4, 4, cudaMemcpyDeviceToHost, s);
+    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_status(e);
+    uint64_t samples = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        scenes[i]->samples_done += opts[i].spp;
+        samples += (uint64_t)opts[i].spp * jobs[i].npix;
+    }
+    if (stats) {
+        stats->ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        stats->closest_rays = after.closest_rays - before.closest_rays;
+        stats->shadow_rays = after.shadow_rays - before.shadow_rays;
+        stats->samples = samples;
+        stats->waves = waves;
+        stats->device_errors = err;
+    }
+    if (err) {
+        ctx->last_error = "gr_render_batch: device error bits set";
+        return (err & gr::ERR_STACK) ? GR_ERR_OVERFLOW : GR_ERR_CUDA;
+    }
+    return GR_OK;
+}
+
+// ---- server ---------------------------------------------------------------------------------
+
+namespace {
+
+// Free lists of device and pinned host buffers by size, so jobs coming and
+// going do not call cudaMalloc / cudaFree (which would synchronise the device)
+// once the pool is warm.
+struct BufCache {
+    std::multimap<size_t, void*> dev_free, host_free;
+    void* get_dev(size_t bytes, cudaError_t* e) {
+        auto it = dev_free.find(bytes);
+        if (it != dev_free.end()) {
+            void* p = it->second;
+            dev_free.erase(it);
+            return p;
+        }
+        void* p = nullptr;
+        *e = cudaMalloc(&p, bytes);
+        return *e == cudaSuccess ? p : nullptr;
+    }
+    void* get_host(size_t bytes, cudaError_t* e) {
+        auto it = host_free.find(bytes);
+        if (it != host_free.end()) {
+            void* p = it->second;
+            host_free.erase(it);
+            return p;
+        }
+        void* p = nullptr;
+        *e = cudaMallocHost(&p, bytes);
+        return *e == cudaSuccess ? p : nullptr;
+    }
+    void put_dev(size_t bytes, void* p) { dev_free.emplace(bytes, p); }
+    void put_host(size_t bytes, void* p) { host_free.emplace(bytes, p); }
+    void clear() {
+        for (auto& kv : dev_free) cudaFree(kv.second);
+        for (auto& kv : host_free) cudaFreeHost(kv.second);
+        dev_free.clear();
+        host_free.clear();
+    }
+};
+
+struct Job {
+    uint64_t ticket = 0;
+    gr_scene* scene = nullptr;
+    gr_render_opts opts{};
+    gr::HostJob hj{};
+    double* d_sum = nullptr;
+    uint32_t* d_cnt = nullptr;
+    void* h_res = nullptr;  // pinned: sums then counts
+    size_t dev_bytes = 0, host_bytes = 0;
+    cudaEvent_t done_ev = nullptr;
+    bool scheduled_all = false;
+    bool finished = false;
+    std::vector<float> image;
+    gr_job_stats st{};
+};
+
+}  // namespace
+
+struct gr_server {
+    gr_ctx* ctx = nullptr;
+    gr_server_opts opts{};
+    cudaStream_t stream = nullptr;
+    gr::WavePool pool;
+    BufCache cache;
+    std::thread worker;
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    bool stop = false;
+    uint64_t next_ticket = 1;
+    std::deque<std::shared_ptr<Job>> pending;
+    std::vector<std::shared_ptr<Job>> active;
+    std::unordered_map<uint64_t, std::shared_ptr<Job>> all;
+    std::unordered_map<gr_scene*, int> scene_refs;
+    uint64_t bytes_in_use = 0;
+    gr_server_stats stats{};
+    std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+    std::string error;
+
+    double now() const { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); }
+
+    uint64_t job_bytes(const Job& j) const { return (uint64_t)j.hj.npix * (24 + 4); }
+
+    // Admission under the budget (called with mu held).
+    void admit() {
+        const uint32_t max_active = opts.max_active ? opts.max_active : gr::kMaxJobs;
+        while (!pending.empty() && active.size() < max_active) {
+            Job& j = *pending.front();
+            uint64_t need = job_bytes(j);
+            if (!scene_refs.count(j.scene)) need += gr_scene_device_bytes(j.scene);
+            if (opts.budget_bytes && bytes_in_use + need > opts.budget_bytes && !active.empty()) break;
+            cudaError_t e = cudaSuccess;
+            j.dev_bytes = job_bytes(j);
+            char* d = (char*)cache.get_dev(j.dev_bytes, &e);
+            j.host_bytes = j.dev_bytes;
+            void* h = d ? cache.get_host(j.host_bytes, &e) : nullptr;
+            if (!d || !h) {
+                if (d) cache.put_dev(j.dev_bytes, d);
+                j.st.status = cuda_status(e);
+                j.finished = true;
+                j.st.done_s = now();
+                pending.pop_front();
+                cv_done.notify_all();
+                continue;
+            }
+            j.d_sum = (double*)d;
+            j.d_cnt = (uint32_t*)(d + 24ull * j.hj.npix);
+            j.h_res = h;
+            cudaMemsetAsync(d, 0, j.dev_bytes, stream);
+            j.hj.fb = j.d_sum;
+            j.hj.fbc = j.d_cnt;
+            cudaEventCreateWithFlags(&j.done_ev, cudaEventDisableTiming);
+            j.st.admit_s = now();
+            scene_refs[j.scene]++;
+            bytes_in_use += need;
+            stats.peak_bytes = std::max(stats.peak_bytes, bytes_in_use);
+            stats.admitted++;
+            active.push_back(pending.front());
+            pending.pop_front();
+        }
+    }
+
+    void release_job(Job& j) {  // with mu held
+        cache.put_dev(j.dev_bytes, j.d_sum);
+        cache.put_host(j.host_bytes, j.h_res);
+        uint64_t freed = job_bytes(j);
+        if (--scene_refs[j.scene] == 0) {
+            scene_refs.erase(j.scene);
+            freed += gr_scene_device_bytes(j.scene);
+        }
+        bytes_in_use -= std::min(bytes_in_use, freed);
+        if (j.done_ev) cudaEventDestroy(j.done_ev);
+        j.done_ev = nullptr;
+    }
+
+    void run() {
+        cudaSetDevice(ctx->device);
+        std::vector<gr::JobDev> table;
+        double busy_since = -1.0;
+        for (;;) {
+            std::vector<std::shared_ptr<Job>> act;
+            {
+                std::unique_lock<std::mutex> lk(mu);
+                admit();
+                if (active.empty()) {
+                    if (busy_since >= 0) {
+                        stats.busy_s += now() - busy_since;
+                        busy_since = -1.0;
+                    }
+                    if (stop) break;
+                    cv_work.wait_for(lk, std::chrono::milliseconds(2));
+                    continue;
+                }
+                if (busy_since < 0) busy_since = now();
+                act = active;
+            }
+            // schedule one wave over the active jobs that still need samples
+            std::vector<gr::HostJob*> hjs;
+            for (auto& j : act)
+                if (!j->scheduled_all) hjs.push_back(&j->hj);
+            if (!hjs.empty()) {
+                uint32_t paths = 0, pix = 0, depth = 0;
+                const uint32_t nj = gr::pack_wave(hjs, pool.capacity, table, &paths, &pix, &depth);
+                if (nj) {
+                    const cudaError_t e = gr::run_wave(pool, table.data(), nj, paths, pix, depth, ctx->num_sms, stream, true);
+                    if (e != cudaSuccess) {
+                        std::lock_guard<std::mutex> lk(mu);
+                        error = cudaGetErrorString(e);
+                        for (auto& j : act) {
+                            j->st.status = cuda_status(e);
+                        }
+                    }
+                    std::lock_guard<std::mutex> lk(mu);
+                    stats.waves++;
+                }
+                // jobs whose last samples went into this wave: copy out after it
+                for (auto& j : act) {
+                    if (j->scheduled_all || j->hj.spp_done < j->hj.spp_total) continue;
+                    j->scheduled_all = true;
+                    const size_t npix = j->hj.npix;
+                    cudaMemcpyAsync(j->h_res, j->d_sum, 28 * npix, cudaMemcpyDeviceToHost, stream);
+                    cudaEventRecord(j->done_ev, stream);
+                }
+            } else {
+                std::this_thread::sleep_for(std::chrono::microseconds(50));
+            }
+            // retire finished jobs
+            for (auto& j : act) {
+                if (!j->scheduled_all || j->finished) continue;
+                if (cudaEventQuery(j->done_ev) != cudaSuccess) continue;
+                const uint32_t npix = j->hj.npix;
+                j->image.resize(3ull * npix);
+                const double* sum = (const double*)j->h_res;
+                const uint32_t* cnt = (const uint32_t*)((const char*)j->h_res + 24ull * npix);
+                mean_image(sum, cnt, npix, j->image.data());
+                std::lock_guard<std::mutex> lk(mu);
+                j->st.done_s = now();
+                j->st.samples = (uint64_t)j->hj.spp_total * npix;
+                j->finished = true;
+                release_job(*j);
+                active.erase(std::find(active.begin(), active.end(), j));
+                stats.completed++;
+                cv_done.notify_all();
+            }
+        }
+        cudaStreamSynchronize(stream);
+    }
+};
+
+extern "C" {
+
+gr_status gr_server_create(gr_ctx* ctx, const gr_server_opts* opts, gr_server** out) {
+    if (!ctx || !out) return GR_ERR_INVALID;
+    *out = nullptr;
+    gr_server* sv = new (std::nothrow) gr_server();
+    if (!sv) return GR_ERR_OOM_BUDGET;
+    sv->ctx = ctx;
+    if (opts) sv->opts = *opts;
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&sv->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = sv->pool.ensure(default_capacity(sv->opts.wave_paths));
+    if (e != cudaSuccess) {
+        ctx->last_error = std::string("gr_server_create: ") + cudaGetErrorString(e);
+        sv->pool.release();
+        if (sv->stream) cudaStreamDestroy(sv->stream);
+        delete sv;
+        return cuda_status(e);
+    }
+    sv->bytes_in_use = sv->pool.mem.bytes;
+    sv->stats.peak_bytes = sv->bytes_in_use;
+    gr::ctx_retain(ctx);
+    sv->worker = std::thread([sv] { sv->run(); });
+    *out = sv;
+    return GR_OK;
+}
+
+gr_status gr_server_destroy(gr_server* sv) {
+    if (!sv) return GR_ERR_INVALID;
+    {
+        std::lock_guard<std::mutex> lk(sv->mu);
+        sv->stop = true;
+        sv->pending.clear();
+    }
+    sv->cv_work.notify_all();
+    sv->worker.join();
+    gr_ctx* ctx = sv->ctx;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(sv->stream);
+    for (auto& kv : sv->all)
+        if (kv.second->done_ev) cudaEventDestroy(kv.second->done_ev);
+    sv->pool.release();
+    sv->cache.clear();
+    cudaStreamDestroy(sv->stream);
+    delete sv;
+    gr::ctx_release(ctx);
+    return GR_OK;
+}
+
+double gr_server_now(const gr_server* sv) { return sv ? sv->now() : 0.0; }
+
+gr_status gr_server_submit(gr_server* sv, gr_scene* scene, const gr_camera* camera, const gr_render_opts* opts,
+                           uint64_t* ticket) {
+    if (!sv || !scene || !opts || !ticket || scene->ctx != sv->ctx) return GR_ERR_INVALID;
+    if (opts->max_depth > (uint32_t)gr::kMaxDepth) return GR_ERR_INVALID;
+    gr::SceneDev view = view_of(scene);
+    if (camera) {
+        if (camera->width == 0 || camera->height == 0 || !(camera->fov_deg > 0.0f && camera->fov_deg < 180.0f))
+            return GR_ERR_INVALID;
+        view.cam = gr::make_camera(*camera);
+    }
+    const uint32_t npix = view.cam.width * view.cam.height;
+    if (npix > sv->pool.capacity) return GR_ERR_INVALID;
+    auto j = std::make_shared<Job>();
+    j->scene = scene;
+    j->opts = *opts;
+    j->hj.sc = view;
+    j->hj.npix = npix;
+    j->hj.spp_total = opts->spp;
+    j->hj.spp_done = 0;
+    j->hj.sample_offset = 0;
+    j->hj.max_depth = opts->max_depth;
+    j->hj.rr_depth = opts->rr_depth;
+    j->hj.flags = opts->flags;
+    j->hj.seed = opts->seed;
+    {
+        std::lock_guard<std::mutex> lk(sv->mu);
+        j->ticket = sv->next_ticket++;
+        j->st.submit_s = sv->now();
+        sv->pending.push_back(j);
+        sv->all[j->ticket] = j;
+        sv->stats.submitted++;
+        *ticket = j->ticket;
+    }
+    sv->cv_work.notify_all();
+    return GR_OK;
+}
+
+gr_status gr_server_wait(gr_server* sv, uint64_t ticket, double timeout_s, int* done, float* h_rgb,
+                         gr_job_stats* stats) {
+    if (!sv) return GR_ERR_INVALID;
+    std::unique_lock<std::mutex> lk(sv->mu);
+    auto it = sv->all.find(ticket);
+    if (it == sv->all.end()) return GR_ERR_INVALID;
+    std::shared_ptr<Job> j = it->second;
+    auto pred = [&] { return j->finished; };
+    if (timeout_s < 0) sv->cv_done.wait(lk, pred);
+    else sv->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), pred);
+    if (done) *done = j->finished ? 1 : 0;
+    if (stats) *stats = j->st;
+    if (j->finished && h_rgb && !j->image.empty()) std::memcpy(h_rgb, j->image.data(), j->image.size() * 4);
+    if (j->finished) {
+        sv->all.erase(it);  // a finished job is reported once
+        return (gr_status)j->st.status;
+    }
+    return GR_OK;
+}
+
+gr_status gr_server_stats_get(gr_server* sv, gr_server_stats* out) {
+    if (!sv || !out) return GR_ERR_INVALID;
+    gr::WaveHeader h{};
+    cudaSetDevice(sv->ctx->device);
+    // ray totals live in the pool's device header
+    cudaMemcpyAsync(&h, sv->pool.ps.hdr, sizeof(h), cudaMemcpyDeviceToHost, sv->stream);
+    cudaStreamSynchronize(sv->stream);
+    std::lock_guard<std::mutex> lk(sv->mu);
+    *out = sv->stats;
+    out->closest_rays = h.closest_rays;
+    out->shadow_rays = h.shadow_rays;
+    out->bytes_in_use = sv->bytes_in_use;
+    return GR_OK;
+}
+
+}  // extern "C"

@@ -25,9 +25,15 @@ struct RaySrc {
     const float4* __restrict__ rays;
     float4* __restrict__ hits;
     uint64_t n;
-    __device__ __forceinline__ void load(uint64_t i, float4& r0, float4& r1) const {
+    const Node* nodes;
+    const Tri* tris;
+    uint32_t root;
+    __device__ __forceinline__ uint32_t load(uint64_t i, float4& r0, float4& r1, const Node*& nd, const Tri*& tr) const {
         r0 = __ldg(rays + 2 * i);
         r1 = __ldg(rays + 2 * i + 1);
+        nd = nodes;
+        tr = tris;
+        return root;
     }
     __device__ __forceinline__ void finish(uint64_t i, const trav::Lane& L) const {
         hits[i] = L.best_prim == 0xFFFFFFFFu ? make_float4(L.p.tmax, __int_as_float(-1), 0.0f, 0.0f)
@@ -42,8 +48,8 @@ __global__ void __launch_bounds__(trav::kTraceThreads) k_trace(const Node* __res
                                                                float4* __restrict__ hits, unsigned long long* counter,
                                                                uint32_t* err) {
     __shared__ int2 s_stack[trav::kShortStack][trav::kTraceThreads];
-    RaySrc src{rays, hits, n};
-    trav::traverse_loop<ANY>(nodes, tris, meta->root, src, counter, err, s_stack);
+    RaySrc src{rays, hits, n, nodes, tris, meta->root};
+    trav::traverse_loop<ANY>(src, counter, err, s_stack);
 }
 
 }  // namespace

@@ -102,6 +102,8 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
 // finishes the lane goes idle and is refilled with a new ray once enough lanes
 // of the warp are idle, so long-tailed rays do not hold a whole warp.
 struct Lane {
+    const Node* nodes;  // BVH of this lane's ray (rays of one queue may belong to different scenes)
+    const Tri* tris;
     RayW p;
     float best_t, bu, bv;
     uint32_t best_prim;
@@ -112,9 +114,10 @@ struct Lane {
 
 // Processes one node for the lane; returns true when the ray is finished.
 template <bool ANY>
-__device__ __forceinline__ bool trace_step(const Node* __restrict__ nodes, const Tri* __restrict__ tris, Lane& L,
-                                           int2 (*s_stack)[kTraceThreads], int2* l_stack, uint32_t* err) {
+__device__ __forceinline__ bool trace_step(Lane& L, int2 (*s_stack)[kTraceThreads], int2* l_stack, uint32_t* err) {
     const int tid = threadIdx.x;
+    const Node* __restrict__ nodes = L.nodes;
+    const Tri* __restrict__ tris = L.tris;
     const float4* q = reinterpret_cast<const float4*>(nodes + L.node);
     const float4 q0 = __ldg(q), q1 = __ldg(q + 1), q2 = __ldg(q + 2);
     const int4 q3 = __ldg(reinterpret_cast<const int4*>(q + 3));
@@ -178,13 +181,14 @@ constexpr int kRefillLanes = 8;
 
 
 // Persistent dynamic-fetch loop. `Src` supplies the work:
-//   uint64_t n                         number of rays
-//   void load(uint64_t i, float4& r0, float4& r1)   ray i (reference Ray layout)
-//   void finish(uint64_t i, const Lane& L)          ray i is done (L.best_prim ==
-//                                                   0xFFFFFFFF means a miss)
+//   uint64_t n                                        number of rays
+//   uint32_t load(uint64_t i, float4& r0, float4& r1, const Node*& nodes,
+//                 const Tri*& tris)                   ray i (reference Ray layout) and
+//                                                     its BVH; returns the root node
+//   void finish(uint64_t i, const Lane& L)            ray i is done (L.best_prim ==
+//                                                     0xFFFFFFFF means a miss)
 template <bool ANY, class Src>
-__device__ __forceinline__ void traverse_loop(const Node* __restrict__ nodes, const Tri* __restrict__ tris,
-                                              uint32_t root, Src& src, unsigned long long* counter, uint32_t* err,
+__device__ __forceinline__ void traverse_loop(Src& src, unsigned long long* counter, uint32_t* err,
                                               int2 (*s_stack)[kTraceThreads]) {
     int2 l_stack[kStackMax - kShortStack];
     const int lane = threadIdx.x & 31;
@@ -205,7 +209,7 @@ __device__ __forceinline__ void traverse_loop(const Node* __restrict__ nodes, co
                 const uint64_t i = base + __popc(idle & ltmask);
                 if (i < n) {
                     float4 r0, r1;
-                    src.load(i, r0, r1);
+                    const uint32_t root = src.load(i, r0, r1, L.nodes, L.tris);
                     L.p = prepare(r0, r1);
                     L.best_t = L.p.tmax;
                     L.bu = 0.0f;
@@ -226,7 +230,7 @@ __device__ __forceinline__ void traverse_loop(const Node* __restrict__ nodes, co
             if (exhausted) break;
             continue;
         }
-        if (active && trace_step<ANY>(nodes, tris, L, s_stack, l_stack, err)) {
+        if (active && trace_step<ANY>(L, s_stack, l_stack, err)) {
             src.finish(L.ray, L);
             active = false;
         }

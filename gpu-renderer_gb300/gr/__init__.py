@@ -329,3 +329,106 @@ class PathTracer:
     def reset(self):
         self.scene.reset()
         self.sample_num = 0
+
+
+# ---- batched rendering and serving ---------------------------------------------------
+
+class ServerOpts(ctypes.Structure):
+    _fields_ = [("budget_bytes", ctypes.c_uint64), ("wave_paths", ctypes.c_uint32), ("max_active", ctypes.c_uint32)]
+
+
+class JobStats(ctypes.Structure):
+    _fields_ = [("submit_s", ctypes.c_double), ("admit_s", ctypes.c_double), ("done_s", ctypes.c_double),
+                ("samples", ctypes.c_uint64), ("status", ctypes.c_int32)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_uint64), ("admitted", ctypes.c_uint64), ("completed", ctypes.c_uint64),
+                ("waves", ctypes.c_uint64), ("closest_rays", ctypes.c_uint64), ("shadow_rays", ctypes.c_uint64),
+                ("bytes_in_use", ctypes.c_uint64), ("peak_bytes", ctypes.c_uint64), ("busy_s", ctypes.c_double)]
+
+
+_SERVER_SIGS = {
+    "gr_render_batch": ([_P, _P, _P, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(RenderStats)], ctypes.c_int),
+    "gr_scene_device_bytes": ([_P], ctypes.c_uint64),
+    "gr_server_create": ([_P, ctypes.POINTER(ServerOpts), ctypes.POINTER(_P)], ctypes.c_int),
+    "gr_server_destroy": ([_P], ctypes.c_int),
+    "gr_server_submit": ([_P, _P, _P, ctypes.POINTER(RenderOpts), ctypes.POINTER(ctypes.c_uint64)], ctypes.c_int),
+    "gr_server_wait": ([_P, ctypes.c_uint64, ctypes.c_double, ctypes.POINTER(ctypes.c_int), _P,
+                        ctypes.POINTER(JobStats)], ctypes.c_int),
+    "gr_server_now": ([_P], ctypes.c_double),
+    "gr_server_stats_get": ([_P, ctypes.POINTER(ServerStats)], ctypes.c_int),
+}
+
+
+def camera_record(cam):
+    c = Camera()
+    c.to_world[:] = [float(x) for x in np.asarray(cam["to_world"], np.float32).reshape(16)]
+    c.fov_deg = float(cam["fov"])
+    c.width = int(cam["width"])
+    c.height = int(cam["height"])
+    return c
+
+
+def render_batch(ctx, scenes, opts, wave_paths=0):
+    """Renders jobs (scene, RenderOpts-like dict) in shared waves; each scene
+    accumulates as if rendered alone. Returns RenderStats."""
+    L = _declare(_SERVER_SIGS)
+    n = len(scenes)
+    hs = (_P * max(n, 1))(*[s.h for s in scenes])
+    os_ = (RenderOpts * max(n, 1))()
+    for i, o in enumerate(opts):
+        os_[i] = RenderOpts(o["spp"], o.get("max_depth", 8), o.get("seed", 0), o.get("rr_depth", 3),
+                            o.get("flags", 0), 0)
+    st = RenderStats()
+    ctx.check(L.gr_render_batch(ctx.h, hs, os_, n, wave_paths, ctypes.byref(st)), "gr_render_batch")
+    return st
+
+
+class Server:
+    """Continuous-batching render server (gr_server)."""
+
+    def __init__(self, ctx, budget_bytes=0, wave_paths=0, max_active=0):
+        L = _declare(_SERVER_SIGS)
+        self.ctx = ctx
+        o = ServerOpts(budget_bytes, wave_paths, max_active)
+        h = _P()
+        ctx.check(L.gr_server_create(ctx.h, ctypes.byref(o), ctypes.byref(h)), "gr_server_create")
+        self.h = h
+
+    def submit(self, scene, spp, max_depth=8, seed=0, rr_depth=3, flags=0, camera=None):
+        L = _declare(_SERVER_SIGS)
+        o = RenderOpts(spp, max_depth, seed, rr_depth, flags, 0)
+        t = ctypes.c_uint64()
+        cam = None if camera is None else camera_record(camera)
+        self.ctx.check(L.gr_server_submit(self.h, scene.h, None if cam is None else ctypes.byref(cam), ctypes.byref(o),
+                                          ctypes.byref(t)), "gr_server_submit")
+        return t.value
+
+    def wait(self, ticket, timeout=-1.0, image_shape=None):
+        L = _declare(_SERVER_SIGS)
+        done = ctypes.c_int()
+        js = JobStats()
+        img = None if image_shape is None else np.zeros(tuple(image_shape) + (3,), np.float32)
+        st = L.gr_server_wait(self.h, ticket, timeout, ctypes.byref(done), _ptr(img), ctypes.byref(js))
+        self.ctx.check(st, "gr_server_wait")
+        return bool(done.value), img, js
+
+    def now(self):
+        return _declare(_SERVER_SIGS).gr_server_now(self.h)
+
+    def stats(self):
+        s = ServerStats()
+        self.ctx.check(_declare(_SERVER_SIGS).gr_server_stats_get(self.h, ctypes.byref(s)), "gr_server_stats_get")
+        return s
+
+    def close(self):
+        if getattr(self, "h", None):
+            _declare(_SERVER_SIGS).gr_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -205,8 +205,20 @@ def cornell_box(width=256, height=256, seed_salt=0):
     return SceneDesc(meshes, mats, cam, env=None)
 
 
+_ICO_CACHE = {}
+
+
 def icosphere(level):
-    """Unit icosphere: 20 * 4^level triangles with shared vertices."""
+    """Unit icosphere: 20 * 4^level triangles with shared vertices (cached)."""
+    if level in _ICO_CACHE:
+        V, F = _ICO_CACHE[level]
+        return V.copy(), F.copy()
+    V, F = _icosphere(level)
+    _ICO_CACHE[level] = (V, F)
+    return V.copy(), F.copy()
+
+
+def _icosphere(level):
     t = (1.0 + 5.0 ** 0.5) / 2.0
     V = np.array([[-1, t, 0], [1, t, 0], [-1, -t, 0], [1, -t, 0], [0, -1, t], [0, 1, t], [0, -1, -t], [0, 1, -t],
                   [t, 0, -1], [t, 0, 1], [-t, 0, -1], [-t, 0, 1]], np.float64)
@@ -270,8 +282,9 @@ def displaced_sphere(level, radius, center, amplitude, seed):
     P = V * disp[:, None] * radius + np.asarray(center, np.float64)
     fn = np.cross(P[F[:, 1]] - P[F[:, 0]], P[F[:, 2]] - P[F[:, 0]])
     N = np.zeros_like(P)
-    for k in range(3):
-        np.add.at(N, F[:, k], fn)
+    for c in range(3):
+        for k in range(3):
+            N[:, c] += np.bincount(F[:, k], weights=fn[:, c], minlength=P.shape[0])
     N /= np.linalg.norm(N, axis=1, keepdims=True)
     return P.astype(np.float32), F.astype(np.uint32), N.astype(np.float32)
 
@@ -303,3 +316,74 @@ def glossy_scene(width=1024, height=768, level=8, glass_level=5, seed_salt=0):
     cam = {"to_world": look_at((0.0, 1.3, 4.6), (0.0, 0.5, 0.0), (0.0, 1.0, 0.0)), "fov": 40.0,
            "width": width, "height": height}
     return SceneDesc(meshes, mats, cam, env=(0.3, 0.35, 0.45))
+
+
+_DISPLACED_CACHE = {}
+
+
+def _unit_displaced(level, variant):
+    """Unit icosphere displaced by seeded 3-octave value noise (amplitude 0.05),
+    cached by (level, variant)."""
+    key = (level, variant)
+    if key not in _DISPLACED_CACHE:
+        _DISPLACED_CACHE[key] = displaced_sphere(level, 1.0, (0.0, 0.0, 0.0), 0.05, seed=SEED_BASE + 977 * variant + level)
+    return _DISPLACED_CACHE[key]
+
+
+RESOLUTIONS = (128, 256, 512, 1024)
+SPPS = (4, 16, 64)
+
+
+def batch_job(index, config=4, min_tris=10_000, max_tris=2_000_000):
+    """Config 4 job `index`: a seeded scene with a log-uniform triangle count in
+    [10k, 2M], built from noise-displaced icospheres (levels 5-8) and boxes
+    with Lambert, GGX-conductor or dielectric materials, on a ground plane
+    with one quad light and a constant environment. Returns (SceneDesc, spp)
+    with a resolution drawn from {128, 256, 512, 1024}^2 and spp from {4, 16, 64}."""
+    r = rng(config, index + 1)
+    target = int(np.exp(r.uniform(np.log(min_tris), np.log(max_tris))))
+    res = int(r.choice(RESOLUTIONS))
+    spp = int(r.choice(SPPS))
+    mats = [{"type": 0, "color": (0.6, 0.6, 0.6)},
+            {"type": 0, "color": (0.5, 0.5, 0.5), "emission": (12.0, 12.0, 12.0)}]
+    meshes = []
+    GP, GI = quad((-6, 0, -6), (-6, 0, 6), (6, 0, 6), (6, 0, -6))
+    meshes.append(MeshDesc(GP, GI, 0))
+    LP, LI = quad((-0.6, 4.0, -0.6), (0.6, 4.0, -0.6), (0.6, 4.0, 0.6), (-0.6, 4.0, 0.6))
+    meshes.append(MeshDesc(LP, LI, 1))
+
+    def add_material():
+        kind = int(r.integers(0, 3))
+        if kind == 0:
+            mats.append({"type": 0, "color": tuple(float(x) for x in r.uniform(0.2, 0.9, 3))})
+        elif kind == 1:
+            mats.append({"type": 2, "color": (1.0, 1.0, 1.0), "alpha": float(r.choice((0.01, 0.1, 0.25, 0.5)))})
+        else:
+            mats.append({"type": 1, "color": (1.0, 1.0, 1.0), "ior": 1.5})
+        return len(mats) - 1
+
+    remaining = target - 4
+    while remaining >= 20 * 4 ** 5:
+        level = 5
+        while level < 8 and 20 * 4 ** (level + 1) <= remaining:
+            level += 1
+        if level > 5 and r.random() < 0.3:
+            level -= 1
+        P, F, N = _unit_displaced(level, int(r.integers(0, 4)))
+        radius = float(r.uniform(0.3, 0.8))
+        center = (float(r.uniform(-2.5, 2.5)), radius * 1.05, float(r.uniform(-2.5, 1.5)))
+        meshes.append(MeshDesc(P * radius + np.asarray(center, np.float32), F, add_material(), normals=N))
+        remaining -= F.shape[0]
+    nbox = max(1, remaining // 12)
+    boxes_p, boxes_i = [], []
+    m_box = add_material()
+    for b in range(nbox):
+        s = r.uniform(0.05, 0.4, 3)
+        c = (float(r.uniform(-3, 3)), 0.0, float(r.uniform(-3, 2)))
+        P, I = box_mesh(c, s, float(r.uniform(0, 2 * np.pi)))
+        boxes_i.append(I + 8 * b)
+        boxes_p.append(P)
+    meshes.append(MeshDesc(np.concatenate(boxes_p), np.concatenate(boxes_i), m_box))
+    cam = {"to_world": look_at((0.0, 2.2, 6.5), (0.0, 0.6, 0.0), (0.0, 1.0, 0.0)), "fov": 45.0,
+           "width": res, "height": res}
+    return SceneDesc(meshes, mats, cam, env=(0.25, 0.3, 0.35)), spp

@@ -189,6 +189,9 @@ typedef struct gr_render_opts {
  * see the environment at the next bounce, and the GGX pdf is D|cos h|/(4 wo.h)
  * (pathtracer_kernel.h:738-748, microfacet.h:148-155). Default: corrected. */
 #define GR_RENDER_REFERENCE_COMPAT 1u
+/* Launch each wave's kernels directly instead of replaying the wave as a
+ * captured CUDA graph (the default). The image is the same either way. */
+#define GR_RENDER_NO_GRAPH 2u
 
 typedef struct gr_render_stats {
     double ms;             /* host wall time of the call */
@@ -226,6 +229,66 @@ gr_status gr_scene_accumulation(gr_scene* scene, double* h_sum_rgb, uint32_t* h_
 /* Clears the accumulation and restarts the sample sequence (PathTracer::reset,
  * pathtracer.cu:195-200). */
 gr_status gr_scene_reset(gr_scene* scene);
+
+/* Device bytes the scene holds (geometry, BVH, accumulation). */
+uint64_t gr_scene_device_bytes(const gr_scene* scene);
+
+/* ---- batched rendering (no counterpart in the reference) --------------------
+ * Renders n jobs to completion with their samples packed into shared waves:
+ * each wave's kernels cover every job in it (rays of all scenes share the
+ * queues; each ray traverses its own scene's BVH). Job i adds opts[i].spp
+ * samples to scenes[i]'s accumulation exactly as gr_render would, bit for bit:
+ * a pixel's value does not depend on which jobs share its waves. A scene may
+ * appear at most once. wave_paths = 0 picks the library default. */
+gr_status gr_render_batch(gr_ctx* ctx, gr_scene* const* scenes, const gr_render_opts* opts, uint32_t n,
+                          uint32_t wave_paths, gr_render_stats* stats);
+
+/* ---- serving (no counterpart in the reference) --------------------------------
+ * A render server with its own worker thread and stream. Submitted jobs wait
+ * until they fit the device-memory budget (path pool + per-job accumulation +
+ * the scenes they reference, each scene counted once while any job uses it),
+ * then join the running waves at the next wave boundary (continuous
+ * batching); finished jobs leave and free their budget. Scenes stay resident
+ * as long as the caller keeps them. */
+typedef struct gr_server gr_server;
+
+typedef struct gr_server_opts {
+    uint64_t budget_bytes; /* device-memory budget for admission (0 = no limit) */
+    uint32_t wave_paths;   /* paths per wave (0 = library default) */
+    uint32_t max_active;   /* jobs in flight at most (0 = 1024) */
+} gr_server_opts;
+
+typedef struct gr_job_stats {
+    double submit_s, admit_s, done_s; /* seconds on the server's clock */
+    uint64_t samples;
+    int32_t status;                   /* gr_status of the job */
+} gr_job_stats;
+
+typedef struct gr_server_stats {
+    uint64_t submitted, admitted, completed, waves;
+    uint64_t closest_rays, shadow_rays;
+    uint64_t bytes_in_use, peak_bytes;
+    double busy_s; /* time with at least one job in flight */
+} gr_server_stats;
+
+gr_status gr_server_create(gr_ctx* ctx, const gr_server_opts* opts, gr_server** out);
+/* Stops the worker after the jobs in flight finish; pending jobs are dropped. */
+gr_status gr_server_destroy(gr_server* server);
+/* Queues a job; returns at once with a ticket. The scene must outlive the job.
+ * `camera` (may be NULL) overrides the scene's camera and resolution for this
+ * job only, so one resident scene and BVH serve requests of any resolution.
+ * The job's samples start at sample index 0. */
+gr_status gr_server_submit(gr_server* server, gr_scene* scene, const gr_camera* camera, const gr_render_opts* opts,
+                           uint64_t* ticket);
+/* Waits up to timeout_s (< 0: forever) for a job; *done is 1 when finished.
+ * When finished and h_rgb is not NULL, writes its mean radiance image
+ * (width x height x 3 floats). A finished job is reported once: its ticket is
+ * forgotten after the call that sees it done. */
+gr_status gr_server_wait(gr_server* server, uint64_t ticket, double timeout_s, int* done, float* h_rgb,
+                         gr_job_stats* stats);
+/* Seconds on the server's clock (the clock of gr_job_stats). */
+double gr_server_now(const gr_server* server);
+gr_status gr_server_stats_get(gr_server* server, gr_server_stats* out);
 
 #ifdef __cplusplus
 }
