@@ -248,6 +248,19 @@ def run_gpu(args):
         del d_r2
     clock_info = clocks.stop()
 
+    # render configurations (plain render, batched, serving)
+    if not args.no_render:
+        from gr import workloads as wl
+        log = lambda m: print("[bench] " + m, file=sys.stderr, flush=True)  # noqa: E731
+        log("config 1 (Cornell box 256x256, 16 spp, depth 8)")
+        extras["config1_render"] = wl.plain_render(ctx, scenes.cornell_box(256, 256), 16, 8)
+        log("config 3 (glossy scene 1024x768, 64 spp, depth 16)")
+        extras["config3_render"] = wl.plain_render(ctx, scenes.glossy_scene(), 64, 16)
+        log("config 4 (64-job batch)")
+        extras["config4_batch"] = wl.config4(ctx)
+        log("config 5 (serving sweep)")
+        extras["config5_serving"] = wl.config5(ctx)
+
     # end to end through the C ABI with host buffers (pinned), copies inside
     h_rays = torch.from_numpy(rays).pin_memory()
     h_hits = torch.empty((N_RAYS, 4), dtype=torch.float32).pin_memory()
@@ -311,6 +324,7 @@ def main():
     ap.add_argument("--impl", default="gr", choices=["gr", "reference"])
     ap.add_argument("--tris", type=int, default=N_TRIS, help="triangle count (profiling cases)")
     ap.add_argument("--rays", type=int, default=N_RAYS, help="ray count (profiling cases)")
+    ap.add_argument("--no-render", action="store_true", help="skip the render-configuration extras")
     ap.add_argument("--quick", action="store_true",
                     help="time the main query only (no extras, e2e or CPU baseline); for profiling")
     args = ap.parse_args()

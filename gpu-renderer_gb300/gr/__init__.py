@@ -192,6 +192,7 @@ class RenderStats(ctypes.Structure):
 
 MAT_DIFFUSE, MAT_DIELECTRIC, MAT_CONDUCTOR = 0, 1, 2
 RENDER_REFERENCE_COMPAT = 1
+RENDER_NO_GRAPH = 2
 
 _SCENE_SIGS = {
     "gr_scene_create": ([_P, _P, ctypes.c_uint32, _P, ctypes.c_uint32, _P, _P, ctypes.POINTER(_P)], ctypes.c_int),
@@ -432,3 +433,80 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+# ---- scene files ---------------------------------------------------------------
+
+_DESC_SIGS = {
+    "gr_scene_desc_load_xml": ([ctypes.c_char_p, ctypes.POINTER(_P)], ctypes.c_int),
+    "gr_scene_desc_destroy": ([_P], ctypes.c_int),
+    "gr_scene_desc_error": ([_P], ctypes.c_char_p),
+    "gr_scene_desc_warnings": ([_P], ctypes.c_char_p),
+    "gr_scene_desc_info": ([_P, _P, _P, _P, ctypes.POINTER(Camera), ctypes.POINTER(Environment)], ctypes.c_int),
+    "gr_scene_desc_triangles": ([_P, _P, _P, _P], ctypes.c_int),
+    "gr_scene_create_from_desc": ([_P, _P, ctypes.POINTER(_P)], ctypes.c_int),
+    "gr_scene_load_xml": ([_P, ctypes.c_char_p, ctypes.POINTER(_P)], ctypes.c_int),
+}
+
+
+class ParsedScene:
+    """A Mitsuba-XML scene parsed by the library (no GPU needed)."""
+
+    def __init__(self, path):
+        L = _declare(_DESC_SIGS)
+        h = _P()
+        st = L.gr_scene_desc_load_xml(os.fsencode(path), ctypes.byref(h))
+        self.h = h
+        if st != GR_OK:
+            msg = L.gr_scene_desc_error(h).decode() if h else "out of memory"
+            self.close()
+            raise GrError(st, msg)
+        self.warnings = [w for w in L.gr_scene_desc_warnings(h).decode().splitlines() if w]
+        m, t, li = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint32()
+        cam, env = Camera(), Environment()
+        L.gr_scene_desc_info(h, ctypes.byref(m), ctypes.byref(t), ctypes.byref(li), ctypes.byref(cam),
+                             ctypes.byref(env))
+        self.num_meshes, self.num_triangles, self.num_light_triangles = m.value, t.value, li.value
+        self.camera = {"to_world": np.array(cam.to_world[:], np.float32).reshape(4, 4), "fov": cam.fov_deg,
+                       "width": cam.width, "height": cam.height}
+        self.env = tuple(env.radiance[:]) if env.enabled else None
+
+    def triangles(self):
+        L = _declare(_DESC_SIGS)
+        v = np.zeros((self.num_triangles, 9), np.float32)
+        mesh = np.zeros(self.num_triangles, np.uint32)
+        mats = (Material * max(self.num_meshes, 1))()
+        L.gr_scene_desc_triangles(self.h, _ptr(v), _ptr(mesh), mats)
+        return v, mesh, [mats[i] for i in range(self.num_meshes)]
+
+    def create(self, ctx):
+        h = _P()
+        ctx.check(_declare(_DESC_SIGS).gr_scene_create_from_desc(ctx.h, self.h, ctypes.byref(h)),
+                  "gr_scene_create_from_desc")
+        return _wrap_scene(ctx, h, self.camera["width"], self.camera["height"])
+
+    def close(self):
+        if getattr(self, "h", None):
+            _declare(_DESC_SIGS).gr_scene_desc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _wrap_scene(ctx, h, width, height):
+    s = Scene.__new__(Scene)
+    s.ctx, s.desc, s._keep, s.h, s.width, s.height = ctx, None, [], h, width, height
+    return s
+
+
+def load_xml(ctx, path):
+    """gr_scene_load_xml: the drop-in for the reference's PathTracer(filename)."""
+    h = _P()
+    ctx.check(_declare(_DESC_SIGS).gr_scene_load_xml(ctx.h, os.fsencode(path), ctypes.byref(h)), "gr_scene_load_xml")
+    info = [ctypes.c_uint32() for _ in range(4)]
+    _declare(_SCENE_SIGS).gr_scene_info(h, *[ctypes.byref(x) for x in info])
+    return _wrap_scene(ctx, h, info[0].value, info[1].value)

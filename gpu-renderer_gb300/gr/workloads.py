@@ -1,0 +1,161 @@
+"""Timed workloads for the render configurations (used by bench.py).
+
+config 1: plain render of the procedural Cornell box, 256x256, 16 spp, depth 8.
+config 3: plain render of the glossy scene, 1024x768, 64 spp, depth 16, RR after 3.
+config 4: 64 seeded jobs (10k-2M triangles, 128^2..1024^2, 4/16/64 spp, depth 8)
+          rendered one gr_render call after another, then all in gr_render_batch.
+config 5: Poisson arrivals of config-4-distributed requests served by gr_server
+          (continuous batching, HBM budget, resident BVHs per scene id), with
+          p50/p99 latency, against the same stream served one job at a time.
+"""
+import threading
+import time
+
+import numpy as np
+
+import gr
+from gr import scenes as sc
+
+
+def _timed_render(scene, spp, depth, rr=3, flags=0, reps=3):
+    scene.render(spp, depth, 1, rr, flags, want_image=False)
+    best = None
+    st = None
+    for _ in range(reps):
+        scene.reset()
+        t = time.perf_counter()
+        _, st = scene.render(spp, depth, 1, rr, flags, want_image=False)
+        dt = time.perf_counter() - t
+        best = dt if best is None else min(best, dt)
+    return best, st
+
+
+def plain_render(ctx, desc, spp, depth, rr=3):
+    s = gr.Scene(ctx, desc)
+    dt, st = _timed_render(s, spp, depth, rr)
+    npix = desc.camera["width"] * desc.camera["height"]
+    out = {"ms": dt * 1e3, "samples_per_s": npix * spp / dt, "mrays_s": (st.closest_rays + st.shadow_rays) / dt / 1e6,
+           "triangles": desc.num_triangles, "waves": st.waves}
+    s.close()
+    return out
+
+
+def config4(ctx, n_jobs=64):
+    jobs = [sc.batch_job(i) for i in range(n_jobs)]
+    scenes = [gr.Scene(ctx, d) for d, _ in jobs]
+    opts = [dict(spp=spp, max_depth=8, seed=i) for i, (_, spp) in enumerate(jobs)]
+    samples = sum(d.camera["width"] * d.camera["height"] * spp for d, spp in jobs)
+    # warm-up: one small render per scene (captures graphs, touches memory)
+    for s in scenes:
+        s.render(1, 8, 0, want_image=False)
+        s.reset()
+    gr.render_batch(ctx, scenes, [dict(spp=1, max_depth=8)] * len(scenes))
+    for s in scenes:
+        s.reset()
+    t = time.perf_counter()
+    rays = 0
+    for s, o in zip(scenes, opts):
+        _, st = s.render(o["spp"], 8, o["seed"], want_image=False)
+        rays += st.closest_rays + st.shadow_rays
+    t_seq = time.perf_counter() - t
+    # the reference's schedule: one frame (1 spp) per render() call, launched
+    # kernel by kernel and waited for (PathTracer::render(num), pathtracer.cu:152-170)
+    for s in scenes:
+        s.reset()
+    t = time.perf_counter()
+    for s, o in zip(scenes, opts):
+        for _ in range(o["spp"]):
+            s.render(1, 8, o["seed"], flags=gr.RENDER_NO_GRAPH, want_image=False)
+    t_frames = time.perf_counter() - t
+    for s in scenes:
+        s.reset()
+    t = time.perf_counter()
+    st = gr.render_batch(ctx, scenes, opts)
+    t_batch = time.perf_counter() - t
+    out = {"jobs": n_jobs, "triangles": sum(d.num_triangles for d, _ in jobs), "samples": samples,
+           "per_frame_renders_s": n_jobs / t_frames, "sequential_renders_s": n_jobs / t_seq,
+           "batched_renders_s": n_jobs / t_batch, "speedup_vs_per_frame": t_frames / t_batch,
+           "speedup_vs_sequential": t_seq / t_batch, "per_frame_s": t_frames, "sequential_s": t_seq,
+           "batched_s": t_batch,
+           "batched_mrays_s": (st.closest_rays + st.shadow_rays) / t_batch / 1e6,
+           "sequential_mrays_s": rays / t_seq / 1e6, "batched_waves": st.waves}
+    for s in scenes:
+        s.close()
+    return out
+
+
+def _serve(ctx, scenes, requests, budget, max_active, rate):
+    """Submits `requests` (scene index, camera, spp, seed) at Poisson times of
+    `rate` per second; returns latency and throughput figures."""
+    srv = gr.Server(ctx, budget_bytes=budget, max_active=max_active)
+    r = np.random.default_rng(12345)
+    gaps = r.exponential(1.0 / rate, size=len(requests))
+    tickets = []
+    t0 = time.perf_counter()
+    t_next = t0
+    for (si, cam, spp, seed), gap in zip(requests, gaps):
+        t_next += gap
+        delay = t_next - time.perf_counter()
+        if delay > 0:
+            time.sleep(delay)
+        tickets.append(srv.submit(scenes[si], spp, 8, seed, camera=cam))
+    lat, done_s, sub_s = [], [], []
+    for t in tickets:
+        ok, _, js = srv.wait(t, timeout=600.0)
+        if ok:
+            lat.append(js.done_s - js.submit_s)
+            done_s.append(js.done_s)
+            sub_s.append(js.submit_s)
+    st = srv.stats()
+    srv.close()
+    span = max(done_s) - min(sub_s) if done_s else float("nan")
+    lat = np.asarray(lat)
+    return {"rate": rate, "requests": len(requests), "completed": len(lat),
+            "p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
+            "renders_s": len(lat) / span, "waves": int(st.waves), "peak_bytes": int(st.peak_bytes)}
+
+
+def config5(ctx, rates=(10, 20, 50), window_s=3.0, pool=8, budget=150 * 10**9):
+    descs = [sc.batch_job(i)[0] for i in range(pool)]
+    scenes = [gr.Scene(ctx, d) for d in descs]
+    r = np.random.default_rng(0x5EED0005)
+    out = {"scene_pool": pool, "budget_bytes": budget, "window_s": window_s, "sweep": []}
+
+    def make_requests(n):
+        reqs = []
+        for k in range(n):
+            si = int(r.integers(0, pool))
+            res = int(r.choice(sc.RESOLUTIONS))
+            spp = int(r.choice(sc.SPPS))
+            cam = dict(descs[si].camera, width=res, height=res)
+            reqs.append((si, cam, spp, k))
+        return reqs
+
+    for rate in rates:
+        reqs = make_requests(max(4, int(rate * window_s)))
+        out["sweep"].append(_serve(ctx, scenes, reqs, budget, 0, rate))
+    # the same stream at the highest rate, one job at a time (no batching)
+    reqs = make_requests(max(4, int(rates[-1] * window_s)))
+    out["batched_at_max_rate"] = _serve(ctx, scenes, reqs, budget, 0, rates[-1])
+    out["sequential_at_max_rate"] = _serve(ctx, scenes, reqs, budget, 1, rates[-1])
+    out["speedup_renders_s"] = out["batched_at_max_rate"]["renders_s"] / out["sequential_at_max_rate"]["renders_s"]
+    # the same requests rendered the reference's way, frame by frame, one after
+    # another, on scenes created beforehand for each (scene id, resolution)
+    views = {}
+    for si, cam, _, _ in reqs:
+        if (si, cam["width"]) not in views:
+            d = descs[si]
+            views[(si, cam["width"])] = gr.Scene(ctx, sc.SceneDesc(d.meshes, d.materials, cam, d.env))
+    t = time.perf_counter()
+    for si, cam, spp, seed in reqs:
+        target = views[(si, cam["width"])]
+        target.reset()
+        for _ in range(spp):
+            target.render(1, 8, seed, flags=gr.RENDER_NO_GRAPH, want_image=False)
+    out["per_frame_renders_s"] = len(reqs) / (time.perf_counter() - t)
+    for v in views.values():
+        v.close()
+    out["speedup_vs_per_frame"] = out["batched_at_max_rate"]["renders_s"] / out["per_frame_renders_s"]
+    for s in scenes:
+        s.close()
+    return out

@@ -233,6 +233,33 @@ gr_status gr_scene_reset(gr_scene* scene);
 /* Device bytes the scene holds (geometry, BVH, accumulation). */
 uint64_t gr_scene_device_bytes(const gr_scene* scene);
 
+/* ---- scene files ---------------------------------------------------------------
+ * Replaces load_scene / load_mitsuba_file / load_obj_file (src/renderer/loaders/
+ * loader.h:11-29, mitsubaloader.cpp, objloader.cpp). The Mitsuba-XML subset
+ * the reference reads: sensor (fov, toWorld), film (width, height), bsdf
+ * (diffuse, mirror, glass, dielectric, roughdielectric, conductor,
+ * roughconductor; roughplastic is read as Lambert; twosided; named ids and
+ * ref), emitter (area, constant), shape (obj, sphere, rectangle, cube),
+ * transform (lookat, translate, scale, rotate, matrix). A parsed description
+ * can be inspected without a GPU. */
+typedef struct gr_scene_desc gr_scene_desc;
+
+/* Parses an XML scene and the OBJ files it names. On GR_ERR_PARSE the
+ * description still exists and gr_scene_desc_error tells why. */
+gr_status gr_scene_desc_load_xml(const char* path, gr_scene_desc** out);
+gr_status gr_scene_desc_destroy(gr_scene_desc* desc);
+const char* gr_scene_desc_error(const gr_scene_desc* desc);
+/* Features read approximately (one per line), e.g. a roughplastic bsdf. */
+const char* gr_scene_desc_warnings(const gr_scene_desc* desc);
+gr_status gr_scene_desc_info(const gr_scene_desc* desc, uint32_t* meshes, uint32_t* triangles, uint32_t* lights,
+                             gr_camera* camera, gr_environment* env);
+/* Flattened triangles (9 floats each, world space), the mesh of each triangle,
+ * and one material per mesh. Any pointer may be NULL. */
+gr_status gr_scene_desc_triangles(const gr_scene_desc* desc, float* h_verts, uint32_t* h_mesh, gr_material* h_mats);
+gr_status gr_scene_create_from_desc(gr_ctx* ctx, const gr_scene_desc* desc, gr_scene** out);
+/* Parse + create: the drop-in for PathTracer(filename) (pathtracer.cu:8-11). */
+gr_status gr_scene_load_xml(gr_ctx* ctx, const char* path, gr_scene** out);
+
 /* ---- batched rendering (no counterpart in the reference) --------------------
  * Renders n jobs to completion with their samples packed into shared waves:
  * each wave's kernels cover every job in it (rays of all scenes share the

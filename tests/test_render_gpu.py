@@ -87,3 +87,14 @@ def test_converged_rmse(ctx):
     ratio = errs[64] / errs[1024]
     assert 2.5 < ratio < 6.5, errs  # ideal 4
     assert errs[1024] < 0.05 * float(ref.mean()) * 4, errs
+
+
+def test_xml_scene_renders_like_the_description(ctx, tmp_path):
+    from gr import mitsuba
+    d = sc.glossy_scene(40, 30, level=2, glass_level=1)
+    path = mitsuba.write_scene(d, str(tmp_path))
+    a = gr.load_xml(ctx, path)
+    b = gr.Scene(ctx, d)
+    ia, _ = a.render(4, max_depth=8, seed=21)
+    ib, _ = b.render(4, max_depth=8, seed=21)
+    np.testing.assert_array_equal(ia, ib)
