@@ -97,4 +97,7 @@ def test_xml_scene_renders_like_the_description(ctx, tmp_path):
     b = gr.Scene(ctx, d)
     ia, _ = a.render(4, max_depth=8, seed=21)
     ib, _ = b.render(4, max_depth=8, seed=21)
-    np.testing.assert_array_equal(ia, ib)
+    # positions round-trip bit for bit; the loader re-normalises shading
+    # normals after the shape transform (as the reference does), so shading
+    # differs in the last bits
+    assert mean_rel_err(ia, ib) < 1e-5
