@@ -173,9 +173,14 @@ gr_status gr_bvh_build(gr_bvh* bvh, const float* d_verts, uint32_t n, void* stre
     if (n > 0 && !d_verts) return fail(bvh->ctx, GR_ERR_INVALID, "null vertex pointer");
     GR_CUDA(bvh->ctx, cudaSetDevice(bvh->ctx->device));
     bvh->built = false;
+    bvh->built4 = bvh->built4q = false;
     GR_CUDA(bvh->ctx, gr::lbvh_build(bvh->buf, d_verts, n, bvh->ctx->num_sms, as_stream(stream)));
     bvh->n = n;
     bvh->built = true;
+    if (bvh->layout != 0) {  // keep the requested traversal layout current
+        GR_CUDA(bvh->ctx, gr::bvh4_build(bvh->buf, n, bvh->layout, as_stream(stream)));
+        (bvh->layout == gr::kLayoutBvh4 ? bvh->built4 : bvh->built4q) = true;
+    }
     return GR_OK;
 }
 
@@ -233,8 +238,11 @@ gr_status gr_trace(gr_bvh* bvh, const gr_ray* d_rays, uint64_t n, gr_hit* d_hits
     GR_CUDA(ctx, cudaSetDevice(ctx->device));
     unsigned long long* counter = (unsigned long long*)ctx->counter.p;
     uint32_t* err = (uint32_t*)((char*)ctx->counter.p + 64);
-    GR_CUDA(ctx, gr::trace_launch(device_view(bvh), d_rays, n, d_hits, any_hit, counter, err, ctx->num_sms,
-                                  as_stream(stream)));
+    const void* nodes = bvh->layout == gr::kLayoutBvh4 ? bvh->buf.nodes4.p
+                        : bvh->layout == gr::kLayoutBvh4Q8 ? bvh->buf.nodes4q.p
+                                                             : bvh->buf.nodes.p;
+    GR_CUDA(ctx, gr::trace_launch(device_view(bvh), nodes, bvh->layout, d_rays, n, d_hits, any_hit, counter, err,
+                                  ctx->num_sms, as_stream(stream)));
     return GR_OK;
 }
 
@@ -279,5 +287,34 @@ extern "C" gr_status gr_bvh_build_noalloc(gr_ctx* ctx, const float* d_verts, uin
     GR_CUDA(ctx, cudaSetDevice(ctx->device));
     GR_CUDA(ctx, gr::lbvh_build_static(d_verts, n, (gr::Node*)d_nodes, (gr::Tri*)d_tris, d_sorted_code, d_sorted_prim,
                                        (gr::BvhMeta*)d_header, ctx->device, ctx->num_sms, as_stream(stream)));
+    return GR_OK;
+}
+
+extern "C" gr_status gr_bvh_set_layout(gr_bvh* bvh, int layout, void* stream) {
+    if (!bvh || layout < 0 || layout > 2) return GR_ERR_INVALID;
+    GR_CUDA(bvh->ctx, cudaSetDevice(bvh->ctx->device));
+    if (bvh->built && layout != 0) {
+        bool& done = layout == gr::kLayoutBvh4 ? bvh->built4 : bvh->built4q;
+        if (!done) {
+            GR_CUDA(bvh->ctx, gr::bvh4_build(bvh->buf, bvh->n, layout, as_stream(stream)));
+            done = true;
+        }
+    }
+    bvh->layout = layout;
+    return GR_OK;
+}
+
+extern "C" gr_status gr_bvh_export_layout(gr_bvh* bvh, int layout, void* h_nodes) {
+    if (!bvh || !bvh->built || layout < 1 || layout > 2 || !h_nodes) return GR_ERR_INVALID;
+    const int keep = bvh->layout;
+    gr_status st = gr_bvh_set_layout(bvh, layout, bvh->ctx->stream);
+    bvh->layout = keep;
+    if (st != GR_OK) return st;
+    GR_CUDA(bvh->ctx, cudaStreamSynchronize(bvh->ctx->stream));
+    GR_CUDA(bvh->ctx, cudaDeviceSynchronize());
+    const size_t count = bvh->n > 1 ? bvh->n - 1 : 1;
+    if (bvh->n == 0) return GR_OK;
+    const gr::DevBuf& src = layout == gr::kLayoutBvh4 ? bvh->buf.nodes4 : bvh->buf.nodes4q;
+    GR_CUDA(bvh->ctx, cudaMemcpy(h_nodes, src.p, count * (layout == gr::kLayoutBvh4 ? 128 : 64), cudaMemcpyDeviceToHost));
     return GR_OK;
 }

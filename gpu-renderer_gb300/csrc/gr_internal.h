@@ -38,6 +38,34 @@ struct Node {
 };
 static_assert(sizeof(Node) == 64, "node layout");
 
+// 4-wide node with FP32 child boxes, 128 bytes: boxes in SoA order
+// (lo.x[4], hi.x[4], lo.y[4], hi.y[4], lo.z[4], hi.z[4]), child references
+// (same encoding as Node), and the valid-child mask in w[0].
+struct Node4 {
+    float4 lox, hix, loy, hiy, loz, hiz;
+    int4 child;
+    uint4 meta;  // x: child mask (bit k = slot k valid)
+};
+static_assert(sizeof(Node4) == 128, "node4 layout");
+
+// 4-wide node with 8-bit quantised child boxes, 64 bytes. A child plane is
+// origin + q * 2^e (one FMA), with q rounded outward so the decoded box
+// contains the FP32 child box:
+//   q0 = (origin.x, origin.y, origin.z, meta): meta bits 0-7 / 8-15 / 16-23 are
+//        the biased exponents ex, ey, ez (e + 127), bits 24-27 the child mask
+//   q1 = bytes qlo.x[4], qhi.x[4], qlo.y[4], qhi.y[4]
+//   q2 = bytes qlo.z[4], qhi.z[4], 0, 0
+//   q3 = child references
+struct Node4Q {
+    float4 q0;
+    uint4 q1;
+    uint4 q2;
+    int4 child;
+};
+static_assert(sizeof(Node4Q) == 64, "node4q layout");
+
+enum Layout : int { kLayoutBvh2 = 0, kLayoutBvh4 = 1, kLayoutBvh4Q8 = 2 };
+
 // Leaf-order triangle: three 16-byte words (v0, prim bits), (v1, 0), (v2, 0).
 struct Tri {
     float4 a, b, c;
@@ -69,6 +97,7 @@ struct BvhDevice {
 // Build scratch + outputs, sliced from a few allocations.
 struct BvhBuffers {
     DevBuf nodes, tris, code, prim;  // outputs kept for traversal / export
+    DevBuf nodes4, nodes4q;          // 4-wide layouts (built on request), indexed like `nodes`
     DevBuf scratch;                  // transient build state
     DevBuf meta;                     // small device header (root, unique count, error word)
 };
@@ -91,9 +120,14 @@ uint32_t lbvh_static_max_triangles();
 cudaError_t lbvh_build_static(const float* d_verts, uint32_t n, Node* nodes, Tri* tris, uint32_t* code,
                               uint32_t* prim, BvhMeta* meta, int device, int num_sms, cudaStream_t s);
 
+// bvh4.cu: 4-wide layouts collapsed from the binary nodes (every node at
+// even depth becomes a 4-wide node at the same index)
+cudaError_t bvh4_build(BvhBuffers& b, uint32_t n, int layout, cudaStream_t s);
+
 // trace.cu
-cudaError_t trace_launch(const BvhDevice& bvh, const gr_ray* d_rays, uint64_t n, gr_hit* d_hits, int any_hit,
-                         unsigned long long* d_counter, uint32_t* d_err, int num_sms, cudaStream_t s);
+cudaError_t trace_launch(const BvhDevice& bvh, const void* nodes, int layout, const gr_ray* d_rays, uint64_t n,
+                         gr_hit* d_hits, int any_hit, unsigned long long* d_counter, uint32_t* d_err, int num_sms,
+                         cudaStream_t s);
 
 }  // namespace gr
 
@@ -125,5 +159,7 @@ struct gr_bvh {
     // not copyable: owns device memory
     uint32_t n = 0;
     bool built = false;
+    int layout = 0;       // traversal layout gr_trace uses
+    bool built4 = false, built4q = false;
     gr::BvhBuffers buf;
 };

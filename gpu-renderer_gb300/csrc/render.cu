@@ -245,7 +245,7 @@ struct QueueSrc {
     const uint32_t* __restrict__ q;
     const Paths* ps;
     uint64_t n;
-    __device__ __forceinline__ uint32_t load(uint64_t i, float4& r0, float4& r1, const Node*& nd, const Tri*& tr) const {
+    __device__ __forceinline__ uint32_t load(uint64_t i, float4& r0, float4& r1, const void*& nd, const Tri*& tr) const {
         const uint32_t pid = q[i];
         r0 = ps->ray[2ull * pid];
         r1 = ps->ray[2ull * pid + 1];
@@ -261,11 +261,12 @@ struct QueueSrc {
     }
 };
 
+template <int LAYOUT>
 __global__ void __launch_bounds__(trav::kTraceThreads) k_trace_queue(Paths ps, int b) {
     __shared__ int2 s_stack[trav::kShortStack][trav::kTraceThreads];
     if (b > (int)ps.hdr->max_depth) return;
     QueueSrc src{(b & 1) ? ps.qb : ps.qa, &ps, ps.cnt[b]};
-    trav::traverse_loop<false>(src, ps.work + b, ps.cnt + kErrWord, s_stack);
+    trav::traverse_loop<false, LAYOUT>(src, ps.work + b, ps.cnt + kErrWord, s_stack);
 }
 
 // Shadow rays: an unoccluded ray adds its contribution to its path
@@ -273,7 +274,7 @@ __global__ void __launch_bounds__(trav::kTraceThreads) k_trace_queue(Paths ps, i
 struct ShadowSrc {
     const Paths* ps;
     uint64_t n;
-    __device__ __forceinline__ uint32_t load(uint64_t i, float4& r0, float4& r1, const Node*& nd, const Tri*& tr) const {
+    __device__ __forceinline__ uint32_t load(uint64_t i, float4& r0, float4& r1, const void*& nd, const Tri*& tr) const {
         r0 = ps->sray[2 * i];
         r1 = ps->sray[2 * i + 1];
         const uint32_t pid = __float_as_uint(ps->scon[i].w);
@@ -294,11 +295,12 @@ struct ShadowSrc {
     }
 };
 
+template <int LAYOUT>
 __global__ void __launch_bounds__(trav::kTraceThreads) k_trace_shadow(Paths ps, int b) {
     __shared__ int2 s_stack[trav::kShortStack][trav::kTraceThreads];
     if (b >= (int)ps.hdr->max_depth) return;
     ShadowSrc src{&ps, ps.cnt[kShadowBase + b]};
-    trav::traverse_loop<true>(src, ps.work + kShadowBase + b, ps.cnt + kErrWord, s_stack);
+    trav::traverse_loop<true, LAYOUT>(src, ps.work + kShadowBase + b, ps.cnt + kErrWord, s_stack);
 }
 
 // ---- shading --------------------------------------------------------------------------
@@ -475,7 +477,8 @@ __global__ void k_wave_end(Paths ps) {
 
 // One wave: clear counters, camera rays, kMaxWaveDepth x (trace, shade, shadow)
 // (steps past the wave's max_depth return at once), resolve, ray counts.
-cudaError_t issue_wave(const Paths& ps, uint32_t depth_steps, int tgrid, int sgrid, cudaStream_t s) {
+template <int LAYOUT>
+cudaError_t issue_wave_l(const Paths& ps, uint32_t depth_steps, int tgrid, int sgrid, cudaStream_t s) {
     cudaError_t e;
     const size_t cnt_bytes = sizeof(uint32_t) * (2 * kMaxDepth + 4);
     const size_t work_bytes = sizeof(unsigned long long) * (2 * kMaxDepth + 4);
@@ -483,13 +486,19 @@ cudaError_t issue_wave(const Paths& ps, uint32_t depth_steps, int tgrid, int sgr
     if ((e = cudaMemsetAsync(ps.work, 0, work_bytes, s)) != cudaSuccess) return e;
     k_camera<<<sgrid, kShadeThreads, 0, s>>>(ps);
     for (int b = 0; b <= (int)depth_steps; ++b) {
-        k_trace_queue<<<tgrid, trav::kTraceThreads, 0, s>>>(ps, b);
+        k_trace_queue<LAYOUT><<<tgrid, trav::kTraceThreads, 0, s>>>(ps, b);
         k_shade<<<sgrid, kShadeThreads, 0, s>>>(ps, b);
-        if (b < (int)depth_steps) k_trace_shadow<<<tgrid, trav::kTraceThreads, 0, s>>>(ps, b);
+        if (b < (int)depth_steps) k_trace_shadow<LAYOUT><<<tgrid, trav::kTraceThreads, 0, s>>>(ps, b);
     }
     k_resolve<<<sgrid, kShadeThreads, 0, s>>>(ps);
     k_wave_end<<<1, 32, 0, s>>>(ps);
     return cudaGetLastError();
+}
+
+cudaError_t issue_wave(const Paths& ps, uint32_t depth_steps, int tgrid, int sgrid, cudaStream_t s, int layout) {
+    if (layout == kLayoutBvh4) return issue_wave_l<kLayoutBvh4>(ps, depth_steps, tgrid, sgrid, s);
+    if (layout == kLayoutBvh4Q8) return issue_wave_l<kLayoutBvh4Q8>(ps, depth_steps, tgrid, sgrid, s);
+    return issue_wave_l<kLayoutBvh2>(ps, depth_steps, tgrid, sgrid, s);
 }
 
 uint64_t mix64(uint64_t h, uint64_t v) {
@@ -613,12 +622,13 @@ uint32_t pack_wave(std::vector<HostJob*>& jobs, uint32_t capacity, std::vector<J
 }
 
 cudaError_t run_wave(WavePool& pool, const JobDev* h_jobs, uint32_t njobs, uint32_t total_paths, uint32_t total_pix,
-                     uint32_t max_depth, int num_sms, cudaStream_t s, bool use_graph) {
+                     uint32_t max_depth, int num_sms, cudaStream_t s, bool use_graph, int layout) {
     static int occ = 0;
     cudaError_t e;
     if (occ == 0) {
-        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_trace_queue, trav::kTraceThreads, 0)) !=
-            cudaSuccess)
+        // the 4-wide kernels use the most registers; size the grid for them
+        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_trace_queue<kLayoutBvh4>, trav::kTraceThreads,
+                                                               0)) != cudaSuccess)
             return e;
         occ = std::max(occ, 1);
     }
@@ -645,16 +655,17 @@ cudaError_t run_wave(WavePool& pool, const JobDev* h_jobs, uint32_t njobs, uint3
     const int tgrid = num_sms * occ;
     const int sgrid = num_sms * 4;
     const uint32_t steps = std::max(max_depth, kGraphDepthSteps);
-    if (!use_graph) return issue_wave(ps, max_depth, tgrid, sgrid, s);
+    if (!use_graph) return issue_wave(ps, max_depth, tgrid, sgrid, s, layout);
     uint64_t key = 0x51ED270B27A3C1F5ull;
-    const uint64_t words[] = {(uint64_t)(uintptr_t)ps.ray, ps.capacity, steps, (uint64_t)tgrid, (uint64_t)sgrid};
+    const uint64_t words[] = {(uint64_t)(uintptr_t)ps.ray, ps.capacity, steps, (uint64_t)tgrid, (uint64_t)sgrid,
+                              (uint64_t)layout};
     for (uint64_t w : words) key = mix64(key, w);
     WaveGraph& g = pool.graph;
     if (!g.exec || g.key != key) {
         g.release();
         cudaGraph_t graph = nullptr;
         if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return e;
-        const cudaError_t ei = issue_wave(ps, steps, tgrid, sgrid, s);
+        const cudaError_t ei = issue_wave(ps, steps, tgrid, sgrid, s, layout);
         e = cudaStreamEndCapture(s, &graph);
         if (ei != cudaSuccess) {
             if (graph) cudaGraphDestroy(graph);

@@ -41,7 +41,7 @@ struct SceneDev {
     const uint32_t* lights;   // emissive triangle ids
     uint32_t num_lights;
     uint32_t num_tris;
-    const Node* nodes;
+    const void* nodes;  // traversal nodes in the wave's layout
     const Tri* tris;
     const BvhMeta* meta;
     DevCamera cam;
@@ -147,7 +147,10 @@ struct HostJob {
 // wave_samples, sample_base filled in). Uses the pool's captured graph unless
 // use_graph is false.
 cudaError_t run_wave(WavePool& pool, const JobDev* h_jobs, uint32_t njobs, uint32_t total_paths, uint32_t total_pix,
-                     uint32_t max_depth, int num_sms, cudaStream_t s, bool use_graph);
+                     uint32_t max_depth, int num_sms, cudaStream_t s, bool use_graph, int layout);
+
+// Scene view for a wave of the given node layout (the layout must be built).
+SceneDev scene_view(gr_scene* sc, int layout);
 
 // Packs as many samples of `jobs` (in order) as fit into `capacity` paths;
 // returns the number of jobs in the wave (0 when nothing fits). Advances

@@ -56,7 +56,9 @@ gr_status cuda_fail(gr_ctx* ctx, cudaError_t e, const char* where) {
 
 bool emissive(const gr_material& m) { return m.emission[0] != 0.0f || m.emission[1] != 0.0f || m.emission[2] != 0.0f; }
 
-gr::SceneDev scene_view(gr_scene* sc) {
+}  // namespace
+
+gr::SceneDev gr::scene_view(gr_scene* sc, int layout) {
     gr::SceneDev d{};
     d.verts = (const float*)sc->verts.p;
     d.normals = (const float4*)sc->normals.p;
@@ -65,7 +67,9 @@ gr::SceneDev scene_view(gr_scene* sc) {
     d.lights = (const uint32_t*)sc->lights.p;
     d.num_lights = sc->num_lights;
     d.num_tris = sc->num_tris;
-    d.nodes = (const gr::Node*)sc->bvh->buf.nodes.p;
+    d.nodes = layout == gr::kLayoutBvh4 ? sc->bvh->buf.nodes4.p
+              : layout == gr::kLayoutBvh4Q8 ? sc->bvh->buf.nodes4q.p
+                                            : sc->bvh->buf.nodes.p;
     d.tris = (const gr::Tri*)sc->bvh->buf.tris.p;
     d.meta = (const gr::BvhMeta*)sc->bvh->buf.meta.p;
     d.cam = sc->cam;
@@ -76,9 +80,17 @@ gr::SceneDev scene_view(gr_scene* sc) {
     return d;
 }
 
-}  // namespace
-
 extern "C" {
+
+gr_status gr_scene_set_layout(gr_scene* sc, int layout) {
+    if (!sc) return GR_ERR_INVALID;
+    gr_status st = gr_bvh_set_layout(sc->bvh, layout, sc->ctx->stream);
+    if (st != GR_OK) return st;
+    SC_CUDA(sc->ctx, cudaStreamSynchronize(sc->ctx->stream));
+    return GR_OK;
+}
+
+int gr_scene_layout(const gr_scene* sc) { return sc && sc->bvh ? sc->bvh->layout : -1; }
 
 gr_status gr_scene_create(gr_ctx* ctx, const gr_mesh* meshes, uint32_t num_meshes, const gr_material* materials,
                           uint32_t num_materials, const gr_camera* camera, const gr_environment* env,
@@ -228,7 +240,8 @@ gr_status gr_render(gr_scene* sc, const gr_render_opts* opts, float* h_rgb, gr_r
     gr::WaveHeader before{};
     SC_CUDA(ctx, cudaMemcpyAsync(&before, sc->pool.ps.hdr, sizeof(before), cudaMemcpyDeviceToHost, s));
     gr::HostJob job;
-    job.sc = scene_view(sc);
+    const int layout = sc->bvh->layout;
+    job.sc = gr::scene_view(sc, layout);
     job.fb = (double*)sc->fb.p;
     job.fbc = (uint32_t*)sc->fb_count.p;
     job.npix = npix;
@@ -247,7 +260,7 @@ gr_status gr_render(gr_scene* sc, const gr_render_opts* opts, float* h_rgb, gr_r
         const uint32_t nj = gr::pack_wave(jobs, (uint32_t)cap64, table, &paths, &pix, &depth);
         if (nj == 0) break;
         SC_CUDA(ctx, gr::run_wave(sc->pool, table.data(), nj, paths, pix, depth, ctx->num_sms, s,
-                                  (opts->flags & GR_RENDER_NO_GRAPH) == 0));
+                                  (opts->flags & GR_RENDER_NO_GRAPH) == 0, layout));
         ++waves;
     }
     gr::WaveHeader after{};

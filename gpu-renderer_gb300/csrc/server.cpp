@@ -26,26 +26,6 @@ namespace {
 
 gr_status cuda_status(cudaError_t e) { return e == cudaErrorMemoryAllocation ? GR_ERR_OOM_BUDGET : GR_ERR_CUDA; }
 
-gr::SceneDev view_of(gr_scene* sc) {
-    gr::SceneDev d{};
-    d.verts = (const float*)sc->verts.p;
-    d.normals = (const float4*)sc->normals.p;
-    d.tri_mat = (const uint32_t*)sc->tri_mat.p;
-    d.mats = (const gr::DevMaterial*)sc->mats.p;
-    d.lights = (const uint32_t*)sc->lights.p;
-    d.num_lights = sc->num_lights;
-    d.num_tris = sc->num_tris;
-    d.nodes = (const gr::Node*)sc->bvh->buf.nodes.p;
-    d.tris = (const gr::Tri*)sc->bvh->buf.tris.p;
-    d.meta = (const gr::BvhMeta*)sc->bvh->buf.meta.p;
-    d.cam = sc->cam;
-    d.env_r = sc->env[0];
-    d.env_g = sc->env[1];
-    d.env_b = sc->env[2];
-    d.has_env = sc->has_env;
-    return d;
-}
-
 uint32_t default_capacity(uint32_t wave_paths) { return wave_paths ? wave_paths : (1u << 22); }
 
 // Per-pixel mean of an accumulation (for the server's results).
@@ -87,8 +67,12 @@ extern "C" gr_status gr_render_batch(gr_ctx* ctx, gr_scene* const* scenes, const
                 ctx->last_error = "gr_render_batch: a scene appears twice";
                 return GR_ERR_INVALID;
             }
+        if (sc->bvh->layout != scenes[0]->bvh->layout) {
+            ctx->last_error = "gr_render_batch: scenes use different node layouts";
+            return GR_ERR_INVALID;
+        }
         gr::HostJob& j = jobs[i];
-        j.sc = view_of(sc);
+        j.sc = gr::scene_view(sc, sc->bvh->layout);
         j.fb = (double*)sc->fb.p;
         j.fbc = (uint32_t*)sc->fb_count.p;
         j.npix = sc->cam.width * sc->cam.height;
@@ -126,7 +110,8 @@ extern "C" gr_status gr_render_batch(gr_ctx* ctx, gr_scene* const* scenes, const
         uint32_t paths = 0, pix = 0, depth = 0;
         const uint32_t nj = gr::pack_wave(order, pool.capacity, table, &paths, &pix, &depth);
         if (nj == 0) break;
-        if ((e = gr::run_wave(pool, table.data(), nj, paths, pix, depth, ctx->num_sms, s, graph)) != cudaSuccess) {
+        if ((e = gr::run_wave(pool, table.data(), nj, paths, pix, depth, ctx->num_sms, s, graph,
+                              scenes[0]->bvh->layout)) != cudaSuccess) {
             ctx->last_error = std::string("gr_render_batch: ") + cudaGetErrorString(e);
             cudaGetLastError();
             return cuda_status(e);
@@ -322,7 +307,8 @@ struct gr_server {
                 uint32_t paths = 0, pix = 0, depth = 0;
                 const uint32_t nj = gr::pack_wave(hjs, pool.capacity, table, &paths, &pix, &depth);
                 if (nj) {
-                    const cudaError_t e = gr::run_wave(pool, table.data(), nj, paths, pix, depth, ctx->num_sms, stream, true);
+                    const cudaError_t e = gr::run_wave(pool, table.data(), nj, paths, pix, depth, ctx->num_sms, stream,
+                                                       true, opts.layout);
                     if (e != cudaSuccess) {
                         std::lock_guard<std::mutex> lk(mu);
                         error = cudaGetErrorString(e);
@@ -422,7 +408,12 @@ gr_status gr_server_submit(gr_server* sv, gr_scene* scene, const gr_camera* came
                            uint64_t* ticket) {
     if (!sv || !scene || !opts || !ticket || scene->ctx != sv->ctx) return GR_ERR_INVALID;
     if (opts->max_depth > (uint32_t)gr::kMaxDepth) return GR_ERR_INVALID;
-    gr::SceneDev view = view_of(scene);
+    // the scene must have the server's node layout built before it joins a wave
+    if (scene->bvh->layout != sv->opts.layout || !scene->bvh->built) {
+        gr_status st = gr_scene_set_layout(scene, sv->opts.layout);
+        if (st != GR_OK) return st;
+    }
+    gr::SceneDev view = gr::scene_view(scene, sv->opts.layout);
     if (camera) {
         if (camera->width == 0 || camera->height == 0 || !(camera->fov_deg > 0.0f && camera->fov_deg < 180.0f))
             return GR_ERR_INVALID;

@@ -25,10 +25,10 @@ struct RaySrc {
     const float4* __restrict__ rays;
     float4* __restrict__ hits;
     uint64_t n;
-    const Node* nodes;
+    const void* nodes;
     const Tri* tris;
     uint32_t root;
-    __device__ __forceinline__ uint32_t load(uint64_t i, float4& r0, float4& r1, const Node*& nd, const Tri*& tr) const {
+    __device__ __forceinline__ uint32_t load(uint64_t i, float4& r0, float4& r1, const void*& nd, const Tri*& tr) const {
         r0 = __ldg(rays + 2 * i);
         r1 = __ldg(rays + 2 * i + 1);
         nd = nodes;
@@ -41,42 +41,53 @@ struct RaySrc {
     }
 };
 
-template <bool ANY>
-__global__ void __launch_bounds__(trav::kTraceThreads) k_trace(const Node* __restrict__ nodes, const Tri* __restrict__ tris,
+template <bool ANY, int LAYOUT>
+__global__ void __launch_bounds__(trav::kTraceThreads) k_trace(const void* __restrict__ nodes, const Tri* __restrict__ tris,
                                                                const BvhMeta* __restrict__ meta,
                                                                const float4* __restrict__ rays, uint64_t n,
                                                                float4* __restrict__ hits, unsigned long long* counter,
                                                                uint32_t* err) {
     __shared__ int2 s_stack[trav::kShortStack][trav::kTraceThreads];
     RaySrc src{rays, hits, n, nodes, tris, meta->root};
-    trav::traverse_loop<ANY>(src, counter, err, s_stack);
+    trav::traverse_loop<ANY, LAYOUT>(src, counter, err, s_stack);
+}
+
+template <bool ANY, int LAYOUT>
+cudaError_t launch(const BvhDevice& bvh, const void* nodes, const float4* r, uint64_t n, float4* h,
+                   unsigned long long* counter, uint32_t* err, int num_sms, cudaStream_t s) {
+    static int occ = 0;
+    if (occ == 0) {
+        const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_trace<ANY, LAYOUT>,
+                                                                            trav::kTraceThreads, 0);
+        if (e != cudaSuccess) return e;
+        if (occ < 1) occ = 1;
+    }
+    const uint64_t warps_needed = (n + 31) / 32;
+    const uint64_t blocks_needed = (warps_needed + trav::kTraceThreads / 32 - 1) / (trav::kTraceThreads / 32);
+    const int grid = (int)std::min<uint64_t>((uint64_t)num_sms * occ, blocks_needed);
+    k_trace<ANY, LAYOUT><<<grid, trav::kTraceThreads, 0, s>>>(nodes, bvh.tris, bvh.meta, r, n, h, counter, err);
+    return cudaGetLastError();
 }
 
 }  // namespace
 
-cudaError_t trace_launch(const BvhDevice& bvh, const gr_ray* d_rays, uint64_t n, gr_hit* d_hits, int any_hit,
-                         unsigned long long* d_counter, uint32_t* d_err, int num_sms, cudaStream_t s) {
+cudaError_t trace_launch(const BvhDevice& bvh, const void* nodes, int layout, const gr_ray* d_rays, uint64_t n,
+                         gr_hit* d_hits, int any_hit, unsigned long long* d_counter, uint32_t* d_err, int num_sms,
+                         cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), s);
     if (e != cudaSuccess) return e;
-    static int occ[2] = {0, 0};
-    int& o = occ[any_hit ? 1 : 0];
-    if (o == 0) {
-        e = any_hit ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_trace<true>, trav::kTraceThreads, 0)
-                    : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_trace<false>, trav::kTraceThreads, 0);
-        if (e != cudaSuccess) return e;
-        if (o < 1) o = 1;
-    }
-    const uint64_t warps_needed = (n + 31) / 32;
-    const uint64_t blocks_needed = (warps_needed + trav::kTraceThreads / 32 - 1) / (trav::kTraceThreads / 32);
-    const int grid = (int)std::min<uint64_t>((uint64_t)num_sms * o, blocks_needed);
     const float4* r = reinterpret_cast<const float4*>(d_rays);
     float4* h = reinterpret_cast<float4*>(d_hits);
-    if (any_hit)
-        k_trace<true><<<grid, trav::kTraceThreads, 0, s>>>(bvh.nodes, bvh.tris, bvh.meta, r, n, h, d_counter, d_err);
-    else
-        k_trace<false><<<grid, trav::kTraceThreads, 0, s>>>(bvh.nodes, bvh.tris, bvh.meta, r, n, h, d_counter, d_err);
-    return cudaGetLastError();
+    switch (layout * 2 + (any_hit ? 1 : 0)) {
+        case 0: return launch<false, kLayoutBvh2>(bvh, nodes, r, n, h, d_counter, d_err, num_sms, s);
+        case 1: return launch<true, kLayoutBvh2>(bvh, nodes, r, n, h, d_counter, d_err, num_sms, s);
+        case 2: return launch<false, kLayoutBvh4>(bvh, nodes, r, n, h, d_counter, d_err, num_sms, s);
+        case 3: return launch<true, kLayoutBvh4>(bvh, nodes, r, n, h, d_counter, d_err, num_sms, s);
+        case 4: return launch<false, kLayoutBvh4Q8>(bvh, nodes, r, n, h, d_counter, d_err, num_sms, s);
+        case 5: return launch<true, kLayoutBvh4Q8>(bvh, nodes, r, n, h, d_counter, d_err, num_sms, s);
+        default: return cudaErrorInvalidValue;
+    }
 }
 
 }  // namespace gr

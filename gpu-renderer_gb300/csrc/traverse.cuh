@@ -52,6 +52,13 @@ __device__ __forceinline__ RayW prepare(const float4 r0, const float4 r1) {
     return p;
 }
 
+// Relative slack on every cull: a box (or a deferred stack entry) is kept
+// while its entry distance is within (1 + 2^-20) of the exit / closest-hit
+// distance, so a triangle whose hit distance rounds an ulp below its box's
+// entry distance is still reached and the closest hit does not depend on the
+// order boxes are visited in.
+constexpr float kCullSlack = 1.00000095367431640625f;  // 1 + 2^-20
+
 __device__ __forceinline__ bool slab(const RayW& p, float lox, float hix, float loy, float hiy, float loz, float hiz,
                                      float tbest, float& tn) {
     const float x0 = __fmaf_rn(lox, p.ix, p.nox), x1 = __fmaf_rn(hix, p.ix, p.nox);
@@ -60,7 +67,7 @@ __device__ __forceinline__ bool slab(const RayW& p, float lox, float hix, float 
     const float tnear = fmaxf(fmaxf(fminf(x0, x1), fminf(y0, y1)), fmaxf(fminf(z0, z1), p.tmin));
     const float tfar = fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fminf(fmaxf(z0, z1), tbest));
     tn = tnear;
-    return tnear <= tfar;
+    return tnear <= __fmul_rn(tfar, kCullSlack);
 }
 
 __device__ __forceinline__ bool tri_test(const RayW& p, const float4 a, const float4 b, const float4 c, float tbest,
@@ -102,7 +109,7 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
 // finishes the lane goes idle and is refilled with a new ray once enough lanes
 // of the warp are idle, so long-tailed rays do not hold a whole warp.
 struct Lane {
-    const Node* nodes;  // BVH of this lane's ray (rays of one queue may belong to different scenes)
+    const void* nodes;  // BVH of this lane's ray (rays of one queue may belong to different scenes)
     const Tri* tris;
     RayW p;
     float best_t, bu, bv;
@@ -112,13 +119,60 @@ struct Lane {
     int sp;
 };
 
-// Processes one node for the lane; returns true when the ray is finished.
+// Tests leaf triangle `c` (~sorted position); returns true when an any-hit
+// query is answered. Closest-hit ties at equal t go to the smaller prim id.
 template <bool ANY>
-__device__ __forceinline__ bool trace_step(Lane& L, int2 (*s_stack)[kTraceThreads], int2* l_stack, uint32_t* err) {
-    const int tid = threadIdx.x;
-    const Node* __restrict__ nodes = L.nodes;
-    const Tri* __restrict__ tris = L.tris;
-    const float4* q = reinterpret_cast<const float4*>(nodes + L.node);
+__device__ __forceinline__ bool leaf(Lane& L, int32_t c) {
+    const Tri* tr = L.tris + (uint32_t)(~c);
+    const float4 a = __ldg(&tr->a), b = __ldg(&tr->b), cc = __ldg(&tr->c);
+    float t, u, v;
+    if (!tri_test(L.p, a, b, cc, L.best_t, t, u, v)) return false;
+    const uint32_t prim = __float_as_uint(a.w);
+    if (ANY) {
+        L.best_t = t; L.bu = u; L.bv = v; L.best_prim = prim;
+        return true;
+    }
+    if (t < L.best_t || prim < L.best_prim) {
+        L.best_t = t; L.bu = u; L.bv = v; L.best_prim = prim;
+    }
+    return false;
+}
+
+// Pushes a deferred node with its entry distance; false on overflow.
+__device__ __forceinline__ bool push(Lane& L, int32_t c, float tn, int2 (*s_stack)[kTraceThreads], int2* l_stack,
+                                     uint32_t* err) {
+    if (L.sp < kShortStack) {
+        s_stack[L.sp][threadIdx.x] = make_int2(c, __float_as_int(tn));
+    } else if (L.sp < kStackMax) {
+        l_stack[L.sp - kShortStack] = make_int2(c, __float_as_int(tn));
+    } else {
+        atomicOr(err, ERR_STACK);
+        return false;
+    }
+    ++L.sp;
+    return true;
+}
+
+// Pops the next deferred node still in front of the closest hit; false when
+// the stack is empty (the ray is finished).
+template <bool ANY>
+__device__ __forceinline__ bool pop(Lane& L, int2 (*s_stack)[kTraceThreads], const int2* l_stack, int32_t& next) {
+    for (;;) {
+        if (L.sp == 0) return false;
+        --L.sp;
+        const int2 e = L.sp < kShortStack ? s_stack[L.sp][threadIdx.x] : l_stack[L.sp - kShortStack];
+        if (ANY || __int_as_float(e.y) <= __fmul_rn(L.best_t, kCullSlack)) {
+            next = e.x;
+            return true;
+        }
+    }
+}
+
+// One binary node: both child boxes, nearer first; leaves tested inline.
+// Returns true when the ray is finished.
+template <bool ANY>
+__device__ __forceinline__ bool trace_step2(Lane& L, int2 (*s_stack)[kTraceThreads], int2* l_stack, uint32_t* err) {
+    const float4* q = reinterpret_cast<const float4*>(static_cast<const Node*>(L.nodes) + L.node);
     const float4 q0 = __ldg(q), q1 = __ldg(q + 1), q2 = __ldg(q + 2);
     const int4 q3 = __ldg(reinterpret_cast<const int4*>(q + 3));
     float tn0, tn1;
@@ -136,58 +190,135 @@ __device__ __forceinline__ bool trace_step(Lane& L, int2 (*s_stack)[kTraceThread
         const int32_t c = s == 0 ? cn : cf;
         if (!h) continue;
         if (c < 0) {
-            const Tri* tr = tris + (uint32_t)(~c);
-            const float4 a = __ldg(&tr->a), b = __ldg(&tr->b), cc = __ldg(&tr->c);
-            float t, u, v;
-            if (tri_test(L.p, a, b, cc, L.best_t, t, u, v)) {
-                const uint32_t prim = __float_as_uint(a.w);
-                if (ANY) {
-                    L.best_t = t; L.bu = u; L.bv = v; L.best_prim = prim;
-                    return true;
-                }
-                if (t < L.best_t || prim < L.best_prim) {
-                    L.best_t = t; L.bu = u; L.bv = v; L.best_prim = prim;
-                }
-            }
+            if (leaf<ANY>(L, c)) return true;
         } else if (!have) {
             next = c;
             have = true;
-        } else {
-            if (L.sp < kShortStack) {
-                s_stack[L.sp][tid] = make_int2(c, __float_as_int(tnf));
-            } else if (L.sp < kStackMax) {
-                l_stack[L.sp - kShortStack] = make_int2(c, __float_as_int(tnf));
-            } else {
-                atomicOr(err, ERR_STACK);
-                return true;
-            }
-            ++L.sp;
+        } else if (!push(L, c, tnf, s_stack, l_stack, err)) {
+            return true;
         }
     }
-    if (!have) {
-        for (;;) {
-            if (L.sp == 0) return true;
-            --L.sp;
-            const int2 e = L.sp < kShortStack ? s_stack[L.sp][tid] : l_stack[L.sp - kShortStack];
-            if (ANY || __int_as_float(e.y) <= L.best_t) { next = e.x; break; }
-        }
-    }
+    if (!have && !pop<ANY>(L, s_stack, l_stack, next)) return true;
     L.node = next;
     return false;
+}
+
+// Decoded quantised plane: origin + q * 2^e in one rounding.
+__device__ __forceinline__ float qplane(uint32_t word, int k, float scale, float origin) {
+    return __fmaf_rn((float)((word >> (8 * k)) & 0xFFu), scale, origin);
+}
+
+// One 4-wide node (FP32 or 8-bit quantised boxes): the hit children are
+// visited in order of (entry distance, slot); leaves tested inline, the nearest
+// inner child visited next, the other inner children pushed so the nearer pop
+// first. Returns true when the ray is finished.
+template <bool ANY, bool QUANT>
+__device__ __forceinline__ bool trace_step4(Lane& L, int2 (*s_stack)[kTraceThreads], int2* l_stack, uint32_t* err) {
+    float tn[4];
+    bool h[4];
+    int32_t c[4];
+    if (QUANT) {
+        const Node4Q* nd = static_cast<const Node4Q*>(L.nodes) + L.node;
+        const float4 q0 = __ldg(&nd->q0);
+        const uint4 q1 = __ldg(&nd->q1), q2 = __ldg(&nd->q2);
+        const int4 ch = __ldg(&nd->child);
+        const uint32_t meta = __float_as_uint(q0.w);
+        const float sx = __uint_as_float((meta & 0xFFu) << 23);
+        const float sy = __uint_as_float(((meta >> 8) & 0xFFu) << 23);
+        const float sz = __uint_as_float(((meta >> 16) & 0xFFu) << 23);
+        const uint32_t mask = meta >> 24;
+        c[0] = ch.x; c[1] = ch.y; c[2] = ch.z; c[3] = ch.w;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            h[k] = false;
+            tn[k] = 0.0f;
+            if (mask & (1u << k))
+                h[k] = slab(L.p, qplane(q1.x, k, sx, q0.x), qplane(q1.y, k, sx, q0.x), qplane(q1.z, k, sy, q0.y),
+                            qplane(q1.w, k, sy, q0.y), qplane(q2.x, k, sz, q0.z), qplane(q2.y, k, sz, q0.z),
+                            L.best_t, tn[k]);
+        }
+    } else {
+        const Node4* nd = static_cast<const Node4*>(L.nodes) + L.node;
+        const float4 lox = __ldg(&nd->lox), hix = __ldg(&nd->hix), loy = __ldg(&nd->loy), hiy = __ldg(&nd->hiy);
+        const float4 loz = __ldg(&nd->loz), hiz = __ldg(&nd->hiz);
+        const int4 ch = __ldg(&nd->child);
+        const uint32_t mask = __ldg(&nd->meta.x);
+        c[0] = ch.x; c[1] = ch.y; c[2] = ch.z; c[3] = ch.w;
+        const float lx[4] = {lox.x, lox.y, lox.z, lox.w}, hx[4] = {hix.x, hix.y, hix.z, hix.w};
+        const float ly[4] = {loy.x, loy.y, loy.z, loy.w}, hy[4] = {hiy.x, hiy.y, hiy.z, hiy.w};
+        const float lz[4] = {loz.x, loz.y, loz.z, loz.w}, hz[4] = {hiz.x, hiz.y, hiz.z, hiz.w};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            h[k] = false;
+            tn[k] = 0.0f;
+            if (mask & (1u << k)) h[k] = slab(L.p, lx[k], hx[k], ly[k], hy[k], lz[k], hz[k], L.best_t, tn[k]);
+        }
+    }
+    int rank[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        int r = 0;
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if (j != k && h[j] && (tn[j] < tn[k] || (tn[j] == tn[k] && j < k))) ++r;
+        rank[k] = r;
+    }
+    int32_t next = -1;
+    bool have = false;
+    int np = 0;
+    int32_t pc0 = 0, pc1 = 0, pc2 = 0;
+    float pt0 = 0.0f, pt1 = 0.0f, pt2 = 0.0f;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        int32_t cr = 0;
+        float tr = 0.0f;
+        bool hr = false;
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (h[k] && rank[k] == r) {
+                cr = c[k];
+                tr = tn[k];
+                hr = true;
+            }
+        if (!hr) continue;
+        if (cr < 0) {
+            if (leaf<ANY>(L, cr)) return true;
+        } else if (!have) {
+            next = cr;
+            have = true;
+        } else {
+            if (np == 0) { pc0 = cr; pt0 = tr; }
+            else if (np == 1) { pc1 = cr; pt1 = tr; }
+            else { pc2 = cr; pt2 = tr; }
+            ++np;
+        }
+    }
+    if (np > 2 && !push(L, pc2, pt2, s_stack, l_stack, err)) return true;
+    if (np > 1 && !push(L, pc1, pt1, s_stack, l_stack, err)) return true;
+    if (np > 0 && !push(L, pc0, pt0, s_stack, l_stack, err)) return true;
+    if (!have && !pop<ANY>(L, s_stack, l_stack, next)) return true;
+    L.node = next;
+    return false;
+}
+
+template <bool ANY, int LAYOUT>
+__device__ __forceinline__ bool trace_step(Lane& L, int2 (*s_stack)[kTraceThreads], int2* l_stack, uint32_t* err) {
+    if (LAYOUT == kLayoutBvh2) return trace_step2<ANY>(L, s_stack, l_stack, err);
+    return trace_step4<ANY, LAYOUT == kLayoutBvh4Q8>(L, s_stack, l_stack, err);
 }
 
 // Refill when at least this many lanes of a warp are idle.
 constexpr int kRefillLanes = 8;
 
-
 // Persistent dynamic-fetch loop. `Src` supplies the work:
 //   uint64_t n                                        number of rays
-//   uint32_t load(uint64_t i, float4& r0, float4& r1, const Node*& nodes,
+//   uint32_t load(uint64_t i, float4& r0, float4& r1, const void*& nodes,
 //                 const Tri*& tris)                   ray i (reference Ray layout) and
-//                                                     its BVH; returns the root node
+//                                                     its BVH (nodes of layout LAYOUT);
+//                                                     returns the root node
 //   void finish(uint64_t i, const Lane& L)            ray i is done (L.best_prim ==
 //                                                     0xFFFFFFFF means a miss)
-template <bool ANY, class Src>
+template <bool ANY, int LAYOUT, class Src>
 __device__ __forceinline__ void traverse_loop(Src& src, unsigned long long* counter, uint32_t* err,
                                               int2 (*s_stack)[kTraceThreads]) {
     int2 l_stack[kStackMax - kShortStack];
@@ -230,7 +361,7 @@ __device__ __forceinline__ void traverse_loop(Src& src, unsigned long long* coun
             if (exhausted) break;
             continue;
         }
-        if (active && trace_step<ANY>(L, s_stack, l_stack, err)) {
+        if (active && trace_step<ANY, LAYOUT>(L, s_stack, l_stack, err)) {
             src.finish(L.ray, L);
             active = false;
         }

@@ -14,6 +14,8 @@ PKG_ROOT = os.path.dirname(_HERE)
 LIB_PATH = os.path.join(PKG_ROOT, "lib", "libgr.so")
 
 GR_OK = 0
+LAYOUT_BVH2, LAYOUT_BVH4, LAYOUT_BVH4_Q8 = 0, 1, 2
+LAYOUT_NAMES = {0: "bvh2", 1: "bvh4", 2: "bvh4_q8"}
 STATUS = {
     0: "GR_OK", 1: "GR_ERR_INVALID", 2: "GR_ERR_CUDA", 3: "GR_ERR_OOM_BUDGET",
     4: "GR_ERR_PARSE", 5: "GR_ERR_TIMEOUT", 6: "GR_ERR_OVERFLOW",
@@ -54,6 +56,10 @@ def load():
         "gr_bvh_export": ([_P, _P, _P, _P, _P, _P, _P], ctypes.c_int),
         "gr_trace": ([_P, _P, ctypes.c_uint64, _P, ctypes.c_int, _P], ctypes.c_int),
         "gr_trace_host": ([_P, _P, ctypes.c_uint64, _P, ctypes.c_int], ctypes.c_int),
+        "gr_bvh_set_layout": ([_P, ctypes.c_int, _P], ctypes.c_int),
+        "gr_bvh_export_layout": ([_P, ctypes.c_int, _P], ctypes.c_int),
+        "gr_scene_set_layout": ([_P, ctypes.c_int], ctypes.c_int),
+        "gr_scene_layout": ([_P], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -134,6 +140,15 @@ class BVH:
                                             ctypes.byref(root)), "gr_bvh_export")
         return {"sorted_prim": sp, "sorted_code": sc, "ref_nodes": rn, "nodes": nodes, "tris": tris,
                 "root": root.value}
+
+    def set_layout(self, layout, stream=None):
+        self.ctx.check(load().gr_bvh_set_layout(self.h, layout, _P(stream) if stream else None), "gr_bvh_set_layout")
+
+    def export_layout(self, layout):
+        n = self.size
+        out = np.zeros(max(n - 1, 1) * (32 if layout == LAYOUT_BVH4 else 16), np.uint32)
+        self.ctx.check(load().gr_bvh_export_layout(self.h, layout, _ptr(out)), "gr_bvh_export_layout")
+        return out
 
     def trace_host(self, rays, any_hit=False):
         r = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 8)
@@ -287,6 +302,9 @@ class Scene:
     def reset(self):
         self.ctx.check(_declare(_SCENE_SIGS).gr_scene_reset(self.h), "gr_scene_reset")
 
+    def set_layout(self, layout):
+        self.ctx.check(load().gr_scene_set_layout(self.h, layout), "gr_scene_set_layout")
+
     def info(self):
         v = [ctypes.c_uint32() for _ in range(4)]
         self.ctx.check(_declare(_SCENE_SIGS).gr_scene_info(self.h, *[ctypes.byref(x) for x in v]), "gr_scene_info")
@@ -335,7 +353,8 @@ class PathTracer:
 # ---- batched rendering and serving ---------------------------------------------------
 
 class ServerOpts(ctypes.Structure):
-    _fields_ = [("budget_bytes", ctypes.c_uint64), ("wave_paths", ctypes.c_uint32), ("max_active", ctypes.c_uint32)]
+    _fields_ = [("budget_bytes", ctypes.c_uint64), ("wave_paths", ctypes.c_uint32), ("max_active", ctypes.c_uint32),
+                ("layout", ctypes.c_int32)]
 
 
 class JobStats(ctypes.Structure):
@@ -389,10 +408,10 @@ def render_batch(ctx, scenes, opts, wave_paths=0):
 class Server:
     """Continuous-batching render server (gr_server)."""
 
-    def __init__(self, ctx, budget_bytes=0, wave_paths=0, max_active=0):
+    def __init__(self, ctx, budget_bytes=0, wave_paths=0, max_active=0, layout=LAYOUT_BVH2):
         L = _declare(_SERVER_SIGS)
         self.ctx = ctx
-        o = ServerOpts(budget_bytes, wave_paths, max_active)
+        o = ServerOpts(budget_bytes, wave_paths, max_active, layout)
         h = _P()
         ctx.check(L.gr_server_create(ctx.h, ctypes.byref(o), ctypes.byref(h)), "gr_server_create")
         self.h = h

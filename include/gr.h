@@ -119,6 +119,28 @@ gr_status gr_bvh_build_noalloc(gr_ctx* ctx, const float* d_verts, uint32_t n, vo
 gr_status gr_bvh_export(gr_bvh* bvh, uint32_t* h_sorted_prim, uint32_t* h_sorted_code, uint32_t* h_ref_nodes,
                         uint32_t* h_nodes, float* h_tris, uint32_t* h_root);
 
+/* Node layouts for traversal (no counterpart in the reference, whose nodes are
+ * binary 32-byte records tested one at a time):
+ *   GR_LAYOUT_BVH2     binary nodes with both child boxes in the parent (64 B)
+ *   GR_LAYOUT_BVH4     4-wide nodes with FP32 child boxes (128 B), the binary
+ *                      tree with every other level folded
+ *   GR_LAYOUT_BVH4_Q8  the same 4-wide tree with 8-bit child boxes quantised
+ *                      outward against a per-node origin and power-of-two
+ *                      scale (64 B); the boxes contain the FP32 boxes, so the
+ *                      closest hit is the same
+ * The binary tree is always built; a 4-wide layout is derived from it on the
+ * GPU when first requested and kept until the next build. */
+#define GR_LAYOUT_BVH2 0
+#define GR_LAYOUT_BVH4 1
+#define GR_LAYOUT_BVH4_Q8 2
+
+/* Selects the layout gr_trace uses (building it if needed; stream-ordered). */
+gr_status gr_bvh_set_layout(gr_bvh* bvh, int layout, void* stream);
+
+/* Copies a 4-wide layout to host memory (128 or 64 bytes x max(n-1, 1); only
+ * even-depth entries are nodes, the others are zero). Waits for the device. */
+gr_status gr_bvh_export_layout(gr_bvh* bvh, int layout, void* h_nodes);
+
 /* ---- traversal -------------------------------------------------------------
  * Replaces trace / trace_shadow (src/renderer/pathtracer_kernel.h:235-246 and
  * :310-321) on a queue of rays: closest hit (any_hit = 0) or first hit found
@@ -233,6 +255,12 @@ gr_status gr_scene_reset(gr_scene* scene);
 /* Device bytes the scene holds (geometry, BVH, accumulation). */
 uint64_t gr_scene_device_bytes(const gr_scene* scene);
 
+/* Node layout the scene's renders traverse (GR_LAYOUT_*; default binary).
+ * Builds the layout if needed and waits. All scenes of one gr_render_batch
+ * must use the same layout. */
+gr_status gr_scene_set_layout(gr_scene* scene, int layout);
+int gr_scene_layout(const gr_scene* scene);
+
 /* ---- scene files ---------------------------------------------------------------
  * Replaces load_scene / load_mitsuba_file / load_obj_file (src/renderer/loaders/
  * loader.h:11-29, mitsubaloader.cpp, objloader.cpp). The Mitsuba-XML subset
@@ -283,6 +311,7 @@ typedef struct gr_server_opts {
     uint64_t budget_bytes; /* device-memory budget for admission (0 = no limit) */
     uint32_t wave_paths;   /* paths per wave (0 = library default) */
     uint32_t max_active;   /* jobs in flight at most (0 = 1024) */
+    int32_t layout;        /* node layout of every job (GR_LAYOUT_*); set on the scenes at submit */
 } gr_server_opts;
 
 typedef struct gr_job_stats {

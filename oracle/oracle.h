@@ -50,6 +50,13 @@ int or_lbvh_build(const float* verts, uint32_t n, uint32_t* sorted_prim, uint32_
 void or_trace(const uint32_t* bvh2_nodes, const float* tri_sorted, uint32_t root, const float* rays,
               uint64_t nrays, int any_hit, float* hits, uint32_t* stats, int threads);
 
+/* 4-wide layouts restated: collapse (quant = 0: 32 words per node, FP32 boxes;
+ * quant = 1: 16 words per node, 8-bit outward-quantised boxes) and traversal
+ * in the product's child order. out holds max(n-1,1) nodes. */
+void or_bvh4_build(const uint32_t* bvh2_nodes, uint32_t n, int quant, uint32_t* out);
+void or_trace4(const uint32_t* nodes4, int quant, const float* tri_sorted, uint32_t root, const float* rays,
+               uint64_t nrays, int any_hit, float* hits, uint32_t* stats, int threads);
+
 /* Brute force over all triangles with the same watertight FP32 test and the
  * (t, prim) lexicographic rule. any_hit returns the lowest-index hit. */
 void or_trace_brute(const float* verts, uint32_t n, const float* rays, uint64_t nrays, int any_hit,

@@ -84,6 +84,24 @@ def trace(bvh, rays, any_hit=False, stats=False, nthreads=None):
     return (hits, st) if stats else hits
 
 
+def bvh4(bvh, quant):
+    """4-wide layout collapsed from the oracle's binary nodes."""
+    n = bvh["tris"].size // 12
+    out = np.zeros(max(n - 1, 1) * (16 if quant else 32), np.uint32)
+    load().or_bvh4_build(_p(bvh["nodes"]), ctypes.c_uint32(n), int(quant), _p(out))
+    return out
+
+
+def trace4(bvh, nodes4, quant, rays, any_hit=False, stats=False, nthreads=None):
+    r = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
+    m = r.shape[0]
+    hits = np.zeros((m, 4), np.float32)
+    st = np.zeros((m, 2), np.uint32) if stats else None
+    load().or_trace4(_p(nodes4), int(quant), _p(bvh["tris"]), ctypes.c_uint32(bvh["root"]), _p(r), ctypes.c_uint64(m),
+                     int(any_hit), _p(hits), _p(st), nthreads or threads())
+    return (hits, st) if stats else hits
+
+
 def trace_brute(verts, rays, any_hit=False, nthreads=None):
     v = np.ascontiguousarray(verts, np.float32).reshape(-1, 9)
     r = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)

@@ -82,6 +82,10 @@ inline void prepare(const float* r, RayPre& p) {
     }
 }
 
+// Every cull keeps a box (or a deferred entry) while its entry distance is
+// within (1 + 2^-20) of the exit / closest-hit distance.
+constexpr float kCullSlack = 1.00000095367431640625f;
+
 // Child-box slab test; returns entry distance through *tn.
 inline bool slab(const RayPre& p, float lox, float hix, float loy, float hiy, float loz, float hiz, float tbest,
                  float* tn) {
@@ -91,7 +95,7 @@ inline bool slab(const RayPre& p, float lox, float hix, float loy, float hiy, fl
     float tnear = std::fmax(std::fmax(std::fmin(x0, x1), std::fmin(y0, y1)), std::fmax(std::fmin(z0, z1), p.tmin));
     float tfar = std::fmin(std::fmin(std::fmax(x0, x1), std::fmax(y0, y1)), std::fmin(std::fmax(z0, z1), tbest));
     *tn = tnear;
-    return tnear <= tfar;
+    return tnear <= tfar * kCullSlack;
 }
 
 // Watertight FP32 test. Edge functions are plain products and differences so a
@@ -189,13 +193,232 @@ void trace_one(const uint32_t* nodes, const float* tris, uint32_t root, const fl
             for (;;) {
                 if (sp == 0) { done = true; break; }
                 --sp;
-                if (any || stack[sp].tn <= b.t) { next = stack[sp].node; have_next = true; break; }
+                if (any || stack[sp].tn <= b.t * kCullSlack) { next = stack[sp].node; have_next = true; break; }
             }
         }
         node = next;
     }
     if (b.prim == 0xFFFFFFFFu) {
         hit[0] = p.tmax;  // t of a miss is left at tMax; prim -1; u = v = 0
+        uint32_t m = 0xFFFFFFFFu;
+        std::memcpy(hit + 1, &m, 4);
+        hit[2] = 0.0f; hit[3] = 0.0f;
+    } else {
+        hit[0] = b.t;
+        std::memcpy(hit + 1, &b.prim, 4);
+        hit[2] = b.u; hit[3] = b.v;
+    }
+    if (st) { st[0] = visits; st[1] = tests; }
+}
+
+// ---------------------------------------------------------------------------
+// 4-wide layouts (product specification): every binary node at even depth
+// becomes a 4-wide node at its own index; slots are its children, an inner
+// child replaced by its two children. Boxes are copied (FP32) or quantised
+// outward to 8 bits against origin + q * 2^e (one fma).
+// ---------------------------------------------------------------------------
+struct CB { float lo[3], hi[3]; };
+
+inline CB child_box(const uint32_t* w, int slot) {
+    const float* f = reinterpret_cast<const float*>(w);
+    CB b;
+    const float* xy = f + (slot == 0 ? 0 : 4);
+    b.lo[0] = xy[0]; b.hi[0] = xy[1]; b.lo[1] = xy[2]; b.hi[1] = xy[3];
+    b.lo[2] = f[slot == 0 ? 8 : 10];
+    b.hi[2] = f[slot == 0 ? 9 : 11];
+    return b;
+}
+
+inline float pow2(int e) { return f_of((uint32_t)(e + 127) << 23); }
+inline float qdecode(int q, float scale, float origin) { return std::fmaf((float)q, scale, origin); }
+
+inline int pick_exponent(float lo, float hi) {
+    const float extent = hi - lo;
+    int e = -126;
+    if (extent > 0.0f) {
+        int ex;
+        std::frexp(extent / 255.0f, &ex);
+        e = std::max(-126, std::min(127, ex));
+    }
+    while (e < 127 && qdecode(255, pow2(e), lo) < hi) ++e;
+    return e;
+}
+
+inline uint32_t quant_lo(float v, float scale, float origin) {
+    int q = (int)std::fmin(std::fmax(std::floor((v - origin) / scale), 0.0f), 255.0f);
+    while (q > 0 && qdecode(q, scale, origin) > v) --q;
+    while (q < 255 && qdecode(q + 1, scale, origin) <= v) ++q;
+    return (uint32_t)q;
+}
+
+inline uint32_t quant_hi(float v, float scale, float origin) {
+    int q = (int)std::fmin(std::fmax(std::ceil((v - origin) / scale), 0.0f), 255.0f);
+    while (q < 255 && qdecode(q, scale, origin) < v) ++q;
+    while (q > 0 && qdecode(q - 1, scale, origin) >= v) --q;
+    return (uint32_t)q;
+}
+
+void build4(const uint32_t* nodes, uint32_t n, int quant, uint32_t* out) {
+    const uint32_t count = n > 1 ? n - 1 : 1;
+    const size_t words = quant ? 16 : 32;
+    std::memset(out, 0, 4ull * words * count);
+    for (uint32_t G = 0; G < count; ++G) {
+        uint32_t depth = 0, x = G;
+        while (nodes[16ull * x + 14] != 0xFFFFFFFFu) {
+            x = nodes[16ull * x + 14];
+            ++depth;
+        }
+        if (depth & 1u) continue;
+        const uint32_t* nd = nodes + 16ull * G;
+        CB box[4];
+        int32_t ref[4] = {0, 0, 0, 0};
+        int ns = 0;
+        for (int k = 0; k < 2; ++k) {
+            const int32_t c = (int32_t)nd[12 + k];
+            if (c < 0) {
+                box[ns] = child_box(nd, k);
+                ref[ns++] = c;
+            } else {
+                const uint32_t* cn = nodes + 16ull * (uint32_t)c;
+                box[ns] = child_box(cn, 0);
+                ref[ns++] = (int32_t)cn[12];
+                box[ns] = child_box(cn, 1);
+                ref[ns++] = (int32_t)cn[13];
+            }
+        }
+        const uint32_t mask = (1u << ns) - 1u;
+        uint32_t* o = out + words * G;
+        if (!quant) {  // lo.x[4] hi.x[4] lo.y[4] hi.y[4] lo.z[4] hi.z[4] child[4] meta[4]
+            float* f = reinterpret_cast<float*>(o);
+            for (int k = 0; k < ns; ++k)
+                for (int a = 0; a < 3; ++a) {
+                    f[8 * a + k] = box[k].lo[a];
+                    f[8 * a + 4 + k] = box[k].hi[a];
+                }
+            for (int k = 0; k < 4; ++k) o[24 + k] = (uint32_t)ref[k];
+            o[28] = mask;
+        } else {
+            float org[3], scale[3];
+            uint32_t be[3];
+            for (int a = 0; a < 3; ++a) {
+                float lo = box[0].lo[a], hi = box[0].hi[a];
+                for (int k = 1; k < ns; ++k) {
+                    lo = std::fmin(lo, box[k].lo[a]);
+                    hi = std::fmax(hi, box[k].hi[a]);
+                }
+                const int e = pick_exponent(lo, hi);
+                org[a] = lo;
+                be[a] = (uint32_t)(e + 127);
+                scale[a] = pow2(e);
+            }
+            uint32_t wq[6] = {0, 0, 0, 0, 0, 0};
+            for (int k = 0; k < ns; ++k)
+                for (int a = 0; a < 3; ++a) {
+                    wq[2 * a] |= quant_lo(box[k].lo[a], scale[a], org[a]) << (8 * k);
+                    wq[2 * a + 1] |= quant_hi(box[k].hi[a], scale[a], org[a]) << (8 * k);
+                }
+            std::memcpy(o, org, 12);
+            o[3] = be[0] | (be[1] << 8) | (be[2] << 16) | (mask << 24);
+            for (int k = 0; k < 6; ++k) o[4 + k] = wq[k];
+            for (int k = 0; k < 4; ++k) o[12 + k] = (uint32_t)ref[k];
+        }
+    }
+}
+
+void trace4_one(const uint32_t* nodes, int quant, const float* tris, uint32_t root, const float* ray, int any,
+                float* hit, uint32_t* st) {
+    RayPre p;
+    prepare(ray, p);
+    Best b{p.tmax, 0.0f, 0.0f, 0xFFFFFFFFu};
+    uint32_t visits = 0, tests = 0;
+    struct Entry { int32_t node; float tn; };
+    Entry stack[256];
+    int sp = 0;
+    int32_t node = (int32_t)root;
+    bool done = root == 0xFFFFFFFFu;
+    const size_t words = quant ? 16 : 32;
+    while (!done) {
+        const uint32_t* o = nodes + words * (uint32_t)node;
+        ++visits;
+        float tn[4] = {0, 0, 0, 0};
+        bool h[4] = {false, false, false, false};
+        int32_t c[4];
+        if (quant) {
+            const float* org = reinterpret_cast<const float*>(o);
+            const uint32_t meta = o[3];
+            const float sc[3] = {f_of((meta & 0xFFu) << 23), f_of(((meta >> 8) & 0xFFu) << 23),
+                                 f_of(((meta >> 16) & 0xFFu) << 23)};
+            const uint32_t mask = meta >> 24;
+            for (int k = 0; k < 4; ++k) {
+                c[k] = (int32_t)o[12 + k];
+                if (!(mask & (1u << k))) continue;
+                float pl[6];
+                for (int a = 0; a < 3; ++a) {
+                    pl[2 * a] = qdecode((int)((o[4 + 2 * a] >> (8 * k)) & 0xFFu), sc[a], org[a]);
+                    pl[2 * a + 1] = qdecode((int)((o[5 + 2 * a] >> (8 * k)) & 0xFFu), sc[a], org[a]);
+                }
+                h[k] = slab(p, pl[0], pl[1], pl[2], pl[3], pl[4], pl[5], b.t, &tn[k]);
+            }
+        } else {
+            const float* f = reinterpret_cast<const float*>(o);
+            const uint32_t mask = o[28];
+            for (int k = 0; k < 4; ++k) {
+                c[k] = (int32_t)o[24 + k];
+                if (!(mask & (1u << k))) continue;
+                h[k] = slab(p, f[k], f[4 + k], f[8 + k], f[12 + k], f[16 + k], f[20 + k], b.t, &tn[k]);
+            }
+        }
+        int rank[4];
+        for (int k = 0; k < 4; ++k) {
+            int r = 0;
+            for (int j = 0; j < 4; ++j)
+                if (j != k && h[j] && (tn[j] < tn[k] || (tn[j] == tn[k] && j < k))) ++r;
+            rank[k] = r;
+        }
+        int32_t next = -1;
+        bool have = false;
+        int np = 0;
+        int32_t pc[3];
+        float pt[3];
+        for (int r = 0; r < 4 && !done; ++r) {
+            int k = -1;
+            for (int j = 0; j < 4; ++j)
+                if (h[j] && rank[j] == r) k = j;
+            if (k < 0) continue;
+            if (c[k] < 0) {
+                const float* tri = tris + 12ull * (uint32_t)(~c[k]);
+                ++tests;
+                if (any) {
+                    float t, u, v;
+                    if (tri_test(p, tri, tri + 4, tri + 8, b.t, &t, &u, &v)) {
+                        b.t = t; b.u = u; b.v = v; b.prim = w_of(tri[3]);
+                        done = true;
+                    }
+                } else {
+                    consider(p, tri, b);
+                }
+            } else if (!have) {
+                next = c[k];
+                have = true;
+            } else {
+                pc[np] = c[k];
+                pt[np] = tn[k];
+                ++np;
+            }
+        }
+        if (done) break;
+        for (int k = np - 1; k >= 0; --k) stack[sp++] = {pc[k], pt[k]};
+        if (!have) {
+            for (;;) {
+                if (sp == 0) { done = true; break; }
+                --sp;
+                if (any || stack[sp].tn <= b.t * kCullSlack) { next = stack[sp].node; have = true; break; }
+            }
+        }
+        node = next;
+    }
+    if (b.prim == 0xFFFFFFFFu) {
+        hit[0] = p.tmax;
         uint32_t m = 0xFFFFFFFFu;
         std::memcpy(hit + 1, &m, 4);
         hit[2] = 0.0f; hit[3] = 0.0f;
@@ -455,5 +678,18 @@ extern "C" void or_fp64_check(const uint32_t* ref_nodes, const float* verts, uin
             }
             ambiguous[i] = amb ? 1 : 0;
         }
+    });
+}
+
+extern "C" void or_bvh4_build(const uint32_t* bvh2_nodes, uint32_t n, int quant, uint32_t* out) {
+    if (n == 0) return;
+    build4(bvh2_nodes, n, quant, out);
+}
+
+extern "C" void or_trace4(const uint32_t* nodes4, int quant, const float* tris, uint32_t root, const float* rays,
+                          uint64_t nrays, int any_hit, float* hits, uint32_t* stats, int threads) {
+    parallel_rays(nrays, threads, [&](uint64_t b, uint64_t e) {
+        for (uint64_t i = b; i < e; ++i)
+            trace4_one(nodes4, quant, tris, root, rays + 8 * i, any_hit, hits + 4 * i, stats ? stats + 2 * i : nullptr);
     });
 }

@@ -1,0 +1,73 @@
+"""4-wide node layouts (FP32 and 8-bit quantised child boxes): the GPU
+collapse and quantisation equal the oracle's word for word, traversal results
+equal the oracle's bit for bit, closest hits equal the binary layout's, and
+renders are identical across layouts."""
+import numpy as np
+import pytest
+
+import gr
+from gr import scenes as sc
+
+pytestmark = pytest.mark.gpu
+
+
+def _bits(h):
+    return np.ascontiguousarray(h).view(np.uint32)
+
+
+@pytest.mark.parametrize("n,scale", [(1, 100.0), (2, 100.0), (7, 50.0), (5000, 8.0), (1000000, 1.0)])
+@pytest.mark.parametrize("layout", [gr.LAYOUT_BVH4, gr.LAYOUT_BVH4_Q8])
+def test_layout_build_and_trace_match_oracle(ctx, oracle, n, scale, layout):
+    v = sc.triangle_soup(n, seed_salt=400 + n % 13).reshape(n, 3, 3)
+    c = v.mean(axis=1, keepdims=True)
+    v = np.ascontiguousarray(((v - c) * scale + c).reshape(n, 9), np.float32)
+    b = gr.BVH(ctx)
+    b.build_host(v)
+    ob = oracle.lbvh(v)
+    quant = layout == gr.LAYOUT_BVH4_Q8
+    want_nodes = oracle.bvh4(ob, quant)
+    np.testing.assert_array_equal(b.export_layout(layout), want_nodes)
+    b.set_layout(layout)
+    m = 131072 if n >= 1000000 else 40000
+    rays = sc.incoherent_rays(m, seed_salt=401)
+    got = b.trace_host(rays)
+    np.testing.assert_array_equal(_bits(got), _bits(oracle.trace4(ob, want_nodes, quant, rays)))
+    np.testing.assert_array_equal(_bits(got), _bits(oracle.trace(ob, rays)))  # same closest hits as binary
+    s = sc.shadow_rays(m, seed_salt=402)
+    ga = b.trace_host(s, any_hit=True)
+    np.testing.assert_array_equal(_bits(ga), _bits(oracle.trace4(ob, want_nodes, quant, s, any_hit=True)))
+
+
+def test_quantised_boxes_contain_fp32_boxes(ctx, oracle):
+    n = 20000
+    v = sc.triangle_soup(n, seed_salt=410)
+    b = gr.BVH(ctx)
+    b.build_host(v)
+    f = b.export_layout(gr.LAYOUT_BVH4).reshape(-1, 32)
+    q = b.export_layout(gr.LAYOUT_BVH4_Q8).reshape(-1, 16)
+    ff = f.view(np.float32)
+    for G in np.nonzero(f[:, 28])[0][:2000]:
+        mask = int(f[G, 28])
+        org = q[G, :3].view(np.float32)
+        meta = int(q[G, 3])
+        for k in range(4):
+            if not mask & (1 << k):
+                continue
+            for a in range(3):
+                sc_ = np.float32(2.0) ** (((meta >> (8 * a)) & 0xFF) - 127)
+                qlo = (int(q[G, 4 + 2 * a]) >> (8 * k)) & 0xFF
+                qhi = (int(q[G, 5 + 2 * a]) >> (8 * k)) & 0xFF
+                lo = np.float32(np.float32(qlo) * sc_ + org[a])
+                hi = np.float32(np.float32(qhi) * sc_ + org[a])
+                assert lo <= ff[G, 8 * a + k] and hi >= ff[G, 8 * a + 4 + k]
+
+
+@pytest.mark.parametrize("layout", [gr.LAYOUT_BVH4, gr.LAYOUT_BVH4_Q8])
+def test_render_identical_across_layouts(ctx, layout):
+    d = sc.glossy_scene(64, 48, level=3, glass_level=2)
+    a = gr.Scene(ctx, d)
+    a.render(4, max_depth=10, seed=5, want_image=False)
+    b = gr.Scene(ctx, d)
+    b.set_layout(layout)
+    b.render(4, max_depth=10, seed=5, want_image=False)
+    np.testing.assert_array_equal(a.accumulation()[0], b.accumulation()[0])
