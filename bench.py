@@ -196,6 +196,22 @@ def run_gpu(args):
     def step(buf_rays, buf_hits, n, any_hit=False):
         bvh.trace_device(buf_rays, n, buf_hits, any_hit=any_hit, stream=sp)
 
+    # traversal configuration: the autotuner times every node layout x block
+    # x short-stack configuration on the workload's rays (untimed for the
+    # result) and keeps the fastest; all of them return the same hits
+    names = {v: k for k, v in gr.LAYOUT_NAMES.items()}
+    torch.cuda.synchronize()
+    if args.layout == "auto":
+        table = bvh.autotune(d_rays, n_rays, d_hits)
+    else:
+        bvh.set_tuning(names[args.layout], args.block, args.short_stack)
+        table = []
+    torch.cuda.synchronize()
+    tuning = bvh.tuning()
+    layout = names[tuning["layout"]]
+    layout_rates = {"%s/%d/%d" % (t["layout"], t["block"], t["short_stack"]): round(n_rays / ms / 1e3, 1)
+                    for t, ms in table}
+
     for _ in range(max(args.warmup, 3)):
         step(d_rays, d_hits, n_rays)
     torch.cuda.synchronize()
@@ -222,7 +238,8 @@ def run_gpu(args):
     if args.quick:
         clocks.stop()
         if rank == 0:
-            print(json.dumps({"quick": True, "tris": n_tris, "rays": n_rays,
+            print(json.dumps({"quick": True, "tris": n_tris, "rays": n_rays, "tuning": tuning,
+                              "autotune_mrays_s": layout_rates,
                               "kernel_ms_median": statistics.median(kernel_ms),
                               "mrays_s": n_rays / (statistics.median(kernel_ms) / 1e3) / 1e6}), flush=True)
         return
@@ -256,10 +273,12 @@ def run_gpu(args):
         extras["config1_render"] = wl.plain_render(ctx, scenes.cornell_box(256, 256), 16, 8)
         log("config 3 (glossy scene 1024x768, 64 spp, depth 16)")
         extras["config3_render"] = wl.plain_render(ctx, scenes.glossy_scene(), 64, 16)
-        log("config 4 (64-job batch)")
+        log("config 4 (64-job batch, default and autotuned configuration)")
         extras["config4_batch"] = wl.config4(ctx)
-        log("config 5 (serving sweep)")
-        extras["config5_serving"] = wl.config5(ctx)
+        log("config 5 (serving sweep, config 4's autotuned configuration)")
+        c4 = extras["config4_batch"].get("autotune")
+        tuned = wl.tuning_args(c4["tuning"], c4["wave_paths"]) if c4 else (gr.LAYOUT_BVH2, 128, 12, 0)
+        extras["config5_serving"] = wl.config5(ctx, tuning=tuned)
 
     # end to end through the C ABI with host buffers (pinned), copies inside
     h_rays = torch.from_numpy(rays).pin_memory()
@@ -298,10 +317,11 @@ def run_gpu(args):
             "warmup": args.warmup, "ms_per_step": t_max * 1e3 / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": WORKLOAD, "triangles": N_TRIS, "rays": N_RAYS, "query": "closest hit",
+                       "tuning": tuning, "autotune_mrays_s": layout_rates,
                        "l2": "flushed (256 MB write) before every timed step", "parallelism": "replicas"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
-                         "kernel": "k_trace<closest>", "bytes_per_ray": BYTES_PER_RAY},
+                         "kernel": "k_trace<closest, %s>" % gr.LAYOUT_NAMES[layout], "bytes_per_ray": BYTES_PER_RAY},
             "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": N_RAYS * 32,
                     "d2h_bytes_per_step": N_RAYS * 16, "api": "gr_trace_host (pinned host rays and hits)"},
@@ -325,6 +345,10 @@ def main():
     ap.add_argument("--tris", type=int, default=N_TRIS, help="triangle count (profiling cases)")
     ap.add_argument("--rays", type=int, default=N_RAYS, help="ray count (profiling cases)")
     ap.add_argument("--no-render", action="store_true", help="skip the render-configuration extras")
+    ap.add_argument("--layout", default="auto", choices=["auto", "bvh2", "bvh4", "bvh4_q8"],
+                    help="node layout of the timed traversal (auto: autotune layout, block and short stack)")
+    ap.add_argument("--block", type=int, default=128, choices=[64, 128, 256])
+    ap.add_argument("--short-stack", type=int, default=12, choices=[8, 12, 16])
     ap.add_argument("--quick", action="store_true",
                     help="time the main query only (no extras, e2e or CPU baseline); for profiling")
     args = ap.parse_args()

@@ -1,4 +1,5 @@
 // C ABI: context, BVH and traversal entry points (include/gr.h).
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -241,7 +242,11 @@ gr_status gr_trace(gr_bvh* bvh, const gr_ray* d_rays, uint64_t n, gr_hit* d_hits
     const void* nodes = bvh->layout == gr::kLayoutBvh4 ? bvh->buf.nodes4.p
                         : bvh->layout == gr::kLayoutBvh4Q8 ? bvh->buf.nodes4q.p
                                                              : bvh->buf.nodes.p;
-    GR_CUDA(ctx, gr::trace_launch(device_view(bvh), nodes, bvh->layout, d_rays, n, d_hits, any_hit, counter, err,
+    gr::TraceTuning tune;
+    tune.layout = bvh->layout;
+    tune.block = bvh->block;
+    tune.sstack = bvh->sstack;
+    GR_CUDA(ctx, gr::trace_launch(device_view(bvh), nodes, tune, d_rays, n, d_hits, any_hit, counter, err,
                                   ctx->num_sms, as_stream(stream)));
     return GR_OK;
 }
@@ -317,4 +322,77 @@ extern "C" gr_status gr_bvh_export_layout(gr_bvh* bvh, int layout, void* h_nodes
     const gr::DevBuf& src = layout == gr::kLayoutBvh4 ? bvh->buf.nodes4 : bvh->buf.nodes4q;
     GR_CUDA(bvh->ctx, cudaMemcpy(h_nodes, src.p, count * (layout == gr::kLayoutBvh4 ? 128 : 64), cudaMemcpyDeviceToHost));
     return GR_OK;
+}
+
+extern "C" gr_status gr_bvh_set_tuning(gr_bvh* bvh, const gr_trace_tuning* t) {
+    if (!bvh || !t) return GR_ERR_INVALID;
+    gr::TraceTuning tt;
+    tt.layout = t->layout;
+    tt.block = t->block;
+    tt.sstack = t->short_stack;
+    if (!gr::tuning_valid(tt)) return fail(bvh->ctx, GR_ERR_INVALID, "gr_bvh_set_tuning: unsupported configuration");
+    gr_status st = gr_bvh_set_layout(bvh, t->layout, bvh->ctx->stream);
+    if (st != GR_OK) return st;
+    bvh->block = t->block;
+    bvh->sstack = t->short_stack;
+    return GR_OK;
+}
+
+extern "C" gr_status gr_bvh_get_tuning(const gr_bvh* bvh, gr_trace_tuning* t) {
+    if (!bvh || !t) return GR_ERR_INVALID;
+    t->layout = bvh->layout;
+    t->block = bvh->block;
+    t->short_stack = bvh->sstack;
+    return GR_OK;
+}
+
+extern "C" gr_status gr_bvh_autotune(gr_bvh* bvh, const gr_ray* d_rays, uint64_t n, int any_hit, gr_hit* d_hits,
+                                     gr_tuning_result* h_table, uint32_t max_results, uint32_t* n_results) {
+    if (!bvh || !bvh->built || !d_rays || !d_hits || n == 0) return GR_ERR_INVALID;
+    gr_ctx* ctx = bvh->ctx;
+    GR_CUDA(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->stream;
+    cudaEvent_t e0, e1;
+    GR_CUDA(ctx, cudaEventCreate(&e0));
+    GR_CUDA(ctx, cudaEventCreate(&e1));
+    const int layouts[] = {0, 1, 2}, blocks[] = {64, 128, 256}, stacks[] = {8, 12, 16};
+    gr_trace_tuning best{bvh->layout, bvh->block, bvh->sstack};
+    float best_ms = 1e30f;
+    uint32_t rows = 0;
+    gr_status st = GR_OK;
+    for (int lay : layouts) {
+        if ((st = gr_bvh_set_layout(bvh, lay, s)) != GR_OK) break;
+        for (int blk : blocks)
+            for (int ss : stacks) {
+                bvh->block = blk;
+                bvh->sstack = ss;
+                float ms = 0.0f;
+                // one warm-up launch, then the faster of two timed launches
+                float m = 1e30f;
+                for (int rep = 0; rep < 3 && st == GR_OK; ++rep) {
+                    cudaEventRecord(e0, s);
+                    st = gr_trace(bvh, d_rays, n, d_hits, any_hit, s);
+                    cudaEventRecord(e1, s);
+                    cudaEventSynchronize(e1);
+                    cudaEventElapsedTime(&ms, e0, e1);
+                    if (rep > 0) m = std::min(m, ms);
+                }
+                if (st != GR_OK) break;
+                if (h_table && rows < max_results) {
+                    h_table[rows].tuning = gr_trace_tuning{lay, blk, ss};
+                    h_table[rows].ms = m;
+                }
+                ++rows;
+                if (m < best_ms) {
+                    best_ms = m;
+                    best = gr_trace_tuning{lay, blk, ss};
+                }
+            }
+        if (st != GR_OK) break;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (n_results) *n_results = rows;
+    if (st != GR_OK) return st;
+    return gr_bvh_set_tuning(bvh, &best);
 }

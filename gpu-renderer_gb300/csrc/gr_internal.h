@@ -66,6 +66,14 @@ static_assert(sizeof(Node4Q) == 64, "node4q layout");
 
 enum Layout : int { kLayoutBvh2 = 0, kLayoutBvh4 = 1, kLayoutBvh4Q8 = 2 };
 
+// Traversal launch configuration chosen by the autotuner (or by the caller).
+struct TraceTuning {
+    int layout = kLayoutBvh2;
+    int block = 128;   // threads per block: 64, 128 or 256
+    int sstack = 12;   // stack entries per thread kept in shared memory: 8, 12 or 16
+};
+bool tuning_valid(const TraceTuning& t);
+
 // Leaf-order triangle: three 16-byte words (v0, prim bits), (v1, 0), (v2, 0).
 struct Tri {
     float4 a, b, c;
@@ -125,9 +133,9 @@ cudaError_t lbvh_build_static(const float* d_verts, uint32_t n, Node* nodes, Tri
 cudaError_t bvh4_build(BvhBuffers& b, uint32_t n, int layout, cudaStream_t s);
 
 // trace.cu
-cudaError_t trace_launch(const BvhDevice& bvh, const void* nodes, int layout, const gr_ray* d_rays, uint64_t n,
-                         gr_hit* d_hits, int any_hit, unsigned long long* d_counter, uint32_t* d_err, int num_sms,
-                         cudaStream_t s);
+cudaError_t trace_launch(const BvhDevice& bvh, const void* nodes, const TraceTuning& tune, const gr_ray* d_rays,
+                         uint64_t n, gr_hit* d_hits, int any_hit, unsigned long long* d_counter, uint32_t* d_err,
+                         int num_sms, cudaStream_t s);
 
 }  // namespace gr
 
@@ -160,6 +168,8 @@ struct gr_bvh {
     uint32_t n = 0;
     bool built = false;
     int layout = 0;       // traversal layout gr_trace uses
+    int block = 128;      // gr_trace launch shape (autotuned or set)
+    int sstack = 12;
     bool built4 = false, built4q = false;
     gr::BvhBuffers buf;
 };

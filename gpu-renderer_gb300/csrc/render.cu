@@ -261,12 +261,12 @@ struct QueueSrc {
     }
 };
 
-template <int LAYOUT>
-__global__ void __launch_bounds__(trav::kTraceThreads) k_trace_queue(Paths ps, int b) {
-    __shared__ int2 s_stack[trav::kShortStack][trav::kTraceThreads];
+template <int LAYOUT, int SSTACK>
+__global__ void __launch_bounds__(trav::kMaxTraceThreads) k_trace_queue(Paths ps, int b) {
+    extern __shared__ int2 s_stack[];
     if (b > (int)ps.hdr->max_depth) return;
     QueueSrc src{(b & 1) ? ps.qb : ps.qa, &ps, ps.cnt[b]};
-    trav::traverse_loop<false, LAYOUT>(src, ps.work + b, ps.cnt + kErrWord, s_stack);
+    trav::traverse_loop<false, LAYOUT, SSTACK>(src, ps.work + b, ps.cnt + kErrWord, s_stack);
 }
 
 // Shadow rays: an unoccluded ray adds its contribution to its path
@@ -295,12 +295,12 @@ struct ShadowSrc {
     }
 };
 
-template <int LAYOUT>
-__global__ void __launch_bounds__(trav::kTraceThreads) k_trace_shadow(Paths ps, int b) {
-    __shared__ int2 s_stack[trav::kShortStack][trav::kTraceThreads];
+template <int LAYOUT, int SSTACK>
+__global__ void __launch_bounds__(trav::kMaxTraceThreads) k_trace_shadow(Paths ps, int b) {
+    extern __shared__ int2 s_stack[];
     if (b >= (int)ps.hdr->max_depth) return;
     ShadowSrc src{&ps, ps.cnt[kShadowBase + b]};
-    trav::traverse_loop<true, LAYOUT>(src, ps.work + kShadowBase + b, ps.cnt + kErrWord, s_stack);
+    trav::traverse_loop<true, LAYOUT, SSTACK>(src, ps.work + kShadowBase + b, ps.cnt + kErrWord, s_stack);
 }
 
 // ---- shading --------------------------------------------------------------------------
@@ -477,8 +477,9 @@ __global__ void k_wave_end(Paths ps) {
 
 // One wave: clear counters, camera rays, kMaxWaveDepth x (trace, shade, shadow)
 // (steps past the wave's max_depth return at once), resolve, ray counts.
-template <int LAYOUT>
-cudaError_t issue_wave_l(const Paths& ps, uint32_t depth_steps, int tgrid, int sgrid, cudaStream_t s) {
+template <int LAYOUT, int SSTACK>
+cudaError_t issue_wave_l(const Paths& ps, uint32_t depth_steps, int tgrid, int tblock, int sgrid, cudaStream_t s) {
+    const size_t smem = sizeof(int2) * SSTACK * tblock;
     cudaError_t e;
     const size_t cnt_bytes = sizeof(uint32_t) * (2 * kMaxDepth + 4);
     const size_t work_bytes = sizeof(unsigned long long) * (2 * kMaxDepth + 4);
@@ -486,19 +487,42 @@ cudaError_t issue_wave_l(const Paths& ps, uint32_t depth_steps, int tgrid, int s
     if ((e = cudaMemsetAsync(ps.work, 0, work_bytes, s)) != cudaSuccess) return e;
     k_camera<<<sgrid, kShadeThreads, 0, s>>>(ps);
     for (int b = 0; b <= (int)depth_steps; ++b) {
-        k_trace_queue<LAYOUT><<<tgrid, trav::kTraceThreads, 0, s>>>(ps, b);
+        k_trace_queue<LAYOUT, SSTACK><<<tgrid, tblock, smem, s>>>(ps, b);
         k_shade<<<sgrid, kShadeThreads, 0, s>>>(ps, b);
-        if (b < (int)depth_steps) k_trace_shadow<LAYOUT><<<tgrid, trav::kTraceThreads, 0, s>>>(ps, b);
+        if (b < (int)depth_steps) k_trace_shadow<LAYOUT, SSTACK><<<tgrid, tblock, smem, s>>>(ps, b);
     }
     k_resolve<<<sgrid, kShadeThreads, 0, s>>>(ps);
     k_wave_end<<<1, 32, 0, s>>>(ps);
     return cudaGetLastError();
 }
 
-cudaError_t issue_wave(const Paths& ps, uint32_t depth_steps, int tgrid, int sgrid, cudaStream_t s, int layout) {
-    if (layout == kLayoutBvh4) return issue_wave_l<kLayoutBvh4>(ps, depth_steps, tgrid, sgrid, s);
-    if (layout == kLayoutBvh4Q8) return issue_wave_l<kLayoutBvh4Q8>(ps, depth_steps, tgrid, sgrid, s);
-    return issue_wave_l<kLayoutBvh2>(ps, depth_steps, tgrid, sgrid, s);
+template <int LAYOUT>
+cudaError_t issue_wave_s(const Paths& ps, uint32_t steps, int tgrid, const TraceTuning& t, int sgrid, cudaStream_t s) {
+    if (t.sstack == 8) return issue_wave_l<LAYOUT, 8>(ps, steps, tgrid, t.block, sgrid, s);
+    if (t.sstack == 16) return issue_wave_l<LAYOUT, 16>(ps, steps, tgrid, t.block, sgrid, s);
+    return issue_wave_l<LAYOUT, 12>(ps, steps, tgrid, t.block, sgrid, s);
+}
+
+cudaError_t issue_wave(const Paths& ps, uint32_t steps, int tgrid, int sgrid, cudaStream_t s, const TraceTuning& t) {
+    if (t.layout == kLayoutBvh4) return issue_wave_s<kLayoutBvh4>(ps, steps, tgrid, t, sgrid, s);
+    if (t.layout == kLayoutBvh4Q8) return issue_wave_s<kLayoutBvh4Q8>(ps, steps, tgrid, t, sgrid, s);
+    return issue_wave_s<kLayoutBvh2>(ps, steps, tgrid, t, sgrid, s);
+}
+
+// Resident blocks per SM of the closest-hit queue kernel for a configuration.
+cudaError_t trace_occupancy(const TraceTuning& t, int* occ) {
+    const size_t smem = sizeof(int2) * t.sstack * t.block;
+    const void* fn = nullptr;
+#define GR_PICK(L, S) \
+    if (t.layout == L && t.sstack == S) fn = (const void*)k_trace_queue<L, S>;
+    GR_PICK(kLayoutBvh2, 8) GR_PICK(kLayoutBvh2, 12) GR_PICK(kLayoutBvh2, 16)
+    GR_PICK(kLayoutBvh4, 8) GR_PICK(kLayoutBvh4, 12) GR_PICK(kLayoutBvh4, 16)
+    GR_PICK(kLayoutBvh4Q8, 8) GR_PICK(kLayoutBvh4Q8, 12) GR_PICK(kLayoutBvh4Q8, 16)
+#undef GR_PICK
+    if (!fn) return cudaErrorInvalidValue;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, fn, t.block, smem);
+    if (*occ < 1) *occ = 1;
+    return e;
 }
 
 uint64_t mix64(uint64_t h, uint64_t v) {
@@ -622,16 +646,14 @@ uint32_t pack_wave(std::vector<HostJob*>& jobs, uint32_t capacity, std::vector<J
 }
 
 cudaError_t run_wave(WavePool& pool, const JobDev* h_jobs, uint32_t njobs, uint32_t total_paths, uint32_t total_pix,
-                     uint32_t max_depth, int num_sms, cudaStream_t s, bool use_graph, int layout) {
-    static int occ = 0;
+                     uint32_t max_depth, int num_sms, cudaStream_t s, bool use_graph, const TraceTuning& tune) {
     cudaError_t e;
-    if (occ == 0) {
-        // the 4-wide kernels use the most registers; size the grid for them
-        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_trace_queue<kLayoutBvh4>, trav::kTraceThreads,
-                                                               0)) != cudaSuccess)
-            return e;
-        occ = std::max(occ, 1);
-    }
+    if (!tuning_valid(tune)) return cudaErrorInvalidValue;
+    static int occ_cache[3][3][3] = {};
+    const int bi = tune.block == 64 ? 0 : (tune.block == 128 ? 1 : 2);
+    const int si = tune.sstack == 8 ? 0 : (tune.sstack == 12 ? 1 : 2);
+    int& occ = occ_cache[tune.layout][bi][si];
+    if (occ == 0 && (e = trace_occupancy(tune, &occ)) != cudaSuccess) return e;
     if (njobs == 0 || njobs > kMaxJobs || total_paths > pool.capacity || max_depth > (uint32_t)kMaxDepth)
         return cudaErrorInvalidValue;
     const Paths& ps = pool.ps;
@@ -655,17 +677,17 @@ cudaError_t run_wave(WavePool& pool, const JobDev* h_jobs, uint32_t njobs, uint3
     const int tgrid = num_sms * occ;
     const int sgrid = num_sms * 4;
     const uint32_t steps = std::max(max_depth, kGraphDepthSteps);
-    if (!use_graph) return issue_wave(ps, max_depth, tgrid, sgrid, s, layout);
+    if (!use_graph) return issue_wave(ps, max_depth, tgrid, sgrid, s, tune);
     uint64_t key = 0x51ED270B27A3C1F5ull;
     const uint64_t words[] = {(uint64_t)(uintptr_t)ps.ray, ps.capacity, steps, (uint64_t)tgrid, (uint64_t)sgrid,
-                              (uint64_t)layout};
+                              (uint64_t)tune.layout, (uint64_t)tune.block, (uint64_t)tune.sstack};
     for (uint64_t w : words) key = mix64(key, w);
     WaveGraph& g = pool.graph;
     if (!g.exec || g.key != key) {
         g.release();
         cudaGraph_t graph = nullptr;
         if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return e;
-        const cudaError_t ei = issue_wave(ps, steps, tgrid, sgrid, s, layout);
+        const cudaError_t ei = issue_wave(ps, steps, tgrid, sgrid, s, tune);
         e = cudaStreamEndCapture(s, &graph);
         if (ei != cudaSuccess) {
             if (graph) cudaGraphDestroy(graph);

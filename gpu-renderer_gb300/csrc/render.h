@@ -147,10 +147,17 @@ struct HostJob {
 // wave_samples, sample_base filled in). Uses the pool's captured graph unless
 // use_graph is false.
 cudaError_t run_wave(WavePool& pool, const JobDev* h_jobs, uint32_t njobs, uint32_t total_paths, uint32_t total_pix,
-                     uint32_t max_depth, int num_sms, cudaStream_t s, bool use_graph, int layout);
+                     uint32_t max_depth, int num_sms, cudaStream_t s, bool use_graph, const TraceTuning& tune);
 
 // Scene view for a wave of the given node layout (the layout must be built).
 SceneDev scene_view(gr_scene* sc, int layout);
+
+}  // namespace gr
+
+// The traversal configuration a scene renders with (its BVH's tuning).
+gr::TraceTuning scene_tuning(const gr_scene* sc);
+
+namespace gr {
 
 // Packs as many samples of `jobs` (in order) as fit into `capacity` paths;
 // returns the number of jobs in the wave (0 when nothing fits). Advances
@@ -168,6 +175,7 @@ struct gr_scene {
     gr::DevBuf fb, fb_count;
     gr::WavePool pool;
     uint32_t samples_done = 0;
+    uint32_t default_wave_paths = 0;  // 0 = library default (autotuned by gr_scene_autotune)
     gr::DevCamera cam{};
     float env[3] = {0, 0, 0};
     int has_env = 0;

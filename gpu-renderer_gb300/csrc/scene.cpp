@@ -58,6 +58,14 @@ bool emissive(const gr_material& m) { return m.emission[0] != 0.0f || m.emission
 
 }  // namespace
 
+gr::TraceTuning scene_tuning(const gr_scene* sc) {
+    gr::TraceTuning t;
+    t.layout = sc->bvh->layout;
+    t.block = sc->bvh->block;
+    t.sstack = sc->bvh->sstack;
+    return t;
+}
+
 gr::SceneDev gr::scene_view(gr_scene* sc, int layout) {
     gr::SceneDev d{};
     d.verts = (const float*)sc->verts.p;
@@ -231,7 +239,8 @@ gr_status gr_render(gr_scene* sc, const gr_render_opts* opts, float* h_rgb, gr_r
     SC_CUDA(ctx, cudaSetDevice(ctx->device));
     cudaStream_t s = ctx->stream;
     const uint32_t npix = sc->cam.width * sc->cam.height;
-    const uint64_t want_paths = opts->wave_paths ? opts->wave_paths : (1u << 22);
+    const uint64_t want_paths = opts->wave_paths ? opts->wave_paths
+                                : (sc->default_wave_paths ? sc->default_wave_paths : (1u << 22));
     uint32_t per_wave = (uint32_t)std::max<uint64_t>(1, want_paths / npix);
     if (opts->spp) per_wave = std::min(per_wave, opts->spp);
     const uint64_t cap64 = (uint64_t)per_wave * npix;
@@ -260,7 +269,7 @@ gr_status gr_render(gr_scene* sc, const gr_render_opts* opts, float* h_rgb, gr_r
         const uint32_t nj = gr::pack_wave(jobs, (uint32_t)cap64, table, &paths, &pix, &depth);
         if (nj == 0) break;
         SC_CUDA(ctx, gr::run_wave(sc->pool, table.data(), nj, paths, pix, depth, ctx->num_sms, s,
-                                  (opts->flags & GR_RENDER_NO_GRAPH) == 0, layout));
+                                  (opts->flags & GR_RENDER_NO_GRAPH) == 0, scene_tuning(sc)));
         ++waves;
     }
     gr::WaveHeader after{};
@@ -316,3 +325,83 @@ gr_status gr_scene_reset(gr_scene* sc) {
 }
 
 }  // extern "C"
+
+extern "C" gr_status gr_scene_autotune(gr_scene* sc, const gr_render_opts* probe, gr_trace_tuning* best_out,
+                                       uint32_t* best_wave_paths) {
+    if (!sc || !probe) return GR_ERR_INVALID;
+    gr_ctx* ctx = sc->ctx;
+    gr_render_opts o = *probe;
+    o.flags &= ~GR_RENDER_NO_GRAPH;
+    auto timed = [&](double* ms) -> gr_status {
+        gr_render_stats st{};
+        // the first call captures the wave's graph; time the second
+        gr_status r = gr_render(sc, &o, nullptr, &st);
+        if (r != GR_OK) return r;
+        r = gr_render(sc, &o, nullptr, &st);
+        *ms = st.ms;
+        return r;
+    };
+    const int layouts[] = {0, 1, 2}, blocks[] = {64, 128, 256}, stacks[] = {8, 12, 16};
+    gr_trace_tuning best{sc->bvh->layout, sc->bvh->block, sc->bvh->sstack};
+    double best_ms = 1e300;
+    for (int lay : layouts)
+        for (int blk : blocks)
+            for (int ss : stacks) {
+                gr_trace_tuning t{lay, blk, ss};
+                gr_status r = gr_bvh_set_tuning(sc->bvh, &t);
+                if (r == GR_OK) {
+                    SC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+                    double ms = 0;
+                    r = timed(&ms);
+                    if (r == GR_OK && ms < best_ms) {
+                        best_ms = ms;
+                        best = t;
+                    }
+                }
+                if (r != GR_OK) return r;
+            }
+    gr_status r = gr_bvh_set_tuning(sc->bvh, &best);
+    if (r != GR_OK) return r;
+    SC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    // wave size (queue capacity): the probe must fill the largest candidate
+    const uint32_t npix = sc->cam.width * sc->cam.height;
+    uint32_t best_wave = 1u << 22;
+    double best_wms = 1e300;
+    const uint32_t waves[] = {1u << 20, 1u << 21, 1u << 22, 1u << 23};
+    const uint32_t fill_spp = (uint32_t)std::max<uint64_t>(probe->spp, ((uint64_t)waves[3] + npix - 1) / npix);
+    for (uint32_t w : waves) {
+        o = *probe;
+        o.flags &= ~GR_RENDER_NO_GRAPH;
+        o.spp = fill_spp;
+        o.wave_paths = w;
+        double ms = 0;
+        r = timed(&ms);
+        if (r != GR_OK) return r;
+        const double per_sample = ms / ((double)o.spp * npix);
+        if (per_sample < best_wms) {
+            best_wms = per_sample;
+            best_wave = w;
+        }
+    }
+    sc->default_wave_paths = best_wave;
+    gr_scene_reset(sc);
+    if (best_out) *best_out = best;
+    if (best_wave_paths) *best_wave_paths = best_wave;
+    return GR_OK;
+}
+
+extern "C" gr_status gr_scene_set_tuning(gr_scene* sc, const gr_trace_tuning* t, uint32_t wave_paths) {
+    if (!sc || !t) return GR_ERR_INVALID;
+    gr_status st = gr_bvh_set_tuning(sc->bvh, t);
+    if (st != GR_OK) return st;
+    SC_CUDA(sc->ctx, cudaStreamSynchronize(sc->ctx->stream));
+    sc->default_wave_paths = wave_paths;
+    return GR_OK;
+}
+
+extern "C" gr_status gr_scene_get_tuning(const gr_scene* sc, gr_trace_tuning* t, uint32_t* wave_paths) {
+    if (!sc) return GR_ERR_INVALID;
+    if (t) gr_bvh_get_tuning(sc->bvh, t);
+    if (wave_paths) *wave_paths = sc->default_wave_paths;
+    return GR_OK;
+}

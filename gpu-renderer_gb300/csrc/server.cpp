@@ -44,7 +44,8 @@ extern "C" uint64_t gr_scene_device_bytes(const gr_scene* sc) {
                  sc->fb.bytes + sc->fb_count.bytes + sc->pool.mem.bytes;
     if (sc->bvh) {
         const gr::BvhBuffers& bb = sc->bvh->buf;
-        b += bb.nodes.bytes + bb.tris.bytes + bb.code.bytes + bb.prim.bytes + bb.scratch.bytes + bb.meta.bytes;
+        b += bb.nodes.bytes + bb.nodes4.bytes + bb.nodes4q.bytes + bb.tris.bytes + bb.code.bytes + bb.prim.bytes +
+             bb.scratch.bytes + bb.meta.bytes;
     }
     return b;
 }
@@ -111,7 +112,7 @@ extern "C" gr_status gr_render_batch(gr_ctx* ctx, gr_scene* const* scenes, const
         const uint32_t nj = gr::pack_wave(order, pool.capacity, table, &paths, &pix, &depth);
         if (nj == 0) break;
         if ((e = gr::run_wave(pool, table.data(), nj, paths, pix, depth, ctx->num_sms, s, graph,
-                              scenes[0]->bvh->layout)) != cudaSuccess) {
+                              scene_tuning(scenes[0]))) != cudaSuccess) {
             ctx->last_error = std::string("gr_render_batch: ") + cudaGetErrorString(e);
             cudaGetLastError();
             return cuda_status(e);
@@ -307,8 +308,12 @@ struct gr_server {
                 uint32_t paths = 0, pix = 0, depth = 0;
                 const uint32_t nj = gr::pack_wave(hjs, pool.capacity, table, &paths, &pix, &depth);
                 if (nj) {
+                    gr::TraceTuning tune;
+                    tune.layout = opts.layout;
+                    tune.block = opts.block;
+                    tune.sstack = opts.short_stack;
                     const cudaError_t e = gr::run_wave(pool, table.data(), nj, paths, pix, depth, ctx->num_sms, stream,
-                                                       true, opts.layout);
+                                                       true, tune);
                     if (e != cudaSuccess) {
                         std::lock_guard<std::mutex> lk(mu);
                         error = cudaGetErrorString(e);
@@ -362,6 +367,17 @@ gr_status gr_server_create(gr_ctx* ctx, const gr_server_opts* opts, gr_server** 
     if (!sv) return GR_ERR_OOM_BUDGET;
     sv->ctx = ctx;
     if (opts) sv->opts = *opts;
+    if (!sv->opts.block) sv->opts.block = 128;
+    if (!sv->opts.short_stack) sv->opts.short_stack = 12;
+    gr::TraceTuning tt;
+    tt.layout = sv->opts.layout;
+    tt.block = sv->opts.block;
+    tt.sstack = sv->opts.short_stack;
+    if (!gr::tuning_valid(tt)) {
+        ctx->last_error = "gr_server_create: unsupported layout / block / short_stack";
+        delete sv;
+        return GR_ERR_INVALID;
+    }
     cudaError_t e = cudaSetDevice(ctx->device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&sv->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = sv->pool.ensure(default_capacity(sv->opts.wave_paths));

@@ -41,51 +41,67 @@ struct RaySrc {
     }
 };
 
-template <bool ANY, int LAYOUT>
-__global__ void __launch_bounds__(trav::kTraceThreads) k_trace(const void* __restrict__ nodes, const Tri* __restrict__ tris,
-                                                               const BvhMeta* __restrict__ meta,
-                                                               const float4* __restrict__ rays, uint64_t n,
-                                                               float4* __restrict__ hits, unsigned long long* counter,
-                                                               uint32_t* err) {
-    __shared__ int2 s_stack[trav::kShortStack][trav::kTraceThreads];
+template <bool ANY, int LAYOUT, int SSTACK>
+__global__ void __launch_bounds__(trav::kMaxTraceThreads) k_trace(const void* __restrict__ nodes, const Tri* __restrict__ tris,
+                                                                  const BvhMeta* __restrict__ meta,
+                                                                  const float4* __restrict__ rays, uint64_t n,
+                                                                  float4* __restrict__ hits, unsigned long long* counter,
+                                                                  uint32_t* err) {
+    extern __shared__ int2 s_stack[];
     RaySrc src{rays, hits, n, nodes, tris, meta->root};
-    trav::traverse_loop<ANY, LAYOUT>(src, counter, err, s_stack);
+    trav::traverse_loop<ANY, LAYOUT, SSTACK>(src, counter, err, s_stack);
+}
+
+template <bool ANY, int LAYOUT, int SSTACK>
+cudaError_t launch(const BvhDevice& bvh, const void* nodes, int block, const float4* r, uint64_t n, float4* h,
+                   unsigned long long* counter, uint32_t* err, int num_sms, cudaStream_t s) {
+    static int occ[3] = {0, 0, 0};  // per block size 64 / 128 / 256
+    const int bi = block == 64 ? 0 : (block == 128 ? 1 : 2);
+    const size_t smem = sizeof(int2) * SSTACK * block;
+    if (occ[bi] == 0) {
+        const cudaError_t e =
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[bi], k_trace<ANY, LAYOUT, SSTACK>, block, smem);
+        if (e != cudaSuccess) return e;
+        if (occ[bi] < 1) occ[bi] = 1;
+    }
+    const uint64_t warps_needed = (n + 31) / 32;
+    const uint64_t blocks_needed = (warps_needed + block / 32 - 1) / (block / 32);
+    const int grid = (int)std::min<uint64_t>((uint64_t)num_sms * occ[bi], blocks_needed);
+    k_trace<ANY, LAYOUT, SSTACK><<<grid, block, smem, s>>>(nodes, bvh.tris, bvh.meta, r, n, h, counter, err);
+    return cudaGetLastError();
 }
 
 template <bool ANY, int LAYOUT>
-cudaError_t launch(const BvhDevice& bvh, const void* nodes, const float4* r, uint64_t n, float4* h,
-                   unsigned long long* counter, uint32_t* err, int num_sms, cudaStream_t s) {
-    static int occ = 0;
-    if (occ == 0) {
-        const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_trace<ANY, LAYOUT>,
-                                                                            trav::kTraceThreads, 0);
-        if (e != cudaSuccess) return e;
-        if (occ < 1) occ = 1;
-    }
-    const uint64_t warps_needed = (n + 31) / 32;
-    const uint64_t blocks_needed = (warps_needed + trav::kTraceThreads / 32 - 1) / (trav::kTraceThreads / 32);
-    const int grid = (int)std::min<uint64_t>((uint64_t)num_sms * occ, blocks_needed);
-    k_trace<ANY, LAYOUT><<<grid, trav::kTraceThreads, 0, s>>>(nodes, bvh.tris, bvh.meta, r, n, h, counter, err);
-    return cudaGetLastError();
+cudaError_t launch_s(const BvhDevice& bvh, const void* nodes, const TraceTuning& t, const float4* r, uint64_t n,
+                     float4* h, unsigned long long* c, uint32_t* err, int num_sms, cudaStream_t s) {
+    if (t.sstack == 8) return launch<ANY, LAYOUT, 8>(bvh, nodes, t.block, r, n, h, c, err, num_sms, s);
+    if (t.sstack == 16) return launch<ANY, LAYOUT, 16>(bvh, nodes, t.block, r, n, h, c, err, num_sms, s);
+    return launch<ANY, LAYOUT, 12>(bvh, nodes, t.block, r, n, h, c, err, num_sms, s);
 }
 
 }  // namespace
 
-cudaError_t trace_launch(const BvhDevice& bvh, const void* nodes, int layout, const gr_ray* d_rays, uint64_t n,
-                         gr_hit* d_hits, int any_hit, unsigned long long* d_counter, uint32_t* d_err, int num_sms,
-                         cudaStream_t s) {
+bool tuning_valid(const TraceTuning& t) {
+    return t.layout >= 0 && t.layout <= 2 && (t.block == 64 || t.block == 128 || t.block == 256) &&
+           (t.sstack == 8 || t.sstack == 12 || t.sstack == 16);
+}
+
+cudaError_t trace_launch(const BvhDevice& bvh, const void* nodes, const TraceTuning& tune, const gr_ray* d_rays,
+                         uint64_t n, gr_hit* d_hits, int any_hit, unsigned long long* d_counter, uint32_t* d_err,
+                         int num_sms, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
+    if (!tuning_valid(tune)) return cudaErrorInvalidValue;
     cudaError_t e = cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), s);
     if (e != cudaSuccess) return e;
     const float4* r = reinterpret_cast<const float4*>(d_rays);
     float4* h = reinterpret_cast<float4*>(d_hits);
-    switch (layout * 2 + (any_hit ? 1 : 0)) {
-        case 0: return launch<false, kLayoutBvh2>(bvh, nodes, r, n, h, d_counter, d_err, num_sms, s);
-        case 1: return launch<true, kLayoutBvh2>(bvh, nodes, r, n, h, d_counter, d_err, num_sms, s);
-        case 2: return launch<false, kLayoutBvh4>(bvh, nodes, r, n, h, d_counter, d_err, num_sms, s);
-        case 3: return launch<true, kLayoutBvh4>(bvh, nodes, r, n, h, d_counter, d_err, num_sms, s);
-        case 4: return launch<false, kLayoutBvh4Q8>(bvh, nodes, r, n, h, d_counter, d_err, num_sms, s);
-        case 5: return launch<true, kLayoutBvh4Q8>(bvh, nodes, r, n, h, d_counter, d_err, num_sms, s);
+    switch (tune.layout * 2 + (any_hit ? 1 : 0)) {
+        case 0: return launch_s<false, kLayoutBvh2>(bvh, nodes, tune, r, n, h, d_counter, d_err, num_sms, s);
+        case 1: return launch_s<true, kLayoutBvh2>(bvh, nodes, tune, r, n, h, d_counter, d_err, num_sms, s);
+        case 2: return launch_s<false, kLayoutBvh4>(bvh, nodes, tune, r, n, h, d_counter, d_err, num_sms, s);
+        case 3: return launch_s<true, kLayoutBvh4>(bvh, nodes, tune, r, n, h, d_counter, d_err, num_sms, s);
+        case 4: return launch_s<false, kLayoutBvh4Q8>(bvh, nodes, tune, r, n, h, d_counter, d_err, num_sms, s);
+        case 5: return launch_s<true, kLayoutBvh4Q8>(bvh, nodes, tune, r, n, h, d_counter, d_err, num_sms, s);
         default: return cudaErrorInvalidValue;
     }
 }

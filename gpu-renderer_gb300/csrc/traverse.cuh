@@ -10,9 +10,12 @@
 namespace gr {
 namespace trav {
 
+// Launch shape and short-stack depth are tuning parameters (the autotuner
+// picks them per device and workload); these are the defaults.
 constexpr int kTraceThreads = 128;
 constexpr int kShortStack = 12;
 constexpr int kStackMax = 64;
+constexpr int kMaxTraceThreads = 256;
 
 struct RayW {
     float ox, oy, oz, tmin, tmax;
@@ -138,13 +141,15 @@ __device__ __forceinline__ bool leaf(Lane& L, int32_t c) {
     return false;
 }
 
-// Pushes a deferred node with its entry distance; false on overflow.
-__device__ __forceinline__ bool push(Lane& L, int32_t c, float tn, int2 (*s_stack)[kTraceThreads], int2* l_stack,
-                                     uint32_t* err) {
-    if (L.sp < kShortStack) {
-        s_stack[L.sp][threadIdx.x] = make_int2(c, __float_as_int(tn));
+// Pushes a deferred node with its entry distance; false on overflow. The
+// first SSTACK entries of a thread live in shared memory ([entry][thread],
+// conflict-free), deeper entries in a local array.
+template <int SSTACK>
+__device__ __forceinline__ bool push(Lane& L, int32_t c, float tn, int2* s_stack, int2* l_stack, uint32_t* err) {
+    if (L.sp < SSTACK) {
+        s_stack[L.sp * blockDim.x + threadIdx.x] = make_int2(c, __float_as_int(tn));
     } else if (L.sp < kStackMax) {
-        l_stack[L.sp - kShortStack] = make_int2(c, __float_as_int(tn));
+        l_stack[L.sp - SSTACK] = make_int2(c, __float_as_int(tn));
     } else {
         atomicOr(err, ERR_STACK);
         return false;
@@ -155,12 +160,12 @@ __device__ __forceinline__ bool push(Lane& L, int32_t c, float tn, int2 (*s_stac
 
 // Pops the next deferred node still in front of the closest hit; false when
 // the stack is empty (the ray is finished).
-template <bool ANY>
-__device__ __forceinline__ bool pop(Lane& L, int2 (*s_stack)[kTraceThreads], const int2* l_stack, int32_t& next) {
+template <bool ANY, int SSTACK>
+__device__ __forceinline__ bool pop(Lane& L, const int2* s_stack, const int2* l_stack, int32_t& next) {
     for (;;) {
         if (L.sp == 0) return false;
         --L.sp;
-        const int2 e = L.sp < kShortStack ? s_stack[L.sp][threadIdx.x] : l_stack[L.sp - kShortStack];
+        const int2 e = L.sp < SSTACK ? s_stack[L.sp * blockDim.x + threadIdx.x] : l_stack[L.sp - SSTACK];
         if (ANY || __int_as_float(e.y) <= __fmul_rn(L.best_t, kCullSlack)) {
             next = e.x;
             return true;
@@ -170,8 +175,8 @@ __device__ __forceinline__ bool pop(Lane& L, int2 (*s_stack)[kTraceThreads], con
 
 // One binary node: both child boxes, nearer first; leaves tested inline.
 // Returns true when the ray is finished.
-template <bool ANY>
-__device__ __forceinline__ bool trace_step2(Lane& L, int2 (*s_stack)[kTraceThreads], int2* l_stack, uint32_t* err) {
+template <bool ANY, int SSTACK>
+__device__ __forceinline__ bool trace_step2(Lane& L, int2* s_stack, int2* l_stack, uint32_t* err) {
     const float4* q = reinterpret_cast<const float4*>(static_cast<const Node*>(L.nodes) + L.node);
     const float4 q0 = __ldg(q), q1 = __ldg(q + 1), q2 = __ldg(q + 2);
     const int4 q3 = __ldg(reinterpret_cast<const int4*>(q + 3));
@@ -194,11 +199,11 @@ __device__ __forceinline__ bool trace_step2(Lane& L, int2 (*s_stack)[kTraceThrea
         } else if (!have) {
             next = c;
             have = true;
-        } else if (!push(L, c, tnf, s_stack, l_stack, err)) {
+        } else if (!push<SSTACK>(L, c, tnf, s_stack, l_stack, err)) {
             return true;
         }
     }
-    if (!have && !pop<ANY>(L, s_stack, l_stack, next)) return true;
+    if (!have && !pop<ANY, SSTACK>(L, s_stack, l_stack, next)) return true;
     L.node = next;
     return false;
 }
@@ -212,8 +217,8 @@ __device__ __forceinline__ float qplane(uint32_t word, int k, float scale, float
 // visited in order of (entry distance, slot); leaves tested inline, the nearest
 // inner child visited next, the other inner children pushed so the nearer pop
 // first. Returns true when the ray is finished.
-template <bool ANY, bool QUANT>
-__device__ __forceinline__ bool trace_step4(Lane& L, int2 (*s_stack)[kTraceThreads], int2* l_stack, uint32_t* err) {
+template <bool ANY, bool QUANT, int SSTACK>
+__device__ __forceinline__ bool trace_step4(Lane& L, int2* s_stack, int2* l_stack, uint32_t* err) {
     float tn[4];
     bool h[4];
     int32_t c[4];
@@ -293,18 +298,18 @@ __device__ __forceinline__ bool trace_step4(Lane& L, int2 (*s_stack)[kTraceThrea
             ++np;
         }
     }
-    if (np > 2 && !push(L, pc2, pt2, s_stack, l_stack, err)) return true;
-    if (np > 1 && !push(L, pc1, pt1, s_stack, l_stack, err)) return true;
-    if (np > 0 && !push(L, pc0, pt0, s_stack, l_stack, err)) return true;
-    if (!have && !pop<ANY>(L, s_stack, l_stack, next)) return true;
+    if (np > 2 && !push<SSTACK>(L, pc2, pt2, s_stack, l_stack, err)) return true;
+    if (np > 1 && !push<SSTACK>(L, pc1, pt1, s_stack, l_stack, err)) return true;
+    if (np > 0 && !push<SSTACK>(L, pc0, pt0, s_stack, l_stack, err)) return true;
+    if (!have && !pop<ANY, SSTACK>(L, s_stack, l_stack, next)) return true;
     L.node = next;
     return false;
 }
 
-template <bool ANY, int LAYOUT>
-__device__ __forceinline__ bool trace_step(Lane& L, int2 (*s_stack)[kTraceThreads], int2* l_stack, uint32_t* err) {
-    if (LAYOUT == kLayoutBvh2) return trace_step2<ANY>(L, s_stack, l_stack, err);
-    return trace_step4<ANY, LAYOUT == kLayoutBvh4Q8>(L, s_stack, l_stack, err);
+template <bool ANY, int LAYOUT, int SSTACK>
+__device__ __forceinline__ bool trace_step(Lane& L, int2* s_stack, int2* l_stack, uint32_t* err) {
+    if (LAYOUT == kLayoutBvh2) return trace_step2<ANY, SSTACK>(L, s_stack, l_stack, err);
+    return trace_step4<ANY, LAYOUT == kLayoutBvh4Q8, SSTACK>(L, s_stack, l_stack, err);
 }
 
 // Refill when at least this many lanes of a warp are idle.
@@ -318,10 +323,10 @@ constexpr int kRefillLanes = 8;
 //                                                     returns the root node
 //   void finish(uint64_t i, const Lane& L)            ray i is done (L.best_prim ==
 //                                                     0xFFFFFFFF means a miss)
-template <bool ANY, int LAYOUT, class Src>
-__device__ __forceinline__ void traverse_loop(Src& src, unsigned long long* counter, uint32_t* err,
-                                              int2 (*s_stack)[kTraceThreads]) {
-    int2 l_stack[kStackMax - kShortStack];
+// The shared stack has SSTACK x blockDim.x int2 entries (dynamic shared memory).
+template <bool ANY, int LAYOUT, int SSTACK, class Src>
+__device__ __forceinline__ void traverse_loop(Src& src, unsigned long long* counter, uint32_t* err, int2* s_stack) {
+    int2 l_stack[kStackMax - SSTACK];
     const int lane = threadIdx.x & 31;
     const uint32_t ltmask = lanemask_lt();
     const uint64_t n = src.n;
@@ -361,7 +366,7 @@ __device__ __forceinline__ void traverse_loop(Src& src, unsigned long long* coun
             if (exhausted) break;
             continue;
         }
-        if (active && trace_step<ANY, LAYOUT>(L, s_stack, l_stack, err)) {
+        if (active && trace_step<ANY, LAYOUT, SSTACK>(L, s_stack, l_stack, err)) {
             src.finish(L.ray, L);
             active = false;
         }

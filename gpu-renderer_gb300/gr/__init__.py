@@ -59,6 +59,13 @@ def load():
         "gr_bvh_set_layout": ([_P, ctypes.c_int, _P], ctypes.c_int),
         "gr_bvh_export_layout": ([_P, ctypes.c_int, _P], ctypes.c_int),
         "gr_scene_set_layout": ([_P, ctypes.c_int], ctypes.c_int),
+        "gr_bvh_set_tuning": ([_P, _P], ctypes.c_int),
+        "gr_bvh_get_tuning": ([_P, _P], ctypes.c_int),
+        "gr_bvh_autotune": ([_P, _P, ctypes.c_uint64, ctypes.c_int, _P, _P, ctypes.c_uint32,
+                             ctypes.POINTER(ctypes.c_uint32)], ctypes.c_int),
+        "gr_scene_autotune": ([_P, _P, _P, ctypes.POINTER(ctypes.c_uint32)], ctypes.c_int),
+        "gr_scene_set_tuning": ([_P, _P, ctypes.c_uint32], ctypes.c_int),
+        "gr_scene_get_tuning": ([_P, _P, ctypes.POINTER(ctypes.c_uint32)], ctypes.c_int),
         "gr_scene_layout": ([_P], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
@@ -78,6 +85,18 @@ def _ptr(a):
     if isinstance(a, int):
         return _P(a)
     return _P(a.data_ptr())  # torch tensor
+
+
+class Tuning(ctypes.Structure):
+    """Traversal launch configuration (gr_trace_tuning)."""
+    _fields_ = [("layout", ctypes.c_int32), ("block", ctypes.c_int32), ("short_stack", ctypes.c_int32)]
+
+    def as_dict(self):
+        return {"layout": LAYOUT_NAMES[self.layout], "block": self.block, "short_stack": self.short_stack}
+
+
+class TuningResult(ctypes.Structure):
+    _fields_ = [("tuning", Tuning), ("ms", ctypes.c_float)]
 
 
 class Context:
@@ -143,6 +162,24 @@ class BVH:
 
     def set_layout(self, layout, stream=None):
         self.ctx.check(load().gr_bvh_set_layout(self.h, layout, _P(stream) if stream else None), "gr_bvh_set_layout")
+
+    def set_tuning(self, layout, block=128, short_stack=12):
+        t = Tuning(layout, block, short_stack)
+        self.ctx.check(load().gr_bvh_set_tuning(self.h, ctypes.byref(t)), "gr_bvh_set_tuning")
+
+    def tuning(self):
+        t = Tuning()
+        self.ctx.check(load().gr_bvh_get_tuning(self.h, ctypes.byref(t)), "gr_bvh_get_tuning")
+        return t.as_dict()
+
+    def autotune(self, d_rays, n, d_hits, any_hit=False):
+        """Times every layout x block x short-stack configuration on the rays
+        and keeps the fastest; returns [(tuning dict, ms)]."""
+        table = (TuningResult * 64)()
+        rows = ctypes.c_uint32()
+        self.ctx.check(load().gr_bvh_autotune(self.h, _ptr(d_rays), n, int(bool(any_hit)), _ptr(d_hits), table, 64,
+                                              ctypes.byref(rows)), "gr_bvh_autotune")
+        return [(table[i].tuning.as_dict(), float(table[i].ms)) for i in range(min(rows.value, 64))]
 
     def export_layout(self, layout):
         n = self.size
@@ -305,6 +342,26 @@ class Scene:
     def set_layout(self, layout):
         self.ctx.check(load().gr_scene_set_layout(self.h, layout), "gr_scene_set_layout")
 
+    def autotune(self, spp=1, max_depth=8, seed=0, rr_depth=3, flags=0):
+        """Render autotuner: traversal configuration and wave size (queue
+        capacity) from timed probe renders. Clears the accumulation."""
+        o = RenderOpts(spp, max_depth, seed, rr_depth, flags, 0)
+        t = Tuning()
+        w = ctypes.c_uint32()
+        self.ctx.check(load().gr_scene_autotune(self.h, ctypes.byref(o), ctypes.byref(t), ctypes.byref(w)),
+                       "gr_scene_autotune")
+        return t.as_dict(), w.value
+
+    def set_tuning(self, layout, block=128, short_stack=12, wave_paths=0):
+        t = Tuning(layout, block, short_stack)
+        self.ctx.check(load().gr_scene_set_tuning(self.h, ctypes.byref(t), wave_paths), "gr_scene_set_tuning")
+
+    def tuning(self):
+        t = Tuning()
+        w = ctypes.c_uint32()
+        self.ctx.check(load().gr_scene_get_tuning(self.h, ctypes.byref(t), ctypes.byref(w)), "gr_scene_get_tuning")
+        return t.as_dict(), w.value
+
     def info(self):
         v = [ctypes.c_uint32() for _ in range(4)]
         self.ctx.check(_declare(_SCENE_SIGS).gr_scene_info(self.h, *[ctypes.byref(x) for x in v]), "gr_scene_info")
@@ -354,7 +411,7 @@ class PathTracer:
 
 class ServerOpts(ctypes.Structure):
     _fields_ = [("budget_bytes", ctypes.c_uint64), ("wave_paths", ctypes.c_uint32), ("max_active", ctypes.c_uint32),
-                ("layout", ctypes.c_int32)]
+                ("layout", ctypes.c_int32), ("block", ctypes.c_int32), ("short_stack", ctypes.c_int32)]
 
 
 class JobStats(ctypes.Structure):
@@ -408,10 +465,10 @@ def render_batch(ctx, scenes, opts, wave_paths=0):
 class Server:
     """Continuous-batching render server (gr_server)."""
 
-    def __init__(self, ctx, budget_bytes=0, wave_paths=0, max_active=0, layout=LAYOUT_BVH2):
+    def __init__(self, ctx, budget_bytes=0, wave_paths=0, max_active=0, layout=LAYOUT_BVH2, block=0, short_stack=0):
         L = _declare(_SERVER_SIGS)
         self.ctx = ctx
-        o = ServerOpts(budget_bytes, wave_paths, max_active, layout)
+        o = ServerOpts(budget_bytes, wave_paths, max_active, layout, block, short_stack)
         h = _P()
         ctx.check(L.gr_server_create(ctx.h, ctypes.byref(o), ctypes.byref(h)), "gr_server_create")
         self.h = h

@@ -30,64 +30,98 @@ def _timed_render(scene, spp, depth, rr=3, flags=0, reps=3):
     return best, st
 
 
-def plain_render(ctx, desc, spp, depth, rr=3):
+def _names():
+    return {v: k for k, v in gr.LAYOUT_NAMES.items()}
+
+
+def tuning_args(tune, wave=0):
+    """(layout, block, short_stack, wave_paths) from an autotuner result."""
+    return (_names()[tune["layout"]], tune["block"], tune["short_stack"], wave)
+
+
+def plain_render(ctx, desc, spp, depth, rr=3, autotune=True):
+    """One scene rendered by gr_render; with autotune the scene's traversal
+    configuration and wave size come from gr_scene_autotune (1-spp probes)."""
     s = gr.Scene(ctx, desc)
+    tune = wave = None
+    if autotune:
+        tune, wave = s.autotune(spp=1, max_depth=depth, rr_depth=rr)
     dt, st = _timed_render(s, spp, depth, rr)
     npix = desc.camera["width"] * desc.camera["height"]
     out = {"ms": dt * 1e3, "samples_per_s": npix * spp / dt, "mrays_s": (st.closest_rays + st.shadow_rays) / dt / 1e6,
-           "triangles": desc.num_triangles, "waves": st.waves}
+           "triangles": desc.num_triangles, "waves": st.waves, "tuning": s.tuning()[0], "wave_paths": s.tuning()[1]}
     s.close()
     return out
 
 
-def config4(ctx, n_jobs=64):
+def config4(ctx, n_jobs=64, autotune=True):
+    """Returns renders/s of the 64-job stream rendered the reference's way (one
+    frame per sample per scene), as one multi-sample gr_render per scene, and
+    as one gr_render_batch: once with the default traversal configuration
+    (binary nodes, 128-thread blocks, 12-entry shared stack, 4 Mi-path waves)
+    and once with the configuration and wave size gr_scene_autotune picks on
+    the job with the most samples. Images are identical in all modes and
+    configurations, so RMSE is equal by construction."""
     jobs = [sc.batch_job(i) for i in range(n_jobs)]
     scenes = [gr.Scene(ctx, d) for d, _ in jobs]
     opts = [dict(spp=spp, max_depth=8, seed=i) for i, (_, spp) in enumerate(jobs)]
     samples = sum(d.camera["width"] * d.camera["height"] * spp for d, spp in jobs)
-    # warm-up: one small render per scene (captures graphs, touches memory)
-    for s in scenes:
-        s.render(1, 8, 0, want_image=False)
-        s.reset()
-    gr.render_batch(ctx, scenes, [dict(spp=1, max_depth=8)] * len(scenes))
-    for s in scenes:
-        s.reset()
-    t = time.perf_counter()
-    rays = 0
-    for s, o in zip(scenes, opts):
-        _, st = s.render(o["spp"], 8, o["seed"], want_image=False)
-        rays += st.closest_rays + st.shadow_rays
-    t_seq = time.perf_counter() - t
-    # the reference's schedule: one frame (1 spp) per render() call, launched
-    # kernel by kernel and waited for (PathTracer::render(num), pathtracer.cu:152-170)
-    for s in scenes:
-        s.reset()
-    t = time.perf_counter()
-    for s, o in zip(scenes, opts):
-        for _ in range(o["spp"]):
-            s.render(1, 8, o["seed"], flags=gr.RENDER_NO_GRAPH, want_image=False)
-    t_frames = time.perf_counter() - t
-    for s in scenes:
-        s.reset()
-    t = time.perf_counter()
-    st = gr.render_batch(ctx, scenes, opts)
-    t_batch = time.perf_counter() - t
-    out = {"jobs": n_jobs, "triangles": sum(d.num_triangles for d, _ in jobs), "samples": samples,
-           "per_frame_renders_s": n_jobs / t_frames, "sequential_renders_s": n_jobs / t_seq,
-           "batched_renders_s": n_jobs / t_batch, "speedup_vs_per_frame": t_frames / t_batch,
-           "speedup_vs_sequential": t_seq / t_batch, "per_frame_s": t_frames, "sequential_s": t_seq,
-           "batched_s": t_batch,
-           "batched_mrays_s": (st.closest_rays + st.shadow_rays) / t_batch / 1e6,
-           "sequential_mrays_s": rays / t_seq / 1e6, "batched_waves": st.waves}
+    out = {"jobs": n_jobs, "triangles": sum(d.num_triangles for d, _ in jobs), "samples": samples}
+    modes = [("default", (gr.LAYOUT_BVH2, 128, 12, 0))]
+    if autotune:
+        big = max(range(n_jobs), key=lambda i: jobs[i][0].camera["width"] * jobs[i][0].camera["height"] * jobs[i][1])
+        t0 = time.perf_counter()
+        tune, wave = scenes[big].autotune(spp=1, max_depth=8)
+        out["autotune"] = {"probe_job": big, "tuning": tune, "wave_paths": wave,
+                           "seconds": time.perf_counter() - t0}
+        modes.append(("autotuned", tuning_args(tune, wave)))
+    for name, (layout, block, sstack, wave) in modes:
+        for s in scenes:
+            s.set_tuning(layout, block, sstack, wave)
+        # warm-up: one small render per scene (captures graphs, touches memory)
+        for s in scenes:
+            s.render(1, 8, 0, want_image=False)
+            s.reset()
+        gr.render_batch(ctx, scenes, [dict(spp=1, max_depth=8)] * len(scenes), wave_paths=wave)
+        for s in scenes:
+            s.reset()
+        t = time.perf_counter()
+        rays = 0
+        for s, o in zip(scenes, opts):
+            _, st = s.render(o["spp"], 8, o["seed"], want_image=False)
+            rays += st.closest_rays + st.shadow_rays
+        t_seq = time.perf_counter() - t
+        # the reference's schedule: one frame (1 spp) per render() call, launched
+        # kernel by kernel and waited for (PathTracer::render(num), pathtracer.cu:152-170)
+        for s in scenes:
+            s.reset()
+        t = time.perf_counter()
+        for s, o in zip(scenes, opts):
+            for _ in range(o["spp"]):
+                s.render(1, 8, o["seed"], flags=gr.RENDER_NO_GRAPH, want_image=False)
+        t_frames = time.perf_counter() - t
+        for s in scenes:
+            s.reset()
+        t = time.perf_counter()
+        st = gr.render_batch(ctx, scenes, opts, wave_paths=wave)
+        t_batch = time.perf_counter() - t
+        out[name] = {"tuning": scenes[0].tuning()[0], "wave_paths": wave or (1 << 22),
+                     "per_frame_renders_s": n_jobs / t_frames, "sequential_renders_s": n_jobs / t_seq,
+                     "batched_renders_s": n_jobs / t_batch, "speedup_vs_per_frame": t_frames / t_batch,
+                     "speedup_vs_sequential": t_seq / t_batch, "per_frame_s": t_frames, "sequential_s": t_seq,
+                     "batched_s": t_batch, "batched_mrays_s": (st.closest_rays + st.shadow_rays) / t_batch / 1e6,
+                     "sequential_mrays_s": rays / t_seq / 1e6, "batched_waves": st.waves}
     for s in scenes:
         s.close()
     return out
 
 
-def _serve(ctx, scenes, requests, budget, max_active, rate):
+def _serve(ctx, scenes, requests, budget, max_active, rate, tuning):
     """Submits `requests` (scene index, camera, spp, seed) at Poisson times of
     `rate` per second; returns latency and throughput figures."""
-    srv = gr.Server(ctx, budget_bytes=budget, max_active=max_active)
+    layout, block, sstack, wave = tuning
+    srv = gr.Server(ctx, budget_bytes=budget, wave_paths=wave, max_active=max_active, layout=layout, block=block,
+                    short_stack=sstack)
     r = np.random.default_rng(12345)
     gaps = r.exponential(1.0 / rate, size=len(requests))
     tickets = []
@@ -115,11 +149,16 @@ def _serve(ctx, scenes, requests, budget, max_active, rate):
             "renders_s": len(lat) / span, "waves": int(st.waves), "peak_bytes": int(st.peak_bytes)}
 
 
-def config5(ctx, rates=(10, 20, 50), window_s=3.0, pool=8, budget=150 * 10**9):
+def config5(ctx, rates=(10, 20, 50), window_s=3.0, pool=8, budget=150 * 10**9, tuning=(gr.LAYOUT_BVH2, 128, 12, 0)):
+    """Serving sweep; `tuning` = (layout, block, short_stack, wave_paths) of
+    the server (tuning_args of an autotuner result)."""
     descs = [sc.batch_job(i)[0] for i in range(pool)]
     scenes = [gr.Scene(ctx, d) for d in descs]
     r = np.random.default_rng(0x5EED0005)
-    out = {"scene_pool": pool, "budget_bytes": budget, "window_s": window_s, "sweep": []}
+    layout = tuning[0]
+    out = {"scene_pool": pool, "budget_bytes": budget, "window_s": window_s,
+           "tuning": {"layout": gr.LAYOUT_NAMES[layout], "block": tuning[1], "short_stack": tuning[2],
+                      "wave_paths": tuning[3] or (1 << 22)}, "sweep": []}
 
     def make_requests(n):
         reqs = []
@@ -133,11 +172,11 @@ def config5(ctx, rates=(10, 20, 50), window_s=3.0, pool=8, budget=150 * 10**9):
 
     for rate in rates:
         reqs = make_requests(max(4, int(rate * window_s)))
-        out["sweep"].append(_serve(ctx, scenes, reqs, budget, 0, rate))
+        out["sweep"].append(_serve(ctx, scenes, reqs, budget, 0, rate, tuning))
     # the same stream at the highest rate, one job at a time (no batching)
     reqs = make_requests(max(4, int(rates[-1] * window_s)))
-    out["batched_at_max_rate"] = _serve(ctx, scenes, reqs, budget, 0, rates[-1])
-    out["sequential_at_max_rate"] = _serve(ctx, scenes, reqs, budget, 1, rates[-1])
+    out["batched_at_max_rate"] = _serve(ctx, scenes, reqs, budget, 0, rates[-1], tuning)
+    out["sequential_at_max_rate"] = _serve(ctx, scenes, reqs, budget, 1, rates[-1], tuning)
     out["speedup_renders_s"] = out["batched_at_max_rate"]["renders_s"] / out["sequential_at_max_rate"]["renders_s"]
     # the same requests rendered the reference's way, frame by frame, one after
     # another, on scenes created beforehand for each (scene id, resolution)
@@ -146,6 +185,7 @@ def config5(ctx, rates=(10, 20, 50), window_s=3.0, pool=8, budget=150 * 10**9):
         if (si, cam["width"]) not in views:
             d = descs[si]
             views[(si, cam["width"])] = gr.Scene(ctx, sc.SceneDesc(d.meshes, d.materials, cam, d.env))
+            views[(si, cam["width"])].set_tuning(*tuning)
     t = time.perf_counter()
     for si, cam, spp, seed in reqs:
         target = views[(si, cam["width"])]

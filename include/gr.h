@@ -137,6 +137,31 @@ gr_status gr_bvh_export(gr_bvh* bvh, uint32_t* h_sorted_prim, uint32_t* h_sorted
 /* Selects the layout gr_trace uses (building it if needed; stream-ordered). */
 gr_status gr_bvh_set_layout(gr_bvh* bvh, int layout, void* stream);
 
+/* Traversal launch configuration for gr_trace: node layout, threads per block
+ * (64, 128, 256) and stack entries per thread kept in shared memory (8, 12,
+ * 16; deeper entries spill to local memory). The reference launches 32-thread
+ * blocks with a 64-entry local stack (pathtracer_kernel.h:192, :242). */
+typedef struct gr_trace_tuning {
+    int32_t layout;
+    int32_t block;
+    int32_t short_stack;
+} gr_trace_tuning;
+
+typedef struct gr_tuning_result {
+    gr_trace_tuning tuning;
+    float ms; /* best of two timed launches */
+} gr_tuning_result;
+
+gr_status gr_bvh_set_tuning(gr_bvh* bvh, const gr_trace_tuning* tuning);
+gr_status gr_bvh_get_tuning(const gr_bvh* bvh, gr_trace_tuning* tuning);
+
+/* Autotuner: times every configuration (3 layouts x 3 block sizes x 3 stack
+ * depths) on the caller's rays (device memory; d_hits is overwritten), keeps
+ * the fastest for this BVH, and reports up to max_results timings. All
+ * configurations return the same closest hits. Waits for the device. */
+gr_status gr_bvh_autotune(gr_bvh* bvh, const gr_ray* d_rays, uint64_t n, int any_hit, gr_hit* d_hits,
+                          gr_tuning_result* h_table, uint32_t max_results, uint32_t* n_results);
+
 /* Copies a 4-wide layout to host memory (128 or 64 bytes x max(n-1, 1); only
  * even-depth entries are nodes, the others are zero). Waits for the device. */
 gr_status gr_bvh_export_layout(gr_bvh* bvh, int layout, void* h_nodes);
@@ -261,6 +286,19 @@ uint64_t gr_scene_device_bytes(const gr_scene* scene);
 gr_status gr_scene_set_layout(gr_scene* scene, int layout);
 int gr_scene_layout(const gr_scene* scene);
 
+/* Autotuner for renders: times the probe render (e.g. a few samples per
+ * pixel) for every traversal configuration (layout x block x short-stack
+ * depth), then for wave sizes (queue capacity) of 1, 2, 4 and 8 Mi paths, and
+ * keeps the fastest as the scene's configuration and default wave size.
+ * Images do not depend on any of these. Clears the scene's accumulation. */
+gr_status gr_scene_autotune(gr_scene* scene, const gr_render_opts* probe, gr_trace_tuning* best,
+                            uint32_t* best_wave_paths);
+
+/* Sets / reads a scene's traversal configuration and default wave size
+ * (0 = library default), e.g. to reuse one autotuning result for many scenes. */
+gr_status gr_scene_set_tuning(gr_scene* scene, const gr_trace_tuning* tuning, uint32_t wave_paths);
+gr_status gr_scene_get_tuning(const gr_scene* scene, gr_trace_tuning* tuning, uint32_t* wave_paths);
+
 /* ---- scene files ---------------------------------------------------------------
  * Replaces load_scene / load_mitsuba_file / load_obj_file (src/renderer/loaders/
  * loader.h:11-29, mitsubaloader.cpp, objloader.cpp). The Mitsuba-XML subset
@@ -312,6 +350,8 @@ typedef struct gr_server_opts {
     uint32_t wave_paths;   /* paths per wave (0 = library default) */
     uint32_t max_active;   /* jobs in flight at most (0 = 1024) */
     int32_t layout;        /* node layout of every job (GR_LAYOUT_*); set on the scenes at submit */
+    int32_t block;         /* traversal threads per block (0 = 128; see gr_trace_tuning) */
+    int32_t short_stack;   /* shared-memory stack entries per thread (0 = 12) */
 } gr_server_opts;
 
 typedef struct gr_job_stats {
