@@ -336,6 +336,23 @@ def run_gpu(args):
         torch.distributed.destroy_process_group()
 
 
+def run_render_only(args):
+    import torch
+    import gr
+    from gr import scenes
+    from gr import workloads as wl
+
+    torch.cuda.set_device(0)
+    ctx = gr.Context(0)
+    desc, spp, depth = ((scenes.cornell_box(256, 256), 16, 8) if args.render_only == "config1" else
+                        (scenes.glossy_scene(), 64, 16))
+    names = {v: k for k, v in gr.LAYOUT_NAMES.items()}
+    lay = names["bvh2" if args.layout == "auto" else args.layout]
+    out = wl.plain_render(ctx, desc, args.spp or spp, depth, autotune=False,
+                          tuning=(lay, args.block, args.short_stack, 0))
+    print(json.dumps(dict(out, workload=args.render_only)), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -351,8 +368,14 @@ def main():
     ap.add_argument("--short-stack", type=int, default=12, choices=[8, 12, 16])
     ap.add_argument("--quick", action="store_true",
                     help="time the main query only (no extras, e2e or CPU baseline); for profiling")
+    ap.add_argument("--render-only", default=None, choices=["config1", "config3"],
+                    help="render one configuration with the given --layout/--block/--short-stack and --spp, print "
+                         "its figures and exit (profiling the integrator's kernels)")
+    ap.add_argument("--spp", type=int, default=0, help="samples per pixel of --render-only (0: the configuration's)")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.render_only:
+        run_render_only(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gpu(args)

@@ -656,6 +656,8 @@ cudaError_t run_wave(WavePool& pool, const JobDev* h_jobs, uint32_t njobs, uint3
     if (occ == 0 && (e = trace_occupancy(tune, &occ)) != cudaSuccess) return e;
     if (njobs == 0 || njobs > kMaxJobs || total_paths > pool.capacity || max_depth > (uint32_t)kMaxDepth)
         return cudaErrorInvalidValue;
+    for (uint32_t j = 0; j < njobs; ++j)  // traversal reads nodes with 32-byte loads
+        if (reinterpret_cast<uintptr_t>(h_jobs[j].sc.nodes) & 31) return cudaErrorMisalignedAddress;
     const Paths& ps = pool.ps;
     const int slot = pool.slot;
     pool.slot = (pool.slot + 1) % WavePool::kSlots;

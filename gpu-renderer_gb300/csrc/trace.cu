@@ -1,13 +1,15 @@
-// Closest-hit and any-hit traversal of the binary LBVH.
+// Closest-hit and any-hit traversal (binary, 4-wide and 8-bit quantised
+// 4-wide node layouts).
 //
 // Replaces trace_kernel / trace_shadow_kernel (src/renderer/pathtracer_kernel.h
 // :175-308). Differences by design:
-//   - persistent warps: a fixed grid of warps pulls 32 rays at a time from a
-//     global counter until the queue is drained;
-//   - child boxes live in the parent node and are fetched as 16-byte vector
-//     loads; both children are tested at once and the nearer is visited first;
-//   - a short per-thread stack in shared memory, spilling to local memory only
-//     past kShortStack entries;
+//   - persistent warps with dynamic refill: a fixed grid of warps pulls rays
+//     from a global counter, and a warp refills its idle lanes whenever at
+//     least kRefillLanes of them have finished, until the queue is drained;
+//   - child boxes live in the parent node and are fetched as 32-byte vector
+//     loads; all children are tested at once and the nearest is visited first;
+//   - a short per-thread stack in shared memory (8, 12 or 16 entries, chosen by
+//     the autotuner with the block size), spilling to local memory past it;
 //   - the FP32 watertight triangle test (Woop, Benthin, Wald, JCGT 2013) on
 //     leaf-order triangle copies instead of the reference's FP64
 //     Moller-Trumbore through 408-byte Triangle records.
@@ -91,6 +93,7 @@ cudaError_t trace_launch(const BvhDevice& bvh, const void* nodes, const TraceTun
                          int num_sms, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     if (!tuning_valid(tune)) return cudaErrorInvalidValue;
+    if (reinterpret_cast<uintptr_t>(nodes) & 31) return cudaErrorMisalignedAddress;  // 32-byte node loads
     cudaError_t e = cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), s);
     if (e != cudaSuccess) return e;
     const float4* r = reinterpret_cast<const float4*>(d_rays);

@@ -102,6 +102,19 @@ __device__ __forceinline__ bool tri_test(const RayW& p, const float4 a, const fl
     return true;
 }
 
+// 32-byte read-only load (ld.global.nc.v8, sm_100 and later): one L1 sector
+// per lane per request instead of two 16-byte requests. `p` must be 32-byte
+// aligned; node arrays are separate allocations with 64- or 128-byte records.
+__device__ __forceinline__ void ldg32B(const void* p, float4& a, float4& b) {
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+        : "l"(p));
+}
+
+__device__ __forceinline__ int4 as_int4(const float4 f) {
+    return make_int4(__float_as_int(f.x), __float_as_int(f.y), __float_as_int(f.z), __float_as_int(f.w));
+}
+
 __device__ __forceinline__ uint32_t lanemask_lt() {
     uint32_t m;
     asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
@@ -178,8 +191,10 @@ __device__ __forceinline__ bool pop(Lane& L, const int2* s_stack, const int2* l_
 template <bool ANY, int SSTACK>
 __device__ __forceinline__ bool trace_step2(Lane& L, int2* s_stack, int2* l_stack, uint32_t* err) {
     const float4* q = reinterpret_cast<const float4*>(static_cast<const Node*>(L.nodes) + L.node);
-    const float4 q0 = __ldg(q), q1 = __ldg(q + 1), q2 = __ldg(q + 2);
-    const int4 q3 = __ldg(reinterpret_cast<const int4*>(q + 3));
+    float4 q0, q1, q2, q3f;
+    ldg32B(q, q0, q1);
+    ldg32B(q + 2, q2, q3f);
+    const int4 q3 = as_int4(q3f);
     float tn0, tn1;
     const bool h0 = slab(L.p, q0.x, q0.y, q0.z, q0.w, q2.x, q2.y, L.best_t, tn0);
     const bool h1 = slab(L.p, q1.x, q1.y, q1.z, q1.w, q2.z, q2.w, L.best_t, tn1);
@@ -224,9 +239,11 @@ __device__ __forceinline__ bool trace_step4(Lane& L, int2* s_stack, int2* l_stac
     int32_t c[4];
     if (QUANT) {
         const Node4Q* nd = static_cast<const Node4Q*>(L.nodes) + L.node;
-        const float4 q0 = __ldg(&nd->q0);
-        const uint4 q1 = __ldg(&nd->q1), q2 = __ldg(&nd->q2);
-        const int4 ch = __ldg(&nd->child);
+        float4 q0, q1f, q2f, chf;
+        ldg32B(&nd->q0, q0, q1f);
+        ldg32B(&nd->q2, q2f, chf);
+        const int4 q1i = as_int4(q1f), q2i = as_int4(q2f), ch = as_int4(chf);
+        const uint4 q1 = make_uint4(q1i.x, q1i.y, q1i.z, q1i.w), q2 = make_uint4(q2i.x, q2i.y, q2i.z, q2i.w);
         const uint32_t meta = __float_as_uint(q0.w);
         const float sx = __uint_as_float((meta & 0xFFu) << 23);
         const float sy = __uint_as_float(((meta >> 8) & 0xFFu) << 23);
@@ -244,10 +261,13 @@ __device__ __forceinline__ bool trace_step4(Lane& L, int2* s_stack, int2* l_stac
         }
     } else {
         const Node4* nd = static_cast<const Node4*>(L.nodes) + L.node;
-        const float4 lox = __ldg(&nd->lox), hix = __ldg(&nd->hix), loy = __ldg(&nd->loy), hiy = __ldg(&nd->hiy);
-        const float4 loz = __ldg(&nd->loz), hiz = __ldg(&nd->hiz);
-        const int4 ch = __ldg(&nd->child);
-        const uint32_t mask = __ldg(&nd->meta.x);
+        float4 lox, hix, loy, hiy, loz, hiz, chf, metaf;
+        ldg32B(&nd->lox, lox, hix);
+        ldg32B(&nd->loy, loy, hiy);
+        ldg32B(&nd->loz, loz, hiz);
+        ldg32B(&nd->child, chf, metaf);
+        const int4 ch = as_int4(chf);
+        const uint32_t mask = __float_as_uint(metaf.x);
         c[0] = ch.x; c[1] = ch.y; c[2] = ch.z; c[3] = ch.w;
         const float lx[4] = {lox.x, lox.y, lox.z, lox.w}, hx[4] = {hix.x, hix.y, hix.z, hix.w};
         const float ly[4] = {loy.x, loy.y, loy.z, loy.w}, hy[4] = {hiy.x, hiy.y, hiy.z, hiy.w};

@@ -39,13 +39,15 @@ def tuning_args(tune, wave=0):
     return (_names()[tune["layout"]], tune["block"], tune["short_stack"], wave)
 
 
-def plain_render(ctx, desc, spp, depth, rr=3, autotune=True):
+def plain_render(ctx, desc, spp, depth, rr=3, autotune=True, tuning=None):
     """One scene rendered by gr_render; with autotune the scene's traversal
-    configuration and wave size come from gr_scene_autotune (1-spp probes)."""
+    configuration and wave size come from gr_scene_autotune (1-spp probes),
+    else from `tuning` = (layout, block, short_stack, wave_paths) if given."""
     s = gr.Scene(ctx, desc)
-    tune = wave = None
+    if tuning is not None:
+        s.set_tuning(*tuning)
     if autotune:
-        tune, wave = s.autotune(spp=1, max_depth=depth, rr_depth=rr)
+        s.autotune(spp=1, max_depth=depth, rr_depth=rr)
     dt, st = _timed_render(s, spp, depth, rr)
     npix = desc.camera["width"] * desc.camera["height"]
     out = {"ms": dt * 1e3, "samples_per_s": npix * spp / dt, "mrays_s": (st.closest_rays + st.shadow_rays) / dt / 1e6,
