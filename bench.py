@@ -362,7 +362,7 @@ def main():
     ap.add_argument("--tris", type=int, default=N_TRIS, help="triangle count (profiling cases)")
     ap.add_argument("--rays", type=int, default=N_RAYS, help="ray count (profiling cases)")
     ap.add_argument("--no-render", action="store_true", help="skip the render-configuration extras")
-    ap.add_argument("--layout", default="auto", choices=["auto", "bvh2", "bvh4", "bvh4_q8"],
+    ap.add_argument("--layout", default="auto", choices=["auto", "bvh2", "bvh4", "bvh4_q8", "bvh8_q8"],
                     help="node layout of the timed traversal (auto: autotune layout, block and short stack)")
     ap.add_argument("--block", type=int, default=128, choices=[64, 128, 256])
     ap.add_argument("--short-stack", type=int, default=12, choices=[8, 12, 16])

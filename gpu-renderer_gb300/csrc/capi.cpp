@@ -88,6 +88,44 @@ gr::BvhDevice device_view(gr_bvh* bvh) {
     return v;
 }
 
+// Builds the derived node layout `layout` if it is not current (binary nodes
+// are always built). The 8-wide build waits for `s`.
+cudaError_t ensure_layout(gr_bvh* bvh, int layout, cudaStream_t s) {
+    if (!bvh->built || layout == gr::kLayoutBvh2) return cudaSuccess;
+    if (layout == gr::kLayoutBvh8Q8) {
+        if (bvh->built8) return cudaSuccess;
+        const cudaError_t e = gr::bvh8_build(bvh->buf, bvh->n, s);
+        if (e == cudaSuccess) bvh->built8 = true;
+        return e;
+    }
+    bool& done = layout == gr::kLayoutBvh4 ? bvh->built4 : bvh->built4q;
+    if (done) return cudaSuccess;
+    const cudaError_t e = gr::bvh4_build(bvh->buf, bvh->n, layout, s);
+    if (e == cudaSuccess) done = true;
+    return e;
+}
+
+}  // namespace
+
+namespace gr {
+
+const void* layout_nodes(const gr_bvh* bvh, int layout) {
+    switch (layout) {
+        case kLayoutBvh4: return bvh->buf.nodes4.p;
+        case kLayoutBvh4Q8: return bvh->buf.nodes4q.p;
+        case kLayoutBvh8Q8: return bvh->buf.nodes8.p;
+        default: return bvh->buf.nodes.p;
+    }
+}
+
+const Tri* layout_tris(const gr_bvh* bvh, int layout) {
+    return (const Tri*)(layout == kLayoutBvh8Q8 ? bvh->buf.tris8.p : bvh->buf.tris.p);
+}
+
+}  // namespace gr
+
+namespace {
+
 gr_status read_meta(gr_bvh* bvh, gr::BvhMeta* m) {
     GR_CUDA(bvh->ctx, cudaMemcpy(m, bvh->buf.meta.p, sizeof(gr::BvhMeta), cudaMemcpyDeviceToHost));
     return GR_OK;
@@ -174,14 +212,12 @@ gr_status gr_bvh_build(gr_bvh* bvh, const float* d_verts, uint32_t n, void* stre
     if (n > 0 && !d_verts) return fail(bvh->ctx, GR_ERR_INVALID, "null vertex pointer");
     GR_CUDA(bvh->ctx, cudaSetDevice(bvh->ctx->device));
     bvh->built = false;
-    bvh->built4 = bvh->built4q = false;
+    bvh->built4 = bvh->built4q = bvh->built8 = false;
     GR_CUDA(bvh->ctx, gr::lbvh_build(bvh->buf, d_verts, n, bvh->ctx->num_sms, as_stream(stream)));
     bvh->n = n;
     bvh->built = true;
-    if (bvh->layout != 0) {  // keep the requested traversal layout current
-        GR_CUDA(bvh->ctx, gr::bvh4_build(bvh->buf, n, bvh->layout, as_stream(stream)));
-        (bvh->layout == gr::kLayoutBvh4 ? bvh->built4 : bvh->built4q) = true;
-    }
+    // keep the requested traversal layout current
+    GR_CUDA(bvh->ctx, ensure_layout(bvh, bvh->layout, as_stream(stream)));
     return GR_OK;
 }
 
@@ -239,15 +275,14 @@ gr_status gr_trace(gr_bvh* bvh, const gr_ray* d_rays, uint64_t n, gr_hit* d_hits
     GR_CUDA(ctx, cudaSetDevice(ctx->device));
     unsigned long long* counter = (unsigned long long*)ctx->counter.p;
     uint32_t* err = (uint32_t*)((char*)ctx->counter.p + 64);
-    const void* nodes = bvh->layout == gr::kLayoutBvh4 ? bvh->buf.nodes4.p
-                        : bvh->layout == gr::kLayoutBvh4Q8 ? bvh->buf.nodes4q.p
-                                                             : bvh->buf.nodes.p;
     gr::TraceTuning tune;
     tune.layout = bvh->layout;
     tune.block = bvh->block;
     tune.sstack = bvh->sstack;
-    GR_CUDA(ctx, gr::trace_launch(device_view(bvh), nodes, tune, d_rays, n, d_hits, any_hit, counter, err,
-                                  ctx->num_sms, as_stream(stream)));
+    gr::BvhDevice view = device_view(bvh);
+    view.tris = gr::layout_tris(bvh, bvh->layout);
+    GR_CUDA(ctx, gr::trace_launch(view, gr::layout_nodes(bvh, bvh->layout), tune, d_rays, n, d_hits, any_hit, counter,
+                                  err, ctx->num_sms, as_stream(stream)));
     return GR_OK;
 }
 
@@ -296,31 +331,52 @@ extern "C" gr_status gr_bvh_build_noalloc(gr_ctx* ctx, const float* d_verts, uin
 }
 
 extern "C" gr_status gr_bvh_set_layout(gr_bvh* bvh, int layout, void* stream) {
-    if (!bvh || layout < 0 || layout > 2) return GR_ERR_INVALID;
+    if (!bvh || layout < 0 || layout >= gr::kNumLayouts) return GR_ERR_INVALID;
     GR_CUDA(bvh->ctx, cudaSetDevice(bvh->ctx->device));
-    if (bvh->built && layout != 0) {
-        bool& done = layout == gr::kLayoutBvh4 ? bvh->built4 : bvh->built4q;
-        if (!done) {
-            GR_CUDA(bvh->ctx, gr::bvh4_build(bvh->buf, bvh->n, layout, as_stream(stream)));
-            done = true;
-        }
-    }
+    GR_CUDA(bvh->ctx, ensure_layout(bvh, layout, as_stream(stream)));
     bvh->layout = layout;
     return GR_OK;
 }
 
+extern "C" gr_status gr_bvh_layout_size(gr_bvh* bvh, int layout, uint64_t* node_bytes, uint64_t* tri_bytes) {
+    if (!bvh || !bvh->built || layout < 0 || layout >= gr::kNumLayouts) return GR_ERR_INVALID;
+    GR_CUDA(bvh->ctx, cudaSetDevice(bvh->ctx->device));
+    GR_CUDA(bvh->ctx, ensure_layout(bvh, layout, bvh->ctx->stream));
+    const uint64_t count = bvh->n == 0 ? 0 : (bvh->n > 1 ? bvh->n - 1 : 1);
+    uint64_t nb = 0, tb = sizeof(gr::Tri) * (uint64_t)bvh->n;
+    switch (layout) {
+        case gr::kLayoutBvh4: nb = count * sizeof(gr::Node4); break;
+        case gr::kLayoutBvh4Q8: nb = count * sizeof(gr::Node4Q); break;
+        case gr::kLayoutBvh8Q8:
+            nb = (uint64_t)bvh->buf.count8 * sizeof(gr::Node8Q);
+            tb = (uint64_t)bvh->buf.tris8_count * sizeof(gr::Tri);
+            break;
+        default: nb = count * sizeof(gr::Node); break;
+    }
+    if (node_bytes) *node_bytes = nb;
+    if (tri_bytes) *tri_bytes = tb;
+    return GR_OK;
+}
+
 extern "C" gr_status gr_bvh_export_layout(gr_bvh* bvh, int layout, void* h_nodes) {
-    if (!bvh || !bvh->built || layout < 1 || layout > 2 || !h_nodes) return GR_ERR_INVALID;
-    const int keep = bvh->layout;
-    gr_status st = gr_bvh_set_layout(bvh, layout, bvh->ctx->stream);
-    bvh->layout = keep;
+    if (!bvh || !bvh->built || layout < 1 || layout >= gr::kNumLayouts || !h_nodes) return GR_ERR_INVALID;
+    uint64_t nb = 0;
+    gr_status st = gr_bvh_layout_size(bvh, layout, &nb, nullptr);
     if (st != GR_OK) return st;
     GR_CUDA(bvh->ctx, cudaStreamSynchronize(bvh->ctx->stream));
     GR_CUDA(bvh->ctx, cudaDeviceSynchronize());
-    const size_t count = bvh->n > 1 ? bvh->n - 1 : 1;
-    if (bvh->n == 0) return GR_OK;
-    const gr::DevBuf& src = layout == gr::kLayoutBvh4 ? bvh->buf.nodes4 : bvh->buf.nodes4q;
-    GR_CUDA(bvh->ctx, cudaMemcpy(h_nodes, src.p, count * (layout == gr::kLayoutBvh4 ? 128 : 64), cudaMemcpyDeviceToHost));
+    if (nb) GR_CUDA(bvh->ctx, cudaMemcpy(h_nodes, gr::layout_nodes(bvh, layout), nb, cudaMemcpyDeviceToHost));
+    return GR_OK;
+}
+
+extern "C" gr_status gr_bvh_export_layout_tris(gr_bvh* bvh, int layout, float* h_tris) {
+    if (!bvh || !bvh->built || layout < 0 || layout >= gr::kNumLayouts || !h_tris) return GR_ERR_INVALID;
+    uint64_t tb = 0;
+    gr_status st = gr_bvh_layout_size(bvh, layout, nullptr, &tb);
+    if (st != GR_OK) return st;
+    GR_CUDA(bvh->ctx, cudaStreamSynchronize(bvh->ctx->stream));
+    GR_CUDA(bvh->ctx, cudaDeviceSynchronize());
+    if (tb) GR_CUDA(bvh->ctx, cudaMemcpy(h_tris, gr::layout_tris(bvh, layout), tb, cudaMemcpyDeviceToHost));
     return GR_OK;
 }
 
@@ -355,7 +411,7 @@ extern "C" gr_status gr_bvh_autotune(gr_bvh* bvh, const gr_ray* d_rays, uint64_t
     cudaEvent_t e0, e1;
     GR_CUDA(ctx, cudaEventCreate(&e0));
     GR_CUDA(ctx, cudaEventCreate(&e1));
-    const int layouts[] = {0, 1, 2}, blocks[] = {64, 128, 256}, stacks[] = {8, 12, 16};
+    const int layouts[] = {0, 1, 2, 3}, blocks[] = {64, 128, 256}, stacks[] = {8, 12, 16};
     gr_trace_tuning best{bvh->layout, bvh->block, bvh->sstack};
     float best_ms = 1e30f;
     uint32_t rows = 0;

@@ -64,7 +64,31 @@ struct Node4Q {
 };
 static_assert(sizeof(Node4Q) == 64, "node4q layout");
 
-enum Layout : int { kLayoutBvh2 = 0, kLayoutBvh4 = 1, kLayoutBvh4Q8 = 2 };
+// 8-wide node with 8-bit quantised child boxes, 96 bytes (three 32-byte
+// loads). Slots are assigned so that, for a ray whose direction has sign bits
+// oct (bit a set = negative along axis a), visiting inner children in order of
+// (slot ^ oct) is near to far. Inner children are stored contiguously from
+// child_base in slot order, leaf triangles contiguously from tri_base (in the
+// layout's own triangle array) in slot order.
+//   meta:  bits 0-7 / 8-15 / 16-23 biased exponents (x, y, z), bits 24-31
+//          inner-child mask (slot k holds an inner node)
+//   valid: bits 0-7 slot k holds a child
+//   q:     per axis two words of 8 bytes (byte k = slot k): lo.x, hi.x, lo.y,
+//          hi.y, lo.z, hi.z; a plane decodes as fma(q, 2^e, origin)
+struct Node8Q {
+    float ox, oy, oz;
+    uint32_t meta;
+    uint32_t child_base;
+    uint32_t tri_base;
+    uint32_t valid;
+    uint32_t pad0;
+    uint32_t q[12];
+    uint32_t pad1[4];
+};
+static_assert(sizeof(Node8Q) == 96, "node8q layout");
+
+enum Layout : int { kLayoutBvh2 = 0, kLayoutBvh4 = 1, kLayoutBvh4Q8 = 2, kLayoutBvh8Q8 = 3 };
+constexpr int kNumLayouts = 4;
 
 // Traversal launch configuration chosen by the autotuner (or by the caller).
 struct TraceTuning {
@@ -106,6 +130,10 @@ struct BvhDevice {
 struct BvhBuffers {
     DevBuf nodes, tris, code, prim;  // outputs kept for traversal / export
     DevBuf nodes4, nodes4q;          // 4-wide layouts (built on request), indexed like `nodes`
+    DevBuf nodes8, tris8;            // 8-wide layout (built on request): nodes from 0 (root), leaf-order triangles
+    DevBuf scratch8;                 // 8-wide build state
+    uint32_t count8 = 0;             // 8-wide nodes
+    uint32_t tris8_count = 0;        // triangles in tris8
     DevBuf scratch;                  // transient build state
     DevBuf meta;                     // small device header (root, unique count, error word)
 };
@@ -131,6 +159,8 @@ cudaError_t lbvh_build_static(const float* d_verts, uint32_t n, Node* nodes, Tri
 // bvh4.cu: 4-wide layouts collapsed from the binary nodes (every node at
 // even depth becomes a 4-wide node at the same index)
 cudaError_t bvh4_build(BvhBuffers& b, uint32_t n, int layout, cudaStream_t s);
+// bvh8.cu: level by level, one host read of the level size per level (waits for `s`)
+cudaError_t bvh8_build(BvhBuffers& b, uint32_t n, cudaStream_t s);
 
 // trace.cu
 cudaError_t trace_launch(const BvhDevice& bvh, const void* nodes, const TraceTuning& tune, const gr_ray* d_rays,
@@ -162,6 +192,13 @@ void ctx_release(gr_ctx* ctx);
 void context_free(gr_ctx* ctx);
 }  // namespace gr
 
+struct gr_bvh;
+namespace gr {
+// capi.cpp: the node and triangle arrays a layout's traversal reads.
+const void* layout_nodes(const gr_bvh* bvh, int layout);
+const Tri* layout_tris(const gr_bvh* bvh, int layout);
+}  // namespace gr
+
 struct gr_bvh {
     gr_ctx* ctx = nullptr;
     // not copyable: owns device memory
@@ -170,6 +207,6 @@ struct gr_bvh {
     int layout = 0;       // traversal layout gr_trace uses
     int block = 128;      // gr_trace launch shape (autotuned or set)
     int sstack = 12;
-    bool built4 = false, built4q = false;
+    bool built4 = false, built4q = false, built8 = false;
     gr::BvhBuffers buf;
 };

@@ -506,6 +506,7 @@ cudaError_t issue_wave_s(const Paths& ps, uint32_t steps, int tgrid, const Trace
 cudaError_t issue_wave(const Paths& ps, uint32_t steps, int tgrid, int sgrid, cudaStream_t s, const TraceTuning& t) {
     if (t.layout == kLayoutBvh4) return issue_wave_s<kLayoutBvh4>(ps, steps, tgrid, t, sgrid, s);
     if (t.layout == kLayoutBvh4Q8) return issue_wave_s<kLayoutBvh4Q8>(ps, steps, tgrid, t, sgrid, s);
+    if (t.layout == kLayoutBvh8Q8) return issue_wave_s<kLayoutBvh8Q8>(ps, steps, tgrid, t, sgrid, s);
     return issue_wave_s<kLayoutBvh2>(ps, steps, tgrid, t, sgrid, s);
 }
 
@@ -518,6 +519,7 @@ cudaError_t trace_occupancy(const TraceTuning& t, int* occ) {
     GR_PICK(kLayoutBvh2, 8) GR_PICK(kLayoutBvh2, 12) GR_PICK(kLayoutBvh2, 16)
     GR_PICK(kLayoutBvh4, 8) GR_PICK(kLayoutBvh4, 12) GR_PICK(kLayoutBvh4, 16)
     GR_PICK(kLayoutBvh4Q8, 8) GR_PICK(kLayoutBvh4Q8, 12) GR_PICK(kLayoutBvh4Q8, 16)
+    GR_PICK(kLayoutBvh8Q8, 8) GR_PICK(kLayoutBvh8Q8, 12) GR_PICK(kLayoutBvh8Q8, 16)
 #undef GR_PICK
     if (!fn) return cudaErrorInvalidValue;
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, fn, t.block, smem);
@@ -649,7 +651,7 @@ cudaError_t run_wave(WavePool& pool, const JobDev* h_jobs, uint32_t njobs, uint3
                      uint32_t max_depth, int num_sms, cudaStream_t s, bool use_graph, const TraceTuning& tune) {
     cudaError_t e;
     if (!tuning_valid(tune)) return cudaErrorInvalidValue;
-    static int occ_cache[3][3][3] = {};
+    static int occ_cache[kNumLayouts][3][3] = {};
     const int bi = tune.block == 64 ? 0 : (tune.block == 128 ? 1 : 2);
     const int si = tune.sstack == 8 ? 0 : (tune.sstack == 12 ? 1 : 2);
     int& occ = occ_cache[tune.layout][bi][si];

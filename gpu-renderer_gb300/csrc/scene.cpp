@@ -75,10 +75,8 @@ gr::SceneDev gr::scene_view(gr_scene* sc, int layout) {
     d.lights = (const uint32_t*)sc->lights.p;
     d.num_lights = sc->num_lights;
     d.num_tris = sc->num_tris;
-    d.nodes = layout == gr::kLayoutBvh4 ? sc->bvh->buf.nodes4.p
-              : layout == gr::kLayoutBvh4Q8 ? sc->bvh->buf.nodes4q.p
-                                            : sc->bvh->buf.nodes.p;
-    d.tris = (const gr::Tri*)sc->bvh->buf.tris.p;
+    d.nodes = gr::layout_nodes(sc->bvh, layout);
+    d.tris = gr::layout_tris(sc->bvh, layout);
     d.meta = (const gr::BvhMeta*)sc->bvh->buf.meta.p;
     d.cam = sc->cam;
     d.env_r = sc->env[0];
@@ -341,7 +339,7 @@ extern "C" gr_status gr_scene_autotune(gr_scene* sc, const gr_render_opts* probe
         *ms = st.ms;
         return r;
     };
-    const int layouts[] = {0, 1, 2}, blocks[] = {64, 128, 256}, stacks[] = {8, 12, 16};
+    const int layouts[] = {0, 1, 2, 3}, blocks[] = {64, 128, 256}, stacks[] = {8, 12, 16};
     gr_trace_tuning best{sc->bvh->layout, sc->bvh->block, sc->bvh->sstack};
     double best_ms = 1e300;
     for (int lay : layouts)

@@ -44,8 +44,8 @@ extern "C" uint64_t gr_scene_device_bytes(const gr_scene* sc) {
                  sc->fb.bytes + sc->fb_count.bytes + sc->pool.mem.bytes;
     if (sc->bvh) {
         const gr::BvhBuffers& bb = sc->bvh->buf;
-        b += bb.nodes.bytes + bb.nodes4.bytes + bb.nodes4q.bytes + bb.tris.bytes + bb.code.bytes + bb.prim.bytes +
-             bb.scratch.bytes + bb.meta.bytes;
+        b += bb.nodes.bytes + bb.nodes4.bytes + bb.nodes4q.bytes + bb.nodes8.bytes + bb.tris8.bytes + bb.tris.bytes +
+             bb.code.bytes + bb.prim.bytes + bb.scratch.bytes + bb.meta.bytes;
     }
     return b;
 }

@@ -1,5 +1,5 @@
-// Closest-hit and any-hit traversal (binary, 4-wide and 8-bit quantised
-// 4-wide node layouts).
+// Closest-hit and any-hit traversal (binary, 4-wide FP32, 4-wide and 8-wide
+// 8-bit quantised node layouts).
 //
 // Replaces trace_kernel / trace_shadow_kernel (src/renderer/pathtracer_kernel.h
 // :175-308). Differences by design:
@@ -84,7 +84,7 @@ cudaError_t launch_s(const BvhDevice& bvh, const void* nodes, const TraceTuning&
 }  // namespace
 
 bool tuning_valid(const TraceTuning& t) {
-    return t.layout >= 0 && t.layout <= 2 && (t.block == 64 || t.block == 128 || t.block == 256) &&
+    return t.layout >= 0 && t.layout < kNumLayouts && (t.block == 64 || t.block == 128 || t.block == 256) &&
            (t.sstack == 8 || t.sstack == 12 || t.sstack == 16);
 }
 
@@ -105,6 +105,8 @@ cudaError_t trace_launch(const BvhDevice& bvh, const void* nodes, const TraceTun
         case 3: return launch_s<true, kLayoutBvh4>(bvh, nodes, tune, r, n, h, d_counter, d_err, num_sms, s);
         case 4: return launch_s<false, kLayoutBvh4Q8>(bvh, nodes, tune, r, n, h, d_counter, d_err, num_sms, s);
         case 5: return launch_s<true, kLayoutBvh4Q8>(bvh, nodes, tune, r, n, h, d_counter, d_err, num_sms, s);
+        case 6: return launch_s<false, kLayoutBvh8Q8>(bvh, nodes, tune, r, n, h, d_counter, d_err, num_sms, s);
+        case 7: return launch_s<true, kLayoutBvh8Q8>(bvh, nodes, tune, r, n, h, d_counter, d_err, num_sms, s);
         default: return cudaErrorInvalidValue;
     }
 }

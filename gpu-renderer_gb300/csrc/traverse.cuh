@@ -22,7 +22,6 @@ struct RayW {
     float sx, sy, sz;
     int kx, ky, kz;
     float ix, iy, iz;     // reciprocal direction (near-zero components clamped)
-    float nox, noy, noz;  // -origin * reciprocal direction
 };
 
 __device__ __forceinline__ float pick(float x, float y, float z, int k) { return k == 0 ? x : (k == 1 ? y : z); }
@@ -51,22 +50,29 @@ __device__ __forceinline__ RayW prepare(const float4 r0, const float4 r1) {
     const float cy = fabsf(dy) > eps ? dy : copysignf(eps, dy);
     const float cz = fabsf(dz) > eps ? dz : copysignf(eps, dz);
     p.ix = __frcp_rn(cx); p.iy = __frcp_rn(cy); p.iz = __frcp_rn(cz);
-    p.nox = -__fmul_rn(p.ox, p.ix); p.noy = -__fmul_rn(p.oy, p.iy); p.noz = -__fmul_rn(p.oz, p.iz);
     return p;
 }
 
 // Relative slack on every cull: a box (or a deferred stack entry) is kept
-// while its entry distance is within (1 + 2^-20) of the exit / closest-hit
-// distance, so a triangle whose hit distance rounds an ulp below its box's
-// entry distance is still reached and the closest hit does not depend on the
-// order boxes are visited in.
-constexpr float kCullSlack = 1.00000095367431640625f;  // 1 + 2^-20
+// while its entry distance is within (1 + 2^-16) of the exit / closest-hit
+// distance. A plane's distance is (plane - o) * (1/d), three roundings and so
+// within 3 ulps of the exact value relative to itself, so a box that contains
+// a hit point is never culled by rounding, and a triangle whose computed hit
+// distance is a few ulps below its box's entry distance is still reached: the
+// closest hit does not depend on the order boxes are visited in or on the
+// node layout. (A form like fma(plane, 1/d, -o/d) has an absolute error of
+// order ulp(o/d), which culled grazing rays that start on a surface.)
+constexpr float kCullSlack = 1.0000152587890625f;  // 1 + 2^-16
+
+__device__ __forceinline__ float plane_t(float plane, float o, float inv) {
+    return __fmul_rn(__fsub_rn(plane, o), inv);
+}
 
 __device__ __forceinline__ bool slab(const RayW& p, float lox, float hix, float loy, float hiy, float loz, float hiz,
                                      float tbest, float& tn) {
-    const float x0 = __fmaf_rn(lox, p.ix, p.nox), x1 = __fmaf_rn(hix, p.ix, p.nox);
-    const float y0 = __fmaf_rn(loy, p.iy, p.noy), y1 = __fmaf_rn(hiy, p.iy, p.noy);
-    const float z0 = __fmaf_rn(loz, p.iz, p.noz), z1 = __fmaf_rn(hiz, p.iz, p.noz);
+    const float x0 = plane_t(lox, p.ox, p.ix), x1 = plane_t(hix, p.ox, p.ix);
+    const float y0 = plane_t(loy, p.oy, p.iy), y1 = plane_t(hiy, p.oy, p.iy);
+    const float z0 = plane_t(loz, p.oz, p.iz), z1 = plane_t(hiz, p.oz, p.iz);
     const float tnear = fmaxf(fmaxf(fminf(x0, x1), fminf(y0, y1)), fmaxf(fminf(z0, z1), p.tmin));
     const float tfar = fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fminf(fmaxf(z0, z1), tbest));
     tn = tnear;
@@ -326,9 +332,117 @@ __device__ __forceinline__ bool trace_step4(Lane& L, int2* s_stack, int2* l_stac
     return false;
 }
 
+// ---- 8-wide quantised nodes ----------------------------------------------------
+
+// Byte k of w as a float, exactly: the byte becomes the low mantissa bits of
+// 2^23 (one byte permute), then 2^23 is subtracted.
+__device__ __forceinline__ float qbyte(uint32_t w, int k) {
+    return __fsub_rn(__uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540u | (uint32_t)k)), 8388608.0f);
+}
+
+template <int SSTACK>
+__device__ __forceinline__ int2 stack_at(int i, const int2* s_stack, const int2* l_stack) {
+    return i < SSTACK ? s_stack[i * blockDim.x + threadIdx.x] : l_stack[i - SSTACK];
+}
+
+template <int SSTACK>
+__device__ __forceinline__ void stack_put(int i, int2 v, int2* s_stack, int2* l_stack) {
+    if (i < SSTACK) s_stack[i * blockDim.x + threadIdx.x] = v;
+    else l_stack[i - SSTACK] = v;
+}
+
+// Leaf triangle `idx` of the layout's own triangle array.
+template <bool ANY>
+__device__ __forceinline__ bool leaf_at(Lane& L, uint32_t idx) { return leaf<ANY>(L, ~(int32_t)idx); }
+
+// One 8-wide node. Each plane is decoded as fma(q, 2^e, origin), exactly as
+// the builder quantised it, then measured like an FP32 plane; the near plane
+// of an axis is lo when d >= 0, else hi. Hit leaf
+// triangles are tested in slot order; hit inner children are ranked by
+// slot ^ octant and the lowest rank is visited next. The remaining inner hits
+// stay on the stack as one group entry (child_base, inner mask | hits << 8),
+// taken one child at a time. Returns true when the ray is finished.
+template <bool ANY, int SSTACK>
+__device__ __forceinline__ bool trace_step8(Lane& L, int2* s_stack, int2* l_stack, uint32_t* err) {
+    const float4* q = reinterpret_cast<const float4*>(static_cast<const Node8Q*>(L.nodes) + L.node);
+    float4 h0, h1, b0, b1, c0, c1;
+    ldg32B(q, h0, h1);
+    ldg32B(q + 2, b0, b1);
+    ldg32B(q + 4, c0, c1);
+    const uint32_t meta = __float_as_uint(h0.w);
+    const uint32_t child_base = __float_as_uint(h1.x), tri_base = __float_as_uint(h1.y);
+    const uint32_t valid = __float_as_uint(h1.z), imask = meta >> 24;
+    const uint32_t sx = __float_as_uint(L.p.ix) >> 31, sy = __float_as_uint(L.p.iy) >> 31;
+    const uint32_t sz = __float_as_uint(L.p.iz) >> 31;
+    const uint32_t oct = sx | (sy << 1) | (sz << 2);
+    const float scx = __uint_as_float((meta & 0xFFu) << 23);
+    const float scy = __uint_as_float(((meta >> 8) & 0xFFu) << 23);
+    const float scz = __uint_as_float(((meta >> 16) & 0xFFu) << 23);
+    // words: b0 = (lo.x[0-3], lo.x[4-7], hi.x[0-3], hi.x[4-7]), b1 the same for y, c0 for z
+    const uint32_t lx0 = __float_as_uint(b0.x), lx1 = __float_as_uint(b0.y);
+    const uint32_t hx0 = __float_as_uint(b0.z), hx1 = __float_as_uint(b0.w);
+    const uint32_t ly0 = __float_as_uint(b1.x), ly1 = __float_as_uint(b1.y);
+    const uint32_t hy0 = __float_as_uint(b1.z), hy1 = __float_as_uint(b1.w);
+    const uint32_t lz0 = __float_as_uint(c0.x), lz1 = __float_as_uint(c0.y);
+    const uint32_t hz0 = __float_as_uint(c0.z), hz1 = __float_as_uint(c0.w);
+    const uint32_t nx0 = sx ? hx0 : lx0, nx1 = sx ? hx1 : lx1, fx0 = sx ? lx0 : hx0, fx1 = sx ? lx1 : hx1;
+    const uint32_t ny0 = sy ? hy0 : ly0, ny1 = sy ? hy1 : ly1, fy0 = sy ? ly0 : hy0, fy1 = sy ? ly1 : hy1;
+    const uint32_t nz0 = sz ? hz0 : lz0, nz1 = sz ? hz1 : lz1, fz0 = sz ? lz0 : hz0, fz1 = sz ? lz1 : hz1;
+    uint32_t ihits = 0, thits = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const int b = k & 3;
+        const float tnx = plane_t(__fmaf_rn(qbyte(k < 4 ? nx0 : nx1, b), scx, h0.x), L.p.ox, L.p.ix);
+        const float tfx = plane_t(__fmaf_rn(qbyte(k < 4 ? fx0 : fx1, b), scx, h0.x), L.p.ox, L.p.ix);
+        const float tny = plane_t(__fmaf_rn(qbyte(k < 4 ? ny0 : ny1, b), scy, h0.y), L.p.oy, L.p.iy);
+        const float tfy = plane_t(__fmaf_rn(qbyte(k < 4 ? fy0 : fy1, b), scy, h0.y), L.p.oy, L.p.iy);
+        const float tnz = plane_t(__fmaf_rn(qbyte(k < 4 ? nz0 : nz1, b), scz, h0.z), L.p.oz, L.p.iz);
+        const float tfz = plane_t(__fmaf_rn(qbyte(k < 4 ? fz0 : fz1, b), scz, h0.z), L.p.oz, L.p.iz);
+        const float tnear = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, L.p.tmin));
+        const float tfar = fminf(fminf(tfx, tfy), fminf(tfz, L.best_t));
+        if (((valid >> k) & 1u) && tnear <= __fmul_rn(tfar, kCullSlack)) {
+            if ((imask >> k) & 1u) ihits |= 1u << (k ^ oct);
+            else thits |= 1u << k;
+        }
+    }
+    if (thits) {
+        const uint32_t leafmask = valid & ~imask;
+        do {
+            const int k = __ffs(thits) - 1;
+            thits &= thits - 1u;
+            if (leaf_at<ANY>(L, tri_base + __popc(leafmask & ((1u << k) - 1u)))) return true;
+        } while (thits);
+    }
+    uint32_t gbase = child_base, gmask = imask, hits = ihits;
+    if (hits) {
+        if (hits & (hits - 1u)) {
+            if (L.sp >= kStackMax) {
+                atomicOr(err, ERR_STACK);
+                return true;
+            }
+            stack_put<SSTACK>(L.sp, make_int2((int32_t)child_base, (int32_t)(imask | ((hits & (hits - 1u)) << 8))),
+                              s_stack, l_stack);
+            ++L.sp;
+        }
+    } else {
+        if (L.sp == 0) return true;
+        const int2 e = stack_at<SSTACK>(L.sp - 1, s_stack, l_stack);
+        gbase = (uint32_t)e.x;
+        gmask = (uint32_t)e.y & 0xFFu;
+        hits = (uint32_t)e.y >> 8;
+        const uint32_t rest = hits & (hits - 1u);
+        if (rest) stack_put<SSTACK>(L.sp - 1, make_int2(e.x, (int32_t)(gmask | (rest << 8))), s_stack, l_stack);
+        else --L.sp;
+    }
+    const uint32_t slot = (uint32_t)(__ffs(hits) - 1) ^ oct;
+    L.node = (int32_t)(gbase + __popc(gmask & ((1u << slot) - 1u)));
+    return false;
+}
+
 template <bool ANY, int LAYOUT, int SSTACK>
 __device__ __forceinline__ bool trace_step(Lane& L, int2* s_stack, int2* l_stack, uint32_t* err) {
     if (LAYOUT == kLayoutBvh2) return trace_step2<ANY, SSTACK>(L, s_stack, l_stack, err);
+    if (LAYOUT == kLayoutBvh8Q8) return trace_step8<ANY, SSTACK>(L, s_stack, l_stack, err);
     return trace_step4<ANY, LAYOUT == kLayoutBvh4Q8, SSTACK>(L, s_stack, l_stack, err);
 }
 
@@ -339,8 +453,9 @@ constexpr int kRefillLanes = 8;
 //   uint64_t n                                        number of rays
 //   uint32_t load(uint64_t i, float4& r0, float4& r1, const void*& nodes,
 //                 const Tri*& tris)                   ray i (reference Ray layout) and
-//                                                     its BVH (nodes of layout LAYOUT);
-//                                                     returns the root node
+//                                                     its BVH (nodes and triangles of
+//                                                     layout LAYOUT); returns the binary
+//                                                     root (kNoNode when empty)
 //   void finish(uint64_t i, const Lane& L)            ray i is done (L.best_prim ==
 //                                                     0xFFFFFFFF means a miss)
 // The shared stack has SSTACK x blockDim.x int2 entries (dynamic shared memory).
@@ -372,7 +487,7 @@ __device__ __forceinline__ void traverse_loop(Src& src, unsigned long long* coun
                     L.bv = 0.0f;
                     L.best_prim = 0xFFFFFFFFu;
                     L.ray = i;
-                    L.node = (int32_t)root;
+                    L.node = (LAYOUT == kLayoutBvh8Q8 && root != kNoNode) ? 0 : (int32_t)root;  // 8-wide root is node 0
                     L.sp = 0;
                     active = true;
                     if (root == kNoNode) {

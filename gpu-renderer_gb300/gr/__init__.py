@@ -14,8 +14,8 @@ PKG_ROOT = os.path.dirname(_HERE)
 LIB_PATH = os.path.join(PKG_ROOT, "lib", "libgr.so")
 
 GR_OK = 0
-LAYOUT_BVH2, LAYOUT_BVH4, LAYOUT_BVH4_Q8 = 0, 1, 2
-LAYOUT_NAMES = {0: "bvh2", 1: "bvh4", 2: "bvh4_q8"}
+LAYOUT_BVH2, LAYOUT_BVH4, LAYOUT_BVH4_Q8, LAYOUT_BVH8_Q8 = 0, 1, 2, 3
+LAYOUT_NAMES = {0: "bvh2", 1: "bvh4", 2: "bvh4_q8", 3: "bvh8_q8"}
 STATUS = {
     0: "GR_OK", 1: "GR_ERR_INVALID", 2: "GR_ERR_CUDA", 3: "GR_ERR_OOM_BUDGET",
     4: "GR_ERR_PARSE", 5: "GR_ERR_TIMEOUT", 6: "GR_ERR_OVERFLOW",
@@ -58,6 +58,9 @@ def load():
         "gr_trace_host": ([_P, _P, ctypes.c_uint64, _P, ctypes.c_int], ctypes.c_int),
         "gr_bvh_set_layout": ([_P, ctypes.c_int, _P], ctypes.c_int),
         "gr_bvh_export_layout": ([_P, ctypes.c_int, _P], ctypes.c_int),
+        "gr_bvh_layout_size": ([_P, ctypes.c_int, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)],
+                               ctypes.c_int),
+        "gr_bvh_export_layout_tris": ([_P, ctypes.c_int, _P], ctypes.c_int),
         "gr_scene_set_layout": ([_P, ctypes.c_int], ctypes.c_int),
         "gr_bvh_set_tuning": ([_P, _P], ctypes.c_int),
         "gr_bvh_get_tuning": ([_P, _P], ctypes.c_int),
@@ -183,8 +186,25 @@ class BVH:
 
     def export_layout(self, layout):
         n = self.size
-        out = np.zeros(max(n - 1, 1) * (32 if layout == LAYOUT_BVH4 else 16), np.uint32)
-        self.ctx.check(load().gr_bvh_export_layout(self.h, layout, _ptr(out)), "gr_bvh_export_layout")
+        nb, _ = self.layout_size(layout)
+        out = np.zeros(nb // 4, np.uint32)
+        if n:
+            self.ctx.check(load().gr_bvh_export_layout(self.h, layout, _ptr(out)), "gr_bvh_export_layout")
+        return out
+
+    def layout_size(self, layout):
+        """(node bytes, triangle bytes) of a layout (built if needed)."""
+        nb, tb = ctypes.c_uint64(), ctypes.c_uint64()
+        self.ctx.check(load().gr_bvh_layout_size(self.h, layout, ctypes.byref(nb), ctypes.byref(tb)),
+                       "gr_bvh_layout_size")
+        return nb.value, tb.value
+
+    def export_layout_tris(self, layout):
+        """The triangles a layout traverses, (m, 12) float32."""
+        _, tb = self.layout_size(layout)
+        out = np.zeros(tb // 4, np.float32)
+        if tb:
+            self.ctx.check(load().gr_bvh_export_layout_tris(self.h, layout, _ptr(out)), "gr_bvh_export_layout_tris")
         return out
 
     def trace_host(self, rays, any_hit=False):

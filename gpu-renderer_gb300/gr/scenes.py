@@ -59,6 +59,32 @@ def shadow_rays(m, seed_salt=2, config=2):
     return R
 
 
+def surface_rays(soup, m, seed_salt=3, config=1, tmin=1e-4):
+    """Secondary-ray-like queries: origins uniform on random triangles of the
+    soup, directions uniform on the sphere with half of them squeezed towards
+    an axis plane (one component scaled by 1e-3, then renormalised), tmin 1e-4.
+    These start on surfaces and graze axis-aligned walls, where a plane
+    distance with an absolute rounding error would cull a hit box."""
+    r = rng(config, seed_salt)
+    v = np.asarray(soup, np.float32).reshape(-1, 3, 3)
+    t = r.integers(0, v.shape[0], m)
+    a, b = r.random(m), r.random(m)
+    sa = np.sqrt(a)
+    w = np.stack([1 - sa, sa * (1 - b), sa * b], axis=1)
+    p = np.einsum("mk,mkc->mc", w, v[t].astype(np.float64)).astype(np.float32)
+    d = r.standard_normal((m, 3))
+    g = r.random(m) < 0.5
+    ax = r.integers(0, 3, m)
+    d[g, ax[g]] *= 1e-3
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    R = np.empty((m, 8), np.float32)
+    R[:, 0:3] = p
+    R[:, 3:6] = d
+    R[:, 6] = np.float32(tmin)
+    R[:, 7] = np.float32(1e38)
+    return R
+
+
 def coherent_rays(w=2048, h=2048, fov_deg=40.0, eye=(0.5, 0.5, -1.0), target=(0.5, 0.5, 0.5)):
     """Pixel-centre pinhole rays over a w x h grid."""
     eye = np.asarray(eye, np.float64)

@@ -128,11 +128,18 @@ gr_status gr_bvh_export(gr_bvh* bvh, uint32_t* h_sorted_prim, uint32_t* h_sorted
  *                      outward against a per-node origin and power-of-two
  *                      scale (64 B); the boxes contain the FP32 boxes, so the
  *                      closest hit is the same
- * The binary tree is always built; a 4-wide layout is derived from it on the
- * GPU when first requested and kept until the next build. */
+ *   GR_LAYOUT_BVH8_Q8  8-wide nodes with 8-bit child boxes (96 B), collapsed
+ *                      from the binary tree by opening the largest child
+ *                      first, children placed so a ray's octant gives a
+ *                      near-to-far order, nodes numbered breadth first, and
+ *                      leaf triangles copied into node order
+ * The binary tree is always built; another layout is derived from it on the
+ * GPU when first requested and kept until the next build (the 8-wide build
+ * waits for the stream once per tree level). */
 #define GR_LAYOUT_BVH2 0
 #define GR_LAYOUT_BVH4 1
 #define GR_LAYOUT_BVH4_Q8 2
+#define GR_LAYOUT_BVH8_Q8 3
 
 /* Selects the layout gr_trace uses (building it if needed; stream-ordered). */
 gr_status gr_bvh_set_layout(gr_bvh* bvh, int layout, void* stream);
@@ -162,9 +169,19 @@ gr_status gr_bvh_get_tuning(const gr_bvh* bvh, gr_trace_tuning* tuning);
 gr_status gr_bvh_autotune(gr_bvh* bvh, const gr_ray* d_rays, uint64_t n, int any_hit, gr_hit* d_hits,
                           gr_tuning_result* h_table, uint32_t max_results, uint32_t* n_results);
 
-/* Copies a 4-wide layout to host memory (128 or 64 bytes x max(n-1, 1); only
- * even-depth entries are nodes, the others are zero). Waits for the device. */
+/* Bytes of a layout's nodes and of the triangle array it traverses (the
+ * 8-wide layout has its own, in node order; the others share the leaf-order
+ * triangles of gr_bvh_export). Builds the layout if needed; waits. */
+gr_status gr_bvh_layout_size(gr_bvh* bvh, int layout, uint64_t* node_bytes, uint64_t* tri_bytes);
+
+/* Copies a derived layout's nodes to host memory (node_bytes of
+ * gr_bvh_layout_size; for the 4-wide layouts only even-depth entries are
+ * nodes, the others are zero). Waits for the device. */
 gr_status gr_bvh_export_layout(gr_bvh* bvh, int layout, void* h_nodes);
+
+/* Copies the triangles a layout traverses (tri_bytes of gr_bvh_layout_size,
+ * 12 floats each: v0, prim-id bits, v1, 0, v2, 0). Waits for the device. */
+gr_status gr_bvh_export_layout_tris(gr_bvh* bvh, int layout, float* h_tris);
 
 /* ---- traversal -------------------------------------------------------------
  * Replaces trace / trace_shadow (src/renderer/pathtracer_kernel.h:235-246 and

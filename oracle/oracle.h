@@ -54,6 +54,14 @@ void or_trace(const uint32_t* bvh2_nodes, const float* tri_sorted, uint32_t root
  * quant = 1: 16 words per node, 8-bit outward-quantised boxes) and traversal
  * in the product's child order. out holds max(n-1,1) nodes. */
 void or_bvh4_build(const uint32_t* bvh2_nodes, uint32_t n, int quant, uint32_t* out);
+
+/* 8-wide quantised layout (24 words per node) collapsed from the binary nodes
+ * with the product's rules and numbering; returns the node count (copies at
+ * most max_nodes nodes and max_tris node-order triangles, 12 floats each). */
+uint32_t or_bvh8_build(const uint32_t* bvh2_nodes, const float* tri_sorted, uint32_t n, uint32_t root,
+                       uint32_t* out_nodes, uint32_t max_nodes, float* out_tris, uint32_t max_tris, uint32_t* n_tris);
+void or_trace8(const uint32_t* nodes8, const float* tris8, uint32_t root, const float* rays, uint64_t nrays,
+               int any_hit, float* hits, uint32_t* stats, int threads);
 void or_trace4(const uint32_t* nodes4, int quant, const float* tri_sorted, uint32_t root, const float* rays,
                uint64_t nrays, int any_hit, float* hits, uint32_t* stats, int threads);
 

@@ -92,6 +92,33 @@ def bvh4(bvh, quant):
     return out
 
 
+def bvh8(bvh):
+    """8-wide quantised layout collapsed from the oracle's binary nodes:
+    (nodes as uint32 words, 24 per node; node-order triangles, 12 floats each)."""
+    n = bvh["tris"].size // 12
+    if n == 0:
+        return np.zeros(0, np.uint32), np.zeros(0, np.float32)
+    cap_n, cap_t = max(n - 1, 1), max(n, 2)
+    nodes = np.zeros(cap_n * 24, np.uint32)
+    tris = np.zeros(cap_t * 12, np.float32)
+    nt = ctypes.c_uint32()
+    L = load()
+    L.or_bvh8_build.restype = ctypes.c_uint32
+    count = L.or_bvh8_build(_p(bvh["nodes"]), _p(bvh["tris"]), ctypes.c_uint32(n), ctypes.c_uint32(bvh["root"]),
+                            _p(nodes), ctypes.c_uint32(cap_n), _p(tris), ctypes.c_uint32(cap_t), ctypes.byref(nt))
+    return nodes[:24 * count].copy(), tris[:12 * nt.value].copy()
+
+
+def trace8(bvh, nodes8, tris8, rays, any_hit=False, stats=False, nthreads=None):
+    r = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
+    m = r.shape[0]
+    hits = np.zeros((m, 4), np.float32)
+    st = np.zeros((m, 2), np.uint32) if stats else None
+    load().or_trace8(_p(nodes8), _p(tris8), ctypes.c_uint32(bvh["root"]), _p(r), ctypes.c_uint64(m), int(any_hit),
+                     _p(hits), _p(st), nthreads or threads())
+    return (hits, st) if stats else hits
+
+
 def trace4(bvh, nodes4, quant, rays, any_hit=False, stats=False, nthreads=None):
     r = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
     m = r.shape[0]

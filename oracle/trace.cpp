@@ -12,6 +12,7 @@
 // is written as fmaf().
 #include "oracle.h"
 
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <cstring>
@@ -52,7 +53,7 @@ struct RayPre {
     float o[3], d[3], tmin, tmax;
     int kx, ky, kz;
     float sx, sy, sz;
-    float idir[3], ood[3];
+    float idir[3];
 };
 
 inline void prepare(const float* r, RayPre& p) {
@@ -78,20 +79,22 @@ inline void prepare(const float* r, RayPre& p) {
     for (int k = 0; k < 3; ++k) {
         float dk = std::fabs(p.d[k]) > eps ? p.d[k] : std::copysign(eps, p.d[k]);
         p.idir[k] = 1.0f / dk;
-        p.ood[k] = p.o[k] * p.idir[k];
     }
 }
 
 // Every cull keeps a box (or a deferred entry) while its entry distance is
-// within (1 + 2^-20) of the exit / closest-hit distance.
-constexpr float kCullSlack = 1.00000095367431640625f;
+// within (1 + 2^-16) of the exit / closest-hit distance; plane distances are
+// (plane - o) * (1/d), within 3 ulps relative to themselves.
+constexpr float kCullSlack = 1.0000152587890625f;
+
+inline float plane_t(float plane, float o, float inv) { return (plane - o) * inv; }
 
 // Child-box slab test; returns entry distance through *tn.
 inline bool slab(const RayPre& p, float lox, float hix, float loy, float hiy, float loz, float hiz, float tbest,
                  float* tn) {
-    float x0 = std::fmaf(lox, p.idir[0], -p.ood[0]), x1 = std::fmaf(hix, p.idir[0], -p.ood[0]);
-    float y0 = std::fmaf(loy, p.idir[1], -p.ood[1]), y1 = std::fmaf(hiy, p.idir[1], -p.ood[1]);
-    float z0 = std::fmaf(loz, p.idir[2], -p.ood[2]), z1 = std::fmaf(hiz, p.idir[2], -p.ood[2]);
+    float x0 = plane_t(lox, p.o[0], p.idir[0]), x1 = plane_t(hix, p.o[0], p.idir[0]);
+    float y0 = plane_t(loy, p.o[1], p.idir[1]), y1 = plane_t(hiy, p.o[1], p.idir[1]);
+    float z0 = plane_t(loz, p.o[2], p.idir[2]), z1 = plane_t(hiz, p.o[2], p.idir[2]);
     float tnear = std::fmax(std::fmax(std::fmin(x0, x1), std::fmin(y0, y1)), std::fmax(std::fmin(z0, z1), p.tmin));
     float tfar = std::fmin(std::fmin(std::fmax(x0, x1), std::fmax(y0, y1)), std::fmin(std::fmax(z0, z1), tbest));
     *tn = tnear;
@@ -431,6 +434,222 @@ void trace4_one(const uint32_t* nodes, int quant, const float* tris, uint32_t ro
 }
 
 // ---------------------------------------------------------------------------
+// 8-wide quantised layout: the level-by-level collapse and its traversal,
+// restated sequentially in the same order (nodes breadth first, a level's
+// children in node order then slot order) so nodes, triangles and any-hit
+// results compare word for word.
+// ---------------------------------------------------------------------------
+inline float half_area(const CB& b) {
+    const float dx = b.hi[0] - b.lo[0], dy = b.hi[1] - b.lo[1], dz = b.hi[2] - b.lo[2];
+    return (dx * dy + dy * dz) + dz * dx;
+}
+
+constexpr int32_t kEmpty8 = std::numeric_limits<int32_t>::min();
+
+void build8(const uint32_t* nodes, const float* tris, uint32_t root, std::vector<uint32_t>& out,
+            std::vector<float>& out_tris) {
+    std::vector<uint32_t> frontier{root};
+    uint32_t out_base = 0, tri_cursor = 0;
+    while (!frontier.empty()) {
+        const uint32_t level_n = (uint32_t)frontier.size();
+        const uint32_t next_base = out_base + level_n;
+        std::vector<uint32_t> next;
+        out.resize(24ull * (out_base + level_n), 0u);
+        uint32_t inner_acc = 0, leaf_acc = 0;
+        for (uint32_t i = 0; i < level_n; ++i) {
+            const uint32_t* rw = nodes + 16ull * frontier[i];
+            CB box[8];
+            int32_t ref[8];
+            int cnt = 2;
+            ref[0] = (int32_t)rw[12];
+            box[0] = child_box(rw, 0);
+            ref[1] = (int32_t)rw[13];
+            box[1] = child_box(rw, 1);
+            while (cnt < 8) {
+                int best = -1;
+                float best_a = 0.0f;
+                for (int k = 0; k < cnt; ++k)
+                    if (ref[k] >= 0) {
+                        const float a = half_area(box[k]);
+                        if (best < 0 || a > best_a) { best = k; best_a = a; }
+                    }
+                if (best < 0) break;
+                const uint32_t* cw = nodes + 16ull * (uint32_t)ref[best];
+                ref[best] = (int32_t)cw[12];
+                box[best] = child_box(cw, 0);
+                ref[cnt] = (int32_t)cw[13];
+                box[cnt] = child_box(cw, 1);
+                ++cnt;
+            }
+            float lo[3], hi[3], nc[3];
+            for (int a = 0; a < 3; ++a) {
+                lo[a] = box[0].lo[a];
+                hi[a] = box[0].hi[a];
+                for (int k = 1; k < cnt; ++k) {
+                    lo[a] = std::fmin(lo[a], box[k].lo[a]);
+                    hi[a] = std::fmax(hi[a], box[k].hi[a]);
+                }
+                nc[a] = lo[a] + hi[a];
+            }
+            int slot_of[8];
+            uint32_t used = 0;
+            for (int k = 0; k < 8; ++k) slot_of[k] = -1;
+            for (int it = 0; it < cnt; ++it) {
+                int bk = -1, bs = -1;
+                float bsc = 0.0f;
+                for (int k = 0; k < cnt; ++k) {
+                    if (slot_of[k] >= 0) continue;
+                    const float dx = (box[k].lo[0] + box[k].hi[0]) - nc[0];
+                    const float dy = (box[k].lo[1] + box[k].hi[1]) - nc[1];
+                    const float dz = (box[k].lo[2] + box[k].hi[2]) - nc[2];
+                    for (int s2 = 0; s2 < 8; ++s2) {
+                        if (used & (1u << s2)) continue;
+                        const float sc = (((s2 & 1) ? dx : -dx) + ((s2 & 2) ? dy : -dy)) + ((s2 & 4) ? dz : -dz);
+                        if (bk < 0 || sc > bsc) { bk = k; bs = s2; bsc = sc; }
+                    }
+                }
+                slot_of[bk] = bs;
+                used |= 1u << bs;
+            }
+            float scale[3];
+            uint32_t be[3];
+            for (int a = 0; a < 3; ++a) {
+                const int e = pick_exponent(lo[a], hi[a]);
+                be[a] = (uint32_t)(e + 127);
+                scale[a] = f_of(be[a] << 23);
+            }
+            uint32_t* o = out.data() + 24ull * (out_base + i);
+            o[0] = w_of(lo[0]);
+            o[1] = w_of(lo[1]);
+            o[2] = w_of(lo[2]);
+            int32_t sref[8];
+            for (int s2 = 0; s2 < 8; ++s2) sref[s2] = kEmpty8;
+            uint32_t imask = 0, ni = 0, nl = 0;
+            for (int k = 0; k < cnt; ++k) {
+                const int s2 = slot_of[k];
+                sref[s2] = ref[k];
+                if (ref[k] >= 0) { imask |= 1u << s2; ++ni; } else { ++nl; }
+                for (int a = 0; a < 3; ++a) {
+                    o[8 + 4 * a + (s2 >> 2)] |= quant_lo(box[k].lo[a], scale[a], lo[a]) << (8 * (s2 & 3));
+                    o[8 + 4 * a + 2 + (s2 >> 2)] |= quant_hi(box[k].hi[a], scale[a], lo[a]) << (8 * (s2 & 3));
+                }
+            }
+            o[3] = be[0] | (be[1] << 8) | (be[2] << 16) | (imask << 24);
+            o[4] = next_base + inner_acc;
+            o[5] = tri_cursor + leaf_acc;
+            o[6] = used;
+            uint32_t rl = 0;
+            for (int s2 = 0; s2 < 8; ++s2) {
+                const int32_t r = sref[s2];
+                if (r == kEmpty8) continue;
+                if (r >= 0) {
+                    next.push_back((uint32_t)r);
+                } else {
+                    const size_t dst = 12ull * (tri_cursor + leaf_acc + rl++);
+                    if (out_tris.size() < dst + 12) out_tris.resize(dst + 12);
+                    std::memcpy(out_tris.data() + dst, tris + 12ull * (uint32_t)(~r), 48);
+                }
+            }
+            inner_acc += ni;
+            leaf_acc += nl;
+        }
+        out_base += level_n;
+        tri_cursor += leaf_acc;
+        frontier.swap(next);
+    }
+}
+
+inline uint32_t byte_of(uint32_t w, int k) { return (w >> (8 * k)) & 0xFFu; }
+inline int ctz32(uint32_t x) { int k = 0; while (!(x & 1u)) { x >>= 1; ++k; } return k; }
+inline uint32_t popc32(uint32_t x) { uint32_t c = 0; while (x) { x &= x - 1u; ++c; } return c; }
+
+void trace8_one(const uint32_t* nodes, const float* tris, uint32_t root, const float* ray, int any, float* hit,
+                uint32_t* st) {
+    RayPre p;
+    prepare(ray, p);
+    Best b{p.tmax, 0.0f, 0.0f, 0xFFFFFFFFu};
+    uint32_t visits = 0, tests = 0;
+    struct Group { uint32_t base, word; };
+    Group stack[256];
+    int sp = 0;
+    uint32_t node = 0;
+    bool done = root == 0xFFFFFFFFu;
+    const uint32_t sg[3] = {w_of(p.idir[0]) >> 31, w_of(p.idir[1]) >> 31, w_of(p.idir[2]) >> 31};
+    const uint32_t oct = sg[0] | (sg[1] << 1) | (sg[2] << 2);
+    while (!done) {
+        const uint32_t* o = nodes + 24ull * node;
+        ++visits;
+        const uint32_t meta = o[3], child_base = o[4], tri_base = o[5], valid = o[6], imask = meta >> 24;
+        float scl[3];
+        uint32_t nw[3][2], fw[3][2];
+        for (int a = 0; a < 3; ++a) {
+            scl[a] = f_of(((meta >> (8 * a)) & 0xFFu) << 23);
+            for (int h = 0; h < 2; ++h) {
+                const uint32_t lo = o[8 + 4 * a + h], hi = o[8 + 4 * a + 2 + h];
+                nw[a][h] = sg[a] ? hi : lo;
+                fw[a][h] = sg[a] ? lo : hi;
+            }
+        }
+        uint32_t ihits = 0, thits = 0;
+        for (int k = 0; k < 8; ++k) {
+            float tn[3], tf[3];
+            for (int a = 0; a < 3; ++a) {
+                tn[a] = plane_t(qdecode((int)byte_of(nw[a][k >> 2], k & 3), scl[a], f_of(o[a])), p.o[a], p.idir[a]);
+                tf[a] = plane_t(qdecode((int)byte_of(fw[a][k >> 2], k & 3), scl[a], f_of(o[a])), p.o[a], p.idir[a]);
+            }
+            const float tnear = std::fmax(std::fmax(tn[0], tn[1]), std::fmax(tn[2], p.tmin));
+            const float tfar = std::fmin(std::fmin(tf[0], tf[1]), std::fmin(tf[2], b.t));
+            if (((valid >> k) & 1u) && tnear <= tfar * kCullSlack) {
+                if ((imask >> k) & 1u) ihits |= 1u << (k ^ (int)oct);
+                else thits |= 1u << k;
+            }
+        }
+        const uint32_t leafmask = valid & ~imask;
+        while (thits && !done) {
+            const int k = ctz32(thits);
+            thits &= thits - 1u;
+            const float* tri = tris + 12ull * (tri_base + popc32(leafmask & ((1u << k) - 1u)));
+            ++tests;
+            if (any) {
+                float t, u, v;
+                if (tri_test(p, tri, tri + 4, tri + 8, b.t, &t, &u, &v)) {
+                    b.t = t; b.u = u; b.v = v; b.prim = w_of(tri[3]);
+                    done = true;
+                }
+            } else {
+                consider(p, tri, b);
+            }
+        }
+        if (done) break;
+        uint32_t gbase = child_base, gmask = imask, hits = ihits;
+        if (hits) {
+            if (hits & (hits - 1u)) stack[sp++] = {child_base, imask | ((hits & (hits - 1u)) << 8)};
+        } else {
+            if (sp == 0) break;
+            Group& g = stack[sp - 1];
+            gbase = g.base;
+            gmask = g.word & 0xFFu;
+            hits = g.word >> 8;
+            const uint32_t rest = hits & (hits - 1u);
+            if (rest) g.word = gmask | (rest << 8); else --sp;
+        }
+        const uint32_t slot = (uint32_t)ctz32(hits) ^ oct;
+        node = gbase + popc32(gmask & ((1u << slot) - 1u));
+    }
+    if (b.prim == 0xFFFFFFFFu) {
+        hit[0] = p.tmax;
+        uint32_t m = 0xFFFFFFFFu;
+        std::memcpy(hit + 1, &m, 4);
+        hit[2] = 0.0f; hit[3] = 0.0f;
+    } else {
+        hit[0] = b.t;
+        std::memcpy(hit + 1, &b.prim, 4);
+        hit[2] = b.u; hit[3] = b.v;
+    }
+    if (st) { st[0] = visits; st[1] = tests; }
+}
+
+// ---------------------------------------------------------------------------
 // Reference traversal (pathtracer_kernel.h)
 // ---------------------------------------------------------------------------
 struct V3 { float x, y, z; };
@@ -691,5 +910,27 @@ extern "C" void or_trace4(const uint32_t* nodes4, int quant, const float* tris, 
     parallel_rays(nrays, threads, [&](uint64_t b, uint64_t e) {
         for (uint64_t i = b; i < e; ++i)
             trace4_one(nodes4, quant, tris, root, rays + 8 * i, any_hit, hits + 4 * i, stats ? stats + 2 * i : nullptr);
+    });
+}
+
+extern "C" uint32_t or_bvh8_build(const uint32_t* bvh2_nodes, const float* tri_sorted, uint32_t n, uint32_t root,
+                                  uint32_t* out_nodes, uint32_t max_nodes, float* out_tris, uint32_t max_tris,
+                                  uint32_t* n_tris) {
+    if (n == 0) { if (n_tris) *n_tris = 0; return 0; }
+    std::vector<uint32_t> nodes;
+    std::vector<float> tris;
+    build8(bvh2_nodes, tri_sorted, root, nodes, tris);
+    const uint32_t count = (uint32_t)(nodes.size() / 24), nt = (uint32_t)(tris.size() / 12);
+    if (out_nodes) std::memcpy(out_nodes, nodes.data(), 96ull * std::min(count, max_nodes));
+    if (out_tris) std::memcpy(out_tris, tris.data(), 48ull * std::min(nt, max_tris));
+    if (n_tris) *n_tris = nt;
+    return count;
+}
+
+extern "C" void or_trace8(const uint32_t* nodes8, const float* tris8, uint32_t root, const float* rays,
+                          uint64_t nrays, int any_hit, float* hits, uint32_t* stats, int threads) {
+    parallel_rays(nrays, threads, [&](uint64_t b, uint64_t e) {
+        for (uint64_t i = b; i < e; ++i)
+            trace8_one(nodes8, tris8, root, rays + 8 * i, any_hit, hits + 4 * i, stats ? stats + 2 * i : nullptr);
     });
 }

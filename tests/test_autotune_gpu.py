@@ -1,5 +1,5 @@
 """Autotuner: every (layout, block, short stack) configuration traces the same
-hits bit for bit, the tuner times all 27 and keeps the fastest, invalid
+hits bit for bit, the tuner times all 36 and keeps the fastest, invalid
 configurations are refused, and a tuned scene renders the same image."""
 import numpy as np
 import pytest
@@ -10,7 +10,7 @@ from gr import scenes as sc
 
 pytestmark = pytest.mark.gpu
 
-LAYOUTS = [gr.LAYOUT_BVH2, gr.LAYOUT_BVH4, gr.LAYOUT_BVH4_Q8]
+LAYOUTS = [gr.LAYOUT_BVH2, gr.LAYOUT_BVH4, gr.LAYOUT_BVH4_Q8, gr.LAYOUT_BVH8_Q8]
 
 
 def _bits(h):
@@ -40,8 +40,12 @@ def test_every_configuration_matches_oracle(ctx, oracle, soup_case, layout, bloc
     got = b.trace_host(s, any_hit=True)
     # any-hit: occlusion flags equal the oracle's for the same node layout
     quant = layout == gr.LAYOUT_BVH4_Q8
-    want = (oracle.trace(ob, s, any_hit=True) if layout == gr.LAYOUT_BVH2 else
-            oracle.trace4(ob, oracle.bvh4(ob, quant), quant, s, any_hit=True))
+    if layout == gr.LAYOUT_BVH2:
+        want = oracle.trace(ob, s, any_hit=True)
+    elif layout == gr.LAYOUT_BVH8_Q8:
+        want = oracle.trace8(ob, *oracle.bvh8(ob), s, any_hit=True)
+    else:
+        want = oracle.trace4(ob, oracle.bvh4(ob, quant), quant, s, any_hit=True)
     np.testing.assert_array_equal(_bits(got), _bits(want))
 
 
@@ -49,7 +53,7 @@ def test_invalid_tuning_is_refused(ctx):
     b = gr.BVH(ctx)
     b.build_host(sc.triangle_soup(100, seed_salt=503))
     before = b.tuning()
-    for bad in [(3, 128, 12), (0, 96, 12), (0, 128, 10), (0, 512, 8), (-1, 64, 8)]:
+    for bad in [(4, 128, 12), (0, 96, 12), (0, 128, 10), (0, 512, 8), (-1, 64, 8)]:
         with pytest.raises(gr.GrError):
             b.set_tuning(*bad)
     assert b.tuning() == before
@@ -64,9 +68,9 @@ def test_bvh_autotune_times_all_and_keeps_fastest(ctx, oracle, soup_case):
     dh = torch.zeros((rays.shape[0], 4), dtype=torch.float32, device="cuda")
     torch.cuda.synchronize()
     table = b.autotune(dr, rays.shape[0], dh)
-    assert len(table) == 27
+    assert len(table) == 36
     seen = {(t["layout"], t["block"], t["short_stack"]) for t, _ in table}
-    assert len(seen) == 27
+    assert len(seen) == 36
     assert all(ms > 0 for _, ms in table)
     best = min(table, key=lambda r: r[1])[0]
     assert b.tuning() == best
@@ -91,7 +95,7 @@ def test_scene_autotune_keeps_image(ctx):
 
 
 @pytest.mark.parametrize("tuning", [(gr.LAYOUT_BVH2, 64, 8, 4096), (gr.LAYOUT_BVH4, 256, 16, 65536),
-                                    (gr.LAYOUT_BVH4_Q8, 128, 12, 0)])
+                                    (gr.LAYOUT_BVH4_Q8, 128, 12, 0), (gr.LAYOUT_BVH8_Q8, 64, 16, 8192)])
 def test_scene_tuning_and_wave_size_keep_image(ctx, tuning):
     d = sc.cornell_box(48, 48)
     a = gr.Scene(ctx, d)

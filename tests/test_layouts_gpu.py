@@ -1,7 +1,7 @@
-"""4-wide node layouts (FP32 and 8-bit quantised child boxes): the GPU
-collapse and quantisation equal the oracle's word for word, traversal results
-equal the oracle's bit for bit, closest hits equal the binary layout's, and
-renders are identical across layouts."""
+"""Wide node layouts (4-wide FP32 and 8-bit, 8-wide 8-bit child boxes): the
+GPU collapse and quantisation equal the oracle's word for word, traversal
+results equal the oracle's bit for bit, closest hits equal the binary
+layout's, and renders are identical across layouts."""
 import numpy as np
 import pytest
 
@@ -38,6 +38,41 @@ def test_layout_build_and_trace_match_oracle(ctx, oracle, n, scale, layout):
     np.testing.assert_array_equal(_bits(ga), _bits(oracle.trace4(ob, want_nodes, quant, s, any_hit=True)))
 
 
+@pytest.mark.parametrize("n,scale", [(1, 100.0), (2, 100.0), (7, 50.0), (5000, 8.0), (1000000, 1.0)])
+def test_bvh8_build_and_trace_match_oracle(ctx, oracle, n, scale):
+    v = sc.triangle_soup(n, seed_salt=420 + n % 11).reshape(n, 3, 3)
+    c = v.mean(axis=1, keepdims=True)
+    v = np.ascontiguousarray(((v - c) * scale + c).reshape(n, 9), np.float32)
+    b = gr.BVH(ctx)
+    b.build_host(v)
+    ob = oracle.lbvh(v)
+    want_nodes, want_tris = oracle.bvh8(ob)
+    np.testing.assert_array_equal(b.export_layout(gr.LAYOUT_BVH8_Q8), want_nodes)
+    np.testing.assert_array_equal(_bits(b.export_layout_tris(gr.LAYOUT_BVH8_Q8)), _bits(want_tris))
+    b.set_layout(gr.LAYOUT_BVH8_Q8)
+    m = 131072 if n >= 1000000 else 40000
+    rays = sc.incoherent_rays(m, seed_salt=421)
+    got = b.trace_host(rays)
+    np.testing.assert_array_equal(_bits(got), _bits(oracle.trace8(ob, want_nodes, want_tris, rays)))
+    np.testing.assert_array_equal(_bits(got), _bits(oracle.trace(ob, rays)))  # same closest hits as binary
+    s = sc.shadow_rays(m, seed_salt=422)
+    ga = b.trace_host(s, any_hit=True)
+    np.testing.assert_array_equal(_bits(ga), _bits(oracle.trace8(ob, want_nodes, want_tris, s, any_hit=True)))
+    occluded = _bits(oracle.trace(ob, s, any_hit=True))[:, 1] != 0xFFFFFFFF
+    np.testing.assert_array_equal(_bits(ga)[:, 1] != 0xFFFFFFFF, occluded)
+
+
+def test_bvh8_rebuild_keeps_layout_current(ctx, oracle):
+    b = gr.BVH(ctx)
+    b.set_layout(gr.LAYOUT_BVH8_Q8)
+    for salt in (430, 431):
+        v = sc.triangle_soup(20000, seed_salt=salt)
+        b.build_host(v)
+        ob = oracle.lbvh(v)
+        rays = sc.incoherent_rays(20000, seed_salt=salt)
+        np.testing.assert_array_equal(_bits(b.trace_host(rays)), _bits(oracle.trace(ob, rays)))
+
+
 def test_quantised_boxes_contain_fp32_boxes(ctx, oracle):
     n = 20000
     v = sc.triangle_soup(n, seed_salt=410)
@@ -62,7 +97,7 @@ def test_quantised_boxes_contain_fp32_boxes(ctx, oracle):
                 assert lo <= ff[G, 8 * a + k] and hi >= ff[G, 8 * a + 4 + k]
 
 
-@pytest.mark.parametrize("layout", [gr.LAYOUT_BVH4, gr.LAYOUT_BVH4_Q8])
+@pytest.mark.parametrize("layout", [gr.LAYOUT_BVH4, gr.LAYOUT_BVH4_Q8, gr.LAYOUT_BVH8_Q8])
 def test_render_identical_across_layouts(ctx, layout):
     d = sc.glossy_scene(64, 48, level=3, glass_level=2)
     a = gr.Scene(ctx, d)
@@ -71,3 +106,16 @@ def test_render_identical_across_layouts(ctx, layout):
     b.set_layout(layout)
     b.render(4, max_depth=10, seed=5, want_image=False)
     np.testing.assert_array_equal(a.accumulation()[0], b.accumulation()[0])
+
+
+@pytest.mark.parametrize("layout", [gr.LAYOUT_BVH2, gr.LAYOUT_BVH4, gr.LAYOUT_BVH4_Q8, gr.LAYOUT_BVH8_Q8])
+def test_surface_rays_equal_brute_force(ctx, oracle, layout):
+    """Secondary-ray-like queries on the Cornell box (origins on walls, grazing
+    directions): every layout returns the brute-force closest hit bit for bit."""
+    v = sc.cornell_box(32, 32).flatten()[0]
+    b = gr.BVH(ctx)
+    b.build_host(v)
+    b.set_layout(layout)
+    rays = sc.surface_rays(v, 400000, seed_salt=12)
+    np.testing.assert_array_equal(_bits(b.trace_host(rays)), _bits(oracle.trace_brute(v, rays)))
+

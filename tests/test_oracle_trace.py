@@ -85,3 +85,44 @@ def test_empty_scene(oracle):
     rays = sc.incoherent_rays(100, seed_salt=82)
     h = oracle.trace(bvh, rays)
     assert np.all(h.view(np.int32)[:, 1] == -1)
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 9, 777, 20000])
+def test_wide_layouts_equal_binary(oracle, n):
+    """The 4- and 8-wide restatements find the binary traversal's closest hits
+    and the same occlusion; the 8-wide build places every leaf triangle once."""
+    v = sc.triangle_soup(n, seed_salt=900 + n % 7)
+    bvh = oracle.lbvh(v)
+    rays = sc.incoherent_rays(8000, seed_salt=901)
+    shadow = sc.shadow_rays(8000, seed_salt=902)
+    want = oracle.trace(bvh, rays)
+    occ = oracle.trace(bvh, shadow, any_hit=True).view(np.uint32)[:, 1] != 0xFFFFFFFF
+    nodes8, tris8 = oracle.bvh8(bvh)
+    got = oracle.trace8(bvh, nodes8, tris8, rays)
+    np.testing.assert_array_equal(got.view(np.uint32), want.view(np.uint32))
+    a8 = oracle.trace8(bvh, nodes8, tris8, shadow, any_hit=True).view(np.uint32)[:, 1] != 0xFFFFFFFF
+    np.testing.assert_array_equal(a8, occ)
+    prims = np.sort(tris8.reshape(-1, 12)[:, 3].view(np.uint32))
+    if n > 1:
+        np.testing.assert_array_equal(prims, np.arange(n, dtype=np.uint32))
+    for quant in (False, True):
+        n4 = oracle.bvh4(bvh, quant)
+        np.testing.assert_array_equal(oracle.trace4(bvh, n4, quant, rays).view(np.uint32), want.view(np.uint32))
+
+
+@pytest.mark.parametrize("scene", ["cornell", "glossy"])
+def test_surface_rays_equal_brute_force_in_every_layout(oracle, scene):
+    """Rays that start on surfaces and graze axis-aligned walls: every layout's
+    traversal finds exactly the brute-force closest hit (a plane distance with
+    an absolute rounding error used to cull such hits)."""
+    d = sc.cornell_box(32, 32) if scene == "cornell" else sc.glossy_scene(32, 24, level=3, glass_level=2)
+    v = d.flatten()[0]
+    bvh = oracle.lbvh(v)
+    rays = sc.surface_rays(v, 200000 if scene == "cornell" else 50000, seed_salt=11)
+    want = oracle.trace_brute(v, rays).view(np.uint32)
+    np.testing.assert_array_equal(oracle.trace(bvh, rays).view(np.uint32), want)
+    for quant in (False, True):
+        n4 = oracle.bvh4(bvh, quant)
+        np.testing.assert_array_equal(oracle.trace4(bvh, n4, quant, rays).view(np.uint32), want)
+    n8, t8 = oracle.bvh8(bvh)
+    np.testing.assert_array_equal(oracle.trace8(bvh, n8, t8, rays).view(np.uint32), want)
