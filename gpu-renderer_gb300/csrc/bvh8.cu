@@ -8,7 +8,9 @@
 // high side along axis a", chosen greedily by the score
 // sum_a (+/-)(child centre - node centre)_a, so that a ray visiting inner
 // children in order of (slot ^ octant) goes roughly near to far. Boxes are
-// quantised outward against fma(q, 2^e, origin) as in the 4-wide layout.
+// quantised outward against the layout's decode fma(2^23 + q, 2^e, origin8)
+// (origin8 = lo - 2^(23+e) rounded down), which the traversal evaluates with
+// one byte permute and one FMA per plane.
 //
 // Nodes are numbered breadth first, level by level: a level's nodes are
 // collapsed (one thread each), their inner-child and leaf counts are prefix-
@@ -31,6 +33,52 @@ constexpr int kBlock8 = 256;
 constexpr int kScanThreads = 1024;
 constexpr int32_t kEmptySlot = INT32_MIN;
 constexpr int kMaxLevels8 = 72;
+
+// 8-wide decode: plane(q) = fma(2^23 + q, 2^e, origin8) with
+// origin8 = round_down(lo - 2^(23+e)), so the traversal turns a byte into
+// 2^23 + q with one byte permute and decodes with one FMA. Rounding origin8
+// down keeps plane(0) <= lo; e grows until plane(255) >= hi.
+constexpr int kMaxExp8 = 104;  // 2^(23+e) stays finite
+
+__device__ __forceinline__ float decode8(int q, float scale, float origin8) {
+    return __fmaf_rn(__int2float_rn(8388608 + q), scale, origin8);
+}
+
+__device__ __forceinline__ float origin8_for(float lo, int e) {
+    return __fsub_rd(lo, __uint_as_float((uint32_t)(e + 23 + 127) << 23));
+}
+
+__device__ __forceinline__ int pick_exponent8(float lo, float hi, uint32_t* err) {
+    const float extent = __fsub_rn(hi, lo);
+    int e = -126;
+    if (extent > 0.0f) {
+        int ex;
+        frexpf(__fdiv_rn(extent, 255.0f), &ex);
+        e = max(-126, min(kMaxExp8, ex - 1));
+    }
+    while (decode8(255, __uint_as_float((uint32_t)(e + 127) << 23), origin8_for(lo, e)) < hi) {
+        if (e >= kMaxExp8) {
+            atomicOr(err, ERR_RANGE);  // coordinates beyond about 2^126: not representable
+            break;
+        }
+        ++e;
+    }
+    return e;
+}
+
+__device__ __forceinline__ uint32_t quant_lo8(float v, float scale, float origin8) {
+    int q = 0;
+    for (int step = 128; step > 0; step >>= 1)  // largest q with plane(q) <= v (plane(0) <= v)
+        if (q + step <= 255 && decode8(q + step, scale, origin8) <= v) q += step;
+    return (uint32_t)q;
+}
+
+__device__ __forceinline__ uint32_t quant_hi8(float v, float scale, float origin8) {
+    int q = 255;
+    for (int step = 128; step > 0; step >>= 1)  // smallest q with plane(q) >= v (plane(255) >= v)
+        if (q - step >= 0 && decode8(q - step, scale, origin8) >= v) q -= step;
+    return (uint32_t)q;
+}
 
 __device__ __forceinline__ float half_area(const CBox& b) {
     const float dx = __fsub_rn(b.hi[0], b.lo[0]);
@@ -77,7 +125,7 @@ __global__ void __launch_bounds__(kBlock8) k8_collapse(const Node* __restrict__ 
                                                        const uint32_t* __restrict__ frontier, uint32_t level_n,
                                                        uint32_t out_base, Node8Q* __restrict__ out,
                                                        int32_t* __restrict__ slots, unsigned long long* __restrict__ cnt,
-                                                       unsigned long long* __restrict__ bsum) {
+                                                       unsigned long long* __restrict__ bsum, uint32_t* err) {
     const uint32_t i = blockIdx.x * kBlock8 + threadIdx.x;
     unsigned long long c = 0;
     if (i < level_n) {
@@ -145,17 +193,18 @@ __global__ void __launch_bounds__(kBlock8) k8_collapse(const Node* __restrict__ 
             used |= 1u << bs;
         }
         // quantise
-        float scale[3];
+        float scale[3], org[3];
         uint32_t be[3];
         for (int a = 0; a < 3; ++a) {
-            const int e = pick_exponent(lo[a], hi[a]);
+            const int e = pick_exponent8(lo[a], hi[a], err);
             be[a] = (uint32_t)(e + 127);
             scale[a] = __uint_as_float(be[a] << 23);
+            org[a] = origin8_for(lo[a], e);
         }
         Node8Q o;
-        o.ox = lo[0];
-        o.oy = lo[1];
-        o.oz = lo[2];
+        o.ox = org[0];
+        o.oy = org[1];
+        o.oz = org[2];
         for (int w = 0; w < 12; ++w) o.q[w] = 0;
         uint32_t imask = 0;
         int32_t sref[8];
@@ -171,8 +220,8 @@ __global__ void __launch_bounds__(kBlock8) k8_collapse(const Node* __restrict__ 
                 ++n_leaf;
             }
             for (int a = 0; a < 3; ++a) {
-                o.q[4 * a + (s >> 2)] |= quant_lo(box[k].lo[a], scale[a], lo[a]) << (8 * (s & 3));
-                o.q[4 * a + 2 + (s >> 2)] |= quant_hi(box[k].hi[a], scale[a], lo[a]) << (8 * (s & 3));
+                o.q[4 * a + (s >> 2)] |= quant_lo8(box[k].lo[a], scale[a], org[a]) << (8 * (s & 3));
+                o.q[4 * a + 2 + (s >> 2)] |= quant_hi8(box[k].hi[a], scale[a], org[a]) << (8 * (s & 3));
             }
         }
         o.meta = be[0] | (be[1] << 8) | (be[2] << 16) | (imask << 24);
@@ -285,7 +334,7 @@ cudaError_t bvh8_build(BvhBuffers& b, uint32_t n, cudaStream_t s) {
         if (level >= kMaxLevels8 || out_base + (size_t)level_n > maxnodes) return cudaErrorInvalidValue;
         const uint32_t nb = (level_n + kBlock8 - 1) / kBlock8;
         k8_collapse<<<nb, kBlock8, 0, s>>>((const Node*)b.nodes.p, frontier[cur], level_n, out_base, staged, slots, cnt,
-                                           bsum);
+                                           bsum, &((BvhMeta*)b.meta.p)->err);
         k8_scan_blocks<<<1, kScanThreads, 0, s>>>(bsum, nb, total);
         k8_emit<<<nb, kBlock8, 0, s>>>(level_n, out_base, out_base + level_n, tri_cursor, staged, slots, cnt, bsum,
                                        frontier[cur ^ 1], (const Tri*)b.tris.p, (Tri*)b.tris8.p);

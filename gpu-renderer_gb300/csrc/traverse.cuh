@@ -334,10 +334,30 @@ __device__ __forceinline__ bool trace_step4(Lane& L, int2* s_stack, int2* l_stac
 
 // ---- 8-wide quantised nodes ----------------------------------------------------
 
-// Byte k of w as a float, exactly: the byte becomes the low mantissa bits of
-// 2^23 (one byte permute), then 2^23 is subtracted.
-__device__ __forceinline__ float qbyte(uint32_t w, int k) {
-    return __fsub_rn(__uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540u | (uint32_t)k)), 8388608.0f);
+// 2^23 + (byte k of w) as a float, exactly, in one byte permute: the byte
+// becomes the low mantissa bits of 2^23.
+__device__ __forceinline__ float qbyte23(uint32_t w, int k) {
+    return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540u | (uint32_t)k));
+}
+
+__device__ __forceinline__ float max3(float a, float b, float c) {
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+
+__device__ __forceinline__ float min3(float a, float b, float c) {
+    float r;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+
+// Bit k of an 8-bit mask moved to bit k ^ oct.
+__device__ __forceinline__ uint32_t xor_permute8(uint32_t x, uint32_t oct) {
+    if (oct & 1u) x = ((x & 0x55u) << 1) | ((x >> 1) & 0x55u);
+    if (oct & 2u) x = ((x & 0x33u) << 2) | ((x >> 2) & 0x33u);
+    if (oct & 4u) x = ((x & 0x0Fu) << 4) | ((x >> 4) & 0x0Fu);
+    return x;
 }
 
 template <int SSTACK>
@@ -355,13 +375,16 @@ __device__ __forceinline__ void stack_put(int i, int2 v, int2* s_stack, int2* l_
 template <bool ANY>
 __device__ __forceinline__ bool leaf_at(Lane& L, uint32_t idx) { return leaf<ANY>(L, ~(int32_t)idx); }
 
-// One 8-wide node. Each plane is decoded as fma(q, 2^e, origin), exactly as
-// the builder quantised it, then measured like an FP32 plane; the near plane
-// of an axis is lo when d >= 0, else hi. Hit leaf
-// triangles are tested in slot order; hit inner children are ranked by
-// slot ^ octant and the lowest rank is visited next. The remaining inner hits
-// stay on the stack as one group entry (child_base, inner mask | hits << 8),
-// taken one child at a time. Returns true when the ray is finished.
+// One 8-wide node. Each plane is decoded as fma(2^23 + q, 2^e, origin8),
+// exactly as the builder quantised it, and measured like an FP32 plane; the
+// near plane of an axis is lo when d >= 0, else hi. The slack is folded into
+// the far side: far planes are measured with (1/d) * slack and the closest-hit
+// bound is best_t * slack, so a child is hit when max(near, tmin) <=
+// min(far, bound). Hit leaf triangles are tested in slot order; hit inner
+// children are ranked by slot ^ octant and the lowest rank is visited next.
+// The remaining inner hits stay on the stack as one group entry (child_base,
+// inner mask | hits << 8), taken one child at a time. Returns true when the
+// ray is finished.
 template <bool ANY, int SSTACK>
 __device__ __forceinline__ bool trace_step8(Lane& L, int2* s_stack, int2* l_stack, uint32_t* err) {
     const float4* q = reinterpret_cast<const float4*>(static_cast<const Node8Q*>(L.nodes) + L.node);
@@ -378,6 +401,9 @@ __device__ __forceinline__ bool trace_step8(Lane& L, int2* s_stack, int2* l_stac
     const float scx = __uint_as_float((meta & 0xFFu) << 23);
     const float scy = __uint_as_float(((meta >> 8) & 0xFFu) << 23);
     const float scz = __uint_as_float(((meta >> 16) & 0xFFu) << 23);
+    const float fix = __fmul_rn(L.p.ix, kCullSlack), fiy = __fmul_rn(L.p.iy, kCullSlack);
+    const float fiz = __fmul_rn(L.p.iz, kCullSlack);
+    const float bound = __fmul_rn(L.best_t, kCullSlack);
     // words: b0 = (lo.x[0-3], lo.x[4-7], hi.x[0-3], hi.x[4-7]), b1 the same for y, c0 for z
     const uint32_t lx0 = __float_as_uint(b0.x), lx1 = __float_as_uint(b0.y);
     const uint32_t hx0 = __float_as_uint(b0.z), hx1 = __float_as_uint(b0.w);
@@ -388,23 +414,23 @@ __device__ __forceinline__ bool trace_step8(Lane& L, int2* s_stack, int2* l_stac
     const uint32_t nx0 = sx ? hx0 : lx0, nx1 = sx ? hx1 : lx1, fx0 = sx ? lx0 : hx0, fx1 = sx ? lx1 : hx1;
     const uint32_t ny0 = sy ? hy0 : ly0, ny1 = sy ? hy1 : ly1, fy0 = sy ? ly0 : hy0, fy1 = sy ? ly1 : hy1;
     const uint32_t nz0 = sz ? hz0 : lz0, nz1 = sz ? hz1 : lz1, fz0 = sz ? lz0 : hz0, fz1 = sz ? lz1 : hz1;
-    uint32_t ihits = 0, thits = 0;
+    uint32_t hm = 0;
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
         const int b = k & 3;
-        const float tnx = plane_t(__fmaf_rn(qbyte(k < 4 ? nx0 : nx1, b), scx, h0.x), L.p.ox, L.p.ix);
-        const float tfx = plane_t(__fmaf_rn(qbyte(k < 4 ? fx0 : fx1, b), scx, h0.x), L.p.ox, L.p.ix);
-        const float tny = plane_t(__fmaf_rn(qbyte(k < 4 ? ny0 : ny1, b), scy, h0.y), L.p.oy, L.p.iy);
-        const float tfy = plane_t(__fmaf_rn(qbyte(k < 4 ? fy0 : fy1, b), scy, h0.y), L.p.oy, L.p.iy);
-        const float tnz = plane_t(__fmaf_rn(qbyte(k < 4 ? nz0 : nz1, b), scz, h0.z), L.p.oz, L.p.iz);
-        const float tfz = plane_t(__fmaf_rn(qbyte(k < 4 ? fz0 : fz1, b), scz, h0.z), L.p.oz, L.p.iz);
-        const float tnear = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, L.p.tmin));
-        const float tfar = fminf(fminf(tfx, tfy), fminf(tfz, L.best_t));
-        if (((valid >> k) & 1u) && tnear <= __fmul_rn(tfar, kCullSlack)) {
-            if ((imask >> k) & 1u) ihits |= 1u << (k ^ oct);
-            else thits |= 1u << k;
-        }
+        const float tnx = plane_t(__fmaf_rn(qbyte23(k < 4 ? nx0 : nx1, b), scx, h0.x), L.p.ox, L.p.ix);
+        const float tfx = plane_t(__fmaf_rn(qbyte23(k < 4 ? fx0 : fx1, b), scx, h0.x), L.p.ox, fix);
+        const float tny = plane_t(__fmaf_rn(qbyte23(k < 4 ? ny0 : ny1, b), scy, h0.y), L.p.oy, L.p.iy);
+        const float tfy = plane_t(__fmaf_rn(qbyte23(k < 4 ? fy0 : fy1, b), scy, h0.y), L.p.oy, fiy);
+        const float tnz = plane_t(__fmaf_rn(qbyte23(k < 4 ? nz0 : nz1, b), scz, h0.z), L.p.oz, L.p.iz);
+        const float tfz = plane_t(__fmaf_rn(qbyte23(k < 4 ? fz0 : fz1, b), scz, h0.z), L.p.oz, fiz);
+        const float tnear = fmaxf(max3(tnx, tny, tnz), L.p.tmin);
+        const float tfar = fminf(min3(tfx, tfy, tfz), bound);
+        hm |= (tnear <= tfar ? 1u : 0u) << k;
     }
+    hm &= valid;
+    uint32_t thits = hm & ~imask;
+    const uint32_t ihits = xor_permute8(hm & imask, oct);
     if (thits) {
         const uint32_t leafmask = valid & ~imask;
         do {
