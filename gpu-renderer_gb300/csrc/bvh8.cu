@@ -8,9 +8,9 @@
 // high side along axis a", chosen greedily by the score
 // sum_a (+/-)(child centre - node centre)_a, so that a ray visiting inner
 // children in order of (slot ^ octant) goes roughly near to far. Boxes are
-// quantised outward against the layout's decode fma(2^23 + q, 2^e, origin8)
-// (origin8 = lo - 2^(23+e) rounded down), which the traversal evaluates with
-// one byte permute and one FMA per plane.
+// quantised outward against the exact planes q * 2^e + lo (lo the node's
+// lower corner), whose ray distances the traversal measures with one FMA per
+// plane.
 //
 // Nodes are numbered breadth first, level by level: a level's nodes are
 // collapsed (one thread each), their inner-child and leaf counts are prefix-
@@ -34,18 +34,26 @@ constexpr int kScanThreads = 1024;
 constexpr int32_t kEmptySlot = INT32_MIN;
 constexpr int kMaxLevels8 = 72;
 
-// 8-wide decode: plane(q) = fma(2^23 + q, 2^e, origin8) with
-// origin8 = round_down(lo - 2^(23+e)), so the traversal turns a byte into
-// 2^23 + q with one byte permute and decodes with one FMA. Rounding origin8
-// down keeps plane(0) <= lo; e grows until plane(255) >= hi.
-constexpr int kMaxExp8 = 104;  // 2^(23+e) stays finite
+// 8-wide planes: plane(q) = q * 2^e + lo, taken EXACTLY (the traversal
+// measures it as fma(q, 2^e / d, (lo - o) / d) with error margins, never
+// rounding the plane itself); e grows until plane(255) >= hi. q * 2^e is a
+// float, so each comparison of a plane with a coordinate is decided exactly
+// from the rounded sum and its two-sum error.
+constexpr int kMaxExp8 = 119;  // 255 * 2^e stays finite
 
-__device__ __forceinline__ float decode8(int q, float scale, float origin8) {
-    return __fmaf_rn(__int2float_rn(8388608 + q), scale, origin8);
+__device__ __forceinline__ float pow2f(int e) { return __uint_as_float((uint32_t)(e + 127) << 23); }
+
+// Sign of (a + b) - v, exactly: -1, 0 or +1.
+__device__ __forceinline__ int cmp_sum(float a, float b, float v) {
+    const float s = __fadd_rn(a, b);
+    if (s != v) return s < v ? -1 : 1;
+    const float bp = __fsub_rn(s, a);
+    const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bp)), __fsub_rn(b, bp));
+    return e < 0.0f ? -1 : (e > 0.0f ? 1 : 0);
 }
 
-__device__ __forceinline__ float origin8_for(float lo, int e) {
-    return __fsub_rd(lo, __uint_as_float((uint32_t)(e + 23 + 127) << 23));
+__device__ __forceinline__ int cmp_plane(int q, float scale, float lo, float v) {
+    return cmp_sum(__fmul_rn((float)q, scale), lo, v);
 }
 
 __device__ __forceinline__ int pick_exponent8(float lo, float hi, uint32_t* err) {
@@ -56,9 +64,9 @@ __device__ __forceinline__ int pick_exponent8(float lo, float hi, uint32_t* err)
         frexpf(__fdiv_rn(extent, 255.0f), &ex);
         e = max(-126, min(kMaxExp8, ex - 1));
     }
-    while (decode8(255, __uint_as_float((uint32_t)(e + 127) << 23), origin8_for(lo, e)) < hi) {
+    while (cmp_plane(255, pow2f(e), lo, hi) < 0) {
         if (e >= kMaxExp8) {
-            atomicOr(err, ERR_RANGE);  // coordinates beyond about 2^126: not representable
+            atomicOr(err, ERR_RANGE);  // extent beyond about 2^127: not representable
             break;
         }
         ++e;
@@ -66,17 +74,17 @@ __device__ __forceinline__ int pick_exponent8(float lo, float hi, uint32_t* err)
     return e;
 }
 
-__device__ __forceinline__ uint32_t quant_lo8(float v, float scale, float origin8) {
+__device__ __forceinline__ uint32_t quant_lo8(float v, float scale, float lo) {
     int q = 0;
-    for (int step = 128; step > 0; step >>= 1)  // largest q with plane(q) <= v (plane(0) <= v)
-        if (q + step <= 255 && decode8(q + step, scale, origin8) <= v) q += step;
+    for (int step = 128; step > 0; step >>= 1)  // largest q with plane(q) <= v (plane(0) = lo <= v)
+        if (q + step <= 255 && cmp_plane(q + step, scale, lo, v) <= 0) q += step;
     return (uint32_t)q;
 }
 
-__device__ __forceinline__ uint32_t quant_hi8(float v, float scale, float origin8) {
+__device__ __forceinline__ uint32_t quant_hi8(float v, float scale, float lo) {
     int q = 255;
     for (int step = 128; step > 0; step >>= 1)  // smallest q with plane(q) >= v (plane(255) >= v)
-        if (q - step >= 0 && decode8(q - step, scale, origin8) >= v) q -= step;
+        if (q - step >= 0 && cmp_plane(q - step, scale, lo, v) >= 0) q -= step;
     return (uint32_t)q;
 }
 
@@ -193,18 +201,17 @@ __global__ void __launch_bounds__(kBlock8) k8_collapse(const Node* __restrict__ 
             used |= 1u << bs;
         }
         // quantise
-        float scale[3], org[3];
+        float scale[3];
         uint32_t be[3];
         for (int a = 0; a < 3; ++a) {
             const int e = pick_exponent8(lo[a], hi[a], err);
             be[a] = (uint32_t)(e + 127);
             scale[a] = __uint_as_float(be[a] << 23);
-            org[a] = origin8_for(lo[a], e);
         }
         Node8Q o;
-        o.ox = org[0];
-        o.oy = org[1];
-        o.oz = org[2];
+        o.ox = lo[0];
+        o.oy = lo[1];
+        o.oz = lo[2];
         for (int w = 0; w < 12; ++w) o.q[w] = 0;
         uint32_t imask = 0;
         int32_t sref[8];
@@ -220,8 +227,8 @@ __global__ void __launch_bounds__(kBlock8) k8_collapse(const Node* __restrict__ 
                 ++n_leaf;
             }
             for (int a = 0; a < 3; ++a) {
-                o.q[4 * a + (s >> 2)] |= quant_lo8(box[k].lo[a], scale[a], org[a]) << (8 * (s & 3));
-                o.q[4 * a + 2 + (s >> 2)] |= quant_hi8(box[k].hi[a], scale[a], org[a]) << (8 * (s & 3));
+                o.q[4 * a + (s >> 2)] |= quant_lo8(box[k].lo[a], scale[a], lo[a]) << (8 * (s & 3));
+                o.q[4 * a + 2 + (s >> 2)] |= quant_hi8(box[k].hi[a], scale[a], lo[a]) << (8 * (s & 3));
             }
         }
         o.meta = be[0] | (be[1] << 8) | (be[2] << 16) | (imask << 24);

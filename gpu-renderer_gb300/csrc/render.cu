@@ -266,7 +266,7 @@ __global__ void __launch_bounds__(trav::kMaxTraceThreads) k_trace_queue(Paths ps
     extern __shared__ int2 s_stack[];
     if (b > (int)ps.hdr->max_depth) return;
     QueueSrc src{(b & 1) ? ps.qb : ps.qa, &ps, ps.cnt[b]};
-    trav::traverse_loop<false, LAYOUT, SSTACK>(src, ps.work + b, ps.cnt + kErrWord, s_stack);
+    trav::traverse_loop<false, LAYOUT, SSTACK, trav::kRefillQueue>(src, ps.work + b, ps.cnt + kErrWord, s_stack);
 }
 
 // Shadow rays: an unoccluded ray adds its contribution to its path
@@ -300,7 +300,8 @@ __global__ void __launch_bounds__(trav::kMaxTraceThreads) k_trace_shadow(Paths p
     extern __shared__ int2 s_stack[];
     if (b >= (int)ps.hdr->max_depth) return;
     ShadowSrc src{&ps, ps.cnt[kShadowBase + b]};
-    trav::traverse_loop<true, LAYOUT, SSTACK>(src, ps.work + kShadowBase + b, ps.cnt + kErrWord, s_stack);
+    trav::traverse_loop<true, LAYOUT, SSTACK, trav::kRefillQueue>(src, ps.work + kShadowBase + b, ps.cnt + kErrWord,
+                                                                   s_stack);
 }
 
 // ---- shading --------------------------------------------------------------------------

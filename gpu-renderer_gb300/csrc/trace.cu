@@ -5,7 +5,7 @@
 // :175-308). Differences by design:
 //   - persistent warps with dynamic refill: a fixed grid of warps pulls rays
 //     from a global counter, and a warp refills its idle lanes whenever at
-//     least kRefillLanes of them have finished, until the queue is drained;
+//     least kRefillRays of them have finished, until the queue is drained;
 //   - child boxes live in the parent node and are fetched as 32-byte vector
 //     loads; all children are tested at once and the nearest is visited first;
 //   - a short per-thread stack in shared memory (8, 12 or 16 entries, chosen by
@@ -51,7 +51,7 @@ __global__ void __launch_bounds__(trav::kMaxTraceThreads) k_trace(const void* __
                                                                   uint32_t* err) {
     extern __shared__ int2 s_stack[];
     RaySrc src{rays, hits, n, nodes, tris, meta->root};
-    trav::traverse_loop<ANY, LAYOUT, SSTACK>(src, counter, err, s_stack);
+    trav::traverse_loop<ANY, LAYOUT, SSTACK, trav::kRefillRays>(src, counter, err, s_stack);
 }
 
 template <bool ANY, int LAYOUT, int SSTACK>

@@ -334,10 +334,10 @@ __device__ __forceinline__ bool trace_step4(Lane& L, int2* s_stack, int2* l_stac
 
 // ---- 8-wide quantised nodes ----------------------------------------------------
 
-// 2^23 + (byte k of w) as a float, exactly, in one byte permute: the byte
-// becomes the low mantissa bits of 2^23.
-__device__ __forceinline__ float qbyte23(uint32_t w, int k) {
-    return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540u | (uint32_t)k));
+// Byte k of w as a float, exactly: the byte becomes the low mantissa bits of
+// 2^23 (one byte permute), then 2^23 is subtracted.
+__device__ __forceinline__ float qbyte(uint32_t w, int k) {
+    return __fsub_rn(__uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540u | (uint32_t)k)), 8388608.0f);
 }
 
 __device__ __forceinline__ float max3(float a, float b, float c) {
@@ -350,6 +350,17 @@ __device__ __forceinline__ float min3(float a, float b, float c) {
     float r;
     asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
     return r;
+}
+
+// Per node and axis: S = 2^e * (1/d), C = (lo - o) * (1/d), and the near /
+// far offsets C -+ m with m = |C| * 2^-21 + |S| * 2^-14.
+__device__ __forceinline__ void axis_terms8(uint32_t biased_e, float lo, float o, float inv, float& S, float& cn,
+                                            float& cf) {
+    S = __fmul_rn(__uint_as_float(biased_e << 23), inv);
+    const float C = __fmul_rn(__fsub_rn(lo, o), inv);
+    const float m = __fmaf_rn(fabsf(C), 0x1p-21f, __fmul_rn(fabsf(S), 0x1p-14f));
+    cn = __fsub_rn(C, m);
+    cf = __fadd_rn(C, m);
 }
 
 // Bit k of an 8-bit mask moved to bit k ^ oct.
@@ -375,16 +386,18 @@ __device__ __forceinline__ void stack_put(int i, int2 v, int2* s_stack, int2* l_
 template <bool ANY>
 __device__ __forceinline__ bool leaf_at(Lane& L, uint32_t idx) { return leaf<ANY>(L, ~(int32_t)idx); }
 
-// One 8-wide node. Each plane is decoded as fma(2^23 + q, 2^e, origin8),
-// exactly as the builder quantised it, and measured like an FP32 plane; the
-// near plane of an axis is lo when d >= 0, else hi. The slack is folded into
-// the far side: far planes are measured with (1/d) * slack and the closest-hit
-// bound is best_t * slack, so a child is hit when max(near, tmin) <=
-// min(far, bound). Hit leaf triangles are tested in slot order; hit inner
-// children are ranked by slot ^ octant and the lowest rank is visited next.
-// The remaining inner hits stay on the stack as one group entry (child_base,
-// inner mask | hits << 8), taken one child at a time. Returns true when the
-// ray is finished.
+// One 8-wide node. A child plane is q * 2^e + lo, taken exactly; its ray
+// distance is measured as fma(q, S, C) with S = 2^e / d (exact: a power-of-two
+// scaling) and C = (lo - o) / d, evaluated once per node and axis. The
+// rounding of C, of the offsets and of the final FMA stays below
+// |C| * 2^-22 + |S| * 2^-16, so near planes use C - m and far planes C + m
+// with m = |C| * 2^-21 + |S| * 2^-14: the measured interval always contains
+// the quantised box's. The near plane of an axis is lo when d >= 0, else hi.
+// A child is hit when max(near, tmin) <= min(far, best_t * slack). Hit leaf
+// triangles are tested in slot order; hit inner children are ranked by
+// slot ^ octant and the lowest rank is visited next. The remaining inner hits
+// stay on the stack as one group entry (child_base, inner mask | hits << 8),
+// taken one child at a time. Returns true when the ray is finished.
 template <bool ANY, int SSTACK>
 __device__ __forceinline__ bool trace_step8(Lane& L, int2* s_stack, int2* l_stack, uint32_t* err) {
     const float4* q = reinterpret_cast<const float4*>(static_cast<const Node8Q*>(L.nodes) + L.node);
@@ -398,11 +411,10 @@ __device__ __forceinline__ bool trace_step8(Lane& L, int2* s_stack, int2* l_stac
     const uint32_t sx = __float_as_uint(L.p.ix) >> 31, sy = __float_as_uint(L.p.iy) >> 31;
     const uint32_t sz = __float_as_uint(L.p.iz) >> 31;
     const uint32_t oct = sx | (sy << 1) | (sz << 2);
-    const float scx = __uint_as_float((meta & 0xFFu) << 23);
-    const float scy = __uint_as_float(((meta >> 8) & 0xFFu) << 23);
-    const float scz = __uint_as_float(((meta >> 16) & 0xFFu) << 23);
-    const float fix = __fmul_rn(L.p.ix, kCullSlack), fiy = __fmul_rn(L.p.iy, kCullSlack);
-    const float fiz = __fmul_rn(L.p.iz, kCullSlack);
+    float Sx, Sy, Sz, cnx, cfx, cny, cfy, cnz, cfz;
+    axis_terms8(meta & 0xFFu, h0.x, L.p.ox, L.p.ix, Sx, cnx, cfx);
+    axis_terms8((meta >> 8) & 0xFFu, h0.y, L.p.oy, L.p.iy, Sy, cny, cfy);
+    axis_terms8((meta >> 16) & 0xFFu, h0.z, L.p.oz, L.p.iz, Sz, cnz, cfz);
     const float bound = __fmul_rn(L.best_t, kCullSlack);
     // words: b0 = (lo.x[0-3], lo.x[4-7], hi.x[0-3], hi.x[4-7]), b1 the same for y, c0 for z
     const uint32_t lx0 = __float_as_uint(b0.x), lx1 = __float_as_uint(b0.y);
@@ -418,12 +430,12 @@ __device__ __forceinline__ bool trace_step8(Lane& L, int2* s_stack, int2* l_stac
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
         const int b = k & 3;
-        const float tnx = plane_t(__fmaf_rn(qbyte23(k < 4 ? nx0 : nx1, b), scx, h0.x), L.p.ox, L.p.ix);
-        const float tfx = plane_t(__fmaf_rn(qbyte23(k < 4 ? fx0 : fx1, b), scx, h0.x), L.p.ox, fix);
-        const float tny = plane_t(__fmaf_rn(qbyte23(k < 4 ? ny0 : ny1, b), scy, h0.y), L.p.oy, L.p.iy);
-        const float tfy = plane_t(__fmaf_rn(qbyte23(k < 4 ? fy0 : fy1, b), scy, h0.y), L.p.oy, fiy);
-        const float tnz = plane_t(__fmaf_rn(qbyte23(k < 4 ? nz0 : nz1, b), scz, h0.z), L.p.oz, L.p.iz);
-        const float tfz = plane_t(__fmaf_rn(qbyte23(k < 4 ? fz0 : fz1, b), scz, h0.z), L.p.oz, fiz);
+        const float tnx = __fmaf_rn(qbyte(k < 4 ? nx0 : nx1, b), Sx, cnx);
+        const float tfx = __fmaf_rn(qbyte(k < 4 ? fx0 : fx1, b), Sx, cfx);
+        const float tny = __fmaf_rn(qbyte(k < 4 ? ny0 : ny1, b), Sy, cny);
+        const float tfy = __fmaf_rn(qbyte(k < 4 ? fy0 : fy1, b), Sy, cfy);
+        const float tnz = __fmaf_rn(qbyte(k < 4 ? nz0 : nz1, b), Sz, cnz);
+        const float tfz = __fmaf_rn(qbyte(k < 4 ? fz0 : fz1, b), Sz, cfz);
         const float tnear = fmaxf(max3(tnx, tny, tnz), L.p.tmin);
         const float tfar = fminf(min3(tfx, tfy, tfz), bound);
         hm |= (tnear <= tfar ? 1u : 0u) << k;
@@ -472,8 +484,11 @@ __device__ __forceinline__ bool trace_step(Lane& L, int2* s_stack, int2* l_stack
     return trace_step4<ANY, LAYOUT == kLayoutBvh4Q8, SSTACK>(L, s_stack, l_stack, err);
 }
 
-// Refill when at least this many lanes of a warp are idle.
-constexpr int kRefillLanes = 8;
+// A warp refills its idle lanes once at least REFILL of them are idle. The
+// ray-query kernels use 4 (a ray loads in two 16-byte reads); the render's
+// queue kernels use 8 (a queued path also looks up its job and scene).
+constexpr int kRefillRays = 4;
+constexpr int kRefillQueue = 8;
 
 // Persistent dynamic-fetch loop. `Src` supplies the work:
 //   uint64_t n                                        number of rays
@@ -485,7 +500,7 @@ constexpr int kRefillLanes = 8;
 //   void finish(uint64_t i, const Lane& L)            ray i is done (L.best_prim ==
 //                                                     0xFFFFFFFF means a miss)
 // The shared stack has SSTACK x blockDim.x int2 entries (dynamic shared memory).
-template <bool ANY, int LAYOUT, int SSTACK, class Src>
+template <bool ANY, int LAYOUT, int SSTACK, int REFILL, class Src>
 __device__ __forceinline__ void traverse_loop(Src& src, unsigned long long* counter, uint32_t* err, int2* s_stack) {
     int2 l_stack[kStackMax - SSTACK];
     const int lane = threadIdx.x & 31;
@@ -497,7 +512,7 @@ __device__ __forceinline__ void traverse_loop(Src& src, unsigned long long* coun
     for (;;) {
         const uint32_t idle = __ballot_sync(0xFFFFFFFFu, !active);
         const int nidle = __popc(idle);
-        if (!exhausted && (nidle >= kRefillLanes || nidle == 32)) {
+        if (!exhausted && (nidle >= REFILL || nidle == 32)) {
             unsigned long long base = 0;
             if (lane == 0) base = atomicAdd(counter, (unsigned long long)nidle);
             base = __shfl_sync(0xFFFFFFFFu, base, 0);

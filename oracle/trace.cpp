@@ -445,22 +445,20 @@ inline float half_area(const CB& b) {
 }
 
 constexpr int32_t kEmpty8 = std::numeric_limits<int32_t>::min();
-constexpr int kMaxExp8 = 104;
+constexpr int kMaxExp8 = 119;
 
-// 8-wide decode: plane(q) = fma(2^23 + q, 2^e, origin8), origin8 = lo - 2^(23+e)
-// rounded toward -inf (the rounding error of the difference, from the
-// error-free two-sum, decides whether the nearest float must step down).
-inline float decode8(int q, float scale, float origin8) { return std::fmaf((float)(8388608 + q), scale, origin8); }
-
-inline float sub_round_down(float a, float b) {
-    const float s = a - b;
-    const float nb = -b;
+// 8-wide planes: plane(q) = q * 2^e + lo taken exactly. q * 2^e is a float,
+// so a plane compares with a coordinate exactly through the rounded sum and
+// its two-sum error.
+inline int cmp_sum(float a, float b, float v) {
+    const float s = a + b;
+    if (s != v) return s < v ? -1 : 1;
     const float bp = s - a;
-    const float err = (a - (s - bp)) + (nb - bp);
-    return err < 0.0f ? std::nextafter(s, -std::numeric_limits<float>::infinity()) : s;
+    const float e = (a - (s - bp)) + (b - bp);
+    return e < 0.0f ? -1 : (e > 0.0f ? 1 : 0);
 }
 
-inline float origin8_for(float lo, int e) { return sub_round_down(lo, pow2(e + 23)); }
+inline int cmp_plane(int q, float scale, float lo, float v) { return cmp_sum((float)q * scale, lo, v); }
 
 inline int pick_exponent8(float lo, float hi) {
     const float extent = hi - lo;
@@ -470,24 +468,24 @@ inline int pick_exponent8(float lo, float hi) {
         std::frexp(extent / 255.0f, &ex);
         e = std::max(-126, std::min(kMaxExp8, ex - 1));
     }
-    while (decode8(255, pow2(e), origin8_for(lo, e)) < hi) {
+    while (cmp_plane(255, pow2(e), lo, hi) < 0) {
         if (e >= kMaxExp8) break;
         ++e;
     }
     return e;
 }
 
-inline uint32_t quant_lo8(float v, float scale, float origin8) {
+inline uint32_t quant_lo8(float v, float scale, float lo) {
     int q = 0;
     for (int step = 128; step > 0; step >>= 1)
-        if (q + step <= 255 && decode8(q + step, scale, origin8) <= v) q += step;
+        if (q + step <= 255 && cmp_plane(q + step, scale, lo, v) <= 0) q += step;
     return (uint32_t)q;
 }
 
-inline uint32_t quant_hi8(float v, float scale, float origin8) {
+inline uint32_t quant_hi8(float v, float scale, float lo) {
     int q = 255;
     for (int step = 128; step > 0; step >>= 1)
-        if (q - step >= 0 && decode8(q - step, scale, origin8) >= v) q -= step;
+        if (q - step >= 0 && cmp_plane(q - step, scale, lo, v) >= 0) q -= step;
     return (uint32_t)q;
 }
 
@@ -556,18 +554,17 @@ void build8(const uint32_t* nodes, const float* tris, uint32_t root, std::vector
                 slot_of[bk] = bs;
                 used |= 1u << bs;
             }
-            float scale[3], org[3];
+            float scale[3];
             uint32_t be[3];
             for (int a = 0; a < 3; ++a) {
                 const int e = pick_exponent8(lo[a], hi[a]);
                 be[a] = (uint32_t)(e + 127);
                 scale[a] = f_of(be[a] << 23);
-                org[a] = origin8_for(lo[a], e);
             }
             uint32_t* o = out.data() + 24ull * (out_base + i);
-            o[0] = w_of(org[0]);
-            o[1] = w_of(org[1]);
-            o[2] = w_of(org[2]);
+            o[0] = w_of(lo[0]);
+            o[1] = w_of(lo[1]);
+            o[2] = w_of(lo[2]);
             int32_t sref[8];
             for (int s2 = 0; s2 < 8; ++s2) sref[s2] = kEmpty8;
             uint32_t imask = 0, ni = 0, nl = 0;
@@ -576,8 +573,8 @@ void build8(const uint32_t* nodes, const float* tris, uint32_t root, std::vector
                 sref[s2] = ref[k];
                 if (ref[k] >= 0) { imask |= 1u << s2; ++ni; } else { ++nl; }
                 for (int a = 0; a < 3; ++a) {
-                    o[8 + 4 * a + (s2 >> 2)] |= quant_lo8(box[k].lo[a], scale[a], org[a]) << (8 * (s2 & 3));
-                    o[8 + 4 * a + 2 + (s2 >> 2)] |= quant_hi8(box[k].hi[a], scale[a], org[a]) << (8 * (s2 & 3));
+                    o[8 + 4 * a + (s2 >> 2)] |= quant_lo8(box[k].lo[a], scale[a], lo[a]) << (8 * (s2 & 3));
+                    o[8 + 4 * a + 2 + (s2 >> 2)] |= quant_hi8(box[k].hi[a], scale[a], lo[a]) << (8 * (s2 & 3));
                 }
             }
             o[3] = be[0] | (be[1] << 8) | (be[2] << 16) | (imask << 24);
@@ -626,12 +623,15 @@ void trace8_one(const uint32_t* nodes, const float* tris, uint32_t root, const f
         const uint32_t* o = nodes + 24ull * node;
         ++visits;
         const uint32_t meta = o[3], child_base = o[4], tri_base = o[5], valid = o[6], imask = meta >> 24;
-        float scl[3], fi[3];
+        float S[3], cn[3], cf[3];
         uint32_t nw[3][2], fw[3][2];
         const float bound = b.t * kCullSlack;
         for (int a = 0; a < 3; ++a) {
-            scl[a] = f_of(((meta >> (8 * a)) & 0xFFu) << 23);
-            fi[a] = p.idir[a] * kCullSlack;
+            S[a] = f_of(((meta >> (8 * a)) & 0xFFu) << 23) * p.idir[a];
+            const float C = (f_of(o[a]) - p.o[a]) * p.idir[a];
+            const float m = std::fmaf(std::fabs(C), 0x1p-21f, std::fabs(S[a]) * 0x1p-14f);
+            cn[a] = C - m;
+            cf[a] = C + m;
             for (int h = 0; h < 2; ++h) {
                 const uint32_t lo = o[8 + 4 * a + h], hi = o[8 + 4 * a + 2 + h];
                 nw[a][h] = sg[a] ? hi : lo;
@@ -642,8 +642,8 @@ void trace8_one(const uint32_t* nodes, const float* tris, uint32_t root, const f
         for (int k = 0; k < 8; ++k) {
             float tn[3], tf[3];
             for (int a = 0; a < 3; ++a) {
-                tn[a] = plane_t(decode8((int)byte_of(nw[a][k >> 2], k & 3), scl[a], f_of(o[a])), p.o[a], p.idir[a]);
-                tf[a] = plane_t(decode8((int)byte_of(fw[a][k >> 2], k & 3), scl[a], f_of(o[a])), p.o[a], fi[a]);
+                tn[a] = std::fmaf((float)byte_of(nw[a][k >> 2], k & 3), S[a], cn[a]);
+                tf[a] = std::fmaf((float)byte_of(fw[a][k >> 2], k & 3), S[a], cf[a]);
             }
             const float tnear = std::fmax(std::fmax(std::fmax(tn[0], tn[1]), tn[2]), p.tmin);
             const float tfar = std::fmin(std::fmin(std::fmin(tf[0], tf[1]), tf[2]), bound);
