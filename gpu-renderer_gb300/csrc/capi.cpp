@@ -36,7 +36,9 @@ void context_free(gr_ctx* ctx) {
     ctx->counter.release();
     ctx->stage_in.release();
     ctx->stage_out.release();
+    if (ctx->stream2) cudaStreamSynchronize(ctx->stream2);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    if (ctx->stream2) cudaStreamDestroy(ctx->stream2);
     delete ctx;
 }
 
@@ -164,6 +166,7 @@ gr_status gr_context_create(int device, gr_ctx** out) {
     cudaError_t e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream2, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = ctx->counter.ensure(256);
     if (e == cudaSuccess) e = cudaMemset(ctx->counter.p, 0, 256);
     if (e != cudaSuccess) {
@@ -268,12 +271,16 @@ gr_status gr_bvh_export(gr_bvh* bvh, uint32_t* h_sorted_prim, uint32_t* h_sorted
     return GR_OK;
 }
 
-gr_status gr_trace(gr_bvh* bvh, const gr_ray* d_rays, uint64_t n, gr_hit* d_hits, int any_hit, void* stream) {
-    if (!bvh || !bvh->built) return GR_ERR_INVALID;
-    if (n > 0 && (!d_rays || !d_hits)) return fail(bvh->ctx, GR_ERR_INVALID, "null ray or hit pointer");
+}  // extern "C"
+
+namespace {
+
+// One traversal launch with the work counter at `counter_offset` of the
+// context's counter buffer.
+gr_status trace_on(gr_bvh* bvh, const gr_ray* d_rays, uint64_t n, gr_hit* d_hits, int any_hit, cudaStream_t s,
+                   size_t counter_offset) {
     gr_ctx* ctx = bvh->ctx;
-    GR_CUDA(ctx, cudaSetDevice(ctx->device));
-    unsigned long long* counter = (unsigned long long*)ctx->counter.p;
+    unsigned long long* counter = (unsigned long long*)((char*)ctx->counter.p + counter_offset);
     uint32_t* err = (uint32_t*)((char*)ctx->counter.p + 64);
     gr::TraceTuning tune;
     tune.layout = bvh->layout;
@@ -282,26 +289,61 @@ gr_status gr_trace(gr_bvh* bvh, const gr_ray* d_rays, uint64_t n, gr_hit* d_hits
     gr::BvhDevice view = device_view(bvh);
     view.tris = gr::layout_tris(bvh, bvh->layout);
     GR_CUDA(ctx, gr::trace_launch(view, gr::layout_nodes(bvh, bvh->layout), tune, d_rays, n, d_hits, any_hit, counter,
-                                  err, ctx->num_sms, as_stream(stream)));
+                                  err, ctx->num_sms, s));
     return GR_OK;
 }
 
+}  // namespace
+
+extern "C" {
+
+gr_status gr_trace(gr_bvh* bvh, const gr_ray* d_rays, uint64_t n, gr_hit* d_hits, int any_hit, void* stream) {
+    if (!bvh || !bvh->built) return GR_ERR_INVALID;
+    if (n > 0 && (!d_rays || !d_hits)) return fail(bvh->ctx, GR_ERR_INVALID, "null ray or hit pointer");
+    GR_CUDA(bvh->ctx, cudaSetDevice(bvh->ctx->device));
+    return trace_on(bvh, d_rays, n, d_hits, any_hit, as_stream(stream), 0);
+}
+
+// Host-memory traversal, pipelined: the rays are cut into chunks of at least
+// 1 Mi rays (at most 8 chunks); chunk k goes to one of two streams (k & 1)
+// as copy-in, traversal, copy-out, so one chunk's copies overlap another
+// chunk's traversal. Each stream has its own work counter.
 gr_status gr_trace_host(gr_bvh* bvh, const gr_ray* h_rays, uint64_t n, gr_hit* h_hits, int any_hit) {
     if (!bvh || !bvh->built) return GR_ERR_INVALID;
     if (n > 0 && (!h_rays || !h_hits)) return fail(bvh->ctx, GR_ERR_INVALID, "null ray or hit pointer");
     gr_ctx* ctx = bvh->ctx;
     GR_CUDA(ctx, cudaSetDevice(ctx->device));
     if (n == 0) return GR_OK;
-    cudaStream_t s = ctx->stream;
     gr::DevBuf& dr = ctx->stage_in;
     gr::DevBuf& dh = ctx->stage_out;
     GR_CUDA(ctx, dr.ensure(sizeof(gr_ray) * n));
     GR_CUDA(ctx, dh.ensure(sizeof(gr_hit) * n));
-    GR_CUDA(ctx, cudaMemcpyAsync(dr.p, h_rays, sizeof(gr_ray) * n, cudaMemcpyHostToDevice, s));
-    gr_status st = gr_trace(bvh, (const gr_ray*)dr.p, n, (gr_hit*)dh.p, any_hit, s);
-    if (st != GR_OK) return st;
-    GR_CUDA(ctx, cudaMemcpyAsync(h_hits, dh.p, sizeof(gr_hit) * n, cudaMemcpyDeviceToHost, s));
-    GR_CUDA(ctx, cudaStreamSynchronize(s));
+    const uint64_t chunk = std::max<uint64_t>(1ull << 20, (n + 7) / 8);
+    cudaStream_t st[2] = {ctx->stream, ctx->stream2};
+    const size_t counter_at[2] = {128, 192};
+    // both streams start after any work already queued on the context stream
+    cudaEvent_t start;
+    GR_CUDA(ctx, cudaEventCreateWithFlags(&start, cudaEventDisableTiming));
+    gr_status status = GR_OK;
+    cudaError_t e = cudaEventRecord(start, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->stream2, start, 0);
+    for (uint64_t off = 0, k = 0; e == cudaSuccess && status == GR_OK && off < n; off += chunk, ++k) {
+        const uint64_t m = std::min(chunk, n - off);
+        cudaStream_t s = st[k & 1];
+        gr_ray* r = (gr_ray*)dr.p + off;
+        gr_hit* h = (gr_hit*)dh.p + off;
+        e = cudaMemcpyAsync(r, h_rays + off, sizeof(gr_ray) * m, cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess) status = trace_on(bvh, r, m, h, any_hit, s, counter_at[k & 1]);
+        if (e == cudaSuccess && status == GR_OK)
+            e = cudaMemcpyAsync(h_hits + off, h, sizeof(gr_hit) * m, cudaMemcpyDeviceToHost, s);
+    }
+    const cudaError_t e1 = cudaStreamSynchronize(ctx->stream2);
+    const cudaError_t e0 = cudaStreamSynchronize(ctx->stream);
+    cudaEventDestroy(start);
+    if (status != GR_OK) return status;
+    GR_CUDA(ctx, e);
+    GR_CUDA(ctx, e1);
+    GR_CUDA(ctx, e0);
     uint32_t err = 0;
     GR_CUDA(ctx, cudaMemcpy(&err, (char*)ctx->counter.p + 64, 4, cudaMemcpyDeviceToHost));
     return check_device_errors(bvh, err);

@@ -178,8 +178,11 @@ struct gr_ctx {
     int device = 0;
     int num_sms = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t stream2 = nullptr;  // second stream of the pipelined host-memory traversal
     std::string last_error;
-    gr::DevBuf counter;  // traversal work counter (offset 0) + error word (offset 64)
+    // traversal work counters: offset 0 (gr_trace), 128 and 192 (the two streams
+    // of gr_trace_host's pipeline); error word at offset 64
+    gr::DevBuf counter;
     gr::DevBuf stage_in, stage_out;  // device staging for the host-memory entry points
     void* batch_pool = nullptr;          // wave pool of gr_render_batch (owned; freed with the context)
     void (*batch_pool_free)(void*) = nullptr;

@@ -191,7 +191,10 @@ gr_status gr_bvh_export_layout_tris(gr_bvh* bvh, int layout, float* h_tris);
 
 gr_status gr_trace(gr_bvh* bvh, const gr_ray* d_rays, uint64_t n, gr_hit* d_hits, int any_hit, void* stream);
 
-/* Host-memory variant: copies rays in, traces, copies hits out, waits. */
+/* Host-memory variant: copies rays in, traces, copies hits out, waits. Large
+ * queues are cut into chunks of at least 1 Mi rays on two streams so the
+ * copies of one chunk overlap the traversal of another (pinned host memory
+ * lets the copies run asynchronously). */
 gr_status gr_trace_host(gr_bvh* bvh, const gr_ray* h_rays, uint64_t n, gr_hit* h_hits, int any_hit);
 
 /* ---- scene records ----------------------------------------------------------

@@ -126,3 +126,18 @@ def test_surface_rays_equal_brute_force_in_every_layout(oracle, scene):
         np.testing.assert_array_equal(oracle.trace4(bvh, n4, quant, rays).view(np.uint32), want)
     n8, t8 = oracle.bvh8(bvh)
     np.testing.assert_array_equal(oracle.trace8(bvh, n8, t8, rays).view(np.uint32), want)
+
+
+@pytest.mark.parametrize("scale,offset", [(1e4, 1e5), (1e-3, 0.0), (1.0, 1e4), (3e5, -2e6)])
+def test_layouts_agree_at_extreme_scales(oracle, scale, offset):
+    """Far from the origin or at tiny and huge scales the 8-wide quantised
+    traversal, whose plane distances carry explicit error margins, returns the
+    binary traversal's hits bit for bit."""
+    v = (sc.triangle_soup(20000, seed_salt=77).astype(np.float64) * scale + offset).astype(np.float32)
+    bvh = oracle.lbvh(v)
+    n8, t8 = oracle.bvh8(bvh)
+    r = sc.incoherent_rays(20000, seed_salt=78).astype(np.float64)
+    r[:, :3] = r[:, :3] * scale + offset
+    for rays in (r.astype(np.float32), sc.surface_rays(v, 20000, seed_salt=79)):
+        np.testing.assert_array_equal(oracle.trace8(bvh, n8, t8, rays).view(np.uint32),
+                                      oracle.trace(bvh, rays).view(np.uint32))
