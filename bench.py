@@ -310,7 +310,10 @@ def run_gpu(args):
         tp = os.path.join(ROOT, "profiles", "trace_closest_traffic.json")
         if os.path.exists(tp):
             with open(tp) as f:
-                traffic = json.load(f).get("bytes_per_launch")
+                tj = json.load(f)
+            # the capture is of one layout's kernel; other layouts report none
+            if tj.get("layout") == gr.LAYOUT_NAMES[layout]:
+                traffic = tj.get("bytes_per_launch")
         cb = cpu_reference(1, 0)
         out = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
