@@ -466,6 +466,28 @@ __global__ void __launch_bounds__(kShadeThreads) k_resolve(Paths ps) {
     }
 }
 
+// ---- 8-bit output (filter_kernel, pathtracer_kernel.h:792-810) -----------------------
+// sRGB transfer curve (spectrum.h:63-72): 12.92 v below 0.0031308, else
+// 1.055 v^(1/2.4) - 0.055; then 255 v + 0.5 clamped to [0, 255] and truncated.
+__device__ __forceinline__ uint32_t srgb8(float v) {
+    const float g = v <= 0.0031308f ? 12.92f * v : 1.055f * powf(v, 1.0f / 2.4f) - 0.055f;
+    return (uint32_t)fminf(fmaxf(255.0f * g + 0.5f, 0.0f), 255.0f);
+}
+
+__global__ void __launch_bounds__(kShadeThreads) k_filter(const double* __restrict__ fb, const uint32_t* __restrict__ fbc,
+                                                          uint32_t npix, uint32_t* __restrict__ out) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < npix; i += gridDim.x * blockDim.x) {
+        const uint32_t n = fbc[i];
+        uint32_t px = 0xFF000000u;
+        if (n) {
+            const double inv = 1.0 / (double)n;
+            px |= srgb8((float)(fb[3ull * i] * inv)) | (srgb8((float)(fb[3ull * i + 1] * inv)) << 8) |
+                  (srgb8((float)(fb[3ull * i + 2] * inv)) << 16);
+        }
+        out[i] = px;
+    }
+}
+
 __global__ void k_wave_end(Paths ps) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     WaveHeader* h = ps.hdr;
@@ -646,6 +668,13 @@ uint32_t pack_wave(std::vector<HostJob*>& jobs, uint32_t capacity, std::vector<J
     *total_pix = pix;
     *max_depth = depth;
     return (uint32_t)out.size();
+}
+
+cudaError_t filter_rgba8(const double* fb, const uint32_t* fbc, uint32_t npix, uint32_t* out, cudaStream_t s) {
+    if (npix == 0) return cudaSuccess;
+    const int grid = (int)std::min<uint32_t>((npix + kShadeThreads - 1) / kShadeThreads, 4096u);
+    k_filter<<<grid, kShadeThreads, 0, s>>>(fb, fbc, npix, out);
+    return cudaGetLastError();
 }
 
 cudaError_t run_wave(WavePool& pool, const JobDev* h_jobs, uint32_t njobs, uint32_t total_paths, uint32_t total_pix,

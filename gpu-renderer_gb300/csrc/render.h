@@ -165,6 +165,10 @@ namespace gr {
 uint32_t pack_wave(std::vector<HostJob*>& jobs, uint32_t capacity, std::vector<JobDev>& out, uint32_t* total_paths,
                    uint32_t* total_pix, uint32_t* max_depth);
 
+// Mean radiance -> sRGB-encoded RGBA8 (R in the low byte), the reference's
+// filter_kernel (pathtracer_kernel.h:792-810); pixels without samples are black.
+cudaError_t filter_rgba8(const double* fb, const uint32_t* fbc, uint32_t npix, uint32_t* out, cudaStream_t s);
+
 }  // namespace gr
 
 struct gr_scene {
@@ -177,6 +181,7 @@ struct gr_scene {
     uint32_t samples_done = 0;
     uint32_t default_wave_paths = 0;  // 0 = library default (autotuned by gr_scene_autotune)
     gr::DevCamera cam{};
+    gr_camera cam_rec{};  // the camera record cam was made from (view operations edit it)
     float env[3] = {0, 0, 0};
     int has_env = 0;
 };

@@ -194,6 +194,7 @@ gr_status gr_scene_create(gr_ctx* ctx, const gr_mesh* meshes, uint32_t num_meshe
     if ((e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess) return cleanup(cuda_fail(ctx, e, "bvh build"));
 
     sc->cam = gr::make_camera(*camera);
+    sc->cam_rec = *camera;
     if (env && env->enabled) {
         sc->has_env = 1;
         std::memcpy(sc->env, env->radiance, 12);

@@ -273,6 +273,14 @@ _SCENE_SIGS = {
     "gr_render": ([_P, ctypes.POINTER(RenderOpts), _P, ctypes.POINTER(RenderStats)], ctypes.c_int),
     "gr_scene_accumulation": ([_P, _P, _P], ctypes.c_int),
     "gr_scene_reset": ([_P], ctypes.c_int),
+    "gr_scene_get_camera": ([_P, ctypes.POINTER(Camera)], ctypes.c_int),
+    "gr_scene_set_camera": ([_P, ctypes.POINTER(Camera)], ctypes.c_int),
+    "gr_scene_zoom": ([_P, ctypes.c_float], ctypes.c_int),
+    "gr_scene_translate": ([_P, ctypes.c_float, ctypes.c_float], ctypes.c_int),
+    "gr_scene_rotate": ([_P, ctypes.c_float, ctypes.c_float], ctypes.c_int),
+    "gr_scene_resize": ([_P, ctypes.c_uint32, ctypes.c_uint32], ctypes.c_int),
+    "gr_scene_rgba8": ([_P, _P, _P], ctypes.c_int),
+    "gr_scene_rgba8_host": ([_P, _P], ctypes.c_int),
 }
 
 
@@ -340,6 +348,47 @@ class Scene:
         self.h = h
         self._keep = []
         self.width, self.height = cam.width, cam.height
+
+    # ---- view operations (PathTracer::zoom / translate / rotate / resize) ----
+
+    def camera(self):
+        """The scene's camera as a dict (to_world 4x4, fov, width, height)."""
+        c = Camera()
+        self.ctx.check(_declare(_SCENE_SIGS).gr_scene_get_camera(self.h, ctypes.byref(c)), "gr_scene_get_camera")
+        return {"to_world": np.array(c.to_world[:], np.float32).reshape(4, 4), "fov": float(c.fov_deg),
+                "width": int(c.width), "height": int(c.height)}
+
+    def _after_view_change(self, st, what):
+        self.ctx.check(st, what)
+        cam = self.camera()
+        self.width, self.height = cam["width"], cam["height"]
+
+    def set_camera(self, cam):
+        c = camera_record(cam)
+        self._after_view_change(_declare(_SCENE_SIGS).gr_scene_set_camera(self.h, ctypes.byref(c)),
+                                "gr_scene_set_camera")
+
+    def zoom(self, d):
+        self._after_view_change(_declare(_SCENE_SIGS).gr_scene_zoom(self.h, d), "gr_scene_zoom")
+
+    def translate(self, x, y):
+        self._after_view_change(_declare(_SCENE_SIGS).gr_scene_translate(self.h, x, y), "gr_scene_translate")
+
+    def rotate(self, yaw, pitch):
+        self._after_view_change(_declare(_SCENE_SIGS).gr_scene_rotate(self.h, yaw, pitch), "gr_scene_rotate")
+
+    def resize(self, width, height):
+        self._after_view_change(_declare(_SCENE_SIGS).gr_scene_resize(self.h, width, height), "gr_scene_resize")
+
+    def rgba8(self):
+        """The sRGB 8-bit RGBA image (height, width, 4) uint8 of the mean radiance."""
+        out = np.zeros(self.width * self.height, np.uint32)
+        self.ctx.check(_declare(_SCENE_SIGS).gr_scene_rgba8_host(self.h, _ptr(out)), "gr_scene_rgba8_host")
+        return out.view(np.uint8).reshape(self.height, self.width, 4)
+
+    def rgba8_device(self, d_out, stream=None):
+        self.ctx.check(_declare(_SCENE_SIGS).gr_scene_rgba8(self.h, _ptr(d_out), _P(stream) if stream else None),
+                       "gr_scene_rgba8")
 
     def render(self, spp, max_depth=8, seed=0, rr_depth=3, flags=0, wave_paths=0, want_image=True):
         L = _declare(_SCENE_SIGS)
@@ -425,6 +474,30 @@ class PathTracer:
     def reset(self):
         self.scene.reset()
         self.sample_num = 0
+
+    # the viewer's camera operations (pathtracer.cu:177-213); each restarts the sample sequence
+    def zoom(self, d):
+        self.scene.zoom(d)
+        self.sample_num = 0
+
+    def translate(self, x, y):
+        self.scene.translate(x, y)
+        self.sample_num = 0
+
+    def rotate(self, yaw, pitch):
+        self.scene.rotate(yaw, pitch)
+        self.sample_num = 0
+
+    def resize(self, width, height):
+        self.scene.resize(width, height)
+        self.sample_num = 0
+
+    def get_resolution(self):
+        return self.scene.width, self.scene.height
+
+    def display(self):
+        """The 8-bit RGBA display image of render(uint32*) (filter_kernel)."""
+        return self.scene.rgba8()
 
 
 # ---- batched rendering and serving ---------------------------------------------------

@@ -300,6 +300,31 @@ gr_status gr_scene_reset(gr_scene* scene);
 /* Device bytes the scene holds (geometry, BVH, accumulation). */
 uint64_t gr_scene_device_bytes(const gr_scene* scene);
 
+/* ---- view: camera operations and 8-bit output -------------------------------
+ * The interactive operations of the reference's viewer (PathTracer::zoom /
+ * translate / rotate / resize, pathtracer.cu:177-213, camera.h:40-83). Each
+ * camera change clears the accumulation (the reference's m_reset). They act on
+ * the scene's to_world matrix: zoom moves the eye by d along the view
+ * direction; translate by x along normalize(cross(dir, world up)) and y along
+ * the vertical axis normalize(cross(horizontal, dir)); rotate turns the camera
+ * by yaw radians about the world up axis, then by pitch about its horizontal
+ * axis; resize changes the resolution (the field of view stays horizontal). */
+gr_status gr_scene_get_camera(const gr_scene* scene, gr_camera* out);
+gr_status gr_scene_set_camera(gr_scene* scene, const gr_camera* camera);
+gr_status gr_scene_zoom(gr_scene* scene, float d);
+gr_status gr_scene_translate(gr_scene* scene, float x, float y);
+gr_status gr_scene_rotate(gr_scene* scene, float yaw, float pitch);
+gr_status gr_scene_resize(gr_scene* scene, uint32_t width, uint32_t height);
+
+/* The mean radiance as sRGB-encoded 8-bit RGBA, one uint32 per pixel (R in
+ * the low byte, alpha 255, row 0 first): the reference's filter_kernel
+ * (pathtracer_kernel.h:792-810), which fills the viewer's display buffer after
+ * each render(uint32*). Pixels without samples are black. The device variant
+ * is ordered after the scene's renders and runs on `stream`; the host variant
+ * waits. */
+gr_status gr_scene_rgba8(gr_scene* scene, uint32_t* d_rgba, void* stream);
+gr_status gr_scene_rgba8_host(gr_scene* scene, uint32_t* h_rgba);
+
 /* Node layout the scene's renders traverse (GR_LAYOUT_*; default binary).
  * Builds the layout if needed and waits. All scenes of one gr_render_batch
  * must use the same layout. */
