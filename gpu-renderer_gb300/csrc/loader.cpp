@@ -15,13 +15,21 @@
 //     index from the "ior" property only (intIOR/extIOR are read but not used),
 //     and a rough conductor's alphaV is taken from "alphaU";
 //   - shapes: obj, sphere (lat-long, subdiv), rectangle, cube (:53-221).
+//   - textures: "checkerboard" (color0 / color1, the reference's 2 x 2 map) and
+//     "bitmap", with uoffset / voffset / uscale / vscale (createTexture,
+//     :530-555); OBJ texture coordinates ("vt"); "envmap" emitters with their
+//     toWorld (:472-478). Float images are read as stb_image's stbi_loadf with
+//     vertical flip does for the reference (ReadImage, imageio.cpp:45-57): an
+//     8-bit channel c becomes (c / 255)^2.2 and row 0 is the image's bottom row.
 // Differences: "roughplastic" is loaded as Lambert with its diffuse
-// reflectance, textures as their mean colour, and "envmap" emitters are
-// skipped; each is recorded as a warning.
+// reflectance; only binary PPM (P6, 8-bit) and PFM images are read (another
+// image format leaves a texture at its 0.5 grey, an envmap skipped); each is
+// recorded as a warning.
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <deque>
 #include <fstream>
 #include <map>
 #include <memory>
@@ -266,6 +274,10 @@ struct Prop {
     std::string s;
     F3 v{0, 0, 0};
     M4 t = M4::identity();
+    // texture: map index into the description's maps (-1: constant v), size, uv offset and scale
+    int tex = -1;
+    uint32_t tw = 0, th = 0;
+    float uo = 0.0f, vo = 0.0f, us = 1.0f, vs = 1.0f;
 };
 using Props = std::map<std::string, Prop>;
 
@@ -298,9 +310,9 @@ struct Mat {
 };
 
 struct MeshData {
-    std::vector<float> pos, nrm;
+    std::vector<float> pos, nrm, uv;
     std::vector<uint32_t> idx;
-    bool has_normals = false;
+    bool has_normals = false, has_uvs = false;
 };
 
 }  // namespace
@@ -310,6 +322,7 @@ struct gr_scene_desc {
     std::vector<MeshData> meshes;
     std::vector<uint32_t> mesh_mat;
     std::vector<gr_material> mats;
+    std::deque<std::vector<float>> maps;  // texture and environment texels (stable addresses)
     gr_camera cam{};
     gr_environment env{};
     std::string warnings;
@@ -325,8 +338,8 @@ bool load_obj(const std::string& path, MeshData& out, std::string& err) {
         err = "cannot open " + path;
         return false;
     }
-    std::vector<float> P, N;
-    std::map<std::pair<int, int>, uint32_t> remap;  // (position, normal) -> vertex
+    std::vector<float> P, N, T;
+    std::map<std::pair<std::pair<int, int>, int>, uint32_t> remap;  // ((position, texcoord), normal) -> vertex
     std::string line;
     size_t ln = 0;
     auto resolve = [](int i, size_t n) -> int {
@@ -342,6 +355,10 @@ bool load_obj(const std::string& path, MeshData& out, std::string& err) {
             float v[3];
             if (!parse_floats(s + 2, v, 3)) { err = path + ": bad vertex at line " + std::to_string(ln); return false; }
             P.insert(P.end(), v, v + 3);
+        } else if (s[0] == 'v' && s[1] == 't') {
+            float v[2];
+            if (!parse_floats(s + 3, v, 2)) { err = path + ": bad texcoord at line " + std::to_string(ln); return false; }
+            T.insert(T.end(), v, v + 2);
         } else if (s[0] == 'v' && s[1] == 'n') {
             float v[3];
             if (!parse_floats(s + 3, v, 3)) { err = path + ": bad normal at line " + std::to_string(ln); return false; }
@@ -362,14 +379,15 @@ bool load_obj(const std::string& path, MeshData& out, std::string& err) {
                         ni = (int)strtol(t, (char**)&t, 10);
                     }
                 }
-                (void)ti;
                 const int p = resolve(vi, P.size() / 3);
                 const int n = ni ? resolve(ni, N.size() / 3) : -1;
-                if (p < 0 || (size_t)p >= P.size() / 3 || (ni && (n < 0 || (size_t)n >= N.size() / 3))) {
+                const int tc = ti ? resolve(ti, T.size() / 2) : -1;
+                if (p < 0 || (size_t)p >= P.size() / 3 || (ni && (n < 0 || (size_t)n >= N.size() / 3)) ||
+                    (ti && (tc < 0 || (size_t)tc >= T.size() / 2))) {
                     err = path + ": face index out of range at line " + std::to_string(ln);
                     return false;
                 }
-                const auto key = std::make_pair(p, n);
+                const auto key = std::make_pair(std::make_pair(p, tc), n);
                 auto it = remap.find(key);
                 uint32_t v;
                 if (it == remap.end()) {
@@ -380,6 +398,12 @@ bool load_obj(const std::string& path, MeshData& out, std::string& err) {
                         out.has_normals = true;
                     } else {
                         out.nrm.insert(out.nrm.end(), {0.0f, 0.0f, 0.0f});
+                    }
+                    if (tc >= 0) {
+                        out.uv.insert(out.uv.end(), T.begin() + 2 * tc, T.begin() + 2 * tc + 2);
+                        out.has_uvs = true;
+                    } else {
+                        out.uv.insert(out.uv.end(), {0.0f, 0.0f});
                     }
                     remap.emplace(key, v);
                 } else {
@@ -478,6 +502,88 @@ void make_sphere(MeshData& m, float radius, int subdiv) {
     m.has_normals = true;
 }
 
+// ---- float images (ReadImage, imageio.cpp:45-57) -------------------------------------------------
+// Binary PPM (P6, maxval <= 255: each channel (c / maxval)^2.2, as stbi_loadf
+// linearises 8-bit data) and PFM (linear floats); rows returned bottom first,
+// as the reference's loader flips them.
+bool ppm_token(std::istream& f, std::string& tok) {
+    tok.clear();
+    int c;
+    while ((c = f.get()) != EOF) {
+        if (c == '#') {
+            while ((c = f.get()) != EOF && c != '\n') {}
+            continue;
+        }
+        if (isspace(c)) {
+            if (!tok.empty()) return true;
+            continue;
+        }
+        tok.push_back((char)c);
+    }
+    return !tok.empty();
+}
+
+bool read_float_image(const std::string& path, std::vector<float>& rgb, uint32_t& w, uint32_t& h, std::string& why) {
+    std::ifstream f(path, std::ios::binary);
+    if (!f) {
+        why = "cannot open " + path;
+        return false;
+    }
+    std::string magic, sw, sh, sm;
+    if (!ppm_token(f, magic) || (magic != "P6" && magic != "PF")) {
+        why = path + ": only binary PPM (P6) and colour PFM (PF) images are read";
+        return false;
+    }
+    if (!ppm_token(f, sw) || !ppm_token(f, sh) || !ppm_token(f, sm)) {
+        why = path + ": bad header";
+        return false;
+    }
+    const long W = strtol(sw.c_str(), nullptr, 10), H = strtol(sh.c_str(), nullptr, 10);
+    if (W <= 0 || H <= 0 || (uint64_t)W * (uint64_t)H > (1ull << 28)) {
+        why = path + ": bad size";
+        return false;
+    }
+    w = (uint32_t)W;
+    h = (uint32_t)H;
+    const size_t n = (size_t)W * (size_t)H * 3;
+    rgb.assign(n, 0.0f);
+    if (magic == "P6") {
+        const long maxval = strtol(sm.c_str(), nullptr, 10);
+        if (maxval <= 0 || maxval > 255) {
+            why = path + ": only 8-bit PPM is read";
+            return false;
+        }
+        std::vector<unsigned char> px(n);
+        if (!f.read((char*)px.data(), (std::streamsize)n)) {
+            why = path + ": truncated";
+            return false;
+        }
+        for (long y = 0; y < H; ++y)  // file rows run top to bottom
+            for (long k = 0; k < 3 * W; ++k)
+                rgb[(size_t)(H - 1 - y) * 3 * W + k] =
+                    std::pow((float)px[(size_t)y * 3 * W + k] / (float)maxval, 2.2f);
+    } else {
+        const float scale = strtof(sm.c_str(), nullptr);
+        std::vector<unsigned char> raw(4 * n);
+        if (!f.read((char*)raw.data(), (std::streamsize)raw.size())) {
+            why = path + ": truncated";
+            return false;
+        }
+        const bool little = scale < 0.0f;
+        for (size_t k = 0; k < n; ++k) {  // file rows already run bottom to top
+            const unsigned char* b = &raw[4 * k];
+            const uint32_t u = little ? (uint32_t)b[0] | ((uint32_t)b[1] << 8) | ((uint32_t)b[2] << 16) |
+                                            ((uint32_t)b[3] << 24)
+                                      : (uint32_t)b[3] | ((uint32_t)b[2] << 8) | ((uint32_t)b[1] << 16) |
+                                            ((uint32_t)b[0] << 24);
+            float v;
+            std::memcpy(&v, &u, 4);
+            rgb[k] = v;
+        }
+    }
+    return true;
+}
+
 // ---- the Mitsuba interpreter --------------------------------------------------------------------
 struct Interp {
     gr_scene_desc* out;
@@ -504,15 +610,31 @@ struct Interp {
         return m;
     }
 
+    // The color slot `key` of a material: a texture property fills color_map.
+    void color_texture(gr_material& m, const Props& L, const char* key) {
+        auto it = L.find(key);
+        if (it == L.end() || it->second.kind != Prop::Texture || it->second.tex < 0) return;
+        const Prop& t = it->second;
+        m.color_map = out->maps[(size_t)t.tex].data();
+        m.color_map_width = t.tw;
+        m.color_map_height = t.th;
+        m.uv_offset[0] = t.uo;
+        m.uv_offset[1] = t.vo;
+        m.uv_scale[0] = t.us;
+        m.uv_scale[1] = t.vs;
+    }
+
     void create_material(const std::string& type, const Props& L) {
         gr_material m{};
         if (type == "diffuse") {
             m = diffuse(get_color(L, "reflectance", f3(0.3f, 0.3f, 0.3f)));
+            color_texture(m, L, "reflectance");
         } else if (type == "mirror" || type == "glass" || type == "dielectric" || type == "roughdielectric") {
             const F3 c = get_color(L, "reflectance", f3(1, 1, 1));
             m.type = GR_MAT_DIELECTRIC;
             m.color[0] = c.x; m.color[1] = c.y; m.color[2] = c.z;
             m.ior = get_float(L, "ior", type == "mirror" ? 100.0f : 1.5f);
+            color_texture(m, L, "reflectance");
         } else if (type == "roughconductor" || type == "conductor") {
             const F3 c = get_color(L, "specularReflectance", f3(0.3f, 0.3f, 0.3f));
             F3 ei, et;
@@ -539,9 +661,11 @@ struct Interp {
             m.k[0] = k.x; m.k[1] = k.y; m.k[2] = k.z;
             m.alpha_u = au;
             m.alpha_v = av;
+            color_texture(m, L, "specularReflectance");
         } else if (type == "roughplastic") {
             warn("roughplastic loaded as Lambert with its diffuseReflectance");
             m = diffuse(get_color(L, "diffuseReflectance", f3(0.5f, 0.5f, 0.5f)));
+            color_texture(m, L, "diffuseReflectance");
         } else if (type == "disney") {
             return;  // the reference ignores it and keeps the current material
         } else {
@@ -661,7 +785,25 @@ struct Interp {
                 out->env.radiance[2] = r.z;
                 out->env.enabled = 1;
             } else if (type == "envmap") {
-                warn("envmap emitter skipped (constant environments only)");
+                auto fn = mine.find("filename");
+                std::vector<float> rgb;
+                uint32_t w = 0, h = 0;
+                std::string why;
+                if (fn == mine.end() || !read_float_image(dir + fn->second.s, rgb, w, h, why)) {
+                    warn("envmap emitter skipped: " + (fn == mine.end() ? std::string("no filename") : why));
+                    return true;
+                }
+                out->maps.push_back(std::move(rgb));
+                M4 o2w = M4::identity();
+                auto tw = mine.find("toWorld");
+                if (tw != mine.end() && tw->second.kind == Prop::Transform) o2w = tw->second.t;
+                out->env = gr_environment{};
+                out->env.enabled = 1;
+                out->env.map = out->maps.back().data();
+                out->env.map_width = w;
+                out->env.map_height = h;
+                for (int r = 0; r < 4; ++r)
+                    for (int c = 0; c < 4; ++c) out->env.to_world[4 * r + c] = o2w.m[r][c];
             } else {
                 return fail("unsupported emitter type '" + type + "'", n);
             }
@@ -671,11 +813,36 @@ struct Interp {
         if (tag == "texture") {
             Prop p;
             p.kind = Prop::Texture;
-            if (type == "checkerboard") {
+            p.uo = get_float(mine, "uoffset", 0.0f);
+            p.vo = get_float(mine, "voffset", 0.0f);
+            p.us = get_float(mine, "uscale", 1.0f);
+            p.vs = get_float(mine, "vscale", 1.0f);
+            if (type == "checkerboard") {  // the 2 x 2 map (c0, c1; c1, c0) of texture.cpp:45-56
                 const F3 a = get_color(mine, "color0", f3(0.4f, 0.4f, 0.4f));
                 const F3 b = get_color(mine, "color1", f3(0.2f, 0.2f, 0.2f));
                 p.v = f3((a.x + b.x) * 0.5f, (a.y + b.y) * 0.5f, (a.z + b.z) * 0.5f);
-                warn("checkerboard texture '" + name + "' loaded as its mean colour");
+                out->maps.push_back({a.x, a.y, a.z, b.x, b.y, b.z, b.x, b.y, b.z, a.x, a.y, a.z});
+                p.tex = (int)out->maps.size() - 1;
+                p.tw = p.th = 2;
+            } else if (type == "bitmap") {
+                auto fn = mine.find("filename");
+                std::vector<float> rgb;
+                uint32_t w = 0, h = 0;
+                std::string why;
+                if (fn != mine.end() && read_float_image(dir + fn->second.s, rgb, w, h, why)) {
+                    double sum[3] = {0, 0, 0};
+                    for (size_t k = 0; k < rgb.size(); ++k) sum[k % 3] += rgb[k];
+                    const double np = (double)w * h;
+                    p.v = f3((float)(sum[0] / np), (float)(sum[1] / np), (float)(sum[2] / np));
+                    out->maps.push_back(std::move(rgb));
+                    p.tex = (int)out->maps.size() - 1;
+                    p.tw = w;
+                    p.th = h;
+                } else {
+                    p.v = f3(0.5f, 0.5f, 0.5f);
+                    warn("bitmap texture '" + name + "' loaded as 0.5 grey: " +
+                         (fn == mine.end() ? std::string("no filename") : why));
+                }
             } else {
                 p.v = f3(0.5f, 0.5f, 0.5f);
                 warn("texture '" + name + "' of type '" + type + "' loaded as 0.5 grey");
@@ -868,6 +1035,7 @@ gr_status gr_scene_create_from_desc(gr_ctx* ctx, const gr_scene_desc* d, gr_scen
         meshes[i].indices = m.idx.data();
         meshes[i].num_triangles = (uint32_t)(m.idx.size() / 3);
         meshes[i].material = d->mesh_mat[i];
+        meshes[i].texcoords = m.has_uvs ? m.uv.data() : nullptr;
     }
     return gr_scene_create(ctx, meshes.data(), (uint32_t)meshes.size(), d->mats.data(), (uint32_t)d->mats.size(),
                            &d->cam, &d->env, out);

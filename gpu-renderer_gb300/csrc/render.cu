@@ -56,13 +56,12 @@ __device__ __forceinline__ V3 load3(const float* p) { return v3(p[0], p[1], p[2]
 struct Bsdf {
     Frame fr;
     const DevMaterial* m;
+    V3 color;  // the material's color at the shading point (constant or texture lookup)
     bool compat;
 };
 
-__device__ __forceinline__ V3 mcolor(const DevMaterial* m) { return v3(m->cr, m->cg, m->cb); }
-
 // GGX reflection f*cos (MicrofacetReflectEval, microfacet.h:159-181)
-__device__ __forceinline__ V3 mf_eval(const DevMaterial* m, V3 wo, V3 wi) {
+__device__ __forceinline__ V3 mf_eval(const DevMaterial* m, V3 color, V3 wo, V3 wi) {
     const float co = fabsf(wo.z), ci = fabsf(wi.z);
     V3 wh = wi + wo;
     if (ci == 0.0f || co == 0.0f) return vs(0.0f);
@@ -70,7 +69,7 @@ __device__ __forceinline__ V3 mf_eval(const DevMaterial* m, V3 wo, V3 wi) {
     wh = normalize(wh);
     const V3 F = fr_conductor(fabsf(dot(wi, wh)), v3(m->eir, m->eig, m->eib), v3(m->etr, m->etg, m->etb),
                               v3(m->kr, m->kg, m->kb));
-    return mcolor(m) * ggx_d(wh, m->ax, m->ay) * ggx_g(wo, wi, m->ax, m->ay) * F / (4.0f * co);
+    return color * ggx_d(wh, m->ax, m->ay) * ggx_g(wo, wi, m->ax, m->ay) * F / (4.0f * co);
 }
 
 // GGX pdf of reflecting wo about wh. The reference's form D|cos h|/(4 wo.h)
@@ -86,8 +85,8 @@ __device__ __forceinline__ V3 bsdf_eval(const Bsdf& b, V3 wo_w, V3 wi_w) {
     if (wo.z == 0.0f) return vs(0.0f);
     const bool refl = wo.z * wi.z > 0.0f;
     if (!refl) return vs(0.0f);
-    if (b.m->type == GR_MAT_DIFFUSE) return mcolor(b.m) * kInvPi * fabsf(wi.z);
-    if (b.m->type == GR_MAT_CONDUCTOR) return mf_eval(b.m, wo, wi);
+    if (b.m->type == GR_MAT_DIFFUSE) return b.color * kInvPi * fabsf(wi.z);
+    if (b.m->type == GR_MAT_CONDUCTOR) return mf_eval(b.m, b.color, wo, wi);
     return vs(0.0f);
 }
 
@@ -118,26 +117,26 @@ __device__ __forceinline__ Sample bsdf_sample(const Bsdf& b, V3 wo_w, float u0, 
     if (b.m->type == GR_MAT_DIFFUSE) {
         wi = cosine_hemisphere(u0, u1);
         if (wo.z < 0.0f) wi.z = -wi.z;
-        s.f = mcolor(b.m) * kInvPi * fabsf(wi.z);
+        s.f = b.color * kInvPi * fabsf(wi.z);
         s.pdf = fabsf(wi.z) * kInvPi;
     } else if (b.m->type == GR_MAT_CONDUCTOR) {
         const V3 wh = ggx_sample_wh(wo, u0, u1, b.m->ax, b.m->ay);
         wi = reflect(wo, wh);
         if (!(wo.z * wi.z > 0.0f)) return s;
         s.pdf = mf_pdf_wh(b.m, wo, wh, b.compat);
-        s.f = mf_eval(b.m, wo, wi);
+        s.f = mf_eval(b.m, b.color, wo, wi);
     } else {
         const float F = fr_dielectric(wo.z, 1.0f, b.m->ior);
         if (u0 < F) {
             wi = v3(-wo.x, -wo.y, wo.z);
             s.pdf = F;
-            s.f = mcolor(b.m) * F;
+            s.f = b.color * F;
         } else {
             const bool entering = wo.z > 0.0f;
             const float ei = entering ? 1.0f : b.m->ior, et = entering ? b.m->ior : 1.0f;
             const V3 n = wo.z < 0.0f ? v3(0.0f, 0.0f, -1.0f) : v3(0.0f, 0.0f, 1.0f);
             if (!refract(wo, n, ei / et, wi)) return s;
-            s.f = mcolor(b.m) * (1.0f - F) * ((ei * ei) / (et * et));
+            s.f = b.color * (1.0f - F) * ((ei * ei) / (et * et));
             s.pdf = 1.0f - F;
         }
     }
@@ -148,9 +147,9 @@ __device__ __forceinline__ Sample bsdf_sample(const Bsdf& b, V3 wo_w, float u0, 
         if (!refl) {
             s.f = vs(0.0f);
         } else if (b.m->type == GR_MAT_DIFFUSE) {
-            s.f = mcolor(b.m) * kInvPi * fabsf(wi.z);
+            s.f = b.color * kInvPi * fabsf(wi.z);
         } else {
-            s.f = mf_eval(b.m, wo, wi);
+            s.f = mf_eval(b.m, b.color, wo, wi);
         }
     }
     return s;
@@ -159,6 +158,7 @@ __device__ __forceinline__ Sample bsdf_sample(const Bsdf& b, V3 wo_w, float u0, 
 // Surface point on triangle `prim` at barycentrics (u, v) (Triangle::setupDifferential, triangle.h:103-138).
 struct Surf {
     V3 p, ng, ns;
+    float tu, tv;  // texture coordinates (Triangle::setupDifferential, triangle.h:103-135)
 };
 __device__ __forceinline__ Surf surface(const SceneDev& sc, uint32_t prim, float u, float v) {
     const float* t = sc.verts + 9ull * prim;
@@ -167,13 +167,55 @@ __device__ __forceinline__ Surf surface(const SceneDev& sc, uint32_t prim, float
     Surf s;
     s.p = p0 * w + p1 * u + p2 * v;
     s.ng = normalize(cross(p0 - p2, p1 - p2));
-    if (sc.tri_mat[prim] & 0x80000000u) {
+    const uint32_t tm = sc.tri_mat[prim];
+    if (tm & 0x80000000u) {
         const float4 a = sc.normals[3ull * prim], b = sc.normals[3ull * prim + 1], c = sc.normals[3ull * prim + 2];
         s.ns = normalize(v3(a.x, a.y, a.z) * w + v3(b.x, b.y, b.z) * u + v3(c.x, c.y, c.z) * v);
     } else {
         s.ns = s.ng;
     }
+    if (tm & 0x40000000u) {
+        const float* q = sc.uvs + 6ull * prim;
+        s.tu = q[0] * w + q[2] * u + q[4] * v;
+        s.tv = q[1] * w + q[3] * u + q[5] * v;
+    } else {  // without texcoords the barycentrics are the uv
+        s.tu = u;
+        s.tv = v;
+    }
     return s;
+}
+
+// Nearest texel at uv * scale + offset (TextureView::evalSpectrum, texture.h:37-44:
+// truncation toward zero, then the index wrapped into [0, size)).
+__device__ __forceinline__ int wrap_texel(float x, uint32_t size) {
+    const float f = fminf(fmaxf(x * (float)size, -1073741824.0f), 1073741824.0f);
+    const int i = (int)f % (int)size;
+    return i < 0 ? i + (int)size : i;
+}
+
+__device__ __forceinline__ V3 color_at(const SceneDev& sc, const DevMaterial* m, float tu, float tv) {
+    if (m->tex_w == 0) return v3(m->cr, m->cg, m->cb);
+    const int x = wrap_texel(tu * m->tus + m->tuo, m->tex_w);
+    const int y = wrap_texel(tv * m->tvs + m->tvo, m->tex_h);
+    const float4 c = sc.texels[m->tex_off + (uint32_t)y * m->tex_w + (uint32_t)x];
+    return v3(c.x, c.y, c.z);
+}
+
+// Radiance of a ray leaving the scene (EnvironmentLightView::Le, environment.h:15-27).
+__device__ __forceinline__ V3 env_radiance(const SceneDev& sc, V3 o, V3 d) {
+    if (sc.env_w == 0) return v3(sc.env_r, sc.env_g, sc.env_b);
+    V3 w = normalize(o + d * 100000.0f - v3(sc.env_c[0], sc.env_c[1], sc.env_c[2]));
+    const float* M = sc.env_m;
+    w = normalize(v3(M[0] * w.x + M[1] * w.y + M[2] * w.z, M[3] * w.x + M[4] * w.y + M[5] * w.z,
+                     M[6] * w.x + M[7] * w.y + M[8] * w.z));
+    const float theta = acosf(fminf(fmaxf(w.z, -1.0f), 1.0f));
+    float phi = atan2f(w.y, w.x);
+    if (phi < 0.0f) phi += 6.28318530717958647692f;
+    const float u = phi * 0.15915494309189533577f, v = theta * 0.31830988618379067154f;
+    const uint32_t x = min(sc.env_w - 1, (uint32_t)(int)(u * (float)sc.env_w));
+    const uint32_t y = min(sc.env_h - 1, (uint32_t)(int)(v * (float)sc.env_h));
+    const float4 c = sc.env_map[y * sc.env_w + x];
+    return v3(c.x, c.y, c.z);
 }
 
 __device__ __forceinline__ float tri_area(const SceneDev& sc, uint32_t prim) {
@@ -343,7 +385,7 @@ __global__ void __launch_bounds__(kShadeThreads) k_shade(Paths ps, int b) {
             if (alive && b > 0) {
                 const float rr = pcg_float(st, inc);
                 if (prim >= 0 && !(flags & kFlagSpecular)) {
-                    const DevMaterial* lm = sc.mats + (sc.tri_mat[prim] & 0x7FFFFFFFu);
+                    const DevMaterial* lm = sc.mats + (sc.tri_mat[prim] & 0x3FFFFFFFu);
                     if (lm->emissive) {
                         const Surf ls = surface(sc, (uint32_t)prim, hv.z, hv.w);
                         float lpdf = (1.0f / tri_area(sc, (uint32_t)prim)) / (float)sc.num_lights;
@@ -368,10 +410,10 @@ __global__ void __launch_bounds__(kShadeThreads) k_shade(Paths ps, int b) {
 #pragma unroll
                 for (int k = 0; k < 8; ++k) s[k] = pcg_float(st, inc);
                 if (prim < 0 || as_miss) {
-                    if (sc.has_env) add_acc(ps, pid, thr * v3(sc.env_r, sc.env_g, sc.env_b));
+                    if (sc.has_env) add_acc(ps, pid, thr * env_radiance(sc, v3(r0.x, r0.y, r0.z), rd));
                 } else {
                     const uint32_t tm = sc.tri_mat[prim];
-                    const DevMaterial* m = sc.mats + (tm & 0x7FFFFFFFu);
+                    const DevMaterial* m = sc.mats + (tm & 0x3FFFFFFFu);
                     const Surf sf = surface(sc, (uint32_t)prim, hv.z, hv.w);
                     const V3 wo = -normalize(rd);
                     if ((b == 0 || (flags & kFlagSpecular)) && m->emissive && dot(wo, sf.ns) > 0.0f)
@@ -379,6 +421,7 @@ __global__ void __launch_bounds__(kShadeThreads) k_shade(Paths ps, int b) {
                     Bsdf bs;
                     bs.fr = make_frame(sf.ns);
                     bs.m = m;
+                    bs.color = color_at(sc, m, sf.tu, sf.tv);
                     bs.compat = compat;
                     // next-event estimation with MIS
                     if (m->type != GR_MAT_DIELECTRIC && sc.num_lights > 0) {
@@ -392,7 +435,7 @@ __global__ void __launch_bounds__(kShadeThreads) k_shade(Paths ps, int b) {
                         wi = wi / sqrtf(d2);
                         lpdf *= d2 / fabsf(dot(wi, ls.ns));
                         if (isinf(lpdf)) lpdf = 0.0f;
-                        const DevMaterial* lm = sc.mats + (sc.tri_mat[lt] & 0x7FFFFFFFu);
+                        const DevMaterial* lm = sc.mats + (sc.tri_mat[lt] & 0x3FFFFFFFu);
                         const V3 Le = dot(-wi, ls.ns) > 0.0f ? v3(lm->er, lm->eg, lm->eb) : vs(0.0f);
                         const V3 f = bsdf_eval(bs, wo, wi);
                         const float bp = bsdf_pdf(bs, wo, wi);

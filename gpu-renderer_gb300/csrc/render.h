@@ -17,6 +17,10 @@ struct DevMaterial {
     float kr, kg, kb;     // k
     float ior;
     uint32_t emissive;
+    // color texture: tex_w == 0 for the constant color; else texels
+    // [tex_off, tex_off + tex_w * tex_h) of the scene's texel pool
+    uint32_t tex_off, tex_w, tex_h;
+    float tuo, tvo, tus, tvs;  // uv offset and scale
 };
 
 // Camera in the reference's non-free mode: camera-space direction
@@ -36,7 +40,9 @@ DevCamera make_camera(const gr_camera& c);
 struct SceneDev {
     const float* verts;       // 9 floats per triangle, scene order
     const float4* normals;    // 3 per triangle (w unused) or nullptr
-    const uint32_t* tri_mat;  // material index | 0x80000000 when the triangle has normals
+    const uint32_t* tri_mat;  // material index | 0x80000000 with normals | 0x40000000 with texcoords
+    const float* uvs;         // 6 floats per triangle (texcoords of its corners) or nullptr
+    const float4* texels;     // texel pool of the material textures (rgb, unused)
     const DevMaterial* mats;
     const uint32_t* lights;   // emissive triangle ids
     uint32_t num_lights;
@@ -47,6 +53,11 @@ struct SceneDev {
     DevCamera cam;
     float env_r, env_g, env_b;
     int32_t has_env;
+    // latitude-longitude environment map (env_w == 0: the constant radiance above)
+    const float4* env_map;
+    uint32_t env_w, env_h;
+    float env_m[9];        // world-to-map rotation (row-major 3x3)
+    float env_c[3];        // scene bounding-box centre
 };
 
 constexpr int kMaxDepth = 64;
@@ -175,7 +186,10 @@ struct gr_scene {
     gr_ctx* ctx = nullptr;
     gr_bvh* bvh = nullptr;
     uint32_t num_tris = 0, num_lights = 0;
-    gr::DevBuf verts, normals, tri_mat, mats, lights;
+    gr::DevBuf verts, normals, tri_mat, mats, lights, uvs, texels, env_map;
+    uint32_t env_w = 0, env_h = 0;
+    float env_m[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+    float env_c[3] = {0, 0, 0};
     gr::DevBuf fb, fb_count;
     gr::WavePool pool;
     uint32_t samples_done = 0;

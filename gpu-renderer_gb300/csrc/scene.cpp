@@ -71,6 +71,13 @@ gr::SceneDev gr::scene_view(gr_scene* sc, int layout) {
     d.verts = (const float*)sc->verts.p;
     d.normals = (const float4*)sc->normals.p;
     d.tri_mat = (const uint32_t*)sc->tri_mat.p;
+    d.uvs = (const float*)sc->uvs.p;
+    d.texels = (const float4*)sc->texels.p;
+    d.env_map = (const float4*)sc->env_map.p;
+    d.env_w = sc->env_w;
+    d.env_h = sc->env_h;
+    std::memcpy(d.env_m, sc->env_m, sizeof(d.env_m));
+    std::memcpy(d.env_c, sc->env_c, sizeof(d.env_c));
     d.mats = (const gr::DevMaterial*)sc->mats.p;
     d.lights = (const uint32_t*)sc->lights.p;
     d.num_lights = sc->num_lights;
@@ -107,7 +114,7 @@ gr_status gr_scene_create(gr_ctx* ctx, const gr_mesh* meshes, uint32_t num_meshe
     if (camera->width == 0 || camera->height == 0 || !(camera->fov_deg > 0.0f && camera->fov_deg < 180.0f))
         return fail(ctx, GR_ERR_INVALID, "gr_scene_create: bad camera");
     uint64_t ntri = 0;
-    bool any_normals = false;
+    bool any_normals = false, any_uvs = false;
     for (uint32_t i = 0; i < num_meshes; ++i) {
         const gr_mesh& m = meshes[i];
         if (m.num_triangles && (!m.positions || !m.indices))
@@ -117,16 +124,25 @@ gr_status gr_scene_create(gr_ctx* ctx, const gr_mesh* meshes, uint32_t num_meshe
             if (m.indices[k] >= m.num_vertices) return fail(ctx, GR_ERR_INVALID, "gr_scene_create: index out of range");
         ntri += m.num_triangles;
         any_normals |= m.normals != nullptr;
+        any_uvs |= m.texcoords != nullptr;
     }
     if (ntri > gr::kMaxTriangles) return fail(ctx, GR_ERR_INVALID, "gr_scene_create: too many triangles");
     for (uint32_t i = 0; i < num_materials; ++i) {
         const int t = materials[i].type;
         if (t != GR_MAT_DIFFUSE && t != GR_MAT_DIELECTRIC && t != GR_MAT_CONDUCTOR)
             return fail(ctx, GR_ERR_INVALID, "gr_scene_create: unknown material type");
+        if (materials[i].color_map &&
+            (materials[i].color_map_width == 0 || materials[i].color_map_height == 0 ||
+             (uint64_t)materials[i].color_map_width * materials[i].color_map_height > (1ull << 28)))
+            return fail(ctx, GR_ERR_INVALID, "gr_scene_create: bad color_map size");
     }
+    if (env && env->enabled && env->map &&
+        (env->map_width == 0 || env->map_height == 0 || (uint64_t)env->map_width * env->map_height > (1ull << 28)))
+        return fail(ctx, GR_ERR_INVALID, "gr_scene_create: bad environment map size");
 
     std::vector<float> soup(9 * ntri);
     std::vector<float> nrm(any_normals ? 12 * ntri : 0, 0.0f);
+    std::vector<float> uvs(any_uvs ? 6 * ntri : 0, 0.0f);
     std::vector<uint32_t> tmat(ntri);
     std::vector<uint32_t> lights;
     uint64_t t = 0;
@@ -138,12 +154,14 @@ gr_status gr_scene_create(gr_ctx* ctx, const gr_mesh* meshes, uint32_t num_meshe
                 const uint32_t vi = m.indices[3ull * j + c];
                 std::memcpy(&soup[9 * t + 3 * c], m.positions + 3ull * vi, 12);
                 if (m.normals) std::memcpy(&nrm[12 * t + 4 * c], m.normals + 3ull * vi, 12);
+                if (m.texcoords) std::memcpy(&uvs[6 * t + 2 * c], m.texcoords + 2ull * vi, 8);
             }
-            tmat[t] = m.material | (m.normals ? 0x80000000u : 0u);
+            tmat[t] = m.material | (m.normals ? 0x80000000u : 0u) | (m.texcoords ? 0x40000000u : 0u);
             if (light) lights.push_back((uint32_t)t);
         }
     }
     std::vector<gr::DevMaterial> dm(num_materials ? num_materials : 1);
+    std::vector<float> texels;  // 4 floats per texel (rgb, 0)
     for (uint32_t i = 0; i < num_materials; ++i) {
         const gr_material& s = materials[i];
         gr::DevMaterial& d = dm[i];
@@ -156,6 +174,52 @@ gr_status gr_scene_create(gr_ctx* ctx, const gr_mesh* meshes, uint32_t num_meshe
         d.kr = s.k[0]; d.kg = s.k[1]; d.kb = s.k[2];
         d.ior = s.ior;
         d.emissive = emissive(s) ? 1u : 0u;
+        d.tex_off = d.tex_w = d.tex_h = 0;
+        d.tuo = s.uv_offset[0]; d.tvo = s.uv_offset[1];
+        d.tus = s.uv_scale[0]; d.tvs = s.uv_scale[1];
+        if (s.color_map) {
+            const size_t nt = (size_t)s.color_map_width * s.color_map_height;
+            d.tex_off = (uint32_t)(texels.size() / 4);
+            d.tex_w = s.color_map_width;
+            d.tex_h = s.color_map_height;
+            for (size_t k = 0; k < nt; ++k) {
+                texels.push_back(s.color_map[3 * k]);
+                texels.push_back(s.color_map[3 * k + 1]);
+                texels.push_back(s.color_map[3 * k + 2]);
+                texels.push_back(0.0f);
+            }
+        }
+    }
+    // environment map: texels, world-to-map rotation, scene bounding-box centre (scene.cpp:27)
+    std::vector<float> env_texels;
+    float env_m[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1}, env_c[3] = {0, 0, 0};
+    if (env && env->enabled && env->map) {
+        const size_t nt = (size_t)env->map_width * env->map_height;
+        env_texels.resize(4 * nt);
+        for (size_t k = 0; k < nt; ++k) {
+            env_texels[4 * k] = env->map[3 * k];
+            env_texels[4 * k + 1] = env->map[3 * k + 1];
+            env_texels[4 * k + 2] = env->map[3 * k + 2];
+            env_texels[4 * k + 3] = 0.0f;
+        }
+        // inverse of the upper 3x3 of to_world (directions ignore the translation)
+        const float* M = env->to_world;
+        const double a = M[0], b = M[1], c = M[2], d = M[4], e = M[5], f = M[6], g = M[8], h = M[9], i = M[10];
+        const double det = a * (e * i - f * h) - b * (d * i - f * g) + c * (d * h - e * g);
+        if (!(std::fabs(det) > 0.0)) return fail(ctx, GR_ERR_INVALID, "gr_scene_create: singular environment to_world");
+        const double inv[9] = {(e * i - f * h) / det, (c * h - b * i) / det, (b * f - c * e) / det,
+                               (f * g - d * i) / det, (a * i - c * g) / det, (c * d - a * f) / det,
+                               (d * h - e * g) / det, (b * g - a * h) / det, (a * e - b * d) / det};
+        for (int k = 0; k < 9; ++k) env_m[k] = (float)inv[k];
+        if (ntri) {
+            float lo[3] = {soup[0], soup[1], soup[2]}, hi[3] = {soup[0], soup[1], soup[2]};
+            for (size_t k = 0; k < 3 * ntri; ++k)
+                for (int ax = 0; ax < 3; ++ax) {
+                    lo[ax] = std::min(lo[ax], soup[3 * k + ax]);
+                    hi[ax] = std::max(hi[ax], soup[3 * k + ax]);
+                }
+            for (int ax = 0; ax < 3; ++ax) env_c[ax] = (lo[ax] + hi[ax]) * 0.5f;
+        }
     }
 
     gr_scene* sc = new (std::nothrow) gr_scene();
@@ -169,6 +233,12 @@ gr_status gr_scene_create(gr_ctx* ctx, const gr_mesh* meshes, uint32_t num_meshe
     cudaError_t e = cudaSetDevice(ctx->device);
     if (e != cudaSuccess) return cleanup(cuda_fail(ctx, e, "cudaSetDevice"));
     sc->num_tris = (uint32_t)ntri;
+    if (!env_texels.empty()) {
+        sc->env_w = env->map_width;
+        sc->env_h = env->map_height;
+        std::memcpy(sc->env_m, env_m, sizeof(env_m));
+        std::memcpy(sc->env_c, env_c, sizeof(env_c));
+    }
     sc->num_lights = (uint32_t)lights.size();
     struct Up {
         gr::DevBuf* buf;
@@ -180,6 +250,9 @@ gr_status gr_scene_create(gr_ctx* ctx, const gr_mesh* meshes, uint32_t num_meshe
         {&sc->tri_mat, tmat.data(), tmat.size() * 4},
         {&sc->mats, dm.data(), dm.size() * sizeof(gr::DevMaterial)},
         {&sc->lights, lights.data(), lights.size() * 4},
+        {&sc->uvs, uvs.data(), uvs.size() * 4},
+        {&sc->texels, texels.data(), texels.size() * 4},
+        {&sc->env_map, env_texels.data(), env_texels.size() * 4},
     };
     for (auto& u : ups) {
         if (u.bytes == 0) continue;

@@ -41,6 +41,7 @@ void mean_image(const double* sum, const uint32_t* cnt, uint32_t npix, float* ou
 extern "C" uint64_t gr_scene_device_bytes(const gr_scene* sc) {
     if (!sc) return 0;
     uint64_t b = sc->verts.bytes + sc->normals.bytes + sc->tri_mat.bytes + sc->mats.bytes + sc->lights.bytes +
+                 sc->uvs.bytes + sc->texels.bytes + sc->env_map.bytes +
                  sc->fb.bytes + sc->fb_count.bytes + sc->pool.mem.bytes;
     if (sc->bvh) {
         const gr::BvhBuffers& bb = sc->bvh->buf;

@@ -235,12 +235,14 @@ class BVH:
 class Material(ctypes.Structure):
     _fields_ = [("type", ctypes.c_int32), ("color", ctypes.c_float * 3), ("emission", ctypes.c_float * 3),
                 ("alpha_u", ctypes.c_float), ("alpha_v", ctypes.c_float), ("eta_i", ctypes.c_float * 3),
-                ("eta_t", ctypes.c_float * 3), ("k", ctypes.c_float * 3), ("ior", ctypes.c_float)]
+                ("eta_t", ctypes.c_float * 3), ("k", ctypes.c_float * 3), ("ior", ctypes.c_float),
+                ("color_map", _P), ("color_map_width", ctypes.c_uint32), ("color_map_height", ctypes.c_uint32),
+                ("uv_offset", ctypes.c_float * 2), ("uv_scale", ctypes.c_float * 2)]
 
 
 class Mesh(ctypes.Structure):
     _fields_ = [("positions", _P), ("num_vertices", ctypes.c_uint32), ("normals", _P), ("indices", _P),
-                ("num_triangles", ctypes.c_uint32), ("material", ctypes.c_uint32)]
+                ("num_triangles", ctypes.c_uint32), ("material", ctypes.c_uint32), ("texcoords", _P)]
 
 
 class Camera(ctypes.Structure):
@@ -249,7 +251,8 @@ class Camera(ctypes.Structure):
 
 
 class Environment(ctypes.Structure):
-    _fields_ = [("radiance", ctypes.c_float * 3), ("enabled", ctypes.c_int32)]
+    _fields_ = [("radiance", ctypes.c_float * 3), ("enabled", ctypes.c_int32), ("map", _P),
+                ("map_width", ctypes.c_uint32), ("map_height", ctypes.c_uint32), ("to_world", ctypes.c_float * 16)]
 
 
 class RenderOpts(ctypes.Structure):
@@ -307,7 +310,32 @@ def material_record(m):
     r.eta_t[:] = [float(x) for x in m.get("eta_t", (0.200438, 0.924033, 1.10221))]
     r.k[:] = [float(x) for x in m.get("k", (3.91295, 2.45285, 2.14219))]
     r.ior = float(m.get("ior", 1.5))
+    cm = m.get("color_map")
+    if cm is not None:  # (H, W, 3) float32, kept alive by the caller's dict
+        cm = np.ascontiguousarray(cm, np.float32)
+        m["color_map"] = cm
+        r.color_map = cm.ctypes.data
+        r.color_map_height, r.color_map_width = cm.shape[0], cm.shape[1]
+    r.uv_offset[:] = [float(x) for x in m.get("uv_offset", (0.0, 0.0))]
+    r.uv_scale[:] = [float(x) for x in m.get("uv_scale", (1.0, 1.0))]
     return r
+
+
+def environment_record(env):
+    """None / constant radiance / {"map", "to_world"} -> Environment (maps kept alive by the dict)."""
+    e = Environment()
+    if env is None:
+        return e
+    e.enabled = 1
+    if isinstance(env, dict):
+        mp = np.ascontiguousarray(env["map"], np.float32)
+        env["map"] = mp
+        e.map = mp.ctypes.data
+        e.map_height, e.map_width = mp.shape[0], mp.shape[1]
+        e.to_world[:] = [float(x) for x in np.asarray(env.get("to_world", np.eye(4)), np.float32).reshape(16)]
+    else:
+        e.radiance[:] = [float(x) for x in env]
+    return e
 
 
 class Scene:
@@ -332,16 +360,17 @@ class Scene:
             meshes[i].indices = idx.ctypes.data
             meshes[i].num_triangles = idx.shape[0]
             meshes[i].material = m.material
+            if getattr(m, "texcoords", None) is not None:
+                tc = np.ascontiguousarray(m.texcoords, np.float32)
+                self._keep.append(tc)
+                meshes[i].texcoords = tc.ctypes.data
         mats = (Material * max(len(desc.materials), 1))(*[material_record(m) for m in desc.materials])
         cam = Camera()
         cam.to_world[:] = [float(x) for x in np.asarray(desc.camera["to_world"], np.float32).reshape(16)]
         cam.fov_deg = float(desc.camera["fov"])
         cam.width = int(desc.camera["width"])
         cam.height = int(desc.camera["height"])
-        env = Environment()
-        if desc.env is not None:
-            env.radiance[:] = [float(x) for x in desc.env]
-            env.enabled = 1
+        env = environment_record(desc.env)
         h = _P()
         ctx.check(L.gr_scene_create(ctx.h, meshes, len(desc.meshes), mats, len(desc.materials), ctypes.byref(cam),
                                     ctypes.byref(env), ctypes.byref(h)), "gr_scene_create")
@@ -639,6 +668,7 @@ class ParsedScene:
         self.camera = {"to_world": np.array(cam.to_world[:], np.float32).reshape(4, 4), "fov": cam.fov_deg,
                        "width": cam.width, "height": cam.height}
         self.env = tuple(env.radiance[:]) if env.enabled else None
+        self.env_map_size = (int(env.map_width), int(env.map_height)) if env.enabled and env.map else None
 
     def triangles(self):
         L = _declare(_DESC_SIGS)

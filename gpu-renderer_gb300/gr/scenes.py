@@ -112,16 +112,18 @@ def coherent_rays(w=2048, h=2048, fov_deg=40.0, eye=(0.5, 0.5, -1.0), target=(0.
 # ---- scene descriptions for the render configurations -----------------------------
 
 class MeshDesc:
-    def __init__(self, positions, indices, material, normals=None):
+    def __init__(self, positions, indices, material, normals=None, texcoords=None):
         self.positions = np.ascontiguousarray(positions, np.float32).reshape(-1, 3)
         self.indices = np.ascontiguousarray(indices, np.uint32).reshape(-1, 3)
         self.normals = None if normals is None else np.ascontiguousarray(normals, np.float32).reshape(-1, 3)
+        self.texcoords = None if texcoords is None else np.ascontiguousarray(texcoords, np.float32).reshape(-1, 2)
         self.material = int(material)
 
 
 class SceneDesc:
-    """Meshes + materials (dicts for gr.material_record) + camera + constant
-    environment radiance (None for no environment)."""
+    """Meshes + materials (dicts for gr.material_record) + camera +
+    environment: None, a constant radiance (3 floats), or a dict
+    {"map": (H, W, 3) float32 rows bottom first, "to_world": 4x4}."""
 
     def __init__(self, meshes, materials, camera, env=None):
         self.meshes = meshes
@@ -153,6 +155,21 @@ class SceneDesc:
             t += k
         any_n = any(m.normals is not None for m in self.meshes)
         return soup, (nrm if any_n else None), tmat
+
+    def flatten_uv(self):
+        """Per-triangle corner texcoords (n, 6) and the texcoord flag bits
+        (0x40000000 per triangle that has them), or (None, zeros)."""
+        n = self.num_triangles
+        uv = np.zeros((n, 6), np.float32)
+        bits = np.zeros(n, np.uint32)
+        t = 0
+        for m in self.meshes:
+            k = m.indices.shape[0]
+            if m.texcoords is not None:
+                uv[t:t + k] = m.texcoords[m.indices].reshape(k, 6)
+                bits[t:t + k] = 0x40000000
+            t += k
+        return (uv if bits.any() else None), bits
 
 
 def look_at(origin, target, up):
@@ -413,3 +430,42 @@ def batch_job(index, config=4, min_tris=10_000, max_tris=2_000_000):
     cam = {"to_world": look_at((0.0, 2.2, 6.5), (0.0, 0.6, 0.0), (0.0, 1.0, 0.0)), "fov": 45.0,
            "width": res, "height": res}
     return SceneDesc(meshes, mats, cam, env=(0.25, 0.3, 0.35)), spp
+
+
+def checker_map(c0, c1):
+    """The reference's checkerboard texture: the 2 x 2 map (c0, c1; c1, c0)."""
+    return np.array([[c0, c1], [c1, c0]], np.float32)
+
+
+def textured_scene(width=64, height=48, seed_salt=0):
+    """Textures and an environment map: a checkerboard ground quad with
+    texcoords (uv scale 6, offset 0.25), a Lambert icosphere with a seeded
+    16 x 8 bitmap looked up at its barycentrics (no texcoords), a GGX conductor
+    icosphere with a checkerboard specular colour, a quad light, and a seeded
+    64 x 32 latitude-longitude environment map rotated about the vertical."""
+    r = rng(6, seed_salt)
+    mats = [
+        {"type": 0, "color": (0.5, 0.5, 0.5), "color_map": checker_map((0.8, 0.8, 0.8), (0.1, 0.2, 0.5)),
+         "uv_scale": (6.0, 6.0), "uv_offset": (0.25, 0.25)},
+        {"type": 0, "color": (0.5, 0.5, 0.5), "color_map": r.uniform(0.05, 0.95, (8, 16, 3)).astype(np.float32)},
+        {"type": 2, "color": (1.0, 1.0, 1.0), "alpha": 0.2,
+         "color_map": checker_map((1.0, 0.8, 0.3), (0.4, 0.9, 1.0)), "uv_scale": (3.0, 3.0)},
+        {"type": 0, "color": (0.5, 0.5, 0.5), "emission": (20.0, 20.0, 20.0)},
+    ]
+    GP, GI = quad((-4, 0, -4), (-4, 0, 4), (4, 0, 4), (4, 0, -4))
+    GT = np.array([[0, 0], [0, 1], [1, 1], [1, 0]], np.float32)
+    V, F = icosphere(2)
+    LP, LI = quad((-0.5, 3.0, -0.5), (0.5, 3.0, -0.5), (0.5, 3.0, 0.5), (-0.5, 3.0, 0.5))
+    meshes = [MeshDesc(GP, GI, 0, texcoords=GT),
+              MeshDesc(V * 0.7 + np.array([-0.8, 0.7, 0.0]), F, 1),
+              MeshDesc(V * 0.6 + np.array([0.9, 0.6, 0.3]), F, 2),
+              MeshDesc(LP, LI, 3)]
+    ang = 0.7
+    rot = np.array([[np.cos(ang), 0, np.sin(ang), 0], [0, 1, 0, 0], [-np.sin(ang), 0, np.cos(ang), 0], [0, 0, 0, 1]],
+                   np.float32)
+    yy, xx = np.mgrid[0:32, 0:64]
+    env = np.stack([0.3 + 0.6 * xx / 63.0, 0.2 + 0.7 * yy / 31.0, 0.8 - 0.5 * yy / 31.0], axis=-1).astype(np.float32)
+    env += r.uniform(0.0, 0.1, env.shape).astype(np.float32)
+    cam = {"to_world": look_at((0.0, 2.0, 6.0), (0.0, 0.6, 0.0), (0.0, 1.0, 0.0)), "fov": 45.0,
+           "width": width, "height": height}
+    return SceneDesc(meshes, mats, cam, {"map": env, "to_world": rot})

@@ -216,6 +216,17 @@ typedef struct gr_material {
     float alpha_u, alpha_v; /* GGX roughness (conductor) */
     float eta_i[3], eta_t[3], k[3]; /* conductor Fresnel terms */
     float ior;          /* dielectric index of refraction (interior / exterior) */
+    /* Optional color texture (Texture / TextureView, texture.h:15-50): NULL for
+     * the constant color above, else color_map_width x color_map_height RGB
+     * floats, row 0 first, looked up nearest at uv * uv_scale + uv_offset
+     * (uv: the triangle's interpolated texcoords, or its barycentrics when the
+     * mesh has none; texel (int(u * width) mod width, int(v * height) mod
+     * height)). A checkerboard is the 2 x 2 map (c0, c1; c1, c0). The color
+     * scales the Lambert reflectance, the conductor's specular reflectance and
+     * the dielectric's transmission and reflection, as color does. */
+    const float* color_map;
+    uint32_t color_map_width, color_map_height;
+    float uv_offset[2], uv_scale[2];
 } gr_material;
 
 typedef struct gr_mesh {
@@ -225,6 +236,7 @@ typedef struct gr_mesh {
     const uint32_t* indices; /* 3 vertex indices per triangle */
     uint32_t num_triangles;
     uint32_t material;       /* index into the material table */
+    const float* texcoords;  /* NULL, or 2 floats per vertex (texture coordinates) */
 } gr_mesh;
 
 /* Pinhole camera in the reference's Mitsuba convention (camera.h:21-38):
@@ -238,6 +250,15 @@ typedef struct gr_camera {
 typedef struct gr_environment {
     float radiance[3]; /* constant environment radiance (reference "constant" emitter) */
     int32_t enabled;
+    /* Optional latitude-longitude map (EnvironmentLight, environment.h:15-27):
+     * NULL for the constant radiance, else map_width x map_height RGB floats,
+     * row 0 first. A ray that leaves the scene sees the texel of the direction
+     * from the scene's bounding-box centre to o + 1e5 d, turned into the map's
+     * frame by the inverse of to_world (row-major 4x4): theta = acos(z) picks
+     * the row, phi = atan2(y, x) in [0, 2 pi) the column. */
+    const float* map;
+    uint32_t map_width, map_height;
+    float to_world[16];
 } gr_environment;
 
 /* Render options. The reference's PTOptions (pathtracer.h:7-14) fixes

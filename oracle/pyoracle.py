@@ -175,7 +175,14 @@ class _OrMaterial(ctypes.Structure):
     _fields_ = [("type", ctypes.c_int32), ("color", ctypes.c_float * 3), ("emission", ctypes.c_float * 3),
                 ("ax", ctypes.c_float), ("ay", ctypes.c_float), ("eta_i", ctypes.c_float * 3),
                 ("eta_t", ctypes.c_float * 3), ("k", ctypes.c_float * 3), ("ior", ctypes.c_float),
-                ("emissive", ctypes.c_uint32)]
+                ("emissive", ctypes.c_uint32), ("tex_off", ctypes.c_uint32), ("tex_w", ctypes.c_uint32),
+                ("tex_h", ctypes.c_uint32), ("tuo", ctypes.c_float), ("tvo", ctypes.c_float), ("tus", ctypes.c_float),
+                ("tvs", ctypes.c_float)]
+
+
+class _OrEnvmap(ctypes.Structure):
+    _fields_ = [("texels", ctypes.c_void_p), ("w", ctypes.c_uint32), ("h", ctypes.c_uint32),
+                ("m", ctypes.c_float * 9), ("c", ctypes.c_float * 3)]
 
 
 class _OrCamera(ctypes.Structure):
@@ -188,6 +195,10 @@ def render(desc, spp, max_depth=8, seed=0, rr_depth=3, flags=0, sample_base=0, n
     as float64 (H, W, 3), spp). `desc` is a gr.scenes.SceneDesc."""
     import gr
     soup, nrm, tmat = desc.flatten()
+    uvs, uv_bits = desc.flatten_uv()
+    tmat = tmat | uv_bits
+    texels = []
+    n_texels = 0
     mats = (_OrMaterial * max(len(desc.materials), 1))()
     for i, m in enumerate(desc.materials):
         r = gr.material_record(m)
@@ -201,17 +212,44 @@ def render(desc, spp, max_depth=8, seed=0, rr_depth=3, flags=0, sample_base=0, n
         o.k[:] = r.k[:]
         o.ior = r.ior
         o.emissive = 1 if any(x != 0.0 for x in r.emission) else 0
+        cm = m.get("color_map")
+        o.tuo, o.tvo = r.uv_offset[0], r.uv_offset[1]
+        o.tus, o.tvs = r.uv_scale[0], r.uv_scale[1]
+        if cm is not None:
+            cm = np.ascontiguousarray(cm, np.float32).reshape(-1, 3)
+            o.tex_off, o.tex_w, o.tex_h = n_texels, r.color_map_width, r.color_map_height
+            texels.append(cm)
+            n_texels += cm.shape[0]
     cam = _OrCamera()
     M = np.asarray(desc.camera["to_world"], np.float32).reshape(4, 4)
     cam.m[:] = [float(x) for x in M[:3].reshape(12)]
     cam.fov_deg = float(desc.camera["fov"])
     cam.width = int(desc.camera["width"])
     cam.height = int(desc.camera["height"])
-    env = np.zeros(3, np.float32) if desc.env is None else np.asarray(desc.env, np.float32)
+    envmap = None
+    if isinstance(desc.env, dict):
+        env = np.zeros(3, np.float32)
+        mp = np.ascontiguousarray(desc.env["map"], np.float32)
+        envmap = _OrEnvmap()
+        envmap.texels = mp.ctypes.data
+        envmap.h, envmap.w = mp.shape[0], mp.shape[1]
+        # inverse of the upper 3x3 by cofactors in double, as the library computes it
+        M = np.asarray(desc.env.get("to_world", np.eye(4)), np.float32).reshape(4, 4)
+        a, b, c, d, e, f, g, h, i = (float(M[r, k]) for r in range(3) for k in range(3))
+        det = a * (e * i - f * h) - b * (d * i - f * g) + c * (d * h - e * g)
+        inv = [(e * i - f * h) / det, (c * h - b * i) / det, (b * f - c * e) / det,
+               (f * g - d * i) / det, (a * i - c * g) / det, (c * d - a * f) / det,
+               (d * h - e * g) / det, (b * g - a * h) / det, (a * e - b * d) / det]
+        envmap.m[:] = [float(np.float32(x)) for x in inv]
+        lo, hi = soup.reshape(-1, 3).min(axis=0), soup.reshape(-1, 3).max(axis=0)
+        envmap.c[:] = [float(x) for x in ((lo + hi) * np.float32(0.5)).astype(np.float32)]
+    else:
+        env = np.zeros(3, np.float32) if desc.env is None else np.asarray(desc.env, np.float32)
+    tex = np.ascontiguousarray(np.concatenate(texels), np.float32) if texels else None
     fb = np.zeros((cam.height, cam.width, 3), np.float64)
     load().or_render(_p(soup), _p(nrm), _p(tmat), ctypes.c_uint32(soup.shape[0]), mats,
                      ctypes.c_uint32(len(desc.materials)), ctypes.byref(cam), _p(env), int(desc.env is not None),
                      ctypes.c_uint32(spp), ctypes.c_uint32(sample_base), ctypes.c_uint32(max_depth),
                      ctypes.c_uint64(seed), ctypes.c_int32(rr_depth), ctypes.c_uint32(flags), _p(fb),
-                     nthreads or threads())
+                     nthreads or threads(), _p(uvs), _p(tex), ctypes.byref(envmap) if envmap is not None else None)
     return fb

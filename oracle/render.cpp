@@ -209,9 +209,7 @@ bool refract(V3 wi, V3 n, float eta, V3& wt) {
     return true;
 }
 
-V3 color(const or_material& m) { return v3(m.color[0], m.color[1], m.color[2]); }
-
-V3 mf_eval(const or_material& m, V3 wo, V3 wi) {
+V3 mf_eval(const or_material& m, V3 color, V3 wo, V3 wi) {
     const float co = std::fabs(wo.z), ci = std::fabs(wi.z);
     V3 wh = wi + wo;
     if (ci == 0.0f || co == 0.0f) return vs(0.0f);
@@ -219,7 +217,7 @@ V3 mf_eval(const or_material& m, V3 wo, V3 wi) {
     wh = normalize(wh);
     const V3 F = fr_conductor(std::fabs(dot(wi, wh)), v3(m.eta_i[0], m.eta_i[1], m.eta_i[2]),
                               v3(m.eta_t[0], m.eta_t[1], m.eta_t[2]), v3(m.k[0], m.k[1], m.k[2]));
-    return color(m) * ggx_d(wh, m.ax, m.ay) * gg(wo, wi, m.ax, m.ay) * F / (4.0f * co);
+    return color * ggx_d(wh, m.ax, m.ay) * gg(wo, wi, m.ax, m.ay) * F / (4.0f * co);
 }
 float mf_pdf_wh(const or_material& m, V3 wo, V3 wh, bool compat) {
     if (compat) return ggx_d(wh, m.ax, m.ay) * std::fabs(wh.z) / (4.0f * dot(wo, wh));
@@ -230,14 +228,15 @@ struct Bsdf {
     Frame fr;
     const or_material* m;
     bool compat;
+    V3 color;  // the material color at the shading point
 };
 
 V3 bsdf_eval(const Bsdf& b, V3 wo_w, V3 wi_w) {
     const V3 wo = to_local(b.fr, wo_w), wi = to_local(b.fr, wi_w);
     if (wo.z == 0.0f) return vs(0.0f);
     if (!(wo.z * wi.z > 0.0f)) return vs(0.0f);
-    if (b.m->type == 0) return color(*b.m) * kInvPi * std::fabs(wi.z);
-    if (b.m->type == 2) return mf_eval(*b.m, wo, wi);
+    if (b.m->type == 0) return b.color * kInvPi * std::fabs(wi.z);
+    if (b.m->type == 2) return mf_eval(*b.m, b.color, wo, wi);
     return vs(0.0f);
 }
 float bsdf_pdf(const Bsdf& b, V3 wo_w, V3 wi_w) {
@@ -266,26 +265,26 @@ Smp bsdf_sample(const Bsdf& b, V3 wo_w, float u0, float u1) {  // bsdf.h:112-167
     if (b.m->type == 0) {
         wi = cosine_hemisphere(u0, u1);
         if (wo.z < 0.0f) wi.z = -wi.z;
-        s.f = color(*b.m) * kInvPi * std::fabs(wi.z);
+        s.f = b.color * kInvPi * std::fabs(wi.z);
         s.pdf = std::fabs(wi.z) * kInvPi;
     } else if (b.m->type == 2) {
         const V3 wh = sample_wh(wo, u0, u1, b.m->ax, b.m->ay);
         wi = reflect(wo, wh);
         if (!(wo.z * wi.z > 0.0f)) return s;
         s.pdf = mf_pdf_wh(*b.m, wo, wh, b.compat);
-        s.f = mf_eval(*b.m, wo, wi);
+        s.f = mf_eval(*b.m, b.color, wo, wi);
     } else {
         const float F = fr_dielectric(wo.z, 1.0f, b.m->ior);
         if (u0 < F) {
             wi = v3(-wo.x, -wo.y, wo.z);
             s.pdf = F;
-            s.f = color(*b.m) * F;
+            s.f = b.color * F;
         } else {
             const bool entering = wo.z > 0.0f;
             const float ei = entering ? 1.0f : b.m->ior, et = entering ? b.m->ior : 1.0f;
             const V3 n = wo.z < 0.0f ? v3(0.0f, 0.0f, -1.0f) : v3(0.0f, 0.0f, 1.0f);
             if (!refract(wo, n, ei / et, wi)) return s;
-            s.f = color(*b.m) * (1.0f - F) * ((ei * ei) / (et * et));
+            s.f = b.color * (1.0f - F) * ((ei * ei) / (et * et));
             s.pdf = 1.0f - F;
         }
     }
@@ -293,8 +292,8 @@ Smp bsdf_sample(const Bsdf& b, V3 wo_w, float u0, float u1) {  // bsdf.h:112-167
     s.wi = to_world(b.fr, wi);
     if (!s.specular) {
         if (!(wo.z * wi.z > 0.0f)) s.f = vs(0.0f);
-        else if (b.m->type == 0) s.f = color(*b.m) * kInvPi * std::fabs(wi.z);
-        else s.f = mf_eval(*b.m, wo, wi);
+        else if (b.m->type == 0) s.f = b.color * kInvPi * std::fabs(wi.z);
+        else s.f = mf_eval(*b.m, b.color, wo, wi);
     }
     return s;
 }
@@ -308,6 +307,9 @@ struct Scene {
     const or_camera* cam;
     V3 env;
     bool has_env;
+    const float* uvs;
+    const float* texels;
+    const or_envmap* envmap;
     std::vector<uint32_t> lights;
     std::vector<uint32_t> nodes;
     std::vector<float> tris;
@@ -316,6 +318,7 @@ struct Scene {
 
 struct Surf {
     V3 p, ng, ns;
+    float tu, tv;
 };
 V3 vert(const Scene& sc, uint32_t t, int k) {
     const float* p = sc.verts + 9ull * t + 3 * k;
@@ -333,14 +336,55 @@ Surf surface(const Scene& sc, uint32_t prim, float u, float v) {  // triangle.h:
     } else {
         s.ns = s.ng;
     }
+    if (sc.tri_mat[prim] & 0x40000000u) {
+        const float* q = sc.uvs + 6ull * prim;
+        s.tu = q[0] * w + q[2] * u + q[4] * v;
+        s.tv = q[1] * w + q[3] * u + q[5] * v;
+    } else {
+        s.tu = u;
+        s.tv = v;
+    }
     return s;
+}
+
+// Nearest texel (TextureView::evalSpectrum, texture.h:37-44), wrapped into [0, size).
+int wrap_texel(float x, uint32_t size) {
+    const float f = std::fmin(std::fmax(x * (float)size, -1073741824.0f), 1073741824.0f);
+    const int i = (int)f % (int)size;
+    return i < 0 ? i + (int)size : i;
+}
+
+V3 color_at(const Scene& sc, const or_material& m, float tu, float tv) {
+    if (m.tex_w == 0) return v3(m.color[0], m.color[1], m.color[2]);
+    const int x = wrap_texel(tu * m.tus + m.tuo, m.tex_w);
+    const int y = wrap_texel(tv * m.tvs + m.tvo, m.tex_h);
+    const float* c = sc.texels + 3ull * (m.tex_off + (uint32_t)y * m.tex_w + (uint32_t)x);
+    return v3(c[0], c[1], c[2]);
+}
+
+// EnvironmentLightView::Le (environment.h:15-27).
+V3 env_radiance(const Scene& sc, V3 o, V3 d) {
+    const or_envmap* e = sc.envmap;
+    if (!e || e->w == 0) return sc.env;
+    V3 w = normalize(o + d * 100000.0f - v3(e->c[0], e->c[1], e->c[2]));
+    const float* M = e->m;
+    w = normalize(v3(M[0] * w.x + M[1] * w.y + M[2] * w.z, M[3] * w.x + M[4] * w.y + M[5] * w.z,
+                     M[6] * w.x + M[7] * w.y + M[8] * w.z));
+    const float theta = std::acos(std::fmin(std::fmax(w.z, -1.0f), 1.0f));
+    float phi = std::atan2(w.y, w.x);
+    if (phi < 0.0f) phi += 6.28318530717958647692f;
+    const float uu = phi * 0.15915494309189533577f, vv = theta * 0.31830988618379067154f;
+    const uint32_t x = std::min(e->w - 1, (uint32_t)(int)(uu * (float)e->w));
+    const uint32_t y = std::min(e->h - 1, (uint32_t)(int)(vv * (float)e->h));
+    const float* c = e->texels + 3ull * (y * e->w + x);
+    return v3(c[0], c[1], c[2]);
 }
 float area(const Scene& sc, uint32_t prim) {
     const V3 p0 = vert(sc, prim, 0), p1 = vert(sc, prim, 1), p2 = vert(sc, prim, 2);
     const V3 c = cross(p1 - p0, p2 - p0);
     return std::sqrt(dot(c, c)) * 0.5f;
 }
-const or_material& mat_of(const Scene& sc, uint32_t prim) { return sc.mats[sc.tri_mat[prim] & 0x7FFFFFFFu]; }
+const or_material& mat_of(const Scene& sc, uint32_t prim) { return sc.mats[sc.tri_mat[prim] & 0x3FFFFFFFu]; }
 
 struct Hit {
     float t, u, v;
@@ -408,7 +452,7 @@ V3 path(const Scene& sc, uint32_t pixel, uint32_t sample, uint32_t D, uint64_t s
         float s[8];
         for (int k = 0; k < 8; ++k) s[k] = rng.uniform();
         if (hit.prim < 0 || as_miss) {
-            if (sc.has_env) L = L + thr * sc.env;
+            if (sc.has_env) L = L + thr * env_radiance(sc, v3(ray[0], ray[1], ray[2]), rd);
             break;
         }
         const or_material& m = mat_of(sc, (uint32_t)hit.prim);
@@ -416,7 +460,7 @@ V3 path(const Scene& sc, uint32_t pixel, uint32_t sample, uint32_t D, uint64_t s
         const V3 wo = -normalize(rd);
         if ((b == 0 || spec) && m.emissive && dot(wo, sf.ns) > 0.0f)
             L = L + thr * v3(m.emission[0], m.emission[1], m.emission[2]);
-        Bsdf bs{make_frame(sf.ns), &m, compat};
+        Bsdf bs{make_frame(sf.ns), &m, compat, color_at(sc, m, sf.tu, sf.tv)};
         if (m.type != 1 && !sc.lights.empty()) {
             const uint32_t nl = (uint32_t)sc.lights.size();
             const uint32_t lid = std::min((uint32_t)(s[0] * (float)nl), nl - 1);
@@ -463,8 +507,12 @@ V3 path(const Scene& sc, uint32_t pixel, uint32_t sample, uint32_t D, uint64_t s
 extern "C" int or_render(const float* verts, const float* normals, const uint32_t* tri_mat, uint32_t ntri,
                          const or_material* mats, uint32_t nmat, const or_camera* cam, const float* env, int has_env,
                          uint32_t spp, uint32_t sample_base, uint32_t max_depth, uint64_t seed, int32_t rr_depth,
-                         uint32_t flags, double* fb, int threads) {
+                         uint32_t flags, double* fb, int threads, const float* uvs, const float* texels,
+                         const or_envmap* envmap) {
     Scene sc;
+    sc.uvs = uvs;
+    sc.texels = texels;
+    sc.envmap = envmap;
     sc.verts = verts;
     sc.normals = normals;
     sc.tri_mat = tri_mat;
@@ -474,7 +522,7 @@ extern "C" int or_render(const float* verts, const float* normals, const uint32_
     sc.env = env ? v3(env[0], env[1], env[2]) : vs(0.0f);
     sc.has_env = has_env != 0;
     for (uint32_t t = 0; t < ntri; ++t)
-        if (mats[tri_mat[t] & 0x7FFFFFFFu].emissive) sc.lights.push_back(t);
+        if (mats[tri_mat[t] & 0x3FFFFFFFu].emissive) sc.lights.push_back(t);
     sc.nodes.assign(16ull * (ntri > 1 ? ntri - 1 : 1), 0);
     sc.tris.assign(12ull * (ntri ? ntri : 1), 0.0f);
     or_lbvh_build(verts, ntri, nullptr, nullptr, nullptr, sc.nodes.data(), sc.tris.data(), &sc.root);

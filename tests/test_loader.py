@@ -1,6 +1,7 @@
 """Mitsuba-XML / OBJ loading (CPU): round trip of the library's own exporter,
 the reference's CBox fixtures where the reference tree is present, and
 malformed input."""
+import ctypes
 import os
 
 import numpy as np
@@ -90,3 +91,54 @@ def test_procedural_shapes(tmp_path):
     # (m_transform *= X), so the later <translate> acts first: centre (2, 0, 0)
     r = np.linalg.norm(sph - np.array([2, 0, 0], np.float32), axis=1)
     np.testing.assert_allclose(r, 2.0, atol=1e-5)
+
+
+def _write_ppm(path, rgb8):
+    h, w, _ = rgb8.shape
+    path.write_bytes(b"P6\n# test image\n%d %d\n255\n" % (w, h) + rgb8.astype(np.uint8).tobytes())
+
+
+def _write_pfm(path, rgb):
+    h, w, _ = rgb.shape  # rows bottom first, little endian
+    path.write_bytes(b"PF\n%d %d\n-1.0\n" % (w, h) + np.ascontiguousarray(rgb, "<f4").tobytes())
+
+
+def test_textures_envmap_and_texcoords(tmp_path):
+    """Checkerboard and bitmap textures, an envmap and OBJ texcoords load into
+    the material maps and the environment: PPM bytes become (c/255)^2.2 with
+    row 0 the image's bottom row; PFM rows are taken as stored."""
+    img = np.arange(4 * 3 * 3).reshape(4, 3, 3) * 7  # 4 rows, 3 columns
+    _write_ppm(tmp_path / "tex.ppm", img)
+    env = np.random.default_rng(5).random((8, 16, 3)).astype(np.float32)
+    _write_pfm(tmp_path / "sky.pfm", env)
+    (tmp_path / "q.obj").write_text("v 0 0 0\nv 1 0 0\nv 1 1 0\nv 0 1 0\nvt 0 0\nvt 1 0\nvt 1 1\nvt 0 1\n"
+                                    "f 1/1 2/2 3/3\nf 1/1 3/3 4/4\n")
+    x = tmp_path / "t.xml"
+    x.write_text("""<scene>
+      <sensor type="perspective"><float name="fov" value="45"/>
+        <transform name="toWorld"><lookat target="0,0,0" origin="0,0,5" up="0,1,0"/></transform>
+        <film type="ldrfilm"><integer name="width" value="16"/><integer name="height" value="16"/></film></sensor>
+      <emitter type="envmap"><string name="filename" value="sky.pfm"/>
+        <transform name="toWorld"><rotate y="1" angle="30"/></transform></emitter>
+      <shape type="obj"><string name="filename" value="q.obj"/>
+        <bsdf type="diffuse"><texture type="checkerboard" name="reflectance">
+          <rgb name="color0" value="0.9 0.1 0.1"/><rgb name="color1" value="0.1 0.9 0.1"/>
+          <float name="uscale" value="4"/><float name="voffset" value="0.5"/></texture></bsdf></shape>
+      <shape type="cube"><bsdf type="diffuse"><texture type="bitmap" name="reflectance">
+          <string name="filename" value="tex.ppm"/></texture></bsdf></shape>
+      <shape type="rectangle"><bsdf type="diffuse"><texture type="bitmap" name="reflectance">
+          <string name="filename" value="missing.png"/></texture></bsdf></shape>
+    </scene>""")
+    p = gr.ParsedScene(str(x))
+    assert p.env_map_size == (16, 8)
+    assert len(p.warnings) == 1 and "missing.png" in p.warnings[0], p.warnings
+    _, _, mats = p.triangles()
+    chk, bmp, grey = mats[0], mats[1], mats[2]
+    assert (chk.color_map_width, chk.color_map_height) == (2, 2)
+    assert tuple(chk.uv_scale) == (4.0, 1.0) and tuple(chk.uv_offset) == (0.0, 0.5)
+    c = np.ctypeslib.as_array(ctypes.cast(chk.color_map, ctypes.POINTER(ctypes.c_float)), (12,)).reshape(2, 2, 3)
+    np.testing.assert_allclose(c, [[[0.9, 0.1, 0.1], [0.1, 0.9, 0.1]], [[0.1, 0.9, 0.1], [0.9, 0.1, 0.1]]], rtol=1e-6)
+    assert (bmp.color_map_width, bmp.color_map_height) == (3, 4)
+    b = np.ctypeslib.as_array(ctypes.cast(bmp.color_map, ctypes.POINTER(ctypes.c_float)), (36,)).reshape(4, 3, 3)
+    np.testing.assert_allclose(b, (img[::-1] / 255.0) ** 2.2, rtol=1e-5)
+    assert not grey.color_map
