@@ -21,10 +21,10 @@
 //     toWorld (:472-478). Float images are read as stb_image's stbi_loadf with
 //     vertical flip does for the reference (ReadImage, imageio.cpp:45-57): an
 //     8-bit channel c becomes (c / 255)^2.2 and row 0 is the image's bottom row.
-// Differences: "roughplastic" is loaded as Lambert with its diffuse
-// reflectance; only binary PPM (P6, 8-bit) and PFM images are read (another
-// image format leaves a texture at its 0.5 grey, an envmap skipped); each is
-// recorded as a warning.
+// Differences: only binary PPM (P6, 8-bit) and PFM images are read (another
+// image format leaves a texture at its 0.5 grey, an envmap skipped; recorded
+// as a warning); only the colour slots (reflectance, specularReflectance,
+// diffuseReflectance) take textures.
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -663,8 +663,27 @@ struct Interp {
             m.alpha_v = av;
             color_texture(m, L, "specularReflectance");
         } else if (type == "roughplastic") {
-            warn("roughplastic loaded as Lambert with its diffuseReflectance");
-            m = diffuse(get_color(L, "diffuseReflectance", f3(0.5f, 0.5f, 0.5f)));
+            // createMaterial's roughplastic (mitsubaloader.cpp:386-428): with an "etaI" colour the
+            // indices are etaI / etaT, else "eta" / "etaI"; alphaV is read from "alphaU"
+            F3 ei, et;
+            if (has(L, "etaI", Prop::Color)) {
+                ei = get_color(L, "etaI", f3(1.5f, 1.5f, 1.5f));
+                et = get_color(L, "etaT", f3(1, 1, 1));
+            } else {
+                ei = get_color(L, "eta", f3(1.5f, 1.5f, 1.5f));
+                et = get_color(L, "etaI", f3(1, 1, 1));
+            }
+            float au = has(L, "alphaU", Prop::Float) ? get_float(L, "alphaU", 0.1f) : get_float(L, "alpha", 0.1f);
+            const float av = au;
+            const F3 dc = get_color(L, "diffuseReflectance", f3(0.5f, 0.5f, 0.5f));
+            const F3 sp = get_color(L, "specularReflectance", f3(1, 1, 1));
+            m.type = GR_MAT_PLASTIC;
+            m.color[0] = dc.x; m.color[1] = dc.y; m.color[2] = dc.z;
+            m.specular[0] = sp.x; m.specular[1] = sp.y; m.specular[2] = sp.z;
+            m.eta_i[0] = ei.x; m.eta_i[1] = ei.y; m.eta_i[2] = ei.z;
+            m.eta_t[0] = et.x; m.eta_t[1] = et.y; m.eta_t[2] = et.z;
+            m.alpha_u = au;
+            m.alpha_v = av;
             color_texture(m, L, "diffuseReflectance");
         } else if (type == "disney") {
             return;  // the reference ignores it and keeps the current material

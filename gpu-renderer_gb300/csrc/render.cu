@@ -60,15 +60,19 @@ struct Bsdf {
     bool compat;
 };
 
-// GGX reflection f*cos (MicrofacetReflectEval, microfacet.h:159-181)
+// GGX reflection f*cos (MicrofacetReflectEval, microfacet.h:159-181); conductor
+// Fresnel, or for rough plastic dielectric Fresnel of the red indices
+// (Fresnel::eval, optical.h:127-137).
 __device__ __forceinline__ V3 mf_eval(const DevMaterial* m, V3 color, V3 wo, V3 wi) {
     const float co = fabsf(wo.z), ci = fabsf(wi.z);
     V3 wh = wi + wo;
     if (ci == 0.0f || co == 0.0f) return vs(0.0f);
     if (wh.x == 0.0f && wh.y == 0.0f && wh.z == 0.0f) return vs(0.0f);
     wh = normalize(wh);
-    const V3 F = fr_conductor(fabsf(dot(wi, wh)), v3(m->eir, m->eig, m->eib), v3(m->etr, m->etg, m->etb),
-                              v3(m->kr, m->kg, m->kb));
+    const V3 F = m->type == GR_MAT_PLASTIC
+                     ? vs(fr_dielectric(dot(wi, wh), m->eir, m->etr))
+                     : fr_conductor(fabsf(dot(wi, wh)), v3(m->eir, m->eig, m->eib), v3(m->etr, m->etg, m->etb),
+                                    v3(m->kr, m->kg, m->kb));
     return color * ggx_d(wh, m->ax, m->ay) * ggx_g(wo, wi, m->ax, m->ay) * F / (4.0f * co);
 }
 
@@ -80,6 +84,19 @@ __device__ __forceinline__ float mf_pdf_wh(const DevMaterial* m, V3 wo, V3 wh, b
     return ggx_g1(wo, m->ax, m->ay) * ggx_d(wh, m->ax, m->ay) / (4.0f * fabsf(wo.z));
 }
 
+// Rough plastic, both lobes (BSDF::eval over its two BxDFs, bsdf.h:57-78); local directions, same side.
+__device__ __forceinline__ V3 plastic_eval(const Bsdf& b, V3 wo, V3 wi) {
+    return b.color * kInvPi * fabsf(wi.z) + mf_eval(b.m, v3(b.m->sr, b.m->sg, b.m->sb), wo, wi);
+}
+
+// Rough plastic pdf: each lobe is picked with probability 1/2, so the density
+// is the mean of the lobes' densities. The reference sums them (its division
+// by the lobe count is a discarded expression, bsdf.h:98, :142); compat keeps it.
+__device__ __forceinline__ float plastic_pdf(const Bsdf& b, V3 wo, V3 wi) {
+    const float p = fabsf(wi.z) * kInvPi + mf_pdf_wh(b.m, wo, normalize(wo + wi), b.compat);
+    return b.compat ? p : 0.5f * p;
+}
+
 __device__ __forceinline__ V3 bsdf_eval(const Bsdf& b, V3 wo_w, V3 wi_w) {
     const V3 wo = to_local(b.fr, wo_w), wi = to_local(b.fr, wi_w);
     if (wo.z == 0.0f) return vs(0.0f);
@@ -87,6 +104,7 @@ __device__ __forceinline__ V3 bsdf_eval(const Bsdf& b, V3 wo_w, V3 wi_w) {
     if (!refl) return vs(0.0f);
     if (b.m->type == GR_MAT_DIFFUSE) return b.color * kInvPi * fabsf(wi.z);
     if (b.m->type == GR_MAT_CONDUCTOR) return mf_eval(b.m, b.color, wo, wi);
+    if (b.m->type == GR_MAT_PLASTIC) return plastic_eval(b, wo, wi);
     return vs(0.0f);
 }
 
@@ -96,6 +114,7 @@ __device__ __forceinline__ float bsdf_pdf(const Bsdf& b, V3 wo_w, V3 wi_w) {
     if (!(wo.z * wi.z > 0.0f)) return 0.0f;
     if (b.m->type == GR_MAT_DIFFUSE) return fabsf(wi.z) * kInvPi;
     if (b.m->type == GR_MAT_CONDUCTOR) return mf_pdf_wh(b.m, wo, normalize(wo + wi), b.compat);
+    if (b.m->type == GR_MAT_PLASTIC) return plastic_pdf(b, wo, wi);
     return 0.0f;
 }
 
@@ -125,6 +144,19 @@ __device__ __forceinline__ Sample bsdf_sample(const Bsdf& b, V3 wo_w, float u0, 
         if (!(wo.z * wi.z > 0.0f)) return s;
         s.pdf = mf_pdf_wh(b.m, wo, wh, b.compat);
         s.f = mf_eval(b.m, b.color, wo, wi);
+    } else if (b.m->type == GR_MAT_PLASTIC) {
+        // pick a lobe with the first number and reuse its remainder (BSDF::sample, bsdf.h:109-120)
+        const int lobe = min((int)floorf(u0 * 2.0f), 1);
+        const float v0 = u0 * 2.0f - (float)lobe;
+        if (lobe == 0) {
+            wi = cosine_hemisphere(v0, u1);
+            if (wo.z < 0.0f) wi.z = -wi.z;
+        } else {
+            wi = reflect(wo, ggx_sample_wh(wo, v0, u1, b.m->ax, b.m->ay));
+        }
+        if (!(wo.z * wi.z > 0.0f)) return s;
+        s.pdf = plastic_pdf(b, wo, wi);
+        s.f = plastic_eval(b, wo, wi);
     } else {
         const float F = fr_dielectric(wo.z, 1.0f, b.m->ior);
         if (u0 < F) {
@@ -148,6 +180,8 @@ __device__ __forceinline__ Sample bsdf_sample(const Bsdf& b, V3 wo_w, float u0, 
             s.f = vs(0.0f);
         } else if (b.m->type == GR_MAT_DIFFUSE) {
             s.f = b.color * kInvPi * fabsf(wi.z);
+        } else if (b.m->type == GR_MAT_PLASTIC) {
+            s.f = plastic_eval(b, wo, wi);
         } else {
             s.f = mf_eval(b.m, b.color, wo, wi);
         }

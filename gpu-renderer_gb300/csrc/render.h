@@ -21,6 +21,7 @@ struct DevMaterial {
     // [tex_off, tex_off + tex_w * tex_h) of the scene's texel pool
     uint32_t tex_off, tex_w, tex_h;
     float tuo, tvo, tus, tvs;  // uv offset and scale
+    float sr, sg, sb;          // rough plastic: specular lobe reflectance
 };
 
 // Camera in the reference's non-free mode: camera-space direction

@@ -129,7 +129,7 @@ gr_status gr_scene_create(gr_ctx* ctx, const gr_mesh* meshes, uint32_t num_meshe
     if (ntri > gr::kMaxTriangles) return fail(ctx, GR_ERR_INVALID, "gr_scene_create: too many triangles");
     for (uint32_t i = 0; i < num_materials; ++i) {
         const int t = materials[i].type;
-        if (t != GR_MAT_DIFFUSE && t != GR_MAT_DIELECTRIC && t != GR_MAT_CONDUCTOR)
+        if (t != GR_MAT_DIFFUSE && t != GR_MAT_DIELECTRIC && t != GR_MAT_CONDUCTOR && t != GR_MAT_PLASTIC)
             return fail(ctx, GR_ERR_INVALID, "gr_scene_create: unknown material type");
         if (materials[i].color_map &&
             (materials[i].color_map_width == 0 || materials[i].color_map_height == 0 ||
@@ -175,6 +175,7 @@ gr_status gr_scene_create(gr_ctx* ctx, const gr_mesh* meshes, uint32_t num_meshe
         d.ior = s.ior;
         d.emissive = emissive(s) ? 1u : 0u;
         d.tex_off = d.tex_w = d.tex_h = 0;
+        d.sr = s.specular[0]; d.sg = s.specular[1]; d.sb = s.specular[2];
         d.tuo = s.uv_offset[0]; d.tvo = s.uv_offset[1];
         d.tus = s.uv_scale[0]; d.tvs = s.uv_scale[1];
         if (s.color_map) {

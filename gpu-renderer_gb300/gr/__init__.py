@@ -237,7 +237,7 @@ class Material(ctypes.Structure):
                 ("alpha_u", ctypes.c_float), ("alpha_v", ctypes.c_float), ("eta_i", ctypes.c_float * 3),
                 ("eta_t", ctypes.c_float * 3), ("k", ctypes.c_float * 3), ("ior", ctypes.c_float),
                 ("color_map", _P), ("color_map_width", ctypes.c_uint32), ("color_map_height", ctypes.c_uint32),
-                ("uv_offset", ctypes.c_float * 2), ("uv_scale", ctypes.c_float * 2)]
+                ("uv_offset", ctypes.c_float * 2), ("uv_scale", ctypes.c_float * 2), ("specular", ctypes.c_float * 3)]
 
 
 class Mesh(ctypes.Structure):
@@ -265,7 +265,7 @@ class RenderStats(ctypes.Structure):
                 ("samples", ctypes.c_uint64), ("waves", ctypes.c_uint32), ("device_errors", ctypes.c_uint32)]
 
 
-MAT_DIFFUSE, MAT_DIELECTRIC, MAT_CONDUCTOR = 0, 1, 2
+MAT_DIFFUSE, MAT_DIELECTRIC, MAT_CONDUCTOR, MAT_PLASTIC = 0, 1, 2, 3
 RENDER_REFERENCE_COMPAT = 1
 RENDER_NO_GRAPH = 2
 
@@ -318,6 +318,7 @@ def material_record(m):
         r.color_map_height, r.color_map_width = cm.shape[0], cm.shape[1]
     r.uv_offset[:] = [float(x) for x in m.get("uv_offset", (0.0, 0.0))]
     r.uv_scale[:] = [float(x) for x in m.get("uv_scale", (1.0, 1.0))]
+    r.specular[:] = [float(x) for x in m.get("specular", (1.0, 1.0, 1.0))]
     return r
 
 

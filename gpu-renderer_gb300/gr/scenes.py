@@ -469,3 +469,24 @@ def textured_scene(width=64, height=48, seed_salt=0):
     cam = {"to_world": look_at((0.0, 2.0, 6.0), (0.0, 0.6, 0.0), (0.0, 1.0, 0.0)), "fov": 45.0,
            "width": width, "height": height}
     return SceneDesc(meshes, mats, cam, {"map": env, "to_world": rot})
+
+
+def plastic_scene(width=64, height=48, seed_salt=0):
+    """Rough plastic (Lambert + GGX lobes with dielectric Fresnel) at three
+    roughnesses on a grey ground under a quad light and a constant
+    environment."""
+    mats = [{"type": 0, "color": (0.6, 0.6, 0.6)},
+            {"type": 0, "color": (0.5, 0.5, 0.5), "emission": (15.0, 15.0, 15.0)}]
+    meshes = []
+    GP, GI = quad((-4, 0, -4), (-4, 0, 4), (4, 0, 4), (4, 0, -4))
+    meshes.append(MeshDesc(GP, GI, 0))
+    LP, LI = quad((-0.5, 3.0, -0.5), (0.5, 3.0, -0.5), (0.5, 3.0, 0.5), (-0.5, 3.0, 0.5))
+    meshes.append(MeshDesc(LP, LI, 1))
+    V, F = icosphere(3)
+    for k, (alpha, col) in enumerate(((0.05, (0.8, 0.2, 0.1)), (0.2, (0.1, 0.5, 0.8)), (0.5, (0.3, 0.7, 0.2)))):
+        mats.append({"type": 3, "color": col, "specular": (1.0, 1.0, 1.0), "alpha": alpha,
+                     "eta_i": (1.5, 1.5, 1.5), "eta_t": (1.0, 1.0, 1.0)})
+        meshes.append(MeshDesc(V * 0.55 + np.array([-1.3 + 1.3 * k, 0.55, 0.0]), F, len(mats) - 1))
+    cam = {"to_world": look_at((0.0, 1.8, 5.0), (0.0, 0.5, 0.0), (0.0, 1.0, 0.0)), "fov": 45.0,
+           "width": width, "height": height}
+    return SceneDesc(meshes, mats, cam, (0.2, 0.2, 0.25))

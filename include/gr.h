@@ -206,7 +206,10 @@ gr_status gr_trace_host(gr_bvh* bvh, const gr_ray* h_rays, uint64_t n, gr_hit* h
 typedef enum gr_material_type {
     GR_MAT_DIFFUSE = 0,    /* Lambert (reference MATERIAL_DIFFUSE, "diffuse") */
     GR_MAT_DIELECTRIC = 1, /* smooth Fresnel dielectric (MATERIAL_SPECULAR: "dielectric", "glass", "mirror") */
-    GR_MAT_CONDUCTOR = 2   /* GGX rough conductor (MATERIAL_ROUGH_CONDUCTOR: "roughconductor", "conductor") */
+    GR_MAT_CONDUCTOR = 2,  /* GGX rough conductor (MATERIAL_ROUGH_CONDUCTOR: "roughconductor", "conductor") */
+    GR_MAT_PLASTIC = 3     /* rough plastic (MATERIAL_ROUGH_PLASTIC, "roughplastic", bsdf.h:33-39): a Lambert lobe
+                              of color plus a GGX lobe of specular with dielectric Fresnel from eta_i[0] to
+                              eta_t[0], each lobe sampled with probability 1/2 */
 } gr_material_type;
 
 typedef struct gr_material {
@@ -227,6 +230,7 @@ typedef struct gr_material {
     const float* color_map;
     uint32_t color_map_width, color_map_height;
     float uv_offset[2], uv_scale[2];
+    float specular[3];  /* rough plastic: the GGX lobe's reflectance */
 } gr_material;
 
 typedef struct gr_mesh {

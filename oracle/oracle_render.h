@@ -16,7 +16,7 @@ extern "C" {
 
 /* Material record: same field order as the product's device material. */
 typedef struct or_material {
-    int32_t type; /* 0 diffuse, 1 smooth dielectric, 2 GGX conductor */
+    int32_t type; /* 0 diffuse, 1 smooth dielectric, 2 GGX conductor, 3 rough plastic */
     float color[3];
     float emission[3];
     float ax, ay;
@@ -28,6 +28,7 @@ typedef struct or_material {
      * uv * (tus, tvs) + (tuo, tvo) */
     uint32_t tex_off, tex_w, tex_h;
     float tuo, tvo, tus, tvs;
+    float spec[3]; /* rough plastic: specular lobe reflectance */
 } or_material;
 
 /* Latitude-longitude environment map (w == 0: the constant radiance). */

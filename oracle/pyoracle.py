@@ -177,7 +177,7 @@ class _OrMaterial(ctypes.Structure):
                 ("eta_t", ctypes.c_float * 3), ("k", ctypes.c_float * 3), ("ior", ctypes.c_float),
                 ("emissive", ctypes.c_uint32), ("tex_off", ctypes.c_uint32), ("tex_w", ctypes.c_uint32),
                 ("tex_h", ctypes.c_uint32), ("tuo", ctypes.c_float), ("tvo", ctypes.c_float), ("tus", ctypes.c_float),
-                ("tvs", ctypes.c_float)]
+                ("tvs", ctypes.c_float), ("spec", ctypes.c_float * 3)]
 
 
 class _OrEnvmap(ctypes.Structure):
@@ -212,6 +212,7 @@ def render(desc, spp, max_depth=8, seed=0, rr_depth=3, flags=0, sample_base=0, n
         o.k[:] = r.k[:]
         o.ior = r.ior
         o.emissive = 1 if any(x != 0.0 for x in r.emission) else 0
+        o.spec[:] = r.specular[:]
         cm = m.get("color_map")
         o.tuo, o.tvo = r.uv_offset[0], r.uv_offset[1]
         o.tus, o.tvs = r.uv_scale[0], r.uv_scale[1]

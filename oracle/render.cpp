@@ -215,8 +215,9 @@ V3 mf_eval(const or_material& m, V3 color, V3 wo, V3 wi) {
     if (ci == 0.0f || co == 0.0f) return vs(0.0f);
     if (wh.x == 0.0f && wh.y == 0.0f && wh.z == 0.0f) return vs(0.0f);
     wh = normalize(wh);
-    const V3 F = fr_conductor(std::fabs(dot(wi, wh)), v3(m.eta_i[0], m.eta_i[1], m.eta_i[2]),
-                              v3(m.eta_t[0], m.eta_t[1], m.eta_t[2]), v3(m.k[0], m.k[1], m.k[2]));
+    const V3 F = m.type == 3 ? vs(fr_dielectric(dot(wi, wh), m.eta_i[0], m.eta_t[0]))
+                             : fr_conductor(std::fabs(dot(wi, wh)), v3(m.eta_i[0], m.eta_i[1], m.eta_i[2]),
+                                            v3(m.eta_t[0], m.eta_t[1], m.eta_t[2]), v3(m.k[0], m.k[1], m.k[2]));
     return color * ggx_d(wh, m.ax, m.ay) * gg(wo, wi, m.ax, m.ay) * F / (4.0f * co);
 }
 float mf_pdf_wh(const or_material& m, V3 wo, V3 wh, bool compat) {
@@ -231,12 +232,22 @@ struct Bsdf {
     V3 color;  // the material color at the shading point
 };
 
+// rough plastic (bsdf.h:33-39): Lambert + GGX with dielectric Fresnel; lobes picked with probability 1/2
+V3 plastic_eval(const Bsdf& b, V3 wo, V3 wi) {
+    return b.color * kInvPi * std::fabs(wi.z) + mf_eval(*b.m, v3(b.m->spec[0], b.m->spec[1], b.m->spec[2]), wo, wi);
+}
+float plastic_pdf(const Bsdf& b, V3 wo, V3 wi) {
+    const float p = std::fabs(wi.z) * kInvPi + mf_pdf_wh(*b.m, wo, normalize(wo + wi), b.compat);
+    return b.compat ? p : 0.5f * p;  // the reference sums the lobe densities
+}
+
 V3 bsdf_eval(const Bsdf& b, V3 wo_w, V3 wi_w) {
     const V3 wo = to_local(b.fr, wo_w), wi = to_local(b.fr, wi_w);
     if (wo.z == 0.0f) return vs(0.0f);
     if (!(wo.z * wi.z > 0.0f)) return vs(0.0f);
     if (b.m->type == 0) return b.color * kInvPi * std::fabs(wi.z);
     if (b.m->type == 2) return mf_eval(*b.m, b.color, wo, wi);
+    if (b.m->type == 3) return plastic_eval(b, wo, wi);
     return vs(0.0f);
 }
 float bsdf_pdf(const Bsdf& b, V3 wo_w, V3 wi_w) {
@@ -245,6 +256,7 @@ float bsdf_pdf(const Bsdf& b, V3 wo_w, V3 wi_w) {
     if (!(wo.z * wi.z > 0.0f)) return 0.0f;
     if (b.m->type == 0) return std::fabs(wi.z) * kInvPi;
     if (b.m->type == 2) return mf_pdf_wh(*b.m, wo, normalize(wo + wi), b.compat);
+    if (b.m->type == 3) return plastic_pdf(b, wo, wi);
     return 0.0f;
 }
 
@@ -273,6 +285,18 @@ Smp bsdf_sample(const Bsdf& b, V3 wo_w, float u0, float u1) {  // bsdf.h:112-167
         if (!(wo.z * wi.z > 0.0f)) return s;
         s.pdf = mf_pdf_wh(*b.m, wo, wh, b.compat);
         s.f = mf_eval(*b.m, b.color, wo, wi);
+    } else if (b.m->type == 3) {
+        const int lobe = std::min((int)std::floor(u0 * 2.0f), 1);
+        const float v0 = u0 * 2.0f - (float)lobe;
+        if (lobe == 0) {
+            wi = cosine_hemisphere(v0, u1);
+            if (wo.z < 0.0f) wi.z = -wi.z;
+        } else {
+            wi = reflect(wo, sample_wh(wo, v0, u1, b.m->ax, b.m->ay));
+        }
+        if (!(wo.z * wi.z > 0.0f)) return s;
+        s.pdf = plastic_pdf(b, wo, wi);
+        s.f = plastic_eval(b, wo, wi);
     } else {
         const float F = fr_dielectric(wo.z, 1.0f, b.m->ior);
         if (u0 < F) {
@@ -293,6 +317,7 @@ Smp bsdf_sample(const Bsdf& b, V3 wo_w, float u0, float u1) {  // bsdf.h:112-167
     if (!s.specular) {
         if (!(wo.z * wi.z > 0.0f)) s.f = vs(0.0f);
         else if (b.m->type == 0) s.f = b.color * kInvPi * std::fabs(wi.z);
+        else if (b.m->type == 3) s.f = plastic_eval(b, wo, wi);
         else s.f = mf_eval(*b.m, b.color, wo, wi);
     }
     return s;

@@ -84,8 +84,11 @@ def test_procedural_shapes(tmp_path):
     p = gr.ParsedScene(str(x))
     assert p.num_triangles == 9 * 20 * 2 + 2 + 12
     assert p.num_light_triangles == 2
-    assert any("roughplastic" in w for w in p.warnings)
+    assert not p.warnings
     v, mesh, mats = p.triangles()
+    assert mats[2].type == gr.MAT_PLASTIC  # roughplastic: Lambert + GGX lobes (reference defaults)
+    assert tuple(mats[2].color) == pytest.approx((0.5, 0.5, 0.5)) and tuple(mats[2].specular) == (1.0, 1.0, 1.0)
+    assert mats[2].eta_i[0] == pytest.approx(1.5) and mats[2].eta_t[0] == 1.0 and mats[2].alpha_v == mats[2].alpha_u
     sph = v[mesh == 0].reshape(-1, 3)
     # the reference composes a transform's children by right-multiplication
     # (m_transform *= X), so the later <translate> acts first: centre (2, 0, 0)

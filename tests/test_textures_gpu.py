@@ -1,4 +1,4 @@
-"""Textures and environment maps: a scene with a checkerboard (texcoords), a
+"""Textures, environment maps and rough plastic: a scene with a checkerboard (texcoords), a
 bitmap looked up at barycentrics, a textured conductor and a rotated
 latitude-longitude environment map renders like the oracle, alone and in a
 batch, in both integrator modes."""
@@ -49,3 +49,11 @@ def test_textured_batch_equals_alone(ctx):
     gr.render_batch(ctx, scenes, [dict(spp=3, max_depth=6, seed=5)] * 2)
     for s, want in zip(scenes, alone):
         np.testing.assert_array_equal(s.accumulation()[0], want)
+
+
+@pytest.mark.parametrize("flags", [0, gr.RENDER_REFERENCE_COMPAT])
+def test_rough_plastic_matches_oracle(ctx, oracle, flags):
+    d = sc.plastic_scene(64, 48)
+    s = gr.Scene(ctx, d)
+    s.render(4, max_depth=6, seed=13, flags=flags, want_image=False)
+    assert _rel(s.accumulation()[0], oracle.render(d, 4, max_depth=6, seed=13, flags=flags)) < IMAGE_TOL
