@@ -110,7 +110,8 @@ extern "C" gr_status gr_render_batch(gr_ctx* ctx, gr_scene* const* scenes, const
     const bool graph = !(n && (opts[0].flags & GR_RENDER_NO_GRAPH));
     for (;;) {
         uint32_t paths = 0, pix = 0, depth = 0;
-        const uint32_t nj = gr::pack_wave(order, pool.capacity, table, &paths, &pix, &depth);
+        // the requested wave size, not a larger pool an earlier call left behind
+        const uint32_t nj = gr::pack_wave(order, cap, table, &paths, &pix, &depth);
         if (nj == 0) break;
         if ((e = gr::run_wave(pool, table.data(), nj, paths, pix, depth, ctx->num_sms, s, graph,
                               scene_tuning(scenes[0]))) != cudaSuccess) {
