@@ -327,7 +327,8 @@ def run_gpu(args):
                          "kernel": "k_trace<closest, %s>" % gr.LAYOUT_NAMES[layout], "bytes_per_ray": BYTES_PER_RAY},
             "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": N_RAYS * 32,
-                    "d2h_bytes_per_step": N_RAYS * 16, "api": "gr_trace_host (pinned host rays and hits)"},
+                    "d2h_bytes_per_step": N_RAYS * 16, "api": "gr_trace_host with page-locked host rays and hits: the traversal reads the rays and "
+                           "writes the hits in host memory over the host link inside the timed region"},
             "gpu_launches": args.steps,
             "clocks": clock_info,
             "extra": dict(extras, bvh_build_ms=statistics.median(build_ms),

@@ -191,10 +191,11 @@ gr_status gr_bvh_export_layout_tris(gr_bvh* bvh, int layout, float* h_tris);
 
 gr_status gr_trace(gr_bvh* bvh, const gr_ray* d_rays, uint64_t n, gr_hit* d_hits, int any_hit, void* stream);
 
-/* Host-memory variant: copies rays in, traces, copies hits out, waits. Large
- * queues are cut into chunks of at least 1 Mi rays on two streams so the
- * copies of one chunk overlap the traversal of another (pinned host memory
- * lets the copies run asynchronously). */
+/* Host-memory variant: rays in host memory, hits to host memory; waits. With
+ * page-locked buffers (cudaHostAlloc / cudaHostRegister) the traversal reads
+ * and writes them directly over the host link; other buffers are staged
+ * through device memory in chunks of at least 1 Mi rays on two streams, so
+ * the copies of one chunk overlap the traversal of another. */
 gr_status gr_trace_host(gr_bvh* bvh, const gr_ray* h_rays, uint64_t n, gr_hit* h_hits, int any_hit);
 
 /* ---- scene records ----------------------------------------------------------

@@ -4,6 +4,7 @@ traversal, and hit ids agree with the reference's traversal on every ray the
 FP64 oracle calls unambiguous."""
 import numpy as np
 import pytest
+import torch
 
 import gr
 import gr.scenes as sc
@@ -95,3 +96,26 @@ def test_gpu_trace_shared_edge_watertight(ctx):
     rays[:, 7] = 1e34
     h = b.trace_host(rays)
     assert np.all(h.view(np.int32)[:, 1] == 0)
+
+
+@pytest.mark.parametrize("any_hit", [False, True])
+def test_host_paths_equal_device_path(ctx, any_hit):
+    """gr_trace_host with page-locked buffers (traversal reads and writes host
+    memory directly) and with pageable buffers (staged in 1 Mi-ray chunks on
+    two streams) returns the device path's hits bit for bit."""
+    v = sc.triangle_soup(200000, seed_salt=610)
+    b = gr.BVH(ctx)
+    b.build_host(v)
+    b.set_layout(gr.LAYOUT_BVH8_Q8)
+    n = (5 << 20) // 2  # 2.5 Mi rays: three chunks when staged
+    rays = sc.shadow_rays(n, seed_salt=611) if any_hit else sc.incoherent_rays(n, seed_salt=611)
+    dr = torch.from_numpy(rays).cuda()
+    dh = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
+    b.trace_device(dr, n, dh, any_hit=any_hit, stream=torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    want = dh.cpu().numpy().view(np.uint32)
+    np.testing.assert_array_equal(b.trace_host(rays, any_hit=any_hit).view(np.uint32), want)  # pageable: staged
+    hr = torch.from_numpy(rays).pin_memory()
+    hh = torch.zeros((n, 4), dtype=torch.float32).pin_memory()
+    ctx.check(gr.load().gr_trace_host(b.h, gr._P(hr.data_ptr()), n, gr._P(hh.data_ptr()), int(any_hit)))
+    np.testing.assert_array_equal(hh.numpy().view(np.uint32), want)  # page-locked: direct
