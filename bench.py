@@ -12,6 +12,9 @@ HBM. The L2 is flushed (a 256 MB write) before every timed step.
 Prints one JSON line (rank 0). `--impl reference` times the reference's
 traversal semantics (pathtracer_kernel.h:175-233, restated on the CPU because
 the reference has no CPU traversal) on the host cores, on a bounded sample.
+Both lines also carry `reference_gpu`: the reference's own traversal kernels,
+compiled from its sources for sm_103a, timed on the GPU on the same scene and
+rays (when those kernels were built).
 """
 import argparse
 import json
@@ -138,11 +141,67 @@ def cpu_reference(steps, warmup, sample_rays=262144):
             "seconds_per_step": sum(times) / len(times)}
 
 
+def reference_gpu(verts, ref_nodes, rays_by_query, flush, steps):
+    """The reference's own trace_kernel / trace_shadow_kernel
+    (pathtracer_kernel.h:175-321), compiled from its sources for sm_103a with
+    nvcc's default flags and launched as its trace() wrappers do, timed on the
+    same triangles, tree topology and rays as ours (CUDA events, L2 flushed
+    before every launch). None when the kernels were not built."""
+    import torch
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import ref_gpu
+    if not ref_gpu.available("stock"):
+        return {"unavailable": "reference kernels not built (the reference sources were absent at build time)"}
+    rk = ref_gpu.RefKernels("stock")
+    try:
+        scene = rk.scene(ref_nodes, verts)
+        stream = torch.cuda.current_stream()
+        out = {"kernel": "trace_kernel / trace_shadow_kernel (pathtracer_kernel.h:175-321)",
+               "build": "reference sources, nvcc defaults (device -O3, FMA contraction on), sm_103a cubin",
+               "launch": "32-thread blocks, one ray per thread (pathtracer_kernel.h:235-246, 310-321)",
+               "tree": "reference LBVH topology (equal to LBVH_build word for word), depth %d" % scene.depth}
+        for name, (d_rays, any_hit) in rays_by_query.items():
+            m = d_rays.shape[0]
+            d_hits = torch.empty((m, 4), dtype=torch.float32, device=d_rays.device)
+            for _ in range(3):
+                rk.trace(scene, d_rays, d_hits, any_hit)
+            ms = []
+            for _ in range(max(3, min(steps, 10))):
+                l2_flush(flush)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                rk.trace(scene, d_rays, d_hits, any_hit)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                ms.append(e0.elapsed_time(e1))
+            out[name + "_mrays_s"] = m / (statistics.median(ms) / 1e3) / 1e6
+            del d_hits
+        del scene
+        return out
+    finally:
+        rk.close()
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
         return
     cb = cpu_reference(max(args.steps, 1), max(args.warmup, 0) and 1)
+    rg = None
+    if not args.no_reference_gpu:
+        import torch
+        if torch.cuda.is_available():
+            from gr import scenes
+            sys.path.insert(0, os.path.join(ROOT, "oracle"))
+            import pyoracle
+            verts = scenes.triangle_soup(N_TRIS)
+            dev = torch.device("cuda", 0)
+            torch.cuda.set_device(0)
+            flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+            queries = {"closest": (torch.from_numpy(scenes.incoherent_rays(N_RAYS)).to(dev), False),
+                       "coherent_closest": (torch.from_numpy(scenes.coherent_rays()).to(dev), False),
+                       "shadow_anyhit": (torch.from_numpy(scenes.shadow_rays(N_RAYS)).to(dev), True)}
+            rg = reference_gpu(verts, pyoracle.lbvh(verts)["ref_nodes"], queries, flush, args.steps)
     out = {
         "impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": cb["seconds_per_step"] * 1e3,
@@ -151,6 +210,8 @@ def run_reference(args):
         "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
         "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    if rg is not None:
+        out["reference_gpu"] = rg
     print(json.dumps(out), flush=True)
 
 
@@ -263,6 +324,16 @@ def run_gpu(args):
             ms.append(e0.elapsed_time(e1))
         extras[name + "_mrays_s"] = r2.shape[0] / (statistics.median(ms) / 1e3) / 1e6
         del d_r2
+    if rank == 0 and not args.no_reference_gpu:
+        d_s = torch.from_numpy(scenes.shadow_rays(N_RAYS)).to(dev)
+        d_c = torch.from_numpy(scenes.coherent_rays()).to(dev)
+        rg = reference_gpu(verts, bvh.export()["ref_nodes"],
+                           {"closest": (d_rays, False), "coherent_closest": (d_c, False),
+                            "shadow_anyhit": (d_s, True)}, flush, args.steps)
+        if "closest_mrays_s" in rg:
+            rg["gr_over_reference_closest"] = (n_rays / (statistics.median(kernel_ms) / 1e3) / 1e6) / rg["closest_mrays_s"]
+        extras["reference_gpu"] = rg
+        del d_s, d_c
     clock_info = clocks.stop()
 
     # render configurations (plain render, batched, serving)
@@ -366,6 +437,8 @@ def main():
     ap.add_argument("--tris", type=int, default=N_TRIS, help="triangle count (profiling cases)")
     ap.add_argument("--rays", type=int, default=N_RAYS, help="ray count (profiling cases)")
     ap.add_argument("--no-render", action="store_true", help="skip the render-configuration extras")
+    ap.add_argument("--no-reference-gpu", action="store_true",
+                    help="skip timing the reference's own traversal kernels on the GPU")
     ap.add_argument("--layout", default="auto", choices=["auto", "bvh2", "bvh4", "bvh4_q8", "bvh8_q8"],
                     help="node layout of the timed traversal (auto: autotune layout, block and short stack)")
     ap.add_argument("--block", type=int, default=128, choices=[64, 128, 256])

@@ -79,10 +79,12 @@ void or_trace_ref(const uint32_t* ref_nodes, const float* verts, uint32_t n, con
 /* FP64 distance oracle. For each ray: the FP64 distance to triangle prim[i]
  * (NaN if prim < 0), and an ambiguity flag that is 1 when another triangle is
  * hit within rel_gap of the closest distance, or the closest hit lies within
- * bary_margin of an edge. */
+ * bary_margin (barycentric) or within edge_rel times the largest coordinate
+ * magnitude (world units: FP32 rounding of the coordinates) of an edge.
+ * Near misses within the same margins count as hits. */
 void or_fp64_check(const uint32_t* ref_nodes, const float* verts, uint32_t n, const float* rays,
                    uint64_t nrays, const int32_t* prim, double* t64, uint8_t* ambiguous,
-                   double rel_gap, double bary_margin, int threads);
+                   double rel_gap, double bary_margin, double edge_rel, int threads);
 
 #ifdef __cplusplus
 }

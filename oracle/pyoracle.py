@@ -149,7 +149,7 @@ def trace_ref(ref_nodes, verts, rays, any_hit=False, stats=False, nthreads=None)
     return (hits, st) if stats else hits
 
 
-def fp64_check(ref_nodes, verts, rays, prim, rel_gap=1e-6, bary_margin=1e-6, nthreads=None):
+def fp64_check(ref_nodes, verts, rays, prim, rel_gap=1e-6, bary_margin=1e-6, edge_rel=1e-6, nthreads=None):
     v = np.ascontiguousarray(verts, np.float32).reshape(-1, 9)
     r = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
     p = np.ascontiguousarray(prim, np.int32)
@@ -157,7 +157,8 @@ def fp64_check(ref_nodes, verts, rays, prim, rel_gap=1e-6, bary_margin=1e-6, nth
     t64 = np.zeros(m, np.float64)
     amb = np.zeros(m, np.uint8)
     load().or_fp64_check(_p(ref_nodes), _p(v), v.shape[0], _p(r), ctypes.c_uint64(m), _p(p), _p(t64), _p(amb),
-                         ctypes.c_double(rel_gap), ctypes.c_double(bary_margin), nthreads or threads())
+                         ctypes.c_double(rel_gap), ctypes.c_double(bary_margin), ctypes.c_double(edge_rel),
+                         nthreads or threads())
     return t64, amb.astype(bool)
 
 

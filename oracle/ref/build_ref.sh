@@ -1,8 +1,17 @@
 #!/usr/bin/env bash
-# Compiles the reference's host LBVH (bvh.h and the headers it includes) from
-# the reference tree into oracle/_ref/libref_lbvh.so. Needs the reference
-# sources (REF_ROOT, default /root/reference) and nvcc; it runs where both
-# exist and is skipped elsewhere. Nothing from the reference is copied.
+# Compiles reference code from the reference tree into oracle/_ref/ (outputs
+# only; nothing from the reference is copied into this repository):
+#   libref_lbvh.so         the reference's host LBVH (bvh.h and the headers it
+#                          includes), for pinning the LBVH oracle;
+#   ref_kernels.cubin      the reference's own trace_kernel / trace_shadow_kernel
+#                          (pathtracer_kernel.h:175-321) for sm_103a with nvcc's
+#                          default device flags, as its own build compiles them;
+#   ref_kernels_nofma.cubin the same with --fmad=false (every float operation
+#                          rounded as written), for bit-exact pinning of the
+#                          traversal restatement;
+#   ref_layout.json        the byte layout of the records those kernels read.
+# Needs the reference sources (REF_ROOT, default /root/reference) and nvcc; it
+# runs where both exist and is skipped elsewhere.
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
 REF_ROOT="${REF_ROOT:-/root/reference}"
@@ -15,5 +24,18 @@ mkdir -p "$OUT"
 NVCC="${NVCC:-nvcc}"
 "$NVCC" -std=c++17 -O2 -DNDEBUG -Xcompiler -fPIC,-ffp-contract=off -shared \
   -I "$HERE/shim" -I "$REF_ROOT/src" \
-  -o "$OUT/libref_lbvh.so" "$HERE/ref_lbvh.cu"
-echo "built $OUT/libref_lbvh.so"
+  -o "$OUT/libref_lbvh.so" "$HERE/ref_lbvh.cu" &
+# Warnings the reference's headers raise (host functions redeclared host-device,
+# inline __global__, missing returns, unused values) are not ours to fix.
+QUIET="-diag-suppress 20040,20050,940,174,177,550"
+KFLAGS="-std=c++17 -cubin -gencode arch=compute_103a,code=sm_103a $QUIET -I $HERE/shim_assert -I $HERE/shim -I $REF_ROOT/src"
+"$NVCC" $KFLAGS -o "$OUT/ref_kernels.cubin" "$HERE/ref_kernels.cu" &
+"$NVCC" $KFLAGS --fmad=false -o "$OUT/ref_kernels_nofma.cubin" "$HERE/ref_kernels.cu" &
+TMP="$(mktemp -d)"
+"$NVCC" -std=c++17 -O1 $QUIET -Xcompiler -Wno-invalid-offsetof -I "$HERE/shim_assert" -I "$HERE/shim" \
+  -I "$REF_ROOT/src" -o "$TMP/ref_layout" "$HERE/ref_layout.cu"
+"$TMP/ref_layout" > "$OUT/ref_layout.json"
+rm -f "$TMP/ref_layout"
+rmdir "$TMP"
+wait %1 %2 %3
+echo "built $OUT/libref_lbvh.so, ref_kernels.cubin, ref_kernels_nofma.cubin, ref_layout.json"

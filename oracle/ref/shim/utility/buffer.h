@@ -27,6 +27,8 @@ public:
     const T* data() const { return m_host.data(); }
     size_t size() const { return m_host.size(); }
     void copyFrom(size_t count, BufferType, const T* src) { m_host.assign(src, src + count); }
+    void resize(size_t count) { m_host.resize(count); }
+    void clear() { m_host.assign(m_host.size(), T()); }
 
 private:
     std::vector<T> m_host;

@@ -796,9 +796,14 @@ inline D3 dsub(D3 a, D3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
 inline D3 dcross(D3 a, D3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
 inline double ddot(D3 a, D3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 
-// Double-precision Moller-Trumbore with a barycentric tolerance; returns t and
-// the smallest barycentric coordinate.
-inline bool tri64(const float* tv, D3 o, D3 d, double tol, double* t, double* minbary) {
+// Double-precision Moller-Trumbore. Accepts a near miss whose smallest
+// barycentric coordinate is at least -tol, or whose hit point lies at most
+// edge_tol (world units) outside the nearest edge. Returns t, the smallest
+// barycentric coordinate and the signed distance of the hit point from the
+// nearest edge line (each barycentric times its vertex's height over the
+// opposite edge).
+inline bool tri64(const float* tv, D3 o, D3 d, double tol, double edge_tol, double* t, double* minbary,
+                  double* edge_dist) {
     D3 p0{tv[0], tv[1], tv[2]}, p1{tv[3], tv[4], tv[5]}, p2{tv[6], tv[7], tv[8]};
     D3 e1 = dsub(p1, p0), e2 = dsub(p2, p0);
     D3 P = dcross(d, e2);
@@ -811,10 +816,25 @@ inline bool tri64(const float* tv, D3 o, D3 d, double tol, double* t, double* mi
     double v = ddot(Q, d) * inv;
     double w = 1.0 - u - v;
     double mb = std::fmin(u, std::fmin(v, w));
-    if (mb < -tol) return false;
+    D3 nrm = dcross(e1, e2), e12 = dsub(p2, p1);
+    const double twice_area = std::sqrt(ddot(nrm, nrm));
+    const double l0 = std::sqrt(ddot(e12, e12)), l1 = std::sqrt(ddot(e2, e2)), l2 = std::sqrt(ddot(e1, e1));
+    double dist = 0.0;
+    if (l0 > 0 && l1 > 0 && l2 > 0)
+        dist = std::fmin(w * twice_area / l0, std::fmin(u * twice_area / l1, v * twice_area / l2));
+    if (mb < -tol && dist < -edge_tol) return false;
     *t = ddot(Q, e2) * inv;
     *minbary = mb;
+    *edge_dist = dist;
     return true;
+}
+
+// Largest coordinate magnitude among the ray origin and the triangle's
+// vertices: the scale of the FP32 rounding in either traversal's arithmetic.
+inline double coord_scale(const float* tv, D3 o) {
+    double s = std::fmax(std::fabs(o.x), std::fmax(std::fabs(o.y), std::fabs(o.z)));
+    for (int k = 0; k < 9; ++k) s = std::fmax(s, std::fabs((double)tv[k]));
+    return s;
 }
 
 }  // namespace
@@ -878,7 +898,7 @@ extern "C" void or_trace_ref(const uint32_t* ref_nodes, const float* verts, uint
 
 extern "C" void or_fp64_check(const uint32_t* ref_nodes, const float* verts, uint32_t n, const float* rays,
                               uint64_t nrays, const int32_t* prim, double* t64, uint8_t* ambiguous, double rel_gap,
-                              double bary_margin, int threads) {
+                              double bary_margin, double edge_rel, int threads) {
     parallel_rays(nrays, threads, [&](uint64_t b, uint64_t e) {
         std::vector<int> stack;
         stack.reserve(128);
@@ -889,12 +909,13 @@ extern "C" void or_fp64_check(const uint32_t* ref_nodes, const float* verts, uin
             // distance to the reported triangle
             double tp = std::numeric_limits<double>::quiet_NaN();
             if (prim[i] >= 0 && (uint32_t)prim[i] < n) {
-                double t, mb;
-                if (tri64(verts + 9ull * prim[i], o, d, 1e30, &t, &mb)) tp = t;
+                double t, mb, ed;
+                if (tri64(verts + 9ull * prim[i], o, d, 1e30, 1e30, &t, &mb, &ed)) tp = t;
             }
             t64[i] = tp;
             // all candidates within tolerance: closest and runner-up distances
             double best = std::numeric_limits<double>::infinity(), second = best, best_mb = 1.0;
+            double best_ed = 1.0, best_tol = 0.0;
             if (n > 0) {
                 stack.clear();
                 stack.push_back(0);
@@ -924,10 +945,12 @@ extern "C" void or_fp64_check(const uint32_t* ref_nodes, const float* verts, uin
                     if (!in || t0 > t1 || t1 < tmin * (1 - 1e-6) - 1e-9 || t0 > tmax * (1 + 1e-6) + 1e-9) continue;
                     if (t0 > second * (1 + 1e-6) + 1e-9) continue;
                     if (w[7]) {
-                        double t, mb;
-                        if (tri64(verts + 9ull * w[6], o, d, bary_margin, &t, &mb)) {
+                        double t, mb, ed;
+                        const float* tv = verts + 9ull * w[6];
+                        const double etol = edge_rel * coord_scale(tv, o);
+                        if (tri64(tv, o, d, bary_margin, etol, &t, &mb, &ed)) {
                             if (t < tmin * (1 - 1e-7) - 1e-12 || t > tmax * (1 + 1e-7) + 1e-12) continue;
-                            if (t < best) { second = best; best = t; best_mb = mb; }
+                            if (t < best) { second = best; best = t; best_mb = mb; best_ed = ed; best_tol = etol; }
                             else if (t < second) second = t;
                         }
                     } else {
@@ -938,7 +961,7 @@ extern "C" void or_fp64_check(const uint32_t* ref_nodes, const float* verts, uin
             }
             bool amb = false;
             if (best < std::numeric_limits<double>::infinity()) {
-                if (best_mb < bary_margin) amb = true;
+                if (best_mb < bary_margin || best_ed < best_tol) amb = true;
                 if (second - best <= rel_gap * std::fmax(std::fabs(best), 1e-30)) amb = true;
                 if (std::fabs(best - tmin) <= rel_gap * std::fmax(std::fabs(best), 1e-30)) amb = true;
                 if (std::fabs(best - tmax) <= rel_gap * std::fmax(std::fabs(best), 1e-30)) amb = true;
