@@ -12,9 +12,10 @@ HBM. The L2 is flushed (a 256 MB write) before every timed step.
 Prints one JSON line (rank 0). `--impl reference` times the reference's
 traversal semantics (pathtracer_kernel.h:175-233, restated on the CPU because
 the reference has no CPU traversal) on the host cores, on a bounded sample.
-Both lines also carry `reference_gpu`: the reference's own traversal kernels,
-compiled from its sources for sm_103a, timed on the GPU on the same scene and
-rays (when those kernels were built).
+Both lines also carry `reference_gpu`: the reference's own kernels, compiled
+from its sources for sm_103a, timed on the GPU — its traversal kernels on the
+same tree and rays, and its whole frame loop on the Cornell-box and glossy
+render configurations (when those kernels were built).
 """
 import argparse
 import json
@@ -182,6 +183,40 @@ def reference_gpu(verts, ref_nodes, rays_by_query, flush, steps):
         rk.close()
 
 
+def reference_gpu_renders(nodes_for):
+    """The reference's whole frame loop on the GPU — its own kernels (compiled
+    from its sources, nvcc defaults) over the scene records its loader builds,
+    driven as PathTracer::render(uint32*) drives them (pathtracer.cu:41-150, a
+    device synchronise after every kernel) — for the Cornell box (256x256, 16
+    frames, depth 8) and the glossy scene (1024x768, 64 frames, depth 16).
+    `nodes_for(desc)` gives the reference-layout tree of the scene's soup.
+    Wall-clock time of the frames after one warm-up frame."""
+    import torch
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import ref_gpu
+    from gr import scenes
+    if not ref_gpu.render_available("stock"):
+        return {"unavailable": "reference kernels or frame driver not built"}
+    rk = ref_gpu.RefKernels("stock")
+    out = {}
+    try:
+        for name, make, spp, depth in (("config1_render", lambda: scenes.cornell_box(256, 256), 16, 8),
+                                       ("config3_render", scenes.glossy_scene, 64, 16)):
+            desc = make()
+            rr = ref_gpu.RefRender(rk, desc, nodes_for(desc))
+            rr.render(1, depth)
+            secs, rays = rr.render(spp, depth)
+            npix = rr.width * rr.height
+            out[name] = {"ms": secs * 1e3, "samples_per_s": npix * spp / secs, "mrays_s": rays / secs / 1e6,
+                         "frames": spp, "max_path_length": depth, "triangles": rr.triangles}
+            del rr, desc
+            torch.cuda.empty_cache()
+    finally:
+        rk.close()
+    out["timing"] = "wall clock of the frame loop, which synchronises the device after every kernel as the reference does"
+    return out
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -202,6 +237,9 @@ def run_reference(args):
                        "coherent_closest": (torch.from_numpy(scenes.coherent_rays()).to(dev), False),
                        "shadow_anyhit": (torch.from_numpy(scenes.shadow_rays(N_RAYS)).to(dev), True)}
             rg = reference_gpu(verts, pyoracle.lbvh(verts)["ref_nodes"], queries, flush, args.steps)
+            del queries, flush
+            if "unavailable" not in rg:
+                rg.update(reference_gpu_renders(lambda desc: pyoracle.lbvh(desc.flatten()[0])["ref_nodes"]))
     out = {
         "impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": cb["seconds_per_step"] * 1e3,
@@ -350,6 +388,19 @@ def run_gpu(args):
         c4 = extras["config4_batch"].get("autotune")
         tuned = wl.tuning_args(c4["tuning"], c4["wave_paths"]) if c4 else (gr.LAYOUT_BVH2, 128, 12, 0)
         extras["config5_serving"] = wl.config5(ctx, tuning=tuned)
+        if rank == 0 and not args.no_reference_gpu and "reference_gpu" in extras:
+            log("reference kernels: config 1 and config 3 frame loops")
+
+            def gr_nodes(desc):
+                t = gr.BVH(ctx)
+                t.build_host(desc.flatten()[0])
+                return t.export()["ref_nodes"]
+
+            rr = reference_gpu_renders(gr_nodes)
+            for k in ("config1_render", "config3_render"):
+                if k in rr and k in extras:
+                    rr[k]["gr_speedup"] = rr[k]["ms"] / extras[k]["ms"]
+            extras["reference_gpu"].update(rr)
 
     # end to end through the C ABI with host buffers (pinned), copies inside
     h_rays = torch.from_numpy(rays).pin_memory()

@@ -3,13 +3,17 @@
 # only; nothing from the reference is copied into this repository):
 #   libref_lbvh.so         the reference's host LBVH (bvh.h and the headers it
 #                          includes), for pinning the LBVH oracle;
-#   ref_kernels.cubin      the reference's own trace_kernel / trace_shadow_kernel
-#                          (pathtracer_kernel.h:175-321) for sm_103a with nvcc's
-#                          default device flags, as its own build compiles them;
+#   ref_kernels.cubin      the reference's own device kernels (pathtracer_kernel.h:
+#                          primary rays, traversal, shading, accumulation, frame
+#                          finish) for sm_103a with nvcc's default device flags,
+#                          as its own build compiles them;
 #   ref_kernels_nofma.cubin the same with --fmad=false (every float operation
 #                          rounded as written), for bit-exact pinning of the
 #                          traversal restatement;
-#   ref_layout.json        the byte layout of the records those kernels read.
+#   ref_layout.json        the byte layout of the records those kernels read;
+#   libref_records.so      reference scene records (camera, environment) built
+#                          by the reference's own host code, for pinning the
+#                          records ref_gpu.py lays out.
 # Needs the reference sources (REF_ROOT, default /root/reference) and nvcc; it
 # runs where both exist and is skipped elsewhere.
 set -euo pipefail
@@ -31,11 +35,15 @@ QUIET="-diag-suppress 20040,20050,940,174,177,550"
 KFLAGS="-std=c++17 -cubin -gencode arch=compute_103a,code=sm_103a $QUIET -I $HERE/shim_assert -I $HERE/shim -I $REF_ROOT/src"
 "$NVCC" $KFLAGS -o "$OUT/ref_kernels.cubin" "$HERE/ref_kernels.cu" &
 "$NVCC" $KFLAGS --fmad=false -o "$OUT/ref_kernels_nofma.cubin" "$HERE/ref_kernels.cu" &
+HOSTINC="-I $HERE/shim_assert -I $HERE/shim -I $REF_ROOT/src"
+R="$REF_ROOT/src/renderer"
+"$NVCC" -std=c++17 -O1 -shared -Xcompiler -fPIC $QUIET $HOSTINC -o "$OUT/libref_records.so" \
+  "$HERE/ref_records.cu" "$R/transform.cpp" "$R/environment.cpp" "$R/imageio.cpp" &
 TMP="$(mktemp -d)"
-"$NVCC" -std=c++17 -O1 $QUIET -Xcompiler -Wno-invalid-offsetof -I "$HERE/shim_assert" -I "$HERE/shim" \
-  -I "$REF_ROOT/src" -o "$TMP/ref_layout" "$HERE/ref_layout.cu"
+"$NVCC" -std=c++17 -O1 $QUIET -Xcompiler -Wno-invalid-offsetof $HOSTINC \
+  -o "$TMP/ref_layout" "$HERE/ref_layout.cu" "$R/transform.cpp"
 "$TMP/ref_layout" > "$OUT/ref_layout.json"
 rm -f "$TMP/ref_layout"
 rmdir "$TMP"
-wait %1 %2 %3
-echo "built $OUT/libref_lbvh.so, ref_kernels.cubin, ref_kernels_nofma.cubin, ref_layout.json"
+for job in 1 2 3 4; do wait %$job; done
+echo "built $OUT/libref_lbvh.so, libref_records.so, ref_kernels.cubin, ref_kernels_nofma.cubin, ref_layout.json"

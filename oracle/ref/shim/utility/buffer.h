@@ -1,7 +1,8 @@
-// Stand-in for the reference's utility/buffer.h, used only when compiling the
-// reference's host LBVH (bvh.h) into the oracle's reference build. The
+// Stand-in for the reference's utility/buffer.h, used when compiling reference
+// code into the oracle's reference builds (host LBVH, device kernels, record
+// layout and host records); "device" buffers are host vectors here. The
 // reference header does not compile with g++ 13 (a template parameter that
-// shadows another); the LBVH code needs nothing from it but these names.
+// shadows another); the code compiled against it needs nothing but these names.
 #pragma once
 #include <cstddef>
 #include <cstdlib>
@@ -23,8 +24,9 @@ template <BufferType TYPE, typename T>
 class Buffer {
 public:
     Buffer(size_t count = 0) : m_host(count) {}
-    T* data() { return m_host.data(); }
-    const T* data() const { return m_host.data(); }
+    // the reference's Buffer hands out a mutable pointer from a const object
+    // (environment.cpp:5 relies on it)
+    T* data() const { return const_cast<T*>(m_host.data()); }
     size_t size() const { return m_host.size(); }
     void copyFrom(size_t count, BufferType, const T* src) { m_host.assign(src, src + count); }
     void resize(size_t count) { m_host.resize(count); }
