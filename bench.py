@@ -188,9 +188,11 @@ def reference_gpu_renders(nodes_for):
     from its sources, nvcc defaults) over the scene records its loader builds,
     driven as PathTracer::render(uint32*) drives them (pathtracer.cu:41-150, a
     device synchronise after every kernel) — for the Cornell box (256x256, 16
-    frames, depth 8) and the glossy scene (1024x768, 64 frames, depth 16).
-    `nodes_for(desc)` gives the reference-layout tree of the scene's soup.
-    Wall-clock time of the frames after one warm-up frame."""
+    frames, depth 8) and the glossy scene (1024x768, 64 frames, depth 16), and
+    the 64 jobs of the batched configuration one after another (each job's spp
+    as frames, depth 8). `nodes_for(desc)` gives the reference-layout tree of
+    the scene's soup. Wall-clock time of the frames (after one warm-up frame
+    for the two single scenes); building the records is not timed."""
     import torch
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import ref_gpu
@@ -211,6 +213,22 @@ def reference_gpu_renders(nodes_for):
                          "frames": spp, "max_path_length": depth, "triangles": rr.triangles}
             del rr, desc
             torch.cuda.empty_cache()
+        # the 64-job stream of the batched configuration, one reference render
+        # per job (depth 8), as the reference renders scenes one after another
+        total, samples, setup = 0.0, 0, 0.0
+        n_jobs = 64
+        for i in range(n_jobs):
+            desc, spp = scenes.batch_job(i)
+            t0 = time.perf_counter()
+            rr = ref_gpu.RefRender(rk, desc, nodes_for(desc))
+            setup += time.perf_counter() - t0
+            secs, _ = rr.render(spp, 8)
+            total += secs
+            samples += rr.width * rr.height * spp
+            del rr, desc
+            torch.cuda.empty_cache()
+        out["config4_sequential"] = {"jobs": n_jobs, "renders_s": n_jobs / total, "seconds": total,
+                                     "samples_per_s": samples / total, "setup_seconds_excluded": setup}
     finally:
         rk.close()
     out["timing"] = "wall clock of the frame loop, which synchronises the device after every kernel as the reference does"
@@ -400,6 +418,9 @@ def run_gpu(args):
             for k in ("config1_render", "config3_render"):
                 if k in rr and k in extras:
                     rr[k]["gr_speedup"] = rr[k]["ms"] / extras[k]["ms"]
+            c4 = extras.get("config4_batch", {}).get("autotuned")
+            if "config4_sequential" in rr and c4:
+                rr["config4_sequential"]["gr_batched_speedup"] = c4["batched_renders_s"] / rr["config4_sequential"]["renders_s"]
             extras["reference_gpu"].update(rr)
 
     # end to end through the C ABI with host buffers (pinned), copies inside

@@ -360,13 +360,14 @@ def _mesh_view(L, n_tris, n_p, n_n, p_ptr, n_ptr, index_ptr, material):
     return b
 
 
-def _triangles(L, view, n_tris, first_index=0):
+def _triangles(L, view, n_tris, out=None):
     """Triangle records j = 0..n-1 of one mesh view: the view and m_index = 3j
-    (scene.cpp:8-12)."""
+    (scene.cpp:8-12), written into `out` (n_tris, Triangle size) if given."""
     T = L["Triangle"]
-    rec = np.zeros((n_tris, T["size"]), np.uint8)
+    rec = np.zeros((n_tris, T["size"]), np.uint8) if out is None else out
+    rec[:] = 0
     rec[:, T["m_mesh"]:T["m_mesh"] + view.size] = view
-    rec.view(np.uint32)[:, T["m_index"] // 4] = first_index + 3 * np.arange(n_tris, dtype=np.uint32)
+    rec.view(np.uint32)[:, T["m_index"] // 4] = 3 * np.arange(n_tris, dtype=np.uint32)
     return rec
 
 
@@ -424,8 +425,10 @@ class RefRender:
         W, H = int(cam["width"]), int(cam["height"])
         mats = material_records(L, [desc.materials[m.material] for m in desc.meshes])
         # geometry and per-mesh views, in shape order (scene.cpp:6-13)
-        recs, lights = [], []
-        n_total = 0
+        n_total = desc.num_triangles
+        triangles = np.empty((n_total, L["Triangle"]["size"]), np.uint8)
+        lights = []
+        first = 0
         for m, (mat_bytes, tex) in zip(desc.meshes, mats):
             for off, texel in tex.items():
                 ptr = upload(np.asarray(texel, np.float32).reshape(1, 3))
@@ -444,15 +447,13 @@ class RefRender:
                 corner[:, 2] = tri.reshape(-1)
                 n_ptr, n_n = upload(nrm), nrm.shape[0]
             view = _mesh_view(L, tri.shape[0], pos.shape[0], n_n, upload(pos), n_ptr, upload(corner), mat_bytes)
-            r = _triangles(L, view, tri.shape[0])
-            recs.append(r)
+            r = _triangles(L, view, tri.shape[0], triangles[first:first + tri.shape[0]])
             em = desc.materials[m.material].get("emission", (0.0, 0.0, 0.0))
             if any(float(x) != 0.0 for x in em):
-                lights.append(r)
-            n_total += tri.shape[0]
+                lights.append(r.copy())
+            first += tri.shape[0]
         if not lights:
             raise ValueError("the reference's light sampling needs an emissive triangle (sample_lights)")
-        triangles = np.concatenate(recs)
         light_recs = np.concatenate(lights)
         self.depth = tree_depth(ref_nodes, n_total)
         if self.depth > STACK_ENTRIES:
@@ -472,7 +473,7 @@ class RefRender:
         _put(sv, S["m_lights_num"], np.uint32, [light_recs.shape[0]])
         sv[S["m_environment_light"]:S["m_environment_light"] + env.size] = env
         _put(sv, S["m_bvh"], np.uint64, [upload(np.ascontiguousarray(ref_nodes, np.uint32).reshape(-1))])
-        del triangles, recs
+        del triangles
         # framebuffer (framebuffer.h:8-35) and queues sized to the pixel count
         npix = W * H
         self.fb = torch.zeros((npix, 3), dtype=torch.float32, device=dev)
