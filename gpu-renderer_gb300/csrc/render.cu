@@ -32,6 +32,8 @@ constexpr uint32_t kFlagSpecular = 1u;
 constexpr int kShadeThreads = 256;
 constexpr int kShadowBase = kMaxDepth + 1;  // shadow queue counters start here
 constexpr int kErrWord = 2 * kMaxDepth + 4;
+constexpr int kBinBase = 2 * kMaxDepth + 8;  // kShadeBins counters per bounce start here
+constexpr int kCntWords = kBinBase + kShadeBins * (kMaxDepth + 1);
 
 __device__ __forceinline__ uint32_t lane_lt() {
     uint32_t m;
@@ -380,6 +382,46 @@ __global__ void __launch_bounds__(trav::kMaxTraceThreads) k_trace_shadow(Paths p
                                                                    s_stack);
 }
 
+// ---- shading groups -----------------------------------------------------------------
+// Regroups the paths of bounce b by what their ray hit (group 0: a miss; 1 + t:
+// a surface of material type t), appending each path id to its group with one
+// atomic per warp and group. The order inside a group is arbitrary; shading
+// depends on nothing but the path's own state, so images do not change.
+// (Filing the paths in the closest-hit kernel's epilogue instead measured
+// slower: the extra gathers lengthened that kernel by as much as this one takes.)
+__global__ void __launch_bounds__(kShadeThreads) k_bin(Paths ps, int b) {
+    if (b > (int)ps.hdr->max_depth) return;
+    const uint32_t n = ps.cnt[b];
+    const uint32_t* q = (b & 1) ? ps.qb : ps.qa;
+    uint32_t* cnt = ps.cnt + kBinBase + kShadeBins * b;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const int lane = threadIdx.x & 31;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+        const uint32_t i = base + threadIdx.x;
+        int bin = -1;
+        uint32_t pid = 0;
+        if (i < n) {
+            pid = q[i];
+            const int32_t prim = __float_as_int(ps.hit[pid].y);
+            bin = 0;
+            if (prim >= 0) {
+                const SceneDev& sc = ps.jobs[ps.job[pid]].sc;
+                bin = 1 + min((int)sc.mats[sc.tri_mat[prim] & 0x3FFFFFFFu].type, kShadeBins - 2);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < kShadeBins; ++k) {
+            const uint32_t m = __ballot_sync(0xFFFFFFFFu, bin == k);
+            if (!m) continue;
+            const int leader = __ffs(m) - 1;
+            uint32_t at = 0;
+            if (lane == leader) at = atomicAdd(cnt + k, (uint32_t)__popc(m));
+            at = __shfl_sync(0xFFFFFFFFu, at, leader);
+            if (bin == k) ps.bins[(size_t)k * ps.capacity + at + __popc(m & lane_lt())] = pid;
+        }
+    }
+}
+
 // ---- shading --------------------------------------------------------------------------
 // Step b first finishes the rays that shading step b-1 scattered (MIS-weighted
 // emission of a BSDF-sampled light hit, then Russian roulette:
@@ -389,9 +431,24 @@ __global__ void __launch_bounds__(trav::kMaxTraceThreads) k_trace_shadow(Paths p
 // Register cap of 64 (4 blocks of 256 per SM): measured 8 % faster renders than
 // the uncapped 118 registers (2 blocks per SM), whose few warps could not hide
 // instruction-fetch stalls of this large, divergent kernel; the spills are small.
+// BINNED: read the bounce's paths in k_bin's groups, as one array; else the
+// queue itself (waves whose scenes use one material type).
+template <bool BINNED>
 __global__ void __launch_bounds__(kShadeThreads, 4) k_shade(Paths ps, int b) {
     if (b > (int)ps.hdr->max_depth) return;
-    const uint32_t n = ps.cnt[b];
+    __shared__ uint32_t s_first[kShadeBins + 1];
+    if (BINNED) {
+        if (threadIdx.x == 0) {
+            uint32_t a = 0;
+            for (int k = 0; k < kShadeBins; ++k) {
+                s_first[k] = a;
+                a += ps.cnt[kBinBase + kShadeBins * b + k];
+            }
+            s_first[kShadeBins] = a;
+        }
+        __syncthreads();
+    }
+    const uint32_t n = BINNED ? s_first[kShadeBins] : ps.cnt[b];
     const uint32_t* q = (b & 1) ? ps.qb : ps.qa;
     uint32_t* qn = (b & 1) ? ps.qa : ps.qb;
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -403,7 +460,13 @@ __global__ void __launch_bounds__(kShadeThreads, 4) k_shade(Paths ps, int b) {
         float4 new_thr;
         uint32_t new_flags = 0;
         if (i < n) {
-            pid = q[i];
+            if (BINNED) {
+                int k = 0;
+                while (k + 1 < kShadeBins && i >= s_first[k + 1]) ++k;
+                pid = ps.bins[(size_t)k * ps.capacity + (i - s_first[k])];
+            } else {
+                pid = q[i];
+            }
             const JobDev& J = ps.jobs[ps.job[pid]];
             const SceneDev& sc = J.sc;
             const bool compat = (J.flags & GR_RENDER_REFERENCE_COMPAT) != 0;
@@ -581,17 +644,25 @@ __global__ void k_wave_end(Paths ps) {
 // One wave: clear counters, camera rays, kMaxWaveDepth x (trace, shade, shadow)
 // (steps past the wave's max_depth return at once), resolve, ray counts.
 template <int LAYOUT, int SSTACK>
-cudaError_t issue_wave_l(const Paths& ps, uint32_t depth_steps, int tgrid, int tblock, int sgrid, cudaStream_t s) {
+cudaError_t issue_wave_l(const Paths& ps, uint32_t depth_steps, int tgrid, int tblock, int sgrid, bool bin,
+                         cudaStream_t s) {
     const size_t smem = sizeof(int2) * SSTACK * tblock;
     cudaError_t e;
     const size_t cnt_bytes = sizeof(uint32_t) * (2 * kMaxDepth + 4);
+    const size_t bin_bytes = sizeof(uint32_t) * (kCntWords - kBinBase);
     const size_t work_bytes = sizeof(unsigned long long) * (2 * kMaxDepth + 4);
     if ((e = cudaMemsetAsync(ps.cnt, 0, cnt_bytes, s)) != cudaSuccess) return e;
+    if (bin && (e = cudaMemsetAsync(ps.cnt + kBinBase, 0, bin_bytes, s)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(ps.work, 0, work_bytes, s)) != cudaSuccess) return e;
     k_camera<<<sgrid, kShadeThreads, 0, s>>>(ps);
     for (int b = 0; b <= (int)depth_steps; ++b) {
         k_trace_queue<LAYOUT, SSTACK><<<tgrid, tblock, smem, s>>>(ps, b);
-        k_shade<<<sgrid, kShadeThreads, 0, s>>>(ps, b);
+        if (bin) {
+            k_bin<<<sgrid, kShadeThreads, 0, s>>>(ps, b);
+            k_shade<true><<<sgrid, kShadeThreads, 0, s>>>(ps, b);
+        } else {
+            k_shade<false><<<sgrid, kShadeThreads, 0, s>>>(ps, b);
+        }
         if (b < (int)depth_steps) k_trace_shadow<LAYOUT, SSTACK><<<tgrid, tblock, smem, s>>>(ps, b);
     }
     k_resolve<<<sgrid, kShadeThreads, 0, s>>>(ps);
@@ -600,17 +671,21 @@ cudaError_t issue_wave_l(const Paths& ps, uint32_t depth_steps, int tgrid, int t
 }
 
 template <int LAYOUT>
-cudaError_t issue_wave_s(const Paths& ps, uint32_t steps, int tgrid, const TraceTuning& t, int sgrid, cudaStream_t s) {
-    if (t.sstack == 8) return issue_wave_l<LAYOUT, 8>(ps, steps, tgrid, t.block, sgrid, s);
-    if (t.sstack == 16) return issue_wave_l<LAYOUT, 16>(ps, steps, tgrid, t.block, sgrid, s);
-    return issue_wave_l<LAYOUT, 12>(ps, steps, tgrid, t.block, sgrid, s);
+cudaError_t issue_wave_s(const Paths& ps, uint32_t steps, int tgrid, const TraceTuning& t, int sgrid, bool bin,
+                         cudaStream_t s) {
+    if (t.sstack == 8) return issue_wave_l<LAYOUT, 8>(ps, steps, tgrid, t.block, sgrid, bin, s);
+    if (t.sstack == 16) return issue_wave_l<LAYOUT, 16>(ps, steps, tgrid, t.block, sgrid, bin, s);
+    return issue_wave_l<LAYOUT, 12>(ps, steps, tgrid, t.block, sgrid, bin, s);
 }
 
-cudaError_t issue_wave(const Paths& ps, uint32_t steps, int tgrid, int sgrid, cudaStream_t s, const TraceTuning& t) {
-    if (t.layout == kLayoutBvh4) return issue_wave_s<kLayoutBvh4>(ps, steps, tgrid, t, sgrid, s);
-    if (t.layout == kLayoutBvh4Q8) return issue_wave_s<kLayoutBvh4Q8>(ps, steps, tgrid, t, sgrid, s);
-    if (t.layout == kLayoutBvh8Q8) return issue_wave_s<kLayoutBvh8Q8>(ps, steps, tgrid, t, sgrid, s);
-    return issue_wave_s<kLayoutBvh2>(ps, steps, tgrid, t, sgrid, s);
+// bin: group the paths by material before shading (waves whose scenes mix
+// material types).
+cudaError_t issue_wave(const Paths& ps, uint32_t steps, int tgrid, int sgrid, bool bin, cudaStream_t s,
+                       const TraceTuning& t) {
+    if (t.layout == kLayoutBvh4) return issue_wave_s<kLayoutBvh4>(ps, steps, tgrid, t, sgrid, bin, s);
+    if (t.layout == kLayoutBvh4Q8) return issue_wave_s<kLayoutBvh4Q8>(ps, steps, tgrid, t, sgrid, bin, s);
+    if (t.layout == kLayoutBvh8Q8) return issue_wave_s<kLayoutBvh8Q8>(ps, steps, tgrid, t, sgrid, bin, s);
+    return issue_wave_s<kLayoutBvh2>(ps, steps, tgrid, t, sgrid, bin, s);
 }
 
 // Resident blocks per SM of the closest-hit queue kernel for a configuration.
@@ -654,9 +729,10 @@ size_t path_layout(uint32_t cap, char* base, Paths* ps) {
     ps->rng = (unsigned long long*)take(8 * c);
     ps->qa = (uint32_t*)take(4 * c);
     ps->qb = (uint32_t*)take(4 * c);
+    ps->bins = (uint32_t*)take(4 * kShadeBins * c);
     ps->sray = (float4*)take(32 * c);
     ps->scon = (float4*)take(16 * c);
-    ps->cnt = (uint32_t*)take(sizeof(uint32_t) * (2 * kMaxDepth + 8));
+    ps->cnt = (uint32_t*)take(sizeof(uint32_t) * kCntWords);
     ps->work = (unsigned long long*)take(sizeof(unsigned long long) * (2 * kMaxDepth + 4));
     ps->hdr = (WaveHeader*)take(sizeof(WaveHeader));
     ps->jobs = (JobDev*)take(sizeof(JobDev) * kMaxJobs);
@@ -791,17 +867,21 @@ cudaError_t run_wave(WavePool& pool, const JobDev* h_jobs, uint32_t njobs, uint3
     const int tgrid = num_sms * occ;
     const int sgrid = num_sms * 4;
     const uint32_t steps = std::max(max_depth, kGraphDepthSteps);
-    if (!use_graph) return issue_wave(ps, max_depth, tgrid, sgrid, s, tune);
+    // shade in material groups when the wave's scenes mix material types
+    uint32_t types = 0;
+    for (uint32_t j = 0; j < njobs; ++j) types |= h_jobs[j].sc.mat_types;
+    const bool bin = __builtin_popcount(types) >= 2;
+    if (!use_graph) return issue_wave(ps, max_depth, tgrid, sgrid, bin, s, tune);
     uint64_t key = 0x51ED270B27A3C1F5ull;
     const uint64_t words[] = {(uint64_t)(uintptr_t)ps.ray, ps.capacity, steps, (uint64_t)tgrid, (uint64_t)sgrid,
-                              (uint64_t)tune.layout, (uint64_t)tune.block, (uint64_t)tune.sstack};
+                              (uint64_t)tune.layout, (uint64_t)tune.block, (uint64_t)tune.sstack, (uint64_t)bin};
     for (uint64_t w : words) key = mix64(key, w);
     WaveGraph& g = pool.graph;
     if (!g.exec || g.key != key) {
         g.release();
         cudaGraph_t graph = nullptr;
         if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return e;
-        const cudaError_t ei = issue_wave(ps, steps, tgrid, sgrid, s, tune);
+        const cudaError_t ei = issue_wave(ps, steps, tgrid, sgrid, bin, s, tune);
         e = cudaStreamEndCapture(s, &graph);
         if (ei != cudaSuccess) {
             if (graph) cudaGraphDestroy(graph);

@@ -59,9 +59,14 @@ struct SceneDev {
     uint32_t env_w, env_h;
     float env_m[9];        // world-to-map rotation (row-major 3x3)
     float env_c[3];        // scene bounding-box centre
+    uint32_t mat_types;    // bit t set when a triangle has a material of type t
 };
 
 constexpr int kMaxDepth = 64;
+// Shading groups a bounce's paths by what they hit: a miss, or one of the four
+// material types (GR_MAT_DIFFUSE .. GR_MAT_PLASTIC), so that the paths of a warp
+// run one material's code.
+constexpr int kShadeBins = 5;
 constexpr uint32_t kMaxJobs = 1024;  // jobs in one wave
 
 // One render job in a wave: a scene, its accumulation target, and the slice
@@ -103,6 +108,7 @@ struct Paths {
     unsigned long long* rng;
     uint32_t* qa;   // path-id queues, ping-pong by bounce
     uint32_t* qb;
+    uint32_t* bins; // the bounce's queue regrouped for shading: kShadeBins runs of capacity entries
     float4* sray;   // shadow rays, 2 per entry
     float4* scon;   // shadow contribution (rgb, pid bits)
     uint32_t* cnt;  // [0, kMaxDepth]: closest queue sizes; [kMaxDepth+1, ...]: shadow queue sizes
@@ -196,6 +202,7 @@ struct gr_scene {
     uint32_t samples_done = 0;
     uint32_t default_wave_paths = 0;  // 0 = library default (autotuned by gr_scene_autotune)
     gr::DevCamera cam{};
+    uint32_t mat_types = 0;  // material types its triangles use (bit per GR_MAT_*)
     gr_camera cam_rec{};  // the camera record cam was made from (view operations edit it)
     float env[3] = {0, 0, 0};
     int has_env = 0;

@@ -90,6 +90,7 @@ gr::SceneDev gr::scene_view(gr_scene* sc, int layout) {
     d.env_g = sc->env[1];
     d.env_b = sc->env[2];
     d.has_env = sc->has_env;
+    d.mat_types = sc->mat_types;
     return d;
 }
 
@@ -241,6 +242,8 @@ gr_status gr_scene_create(gr_ctx* ctx, const gr_mesh* meshes, uint32_t num_meshe
         std::memcpy(sc->env_c, env_c, sizeof(env_c));
     }
     sc->num_lights = (uint32_t)lights.size();
+    for (uint32_t i = 0; i < num_meshes; ++i)
+        if (meshes[i].num_triangles) sc->mat_types |= 1u << (uint32_t)materials[meshes[i].material].type;
     struct Up {
         gr::DevBuf* buf;
         const void* src;
