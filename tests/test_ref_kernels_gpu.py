@@ -78,17 +78,20 @@ def test_restatement_equals_reference_kernels(oracle, nofma, n, scale):
 
 
 def test_restatement_equals_reference_kernels_config2(ctx, oracle, nofma):
-    """1M-triangle tree built by our GPU LBVH (the reference topology), 262,144
-    incoherent and 262,144 shadow rays (every 16th of the workload's)."""
+    """The full workload: 1M-triangle tree built by our GPU LBVH (the reference
+    topology), all 4,194,304 incoherent rays, 4,194,304 shadow rays and the
+    2048x2048 coherent grid."""
     v = sc.triangle_soup(1000000)
     b = gr.BVH(ctx)
     b.build_host(v)
     nodes = b.export()["ref_nodes"]
     scene = nofma.scene(nodes, v)
-    rays = sc.incoherent_rays(4194304)[::16].copy()
+    rays = sc.incoherent_rays(4194304)
     _assert_same_records(nofma.trace_host(scene, rays), oracle.trace_ref(nodes, v, rays))
-    s = sc.shadow_rays(4194304)[::16].copy()
+    s = sc.shadow_rays(4194304)
     _assert_same_records(nofma.trace_host(scene, s, any_hit=True), oracle.trace_ref(nodes, v, s, any_hit=True))
+    c = sc.coherent_rays()
+    _assert_same_records(nofma.trace_host(scene, c), oracle.trace_ref(nodes, v, c))
 
 
 def test_gr_agrees_with_reference_as_shipped_config2(ctx, oracle, stock):
