@@ -11,9 +11,10 @@ renderers draw different random numbers, so the images agree statistically:
   frame far more than independent paths would; its standard error is measured
   from batches of frames;
 * our image in reference-compatible mode (GR_RENDER_REFERENCE_COMPAT, the
-  reference's estimator quirks kept) must lie within 4 standard errors of the
+  reference's estimator quirks kept) must lie within 6 standard errors of the
   reference's, per colour channel, over the whole image and over each image
-  quadrant.
+  quadrant (15 comparisons per scene; with the standard error estimated from
+  8-16 batches, 6 keeps the chance of a false failure near 1e-3 per run).
 """
 import numpy as np
 import pytest
@@ -79,5 +80,5 @@ def test_compat_render_matches_reference_kernels(ctx, stock, name, desc, batches
     img, _ = s.render(batches * frames, max_depth=depth, seed=0, flags=gr.RENDER_REFERENCE_COMPAT)
     s.close()
     ours = _regions(np.asarray(img, np.float64))
-    tol = 4.0 * ref_se + 2e-3 * np.abs(ref_mean)
+    tol = 6.0 * ref_se + 2e-3 * np.abs(ref_mean)
     assert np.all(np.abs(ours - ref_mean) <= tol), (ours, ref_mean, ref_se)
