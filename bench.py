@@ -271,6 +271,21 @@ def run_reference(args):
     print(json.dumps(out), flush=True)
 
 
+def whole_job(local_seconds, units_per_rank, device):
+    """Replicas (one process per GPU, no exchange on the data path): the job
+    takes as long as its slowest rank, and its work is the units of all ranks.
+    Returns (million units per second over the whole job, max seconds)."""
+    import torch
+    import torch.distributed as dist
+    ws = dist.get_world_size() if dist.is_available() and dist.is_initialized() else 1
+    t = float(local_seconds)
+    if ws > 1:
+        x = torch.tensor([t], device=device, dtype=torch.float64)
+        dist.all_reduce(x, op=dist.ReduceOp.MAX)
+        t = float(x.item())
+    return ws * units_per_rank / t / 1e6, t
+
+
 def l2_flush(buf):
     buf.zero_()
 
@@ -438,12 +453,7 @@ def run_gpu(args):
     e2e_value = N_RAYS * len(e2e_t) / sum(e2e_t) / 1e6
 
     # whole-job value: max time over ranks, rays over all ranks
-    t_max = total_s
-    if ws > 1:
-        t = torch.tensor([total_s], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_max = float(t.item())
-    value = ws * N_RAYS * args.steps / t_max / 1e6
+    value, t_max = whole_job(total_s, n_rays * args.steps, dev)
 
     if rank == 0:
         peak, peak_kind = measured_peaks()
