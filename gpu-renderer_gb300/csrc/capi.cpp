@@ -148,6 +148,7 @@ const char* gr_status_string(int st) {
         case GR_ERR_PARSE: return "parse error";
         case GR_ERR_TIMEOUT: return "device wait timed out";
         case GR_ERR_OVERFLOW: return "device capacity exceeded";
+        case GR_ERR_IO: return "file could not be written";
         default: return "unknown status";
     }
 }

@@ -484,6 +484,10 @@ gr_status gr_server_wait(gr_server* sv, uint64_t ticket, double timeout_s, int* 
     return GR_OK;
 }
 
+gr_status gr_server_poll(gr_server* sv, uint64_t ticket, int* done, float* h_rgb, gr_job_stats* stats) {
+    return gr_server_wait(sv, ticket, 0.0, done, h_rgb, stats);
+}
+
 gr_status gr_server_stats_get(gr_server* sv, gr_server_stats* out) {
     if (!sv || !out) return GR_ERR_INVALID;
     gr::WaveHeader h{};

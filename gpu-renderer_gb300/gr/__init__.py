@@ -18,7 +18,7 @@ LAYOUT_BVH2, LAYOUT_BVH4, LAYOUT_BVH4_Q8, LAYOUT_BVH8_Q8 = 0, 1, 2, 3
 LAYOUT_NAMES = {0: "bvh2", 1: "bvh4", 2: "bvh4_q8", 3: "bvh8_q8"}
 STATUS = {
     0: "GR_OK", 1: "GR_ERR_INVALID", 2: "GR_ERR_CUDA", 3: "GR_ERR_OOM_BUDGET",
-    4: "GR_ERR_PARSE", 5: "GR_ERR_TIMEOUT", 6: "GR_ERR_OVERFLOW",
+    4: "GR_ERR_PARSE", 5: "GR_ERR_TIMEOUT", 6: "GR_ERR_OVERFLOW", 7: "GR_ERR_IO",
 }
 
 RAY_DTYPE = np.dtype([("o", "<f4", 3), ("d", "<f4", 3), ("tmin", "<f4"), ("tmax", "<f4")])
@@ -284,7 +284,23 @@ _SCENE_SIGS = {
     "gr_scene_resize": ([_P, ctypes.c_uint32, ctypes.c_uint32], ctypes.c_int),
     "gr_scene_rgba8": ([_P, _P, _P], ctypes.c_int),
     "gr_scene_rgba8_host": ([_P, _P], ctypes.c_int),
+    "gr_scene_write_image": ([_P, ctypes.c_char_p], ctypes.c_int),
 }
+
+_IMAGE_SIGS = {
+    "gr_image_write": ([ctypes.c_char_p, _P, ctypes.c_uint32, ctypes.c_uint32], ctypes.c_int),
+}
+
+
+def image_write(path, img):
+    """gr_image_write: a linear RGB image (height, width, 3) to a .png (8-bit
+    sRGB, rows flipped as the reference writes them) or .pfm file."""
+    a = np.ascontiguousarray(img, np.float32)
+    if a.ndim != 3 or a.shape[2] != 3:
+        raise ValueError("expected an (height, width, 3) image")
+    st = _declare(_IMAGE_SIGS).gr_image_write(os.fsencode(path), _ptr(a), a.shape[1], a.shape[0])
+    if st != 0:
+        raise GrError(st, "gr_image_write(%s)" % path)
 
 
 def _declare(sigs):
@@ -415,6 +431,10 @@ class Scene:
         out = np.zeros(self.width * self.height, np.uint32)
         self.ctx.check(_declare(_SCENE_SIGS).gr_scene_rgba8_host(self.h, _ptr(out)), "gr_scene_rgba8_host")
         return out.view(np.uint8).reshape(self.height, self.width, 4)
+
+    def write_image(self, path):
+        """The accumulated mean radiance to a .png or .pfm file (PathTracer::output)."""
+        self.ctx.check(_declare(_SCENE_SIGS).gr_scene_write_image(self.h, os.fsencode(path)), "gr_scene_write_image")
 
     def rgba8_device(self, d_out, stream=None):
         self.ctx.check(_declare(_SCENE_SIGS).gr_scene_rgba8(self.h, _ptr(d_out), _P(stream) if stream else None),
@@ -556,6 +576,8 @@ _SERVER_SIGS = {
     "gr_server_submit": ([_P, _P, _P, ctypes.POINTER(RenderOpts), ctypes.POINTER(ctypes.c_uint64)], ctypes.c_int),
     "gr_server_wait": ([_P, ctypes.c_uint64, ctypes.c_double, ctypes.POINTER(ctypes.c_int), _P,
                         ctypes.POINTER(JobStats)], ctypes.c_int),
+    "gr_server_poll": ([_P, ctypes.c_uint64, ctypes.POINTER(ctypes.c_int), _P, ctypes.POINTER(JobStats)],
+                       ctypes.c_int),
     "gr_server_now": ([_P], ctypes.c_double),
     "gr_server_stats_get": ([_P, ctypes.POINTER(ServerStats)], ctypes.c_int),
 }
@@ -612,6 +634,16 @@ class Server:
         img = None if image_shape is None else np.zeros(tuple(image_shape) + (3,), np.float32)
         st = L.gr_server_wait(self.h, ticket, timeout, ctypes.byref(done), _ptr(img), ctypes.byref(js))
         self.ctx.check(st, "gr_server_wait")
+        return bool(done.value), img, js
+
+    def poll(self, ticket, image_shape=None):
+        """wait() without waiting: (done, image or None, JobStats)."""
+        L = _declare(_SERVER_SIGS)
+        done = ctypes.c_int()
+        js = JobStats()
+        img = None if image_shape is None else np.zeros(tuple(image_shape) + (3,), np.float32)
+        self.ctx.check(L.gr_server_poll(self.h, ticket, ctypes.byref(done), _ptr(img), ctypes.byref(js)),
+                       "gr_server_poll")
         return bool(done.value), img, js
 
     def now(self):

@@ -32,7 +32,8 @@ typedef enum gr_status {
     GR_ERR_OOM_BUDGET = 3,  /* allocation failed or exceeds the memory budget */
     GR_ERR_PARSE = 4,       /* scene file could not be parsed */
     GR_ERR_TIMEOUT = 5,     /* a bounded device-side wait gave up */
-    GR_ERR_OVERFLOW = 6     /* a device-side capacity (stack, queue) was exceeded */
+    GR_ERR_OVERFLOW = 6,    /* a device-side capacity (stack, queue) was exceeded */
+    GR_ERR_IO = 7           /* a file could not be written */
 } gr_status;
 
 /* Ray and hit records, byte-compatible with the reference's Ray and Hit
@@ -351,6 +352,19 @@ gr_status gr_scene_resize(gr_scene* scene, uint32_t width, uint32_t height);
 gr_status gr_scene_rgba8(gr_scene* scene, uint32_t* d_rgba, void* stream);
 gr_status gr_scene_rgba8_host(gr_scene* scene, uint32_t* h_rgba);
 
+/* ---- image files: FrameBuffer::output / WriteImage (framebuffer.cpp:11-26, imageio.cpp:59-82) ----
+ * Writes a linear RGB image (width x height x 3 floats, row 0 = the first
+ * framebuffer row) to `path`, chosen by extension:
+ *   ".png": 8-bit sRGB (the reference's GammaCorrect curve, clamp(255 g + 0.5)),
+ *           rows bottom-up as the reference writes them (vertical flip);
+ *   ".pfm": linear 32-bit floats, little-endian, rows bottom-up (PFM order).
+ * GR_ERR_INVALID for another extension or a bad size, GR_ERR_IO when the file
+ * cannot be written. Host-only: no GPU work. */
+gr_status gr_image_write(const char* path, const float* rgb, uint32_t width, uint32_t height);
+/* The scene's accumulated mean radiance written as by gr_image_write
+ * (PathTracer::output, pathtracer.cu:172-175). */
+gr_status gr_scene_write_image(gr_scene* scene, const char* path);
+
 /* Node layout the scene's renders traverse (GR_LAYOUT_*; default binary).
  * Builds the layout if needed and waits. All scenes of one gr_render_batch
  * must use the same layout. */
@@ -453,6 +467,9 @@ gr_status gr_server_submit(gr_server* server, gr_scene* scene, const gr_camera* 
  * forgotten after the call that sees it done. */
 gr_status gr_server_wait(gr_server* server, uint64_t ticket, double timeout_s, int* done, float* h_rgb,
                          gr_job_stats* stats);
+/* gr_server_wait without waiting: *done tells whether the job has finished
+ * (and then the image and stats are written as by gr_server_wait). */
+gr_status gr_server_poll(gr_server* server, uint64_t ticket, int* done, float* h_rgb, gr_job_stats* stats);
 /* Seconds on the server's clock (the clock of gr_job_stats). */
 double gr_server_now(const gr_server* server);
 gr_status gr_server_stats_get(gr_server* server, gr_server_stats* out);

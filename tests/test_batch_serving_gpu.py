@@ -105,3 +105,26 @@ def test_server_camera_override(ctx):
     d2.camera = cam2
     ref, _ = _alone(ctx, d2, dict(spp=4, max_depth=6, seed=9)).render(0)
     np.testing.assert_array_equal(img, ref)
+
+
+def test_server_poll_reports_like_wait(ctx):
+    """gr_server_poll: not done while the job runs (or done at once), then done
+    with the same image a plain render gives; a finished ticket is reported once."""
+    import time
+    d, o = _small_jobs()[0]
+    srv = gr.Server(ctx, wave_paths=5000)
+    s = gr.Scene(ctx, d)
+    t = srv.submit(s, o["spp"], o.get("max_depth", 8), o.get("seed", 0), o.get("rr_depth", 3))
+    shape = (d.camera["height"], d.camera["width"])
+    deadline = time.time() + 60.0
+    while True:
+        done, img, js = srv.poll(t, image_shape=shape)
+        if done or time.time() > deadline:
+            break
+        time.sleep(0.001)
+    assert done and js.status == 0
+    ref, _ = _alone(ctx, d, o).render(0, want_image=True)
+    np.testing.assert_array_equal(img, ref)
+    with pytest.raises(gr.GrError):
+        srv.poll(t)
+    srv.close()

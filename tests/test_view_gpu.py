@@ -96,3 +96,21 @@ def test_resize_renders_like_a_fresh_scene(ctx):
     assert s.rgba8().shape == (50, 80, 4)
     with pytest.raises(gr.GrError):
         s.resize(0, 10)
+
+
+def test_scene_write_image_is_the_mean_radiance(ctx, tmp_path):
+    """gr_scene_write_image (PathTracer::output): the accumulation's mean, as
+    gr_image_write would write it."""
+    from gr import imageio
+    s = gr.Scene(ctx, sc.cornell_box(40, 24))
+    s.render(4, max_depth=8, seed=2, want_image=False)
+    sums, cnt = s.accumulation()
+    mean = (sums / cnt[..., None]).astype(np.float32)
+    s.write_image(tmp_path / "a.pfm")
+    np.testing.assert_array_equal(imageio.read_pfm(tmp_path / "a.pfm")[::-1], mean)
+    s.write_image(tmp_path / "a.png")
+    gr.image_write(tmp_path / "b.png", mean)
+    assert open(tmp_path / "a.png", "rb").read() == open(tmp_path / "b.png", "rb").read()
+    with pytest.raises(gr.GrError):
+        s.write_image(tmp_path / "no_such_dir" / "a.png")
+    s.close()
