@@ -518,8 +518,9 @@ class PathTracer:
         return img, st
 
     def output(self, filename):
-        from . import imageio
-        imageio.write_image(filename, self.image)
+        """PathTracer::output: the accumulated image to a .png (8-bit sRGB,
+        flipped as the reference writes it) or .pfm file, by gr_scene_write_image."""
+        self.scene.write_image(filename)
 
     def reset(self):
         self.scene.reset()
