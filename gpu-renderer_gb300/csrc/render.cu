@@ -340,7 +340,7 @@ struct QueueSrc {
 };
 
 template <int LAYOUT, int SSTACK>
-__global__ void __launch_bounds__(trav::kMaxTraceThreads) k_trace_queue(Paths ps, int b) {
+__global__ void __launch_bounds__(trav::kMaxTraceThreads, 4) k_trace_queue(Paths ps, int b) {
     extern __shared__ int2 s_stack[];
     if (b > (int)ps.hdr->max_depth) return;
     QueueSrc src{(b & 1) ? ps.qb : ps.qa, &ps, ps.cnt[b]};
@@ -374,7 +374,7 @@ struct ShadowSrc {
 };
 
 template <int LAYOUT, int SSTACK>
-__global__ void __launch_bounds__(trav::kMaxTraceThreads) k_trace_shadow(Paths ps, int b) {
+__global__ void __launch_bounds__(trav::kMaxTraceThreads, 4) k_trace_shadow(Paths ps, int b) {
     extern __shared__ int2 s_stack[];
     if (b >= (int)ps.hdr->max_depth) return;
     ShadowSrc src{&ps, ps.cnt[kShadowBase + b]};

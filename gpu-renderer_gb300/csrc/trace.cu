@@ -44,7 +44,7 @@ struct RaySrc {
 };
 
 template <bool ANY, int LAYOUT, int SSTACK>
-__global__ void __launch_bounds__(trav::kMaxTraceThreads) k_trace(const void* __restrict__ nodes, const Tri* __restrict__ tris,
+__global__ void __launch_bounds__(trav::kMaxTraceThreads, 4) k_trace(const void* __restrict__ nodes, const Tri* __restrict__ tris,
                                                                   const BvhMeta* __restrict__ meta,
                                                                   const float4* __restrict__ rays, uint64_t n,
                                                                   float4* __restrict__ hits, unsigned long long* counter,
