@@ -387,6 +387,38 @@ __device__ __forceinline__ void axis_terms8(uint32_t biased_e, float lo, float o
     cf = __fadd_rn(C, m);
 }
 
+// axis_terms8 for the x and y axes at once, in packed two-lane FP32
+// (mul / sub / fma / add .rn.f32x2, |.| as a mask of the sign bits): each lane
+// rounds exactly as the scalar form.
+__device__ __forceinline__ void axis_terms8_xy(uint32_t ex, uint32_t ey, float lox, float loy, float ox, float oy,
+                                               float ix, float iy, float& Sx, float& Sy, float& cnx, float& cny,
+                                               float& cfx, float& cfy) {
+    asm("{\n\t"
+        ".reg .b64 e, inv, S, lo, o, C, aS, aC, k14, k21, t, m, cn, cf;\n\t"
+        "mov.b64 e, {%6, %7};\n\t"
+        "mov.b64 inv, {%12, %13};\n\t"
+        "mul.rn.f32x2 S, e, inv;\n\t"
+        "mov.b64 lo, {%8, %9};\n\t"
+        "mov.b64 o, {%10, %11};\n\t"
+        "sub.rn.f32x2 C, lo, o;\n\t"
+        "mul.rn.f32x2 C, C, inv;\n\t"
+        "and.b64 aS, S, 0x7FFFFFFF7FFFFFFF;\n\t"
+        "and.b64 aC, C, 0x7FFFFFFF7FFFFFFF;\n\t"
+        "mov.b64 k14, 0x3880000038800000;\n\t"  // {2^-14, 2^-14}
+        "mov.b64 k21, 0x3500000035000000;\n\t"  // {2^-21, 2^-21}
+        "mul.rn.f32x2 t, aS, k14;\n\t"
+        "fma.rn.f32x2 m, aC, k21, t;\n\t"
+        "sub.rn.f32x2 cn, C, m;\n\t"
+        "add.rn.f32x2 cf, C, m;\n\t"
+        "mov.b64 {%0, %1}, S;\n\t"
+        "mov.b64 {%2, %3}, cn;\n\t"
+        "mov.b64 {%4, %5}, cf;\n\t"
+        "}"
+        : "=f"(Sx), "=f"(Sy), "=f"(cnx), "=f"(cny), "=f"(cfx), "=f"(cfy)
+        : "f"(__uint_as_float(ex << 23)), "f"(__uint_as_float(ey << 23)), "f"(lox), "f"(loy), "f"(ox), "f"(oy),
+          "f"(ix), "f"(iy));
+}
+
 // Bit k of an 8-bit mask moved to bit k ^ oct.
 __device__ __forceinline__ uint32_t xor_permute8(uint32_t x, uint32_t oct) {
     if (oct & 1u) x = ((x & 0x55u) << 1) | ((x >> 1) & 0x55u);
@@ -436,8 +468,8 @@ __device__ __forceinline__ bool trace_step8(Lane& L, int2* s_stack, int2* l_stac
     const uint32_t sz = __float_as_uint(L.p.iz) >> 31;
     const uint32_t oct = sx | (sy << 1) | (sz << 2);
     float Sx, Sy, Sz, cnx, cfx, cny, cfy, cnz, cfz;
-    axis_terms8(meta & 0xFFu, h0.x, L.p.ox, L.p.ix, Sx, cnx, cfx);
-    axis_terms8((meta >> 8) & 0xFFu, h0.y, L.p.oy, L.p.iy, Sy, cny, cfy);
+    axis_terms8_xy(meta & 0xFFu, (meta >> 8) & 0xFFu, h0.x, h0.y, L.p.ox, L.p.oy, L.p.ix, L.p.iy, Sx, Sy, cnx, cny,
+                   cfx, cfy);
     axis_terms8((meta >> 16) & 0xFFu, h0.z, L.p.oz, L.p.iz, Sz, cnz, cfz);
     const float bound = __fmul_rn(L.best_t, kCullSlack);
     // words: b0 = (lo.x[0-3], lo.x[4-7], hi.x[0-3], hi.x[4-7]), b1 the same for y, c0 for z
