@@ -506,7 +506,7 @@ def run_render_only(args):
     names = {v: k for k, v in gr.LAYOUT_NAMES.items()}
     lay = names["bvh2" if args.layout == "auto" else args.layout]
     out = wl.plain_render(ctx, desc, args.spp or spp, depth, autotune=False,
-                          tuning=(lay, args.block, args.short_stack, 0))
+                          tuning=(lay, args.block, args.short_stack, args.wave_paths))
     print(json.dumps(dict(out, workload=args.render_only)), flush=True)
 
 
@@ -531,6 +531,8 @@ def main():
                     help="render one configuration with the given --layout/--block/--short-stack and --spp, print "
                          "its figures and exit (profiling the integrator's kernels)")
     ap.add_argument("--spp", type=int, default=0, help="samples per pixel of --render-only (0: the configuration's)")
+    ap.add_argument("--wave-paths", type=int, default=0,
+                    help="paths per wave of --render-only (0: the library's default)")
     args = ap.parse_args()
     if args.render_only:
         run_render_only(args)

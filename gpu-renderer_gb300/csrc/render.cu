@@ -791,6 +791,12 @@ cudaError_t WavePool::ensure(uint32_t paths) {
     return cudaMemset(ps.cnt + kErrWord, 0, 4);
 }
 
+cudaError_t WavePool::clear_errors(cudaStream_t s) {
+    return mem.p ? cudaMemsetAsync(ps.cnt + kErrWord, 0, 4, s) : cudaSuccess;
+}
+
+const uint32_t* WavePool::error_word() const { return ps.cnt + kErrWord; }
+
 uint32_t pack_wave(std::vector<HostJob*>& jobs, uint32_t capacity, std::vector<JobDev>& out, uint32_t* total_paths,
                    uint32_t* total_pix, uint32_t* max_depth) {
     out.clear();

@@ -290,7 +290,6 @@ gr_status gr_scene_destroy(gr_scene* sc) {
     gr_ctx* ctx = sc->ctx;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
-    sc->pool.release();
     if (sc->bvh) gr_bvh_destroy(sc->bvh);
     delete sc;
     gr::ctx_release(ctx);
@@ -315,15 +314,26 @@ gr_status gr_render(gr_scene* sc, const gr_render_opts* opts, float* h_rgb, gr_r
     SC_CUDA(ctx, cudaSetDevice(ctx->device));
     cudaStream_t s = ctx->stream;
     const uint32_t npix = sc->cam.width * sc->cam.height;
+    const bool asked = opts->wave_paths || sc->default_wave_paths;
     const uint64_t want_paths = opts->wave_paths ? opts->wave_paths
-                                : (sc->default_wave_paths ? sc->default_wave_paths : (1u << 22));
+                                : (sc->default_wave_paths ? sc->default_wave_paths : gr::kDefaultWavePaths);
     uint32_t per_wave = (uint32_t)std::max<uint64_t>(1, want_paths / npix);
     if (opts->spp) per_wave = std::min(per_wave, opts->spp);
-    const uint64_t cap64 = (uint64_t)per_wave * npix;
+    uint64_t cap64 = (uint64_t)per_wave * npix;
     if (cap64 > 0xFFFFFFFFull / 2) return fail(ctx, GR_ERR_INVALID, "gr_render: wave too large");
-    SC_CUDA(ctx, sc->pool.ensure((uint32_t)cap64));
+    gr::WavePool* pool = gr::context_pool(ctx);
+    if (!pool) return fail(ctx, GR_ERR_OOM_BUDGET, "gr_render: host allocation failed");
+    // a wave size nobody asked for halves until the device has room for it
+    cudaError_t pe;
+    while ((pe = pool->ensure((uint32_t)cap64)) != cudaSuccess && !asked && per_wave > 1) {
+        cudaGetLastError();
+        per_wave /= 2;
+        cap64 = (uint64_t)per_wave * npix;
+    }
+    SC_CUDA(ctx, pe);
+    SC_CUDA(ctx, pool->clear_errors(s));
     gr::WaveHeader before{};
-    SC_CUDA(ctx, cudaMemcpyAsync(&before, sc->pool.ps.hdr, sizeof(before), cudaMemcpyDeviceToHost, s));
+    SC_CUDA(ctx, cudaMemcpyAsync(&before, pool->ps.hdr, sizeof(before), cudaMemcpyDeviceToHost, s));
     gr::HostJob job;
     const int layout = sc->bvh->layout;
     job.sc = gr::scene_view(sc, layout);
@@ -344,14 +354,14 @@ gr_status gr_render(gr_scene* sc, const gr_render_opts* opts, float* h_rgb, gr_r
         uint32_t paths = 0, pix = 0, depth = 0;
         const uint32_t nj = gr::pack_wave(jobs, (uint32_t)cap64, table, &paths, &pix, &depth);
         if (nj == 0) break;
-        SC_CUDA(ctx, gr::run_wave(sc->pool, table.data(), nj, paths, pix, depth, ctx->num_sms, s,
+        SC_CUDA(ctx, gr::run_wave(*pool, table.data(), nj, paths, pix, depth, ctx->num_sms, s,
                                   (opts->flags & GR_RENDER_NO_GRAPH) == 0, scene_tuning(sc)));
         ++waves;
     }
     gr::WaveHeader after{};
     uint32_t err = 0;
-    SC_CUDA(ctx, cudaMemcpyAsync(&after, sc->pool.ps.hdr, sizeof(after), cudaMemcpyDeviceToHost, s));
-    SC_CUDA(ctx, cudaMemcpyAsync(&err, sc->pool.ps.cnt + 2 * gr::kMaxDepth + 4, 4, cudaMemcpyDeviceToHost, s));
+    SC_CUDA(ctx, cudaMemcpyAsync(&after, pool->ps.hdr, sizeof(after), cudaMemcpyDeviceToHost, s));
+    SC_CUDA(ctx, cudaMemcpyAsync(&err, pool->error_word(), 4, cudaMemcpyDeviceToHost, s));
     SC_CUDA(ctx, cudaStreamSynchronize(s));
     sc->samples_done += opts->spp;
     if (h_rgb) {
@@ -441,10 +451,10 @@ extern "C" gr_status gr_scene_autotune(gr_scene* sc, const gr_render_opts* probe
     SC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     // wave size (queue capacity): the probe must fill the largest candidate
     const uint32_t npix = sc->cam.width * sc->cam.height;
-    uint32_t best_wave = 1u << 22;
+    uint32_t best_wave = gr::kDefaultWavePaths;
     double best_wms = 1e300;
-    const uint32_t waves[] = {1u << 20, 1u << 21, 1u << 22, 1u << 23};
-    const uint32_t fill_spp = (uint32_t)std::max<uint64_t>(probe->spp, ((uint64_t)waves[3] + npix - 1) / npix);
+    const uint32_t waves[] = {1u << 22, 1u << 23, 1u << 24, 1u << 25, gr::kDefaultWavePaths};
+    const uint32_t fill_spp = (uint32_t)std::max<uint64_t>(probe->spp, ((uint64_t)waves[4] + npix - 1) / npix);
     for (uint32_t w : waves) {
         o = *probe;
         o.flags &= ~GR_RENDER_NO_GRAPH;

@@ -26,7 +26,21 @@ namespace {
 
 gr_status cuda_status(cudaError_t e) { return e == cudaErrorMemoryAllocation ? GR_ERR_OOM_BUDGET : GR_ERR_CUDA; }
 
+// the server's pool when its options leave the wave size open
 uint32_t default_capacity(uint32_t wave_paths) { return wave_paths ? wave_paths : (1u << 22); }
+
+}  // namespace
+
+gr::WavePool* gr::context_pool(gr_ctx* ctx) {
+    if (!ctx->batch_pool) {
+        ctx->batch_pool = new (std::nothrow) gr::WavePool();
+        if (!ctx->batch_pool) return nullptr;
+        ctx->batch_pool_free = [](void* p) { delete static_cast<gr::WavePool*>(p); };
+    }
+    return static_cast<gr::WavePool*>(ctx->batch_pool);
+}
+
+namespace {
 
 // Per-pixel mean of an accumulation (for the server's results).
 void mean_image(const double* sum, const uint32_t* cnt, uint32_t npix, float* out) {
@@ -42,7 +56,7 @@ extern "C" uint64_t gr_scene_device_bytes(const gr_scene* sc) {
     if (!sc) return 0;
     uint64_t b = sc->verts.bytes + sc->normals.bytes + sc->tri_mat.bytes + sc->mats.bytes + sc->lights.bytes +
                  sc->uvs.bytes + sc->texels.bytes + sc->env_map.bytes +
-                 sc->fb.bytes + sc->fb_count.bytes + sc->pool.mem.bytes;
+                 sc->fb.bytes + sc->fb_count.bytes;
     if (sc->bvh) {
         const gr::BvhBuffers& bb = sc->bvh->buf;
         b += bb.nodes.bytes + bb.nodes4.bytes + bb.nodes4q.bytes + bb.nodes8.bytes + bb.tris8.bytes + bb.tris.bytes +
@@ -90,19 +104,25 @@ extern "C" gr_status gr_render_batch(gr_ctx* ctx, gr_scene* const* scenes, const
     }
     cudaError_t e = cudaSetDevice(ctx->device);
     if (e != cudaSuccess) return cuda_status(e);
-    const uint32_t cap = std::max(default_capacity(wave_paths), max_npix);
-    // one pool per context for batches, owned by the context
-    if (!ctx->batch_pool) {
-        ctx->batch_pool = new (std::nothrow) gr::WavePool();
-        if (!ctx->batch_pool) return GR_ERR_OOM_BUDGET;
-        ctx->batch_pool_free = [](void* p) { delete static_cast<gr::WavePool*>(p); };
+    uint64_t want = wave_paths ? wave_paths : gr::kDefaultWavePaths;
+    uint64_t work = 0;
+    for (uint32_t i = 0; i < n; ++i) work += (uint64_t)opts[i].spp * jobs[i].npix;
+    want = std::min<uint64_t>(want, std::max<uint64_t>(work, 1));  // no larger than the batch
+    gr::WavePool* pp = gr::context_pool(ctx);
+    if (!pp) return GR_ERR_OOM_BUDGET;
+    gr::WavePool& pool = *pp;
+    // the default wave halves until the device has room for it
+    uint32_t cap = (uint32_t)std::max<uint64_t>(want, max_npix);
+    while ((e = pool.ensure(cap)) != cudaSuccess && !wave_paths && cap / 2 >= max_npix) {
+        cudaGetLastError();
+        cap /= 2;
     }
-    gr::WavePool& pool = *static_cast<gr::WavePool*>(ctx->batch_pool);
-    if ((e = pool.ensure(cap)) != cudaSuccess) {
+    if (e != cudaSuccess) {
         ctx->last_error = std::string("gr_render_batch: ") + cudaGetErrorString(e);
         return cuda_status(e);
     }
     cudaStream_t s = ctx->stream;
+    if ((e = pool.clear_errors(s)) != cudaSuccess) return cuda_status(e);
     gr::WaveHeader before{};
     cudaMemcpyAsync(&before, pool.ps.hdr, sizeof(before), cudaMemcpyDeviceToHost, s);
     std::vector<gr::JobDev> table;
@@ -124,7 +144,7 @@ extern "C" gr_status gr_render_batch(gr_ctx* ctx, gr_scene* const* scenes, const
     gr::WaveHeader after{};
     uint32_t err = 0;
     cudaMemcpyAsync(&after, pool.ps.hdr, sizeof(after), cudaMemcpyDeviceToHost, s);
-    cudaMemcpyAsync(&err, pool.ps.cnt + 2 * gr::kMaxDepth + 4, 4, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(&err, pool.error_word(), 4, cudaMemcpyDeviceToHost, s);
     if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_status(e);
     uint64_t samples = 0;
     for (uint32_t i = 0; i < n; ++i) {

@@ -275,7 +275,8 @@ typedef struct gr_render_opts {
     uint64_t seed;       /* RNG seed; a path's stream is keyed by (seed, pixel, sample index) */
     int32_t rr_depth;    /* Russian roulette after this bounce (reference: 3); < 0 disables */
     uint32_t flags;      /* GR_RENDER_* */
-    uint32_t wave_paths; /* paths in flight per wave (0 = library default) */
+    uint32_t wave_paths; /* paths in flight per wave (0 = the scene's default, else the library's: the
+                            whole call as one wave up to 64 Mi paths, smaller when the device lacks room) */
 } gr_render_opts;
 
 /* Reproduce the reference's integrator quirks for comparison with its
@@ -373,9 +374,12 @@ int gr_scene_layout(const gr_scene* scene);
 
 /* Autotuner for renders: times the probe render (e.g. a few samples per
  * pixel) for every traversal configuration (layout x block x short-stack
- * depth), then for wave sizes (queue capacity) of 1, 2, 4 and 8 Mi paths, and
- * keeps the fastest as the scene's configuration and default wave size.
- * Images do not depend on any of these. Clears the scene's accumulation. */
+ * depth), then for wave sizes (queue capacity) of 4, 8, 16, 32 and 64 Mi
+ * paths, and keeps the fastest as the scene's configuration and default wave
+ * size. Images do not depend on any of these. Clears the scene's
+ * accumulation. gr_render and gr_render_batch keep their path state in one
+ * pool per context, sized by the largest wave asked of it (about 172 bytes
+ * per path). */
 gr_status gr_scene_autotune(gr_scene* scene, const gr_render_opts* probe, gr_trace_tuning* best,
                             uint32_t* best_wave_paths);
 
@@ -432,7 +436,7 @@ typedef struct gr_server gr_server;
 
 typedef struct gr_server_opts {
     uint64_t budget_bytes; /* device-memory budget for admission (0 = no limit) */
-    uint32_t wave_paths;   /* paths per wave (0 = library default) */
+    uint32_t wave_paths;   /* paths per wave (0 = 4 Mi) */
     uint32_t max_active;   /* jobs in flight at most (0 = 1024) */
     int32_t layout;        /* node layout of every job (GR_LAYOUT_*); set on the scenes at submit */
     int32_t block;         /* traversal threads per block (0 = 128; see gr_trace_tuning) */

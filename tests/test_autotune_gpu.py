@@ -88,7 +88,7 @@ def test_scene_autotune_keeps_image(ctx):
     tune, wave = b.autotune(spp=2, max_depth=6)
     assert tune["layout"] in gr.LAYOUT_NAMES.values()
     assert tune["block"] in (64, 128, 256) and tune["short_stack"] in (8, 12, 16)
-    assert wave in (1 << 20, 2 << 20, 4 << 20, 8 << 20)
+    assert wave in (4 << 20, 8 << 20, 16 << 20, 32 << 20, 64 << 20)
     assert b.tuning() == (tune, wave)
     b.render(4, max_depth=10, seed=9, want_image=False)  # autotune cleared the accumulation
     np.testing.assert_array_equal(b.accumulation()[0], ref)
