@@ -487,6 +487,17 @@ __device__ __forceinline__ Box3 get_child_box_l2(const Node* nd, int slot) {
     return b;
 }
 
+// Counter increment with acquire-release semantics at GPU scope: this thread's
+// earlier writes (its child box) are visible to the thread that sees the
+// incremented count, and the sibling's box, written before its own increment,
+// is visible to this thread's later reads. One ordered atomic in place of two
+// full fences around a relaxed one.
+__device__ __forceinline__ uint32_t atomic_add_acq_rel(uint32_t* p, uint32_t v) {
+    uint32_t old;
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
+}
+
 __global__ void __launch_bounds__(kBlock) k_refit(const float* __restrict__ verts, uint32_t n,
                                                   const uint32_t* __restrict__ prim, const uint32_t* __restrict__ parent_leaf,
                                                   Node* nodes, Tri* __restrict__ tris, uint32_t* __restrict__ counters,
@@ -525,9 +536,7 @@ __global__ void __launch_bounds__(kBlock) k_refit(const float* __restrict__ vert
             Node* nd = nodes + node;
             const int slot = (nd->q3.x == me) ? 0 : 1;
             put_child_box(nd, slot, box);
-            __threadfence();
-            if (atomicAdd(&counters[node], 1u) == 0) break;  // sibling not done yet
-            __threadfence();
+            if (atomic_add_acq_rel(&counters[node], 1u) == 0) break;  // sibling not done yet
             const Box3 sib = get_child_box_l2(nd, slot ^ 1);
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
