@@ -324,6 +324,18 @@ def run_gpu(args):
         torch.cuda.synchronize()
         if i >= 3:
             build_ms.append(e0.elapsed_time(e1))
+    # the 8-wide 8-bit layout collapsed from a fresh build (wall clock: the
+    # collapse reads each level's size back to the host)
+    collapse_ms = []
+    for i in range(3 + 3):
+        bvh.set_layout(gr.LAYOUT_BVH2, stream=sp)  # a rebuild keeps the current layout built
+        bvh.build_device(d_verts, n_tris, stream=sp)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        bvh.set_layout(gr.LAYOUT_BVH8_Q8, stream=sp)
+        torch.cuda.synchronize()
+        if i >= 3:
+            collapse_ms.append((time.perf_counter() - t0) * 1e3)
 
     def step(buf_rays, buf_hits, n, any_hit=False):
         bvh.trace_device(buf_rays, n, buf_hits, any_hit=any_hit, stream=sp)
@@ -486,6 +498,7 @@ def run_gpu(args):
             "clocks": clock_info,
             "extra": dict(extras, bvh_build_ms=statistics.median(build_ms),
                           bvh_build_mtris_s=N_TRIS / (statistics.median(build_ms) / 1e3) / 1e6,
+                          bvh8_collapse_ms=statistics.median(collapse_ms),
                           kernel_ms_median=statistics.median(kernel_ms)),
         }
         print(json.dumps(out), flush=True)
