@@ -641,7 +641,7 @@ __global__ void k_wave_end(Paths ps) {
     h->shadow_rays += sh;
 }
 
-// One wave: clear counters, camera rays, kMaxWaveDepth x (trace, shade, shadow)
+// One wave: clear counters, camera rays, depth_steps x (trace, shade, shadow)
 // (steps past the wave's max_depth return at once), resolve, ray counts.
 template <int LAYOUT, int SSTACK>
 cudaError_t issue_wave_l(const Paths& ps, uint32_t depth_steps, int tgrid, int tblock, int sgrid, bool bin,
@@ -740,9 +740,7 @@ size_t path_layout(uint32_t cap, char* base, Paths* ps) {
     return off;
 }
 
-// The wave always runs this many bounce steps; steps past the wave's own
-// max_depth return immediately, so one captured graph serves every wave.
-constexpr uint32_t kGraphDepthSteps = 16;
+
 
 }  // namespace
 
@@ -752,8 +750,12 @@ void WaveGraph::release() {
     key = 0;
 }
 
+void WavePool::release_graphs() {
+    for (WaveGraph& g : graphs) g.release();
+}
+
 void WavePool::release() {
-    graph.release();
+    release_graphs();
     for (int i = 0; i < kSlots; ++i)
         if (ev[i]) {
             cudaEventSynchronize(ev[i]);
@@ -777,7 +779,7 @@ cudaError_t WavePool::ensure(uint32_t paths) {
             if ((e = cudaEventCreateWithFlags(&ev[i], cudaEventDisableTiming)) != cudaSuccess) return e;
     }
     if (paths <= capacity && mem.p) return cudaSuccess;
-    graph.release();  // a captured wave points into the old path memory
+    release_graphs();  // a captured wave points into the old path memory
     Paths p;
     const size_t bytes = path_layout(paths, nullptr, &p);
     e = mem.ensure(bytes);
@@ -872,7 +874,9 @@ cudaError_t run_wave(WavePool& pool, const JobDev* h_jobs, uint32_t njobs, uint3
     if ((e = cudaEventRecord(pool.ev[slot], s)) != cudaSuccess) return e;
     const int tgrid = num_sms * occ;
     const int sgrid = num_sms * 4;
-    const uint32_t steps = std::max(max_depth, kGraphDepthSteps);
+    // the captured sequence runs exactly the wave's bounce steps (an empty step
+    // still costs three launches)
+    const uint32_t steps = max_depth;
     // shade in material groups when the wave's scenes mix material types
     uint32_t types = 0;
     for (uint32_t j = 0; j < njobs; ++j) types |= h_jobs[j].sc.mat_types;
@@ -882,9 +886,20 @@ cudaError_t run_wave(WavePool& pool, const JobDev* h_jobs, uint32_t njobs, uint3
     const uint64_t words[] = {(uint64_t)(uintptr_t)ps.ray, ps.capacity, steps, (uint64_t)tgrid, (uint64_t)sgrid,
                               (uint64_t)tune.layout, (uint64_t)tune.block, (uint64_t)tune.sstack, (uint64_t)bin};
     for (uint64_t w : words) key = mix64(key, w);
-    WaveGraph& g = pool.graph;
-    if (!g.exec || g.key != key) {
-        g.release();
+    int hit = -1;
+    for (int i = 0; i < WavePool::kGraphs; ++i)
+        if (pool.graphs[i].exec && pool.graphs[i].key == key) hit = i;
+    if (hit < 0) {
+        // evict the least recently used (the last), then capture into the front
+        pool.graphs[WavePool::kGraphs - 1].release();
+        hit = WavePool::kGraphs - 1;
+    }
+    for (int i = hit; i > 0; --i) {  // the handles move, not the owning objects
+        std::swap(pool.graphs[i].exec, pool.graphs[i - 1].exec);
+        std::swap(pool.graphs[i].key, pool.graphs[i - 1].key);
+    }
+    WaveGraph& g = pool.graphs[0];
+    if (!g.exec) {
         cudaGraph_t graph = nullptr;
         if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return e;
         const cudaError_t ei = issue_wave(ps, steps, tgrid, sgrid, bin, s, tune);

@@ -123,6 +123,9 @@ struct Paths {
 struct WaveGraph {
     cudaGraphExec_t exec = nullptr;
     uint64_t key = 0;
+    WaveGraph() = default;
+    WaveGraph(const WaveGraph&) = delete;  // owns exec
+    WaveGraph& operator=(const WaveGraph&) = delete;
     void release();
     ~WaveGraph() { release(); }
 };
@@ -134,7 +137,11 @@ struct WavePool {
     DevBuf mem;
     Paths ps{};
     uint32_t capacity = 0;
-    WaveGraph graph;
+    // captured waves, most recently used first (waves of different depth,
+    // grouping or tuning each keep their own)
+    static constexpr int kGraphs = 4;
+    WaveGraph graphs[kGraphs];
+    void release_graphs();
     // pinned staging for the per-wave job table and header, one slot per wave
     // in flight; a slot is rewritten only after its event has completed
     JobDev* h_jobs = nullptr;
