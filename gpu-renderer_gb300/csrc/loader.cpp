@@ -1039,6 +1039,19 @@ gr_status gr_scene_desc_triangles(const gr_scene_desc* d, float* h_verts, uint32
     return GR_OK;
 }
 
+gr_status gr_scene_desc_mesh(const gr_scene_desc* d, uint32_t i, uint32_t* num_vertices, uint32_t* num_triangles,
+                             int* has_normals, float* h_positions, float* h_normals, uint32_t* h_indices) {
+    if (!d || i >= d->meshes.size()) return GR_ERR_INVALID;
+    const MeshData& m = d->meshes[i];
+    if (num_vertices) *num_vertices = (uint32_t)(m.pos.size() / 3);
+    if (num_triangles) *num_triangles = (uint32_t)(m.idx.size() / 3);
+    if (has_normals) *has_normals = m.has_normals ? 1 : 0;
+    if (h_positions && !m.pos.empty()) std::memcpy(h_positions, m.pos.data(), m.pos.size() * 4);
+    if (h_normals && m.has_normals) std::memcpy(h_normals, m.nrm.data(), m.nrm.size() * 4);
+    if (h_indices && !m.idx.empty()) std::memcpy(h_indices, m.idx.data(), m.idx.size() * 4);
+    return GR_OK;
+}
+
 gr_status gr_scene_create_from_desc(gr_ctx* ctx, const gr_scene_desc* d, gr_scene** out) {
     if (!ctx || !d || !out) return GR_ERR_INVALID;
     if (!d->error.empty()) {

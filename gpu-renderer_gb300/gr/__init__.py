@@ -676,6 +676,7 @@ _DESC_SIGS = {
     "gr_scene_desc_warnings": ([_P], ctypes.c_char_p),
     "gr_scene_desc_info": ([_P, _P, _P, _P, ctypes.POINTER(Camera), ctypes.POINTER(Environment)], ctypes.c_int),
     "gr_scene_desc_triangles": ([_P, _P, _P, _P], ctypes.c_int),
+    "gr_scene_desc_mesh": ([_P, ctypes.c_uint32, _P, _P, _P, _P, _P, _P], ctypes.c_int),
     "gr_scene_create_from_desc": ([_P, _P, ctypes.POINTER(_P)], ctypes.c_int),
     "gr_scene_load_xml": ([_P, ctypes.c_char_p, ctypes.POINTER(_P)], ctypes.c_int),
 }
@@ -711,6 +712,29 @@ class ParsedScene:
         mats = (Material * max(self.num_meshes, 1))()
         L.gr_scene_desc_triangles(self.h, _ptr(v), _ptr(mesh), mats)
         return v, mesh, [mats[i] for i in range(self.num_meshes)]
+
+    def scene_desc(self):
+        """The parsed scene as a gr.scenes.SceneDesc (one mesh per shape, each
+        with its own material), e.g. to build the same scene from records."""
+        from .scenes import MeshDesc, SceneDesc
+        L = _declare(_DESC_SIGS)
+        _, _, mats = self.triangles()
+        meshes, materials = [], []
+        for i in range(self.num_meshes):
+            nv, nt, hn = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_int()
+            L.gr_scene_desc_mesh(self.h, i, ctypes.byref(nv), ctypes.byref(nt), ctypes.byref(hn), None, None, None)
+            pos = np.zeros((nv.value, 3), np.float32)
+            nrm = np.zeros((nv.value, 3), np.float32) if hn.value else None
+            idx = np.zeros((nt.value, 3), np.uint32)
+            L.gr_scene_desc_mesh(self.h, i, None, None, None, _ptr(pos), _ptr(nrm), _ptr(idx))
+            meshes.append(MeshDesc(pos, idx, i, normals=nrm))
+            r = mats[i]
+            if r.color_map:
+                raise ValueError("textured materials have no record form here")
+            materials.append({"type": r.type, "color": tuple(r.color), "emission": tuple(r.emission),
+                              "alpha_u": r.alpha_u, "alpha_v": r.alpha_v, "eta_i": tuple(r.eta_i),
+                              "eta_t": tuple(r.eta_t), "k": tuple(r.k), "ior": r.ior, "specular": tuple(r.specular)})
+        return SceneDesc(meshes, materials, dict(self.camera), self.env)
 
     def create(self, ctx):
         h = _P()

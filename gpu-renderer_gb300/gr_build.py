@@ -91,6 +91,17 @@ def build_oracle():
         r = subprocess.run(["bash", ref], capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("reference build failed:\n%s\n%s" % (r.stdout, r.stderr))
+    # the reference's Cornell-box fixture as this library's loader parses it
+    # (for rendering it with both integrators on the GPU, where the file is absent)
+    cbox = "/root/reference/scene/CBox/cbox.xml"
+    if os.path.exists(cbox):
+        sys.path.insert(0, odir)
+        import gr
+        import ref_gpu
+        os.makedirs(ref_gpu.REF_DIR, exist_ok=True)
+        parsed = gr.ParsedScene(cbox)
+        ref_gpu.save_desc(parsed.scene_desc(), ref_gpu.CBOX_SCENE)
+        parsed.close()
 
 
 if __name__ == "__main__":

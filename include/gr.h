@@ -411,6 +411,12 @@ gr_status gr_scene_desc_info(const gr_scene_desc* desc, uint32_t* meshes, uint32
 /* Flattened triangles (9 floats each, world space), the mesh of each triangle,
  * and one material per mesh. Any pointer may be NULL. */
 gr_status gr_scene_desc_triangles(const gr_scene_desc* desc, float* h_verts, uint32_t* h_mesh, gr_material* h_mats);
+/* Mesh i as parsed (world space): vertex and triangle counts, whether it has
+ * per-vertex normals, and with non-NULL buffers its positions (3 floats per
+ * vertex), normals (3 per vertex, when it has them) and indices (3 per
+ * triangle). Its material is h_mats[i] of gr_scene_desc_triangles. */
+gr_status gr_scene_desc_mesh(const gr_scene_desc* desc, uint32_t i, uint32_t* num_vertices, uint32_t* num_triangles,
+                             int* has_normals, float* h_positions, float* h_normals, uint32_t* h_indices);
 gr_status gr_scene_create_from_desc(gr_ctx* ctx, const gr_scene_desc* desc, gr_scene** out);
 /* Parse + create: the drop-in for PathTracer(filename) (pathtracer.cu:8-11). */
 gr_status gr_scene_load_xml(gr_ctx* ctx, const char* path, gr_scene** out);

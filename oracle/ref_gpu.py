@@ -67,6 +67,44 @@ def render_available(build="stock"):
     return available(build) and os.path.exists(FRAME_LIB)
 
 
+# ---------------------------------------------------------------------------
+# Scene descriptions as files (the reference's own fixture scenes, parsed here
+# where its tree is, travel to the GPU machine this way)
+# ---------------------------------------------------------------------------
+CBOX_SCENE = os.path.join(REF_DIR, "cbox_scene.npz")
+
+
+def save_desc(desc, path):
+    """A gr.scenes.SceneDesc (constant or no environment) to an .npz file."""
+    arrays = {"camera_to_world": np.asarray(desc.camera["to_world"], np.float32),
+              "camera": np.array([desc.camera["fov"], desc.camera["width"], desc.camera["height"]], np.float64),
+              "materials": np.array(json.dumps(desc.materials)), "n_meshes": np.array(len(desc.meshes))}
+    if desc.env is not None:
+        arrays["env"] = np.asarray(desc.env, np.float32)
+    for i, m in enumerate(desc.meshes):
+        arrays["p%d" % i] = m.positions
+        arrays["i%d" % i] = m.indices
+        arrays["m%d" % i] = np.array(m.material)
+        if m.normals is not None:
+            arrays["n%d" % i] = m.normals
+    np.savez_compressed(path, **arrays)
+
+
+def load_desc(path, width=None, height=None):
+    """The SceneDesc save_desc wrote; width / height replace the camera's
+    resolution (the field of view stays)."""
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(HERE), "gpu-renderer_gb300"))
+    from gr.scenes import MeshDesc, SceneDesc
+    z = np.load(path)
+    meshes = [MeshDesc(z["p%d" % i], z["i%d" % i], int(z["m%d" % i]), normals=z["n%d" % i] if "n%d" % i in z else None)
+              for i in range(int(z["n_meshes"]))]
+    fov, w, h = z["camera"]
+    cam = {"to_world": z["camera_to_world"], "fov": float(fov), "width": int(width or w), "height": int(height or h)}
+    mats = [{k: (tuple(v) if isinstance(v, list) else v) for k, v in m.items()} for m in json.loads(str(z["materials"]))]
+    return SceneDesc(meshes, mats, cam, tuple(z["env"]) if "env" in z else None)
+
+
 def load_layout():
     with open(LAYOUT) as f:
         L = json.load(f)

@@ -145,3 +145,48 @@ def test_textures_envmap_and_texcoords(tmp_path):
     b = np.ctypeslib.as_array(ctypes.cast(bmp.color_map, ctypes.POINTER(ctypes.c_float)), (36,)).reshape(4, 3, 3)
     np.testing.assert_allclose(b, (img[::-1] / 255.0) ** 2.2, rtol=1e-5)
     assert not grey.color_map
+
+
+def test_parsed_scene_as_records_round_trip(tmp_path):
+    """gr_scene_desc_mesh / ParsedScene.scene_desc: a scene written as XML + OBJ
+    and parsed back gives the same meshes, normals, materials and camera."""
+    from gr import mitsuba
+    d = sc.glossy_scene(40, 30, level=1, glass_level=1)
+    path = mitsuba.write_scene(d, str(tmp_path))
+    back = gr.ParsedScene(path).scene_desc()
+    assert len(back.meshes) == len(d.meshes)
+    for a, b in zip(d.meshes, back.meshes):
+        np.testing.assert_array_equal(b.positions[b.indices], a.positions[a.indices])
+        assert (a.normals is None) == (b.normals is None)
+        if a.normals is not None:  # renormalised by the loader, as the reference's does
+            np.testing.assert_allclose(b.normals[b.indices], a.normals[a.indices], atol=1e-6)
+        ma, mb = gr.material_record(d.materials[a.material]), gr.material_record(back.materials[b.material])
+        assert ma.type == mb.type
+        np.testing.assert_allclose(list(mb.color), list(ma.color))
+        np.testing.assert_allclose(list(mb.emission), list(ma.emission))
+    np.testing.assert_allclose(back.camera["to_world"], d.camera["to_world"], atol=1e-6)
+    assert (back.camera["width"], back.camera["height"]) == (40, 30)
+
+
+def test_scene_desc_file_round_trip(tmp_path):
+    import ref_gpu
+    d = sc.glossy_scene(40, 30, level=1, glass_level=1)
+    ref_gpu.save_desc(d, tmp_path / "s.npz")
+    back = ref_gpu.load_desc(tmp_path / "s.npz", 20, 15)
+    assert (back.camera["width"], back.camera["height"]) == (20, 15) and back.camera["fov"] == d.camera["fov"]
+    assert back.env == tuple(np.float32(d.env))
+    for a, b in zip(d.meshes, back.meshes):
+        np.testing.assert_array_equal(a.positions, b.positions)
+        np.testing.assert_array_equal(a.indices, b.indices)
+        assert a.material == b.material
+    assert [gr.material_record(m).type for m in back.materials] == [gr.material_record(m).type for m in d.materials]
+
+
+def test_reference_cbox_parses():
+    if not os.path.exists(REF_CBOX):
+        pytest.skip("reference tree absent")
+    d = gr.ParsedScene(os.path.join(REF_CBOX, "cbox.xml")).scene_desc()
+    assert len(d.meshes) == 6 and sum(m.normals is not None for m in d.meshes) == 2
+    kinds = sorted((gr.material_record(m).type, round(gr.material_record(m).ior, 3)) for m in d.materials)
+    assert kinds.count((gr.MAT_DIELECTRIC, 100.0)) == 1 and kinds.count((gr.MAT_DIELECTRIC, 1.5)) == 1
+    assert sum(1 for m in d.materials if any(m["emission"])) == 1

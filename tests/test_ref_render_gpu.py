@@ -16,6 +16,8 @@ renderers draw different random numbers, so the images agree statistically:
   quadrant (15 comparisons per scene; with the standard error estimated from
   8-16 batches, 6 keeps the chance of a false failure near 1e-3 per run).
 """
+import os
+
 import numpy as np
 import pytest
 import torch
@@ -68,11 +70,22 @@ def _reference_batches(rk, ctx, desc, batches, frames, depth):
     return np.array(means)  # (batches, 5, 3)
 
 
-@pytest.mark.parametrize("name,desc,batches,frames,depth", [
-    ("cornell", sc.cornell_box(64, 64), 16, 64, 8),
-    ("glossy", sc.glossy_scene(128, 96, level=4, glass_level=3), 8, 32, 16),
+def _cbox():
+    """The reference's own fixture scene/CBox/cbox.xml (mirror and glass
+    spheres with vertex normals, coloured walls, area light), as this
+    library's loader parses it, at 160 x 120."""
+    if not os.path.exists(ref_gpu.CBOX_SCENE):
+        pytest.skip("the reference's fixture scene was not parsed at build time")
+    return ref_gpu.load_desc(ref_gpu.CBOX_SCENE, 160, 120)
+
+
+@pytest.mark.parametrize("name,make,batches,frames,depth", [
+    ("cornell", lambda: sc.cornell_box(64, 64), 16, 64, 8),
+    ("glossy", lambda: sc.glossy_scene(128, 96, level=4, glass_level=3), 8, 32, 16),
+    ("reference_cbox", _cbox, 8, 32, 8),
 ])
-def test_compat_render_matches_reference_kernels(ctx, stock, name, desc, batches, frames, depth):
+def test_compat_render_matches_reference_kernels(ctx, stock, name, make, batches, frames, depth):
+    desc = make()
     ref = _reference_batches(stock, ctx, desc, batches, frames, depth)
     ref_mean = ref.mean(0)
     ref_se = ref.std(0, ddof=1) / np.sqrt(batches)
