@@ -390,6 +390,16 @@ extern "C" gr_status gr_bvh_build_noalloc(gr_ctx* ctx, const float* d_verts, uin
     return GR_OK;
 }
 
+extern "C" gr_status gr_diag_bounded_wait(gr_ctx* ctx, uint32_t polls, uint32_t* err_bits) {
+    if (!ctx) return GR_ERR_INVALID;
+    GR_CUDA(ctx, cudaSetDevice(ctx->device));
+    uint32_t bits = 0;
+    GR_CUDA(ctx, gr::lookback_probe(polls, &bits, ctx->stream));
+    if (err_bits) *err_bits = bits;
+    if (bits & gr::ERR_TIMEOUT) return fail(ctx, GR_ERR_TIMEOUT, "gr_diag_bounded_wait: the wait gave up");
+    return GR_OK;
+}
+
 extern "C" gr_status gr_bvh_set_layout(gr_bvh* bvh, int layout, void* stream) {
     if (!bvh || layout < 0 || layout >= gr::kNumLayouts) return GR_ERR_INVALID;
     GR_CUDA(bvh->ctx, cudaSetDevice(bvh->ctx->device));

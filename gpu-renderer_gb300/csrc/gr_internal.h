@@ -149,6 +149,10 @@ struct BvhMeta {
 };
 
 // lbvh.cu
+// Runs the build's bounded look-back wait on a status word nothing publishes,
+// for `polls` polls (at most kSpinLimit); *h_err receives the error bits it set
+// (ERR_TIMEOUT when the wait gave up, as it must).
+cudaError_t lookback_probe(uint32_t polls, uint32_t* h_err, cudaStream_t s);
 cudaError_t lbvh_build(BvhBuffers& b, const float* d_verts, uint32_t n, int num_sms, cudaStream_t s);
 cudaError_t lbvh_export_ref(const BvhBuffers& b, uint32_t n, uint32_t* d_ref_nodes, cudaStream_t s);
 // build whose scratch is a file-scope device array (no allocation); see lbvh.cu

@@ -185,6 +185,32 @@ constexpr int kOsItems = 8;
 constexpr int kOsTile = kOsThreads * kOsItems;
 constexpr int kOsWarps = kOsThreads / 32;
 constexpr uint32_t kFlagAgg = 1u << 30, kFlagInc = 2u << 30, kCountMask = (1u << 30) - 1;
+
+// Decoupled look-back over the tiles before `tile` (their status words `stride`
+// apart): sums their published counts until a tile with its inclusive prefix.
+// A tile that has not published yet is polled again; after `limit` polls in all
+// the wait gives up, sets ERR_TIMEOUT and returns what it has summed (the result
+// is then wrong and the host reports the error bit).
+__device__ __forceinline__ uint32_t lookback(const uint32_t* status, size_t stride, int64_t tile, uint32_t limit,
+                                             uint32_t* err) {
+    uint32_t excl = 0, spins = 0;
+    int64_t t = tile - 1;
+    while (t >= 0) {
+        const uint32_t v = ld_acquire(status + (size_t)t * stride);
+        const uint32_t flag = v & ~kCountMask;
+        if (flag == 0) {
+            if (++spins > limit) {
+                atomicOr(err, ERR_TIMEOUT);
+                break;
+            }
+            continue;
+        }
+        excl += v & kCountMask;
+        if (flag == kFlagInc) break;
+        --t;
+    }
+    return excl;
+}
 constexpr size_t kOsSmem = sizeof(uint32_t) * (kOsWarps * 256 + 256 + 256 + 2 * kOsTile + 8 + 1);
 
 __global__ void __launch_bounds__(kOsThreads) k_onesweep(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
@@ -256,22 +282,7 @@ __global__ void __launch_bounds__(kOsThreads) k_onesweep(const uint32_t* __restr
             st_release(st, kFlagInc | cnt);
         } else {
             st_release(st, kFlagAgg | cnt);
-            int64_t t = (int64_t)tile - 1;
-            uint32_t spins = 0;
-            while (t >= 0) {
-                const uint32_t v = ld_acquire(status + (size_t)t * 256 + d);
-                const uint32_t flag = v & ~kCountMask;
-                if (flag == 0) {
-                    if (++spins > kSpinLimit) {
-                        atomicOr(err, ERR_TIMEOUT);
-                        break;
-                    }
-                    continue;
-                }
-                excl += v & kCountMask;
-                if (flag == kFlagInc) break;
-                --t;
-            }
+            excl = lookback(status + d, 256, (int64_t)tile, kSpinLimit, err);
             st_release(st, kFlagInc | ((excl + cnt) & kCountMask));
         }
         s_gbase[d] = offs[256 * pass + d] + excl;
@@ -336,19 +347,7 @@ __global__ void __launch_bounds__(kRunThreads) k_runs(const uint32_t* __restrict
             st_release(st, kFlagInc | tot);
         } else {
             st_release(st, kFlagAgg | tot);
-            int64_t t = (int64_t)tile - 1;
-            uint32_t spins = 0;
-            while (t >= 0) {
-                const uint32_t v = ld_acquire(status + t);
-                const uint32_t flag = v & ~kCountMask;
-                if (flag == 0) {
-                    if (++spins > kSpinLimit) { atomicOr(err, ERR_TIMEOUT); break; }
-                    continue;
-                }
-                excl += v & kCountMask;
-                if (flag == kFlagInc) break;
-                --t;
-            }
+            excl = lookback(status, 1, (int64_t)tile, kSpinLimit, err);
             st_release(st, kFlagInc | ((excl + tot) & kCountMask));
         }
         s_excl = excl;
@@ -657,7 +656,28 @@ size_t scratch_layout(uint32_t n, char* base, Scratch* s) {
     return off;
 }
 
+// The look-back's bounded wait on its own: tile 1 looks back at tile 0, whose
+// status word nothing publishes, so the wait runs out after `limit` polls.
+__global__ void k_lookback_probe(const uint32_t* status, uint32_t limit, uint32_t* err, uint32_t* out) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) *out = lookback(status, 1, 1, limit, err);
+}
+
 }  // namespace
+
+cudaError_t lookback_probe(uint32_t polls, uint32_t* h_err, cudaStream_t s) {
+    uint32_t* d = nullptr;
+    cudaError_t e = cudaMalloc(&d, 3 * sizeof(uint32_t));  // status word, error word, result
+    if (e != cudaSuccess) return e;
+    e = cudaMemsetAsync(d, 0, 3 * sizeof(uint32_t), s);
+    if (e == cudaSuccess) {
+        k_lookback_probe<<<1, 32, 0, s>>>(d, std::min(polls, kSpinLimit), d + 1, d + 2);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h_err, d + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFree(d);
+    return e;
+}
 
 cudaError_t lbvh_build(BvhBuffers& b, const float* d_verts, uint32_t n, int num_sms, cudaStream_t st) {
     cudaError_t e;

@@ -70,6 +70,7 @@ def load():
         "gr_scene_set_tuning": ([_P, _P, ctypes.c_uint32], ctypes.c_int),
         "gr_scene_get_tuning": ([_P, _P, ctypes.POINTER(ctypes.c_uint32)], ctypes.c_int),
         "gr_scene_layout": ([_P], ctypes.c_int),
+        "gr_diag_bounded_wait": ([_P, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32)], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -117,6 +118,15 @@ class Context:
     def check(self, st, what=""):
         if st != GR_OK:
             raise GrError(st, "%s: %s" % (what, load().gr_last_error(self.h).decode()))
+
+    def bounded_wait(self, polls):
+        """gr_diag_bounded_wait: runs the library's bounded device wait on a flag
+        nothing sets, for `polls` polls. Returns (status, device error bits);
+        the status is GR_ERR_TIMEOUT (5) with bit 1 set, and the context stays
+        usable."""
+        bits = ctypes.c_uint32(0)
+        st = load().gr_diag_bounded_wait(self.h, polls, ctypes.byref(bits))
+        return st, bits.value
 
     def close(self):
         if self.h:

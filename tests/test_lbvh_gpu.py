@@ -72,3 +72,16 @@ def test_gpu_lbvh_empty(ctx):
     b = gr.BVH(ctx)
     b.build_host(np.zeros((0, 9), np.float32))
     assert b.export()["root"] == 0xFFFFFFFF
+
+
+@pytest.mark.parametrize("polls", [1, 1000, 1 << 16])
+def test_bounded_wait_gives_up_and_context_stays_usable(ctx, oracle, polls):
+    # the build's look-back wait on a status word that nothing publishes: it gives
+    # up after its poll limit, the call reports GR_ERR_TIMEOUT with the device bit,
+    # and the same context then builds and traces as before
+    st, bits = ctx.bounded_wait(polls)
+    assert st == 5 and bits == 1
+    v = sc.triangle_soup(5000, seed_salt=95)
+    b = gr.BVH(ctx)
+    b.build_host(v)
+    _compare(b.export(), oracle.lbvh(v))
