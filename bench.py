@@ -75,6 +75,13 @@ class ClockSampler:
             self.t.start()
         except (OSError, ValueError):
             self.proc = None
+            return
+        # nvidia-smi's start-up (NVML initialisation) stalled the next CUDA
+        # launch by about 0.9 s on GB300: the timed region opens only after the
+        # first sample has arrived
+        deadline = time.perf_counter() + 5.0
+        while not self.lines and self.proc.poll() is None and time.perf_counter() < deadline:
+            time.sleep(0.01)
 
     def _read(self):
         for line in self.proc.stdout:
@@ -471,7 +478,7 @@ def run_gpu(args):
         peak, peak_kind = measured_peaks()
         avg_ms = sum(kernel_ms) / len(kernel_ms)
         achieved = BYTES_PER_RAY * N_RAYS / (avg_ms / 1e3) / 1e9
-        traffic = None
+        traffic, l2 = None, None
         tp = os.path.join(ROOT, "profiles", "trace_closest_traffic.json")
         if os.path.exists(tp):
             with open(tp) as f:
@@ -479,6 +486,14 @@ def run_gpu(args):
             # the capture is of one layout's kernel; other layouts report none
             if tj.get("layout") == gr.LAYOUT_NAMES[layout]:
                 traffic = tj.get("bytes_per_launch")
+                c = tj.get("l2")
+                if c:
+                    # an HBM fraction above 1 means the working set sits in L2:
+                    # the L2 side of the same kernel (one ncu capture)
+                    l2 = {"hit_rate_pct": c["l2_hit_rate_pct"], "frac_of_l2_peak": c["l2_throughput_pct_of_peak"] / 100,
+                          "l2_bytes_per_ray": c["lts_bytes_per_ray"], "issue_active_pct": c["issue_active_pct"],
+                          "sample_rays": c["rays"],
+                          "reading": "issue bound: L2 and DRAM are far from their peaks"}
         cb = cpu_reference(1, 0)
         out = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -489,7 +504,8 @@ def run_gpu(args):
                        "l2": "flushed (256 MB write) before every timed step", "parallelism": "replicas"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
-                         "kernel": "k_trace<closest, %s>" % gr.LAYOUT_NAMES[layout], "bytes_per_ray": BYTES_PER_RAY},
+                         "kernel": "k_trace<closest, %s>" % gr.LAYOUT_NAMES[layout], "bytes_per_ray": BYTES_PER_RAY,
+                         "l2": l2},
             "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": N_RAYS * 32,
                     "d2h_bytes_per_step": N_RAYS * 16, "api": "gr_trace_host with page-locked host rays and hits: the traversal reads the rays and "
