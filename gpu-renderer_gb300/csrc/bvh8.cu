@@ -13,7 +13,7 @@
 // plane.
 //
 // Nodes are numbered breadth first, level by level: a level's nodes are
-// collapsed (one thread each), their inner-child and leaf counts are prefix-
+// collapsed (eight lanes each), their inner-child and leaf counts are prefix-
 // summed, and the children become the next level at consecutive indices, so
 // a node's inner children are contiguous from child_base and its leaf
 // triangles contiguous from tri_base (copied into the layout's own triangle
@@ -30,6 +30,9 @@ namespace {
 using namespace q8;
 
 constexpr int kBlock8 = 256;
+constexpr int kLanesPerNode = 8;            // lanes collapsing one 8-wide node
+constexpr int kNodesPerCollapseBlock = 32;  // nodes per collapse block: one emit warp
+constexpr int kCollapseThreads = kNodesPerCollapseBlock * kLanesPerNode;
 constexpr int kScanThreads = 1024;
 constexpr int32_t kEmptySlot = INT32_MIN;
 constexpr int kMaxLevels8 = 72;
@@ -95,11 +98,253 @@ __device__ __forceinline__ float half_area(const CBox& b) {
     return __fadd_rn(__fadd_rn(__fmul_rn(dx, dy), __fmul_rn(dy, dz)), __fmul_rn(dz, dx));
 }
 
-// Exclusive scan of one 64-bit value per thread over a kBlock8-thread block.
-__device__ unsigned long long block_exclusive(unsigned long long v, unsigned long long* block_total) {
-    __shared__ unsigned long long s_warp[kBlock8 / 32];
+__global__ void k8_init(const BvhMeta* __restrict__ meta, uint32_t* frontier) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) frontier[0] = meta->root;
+}
+
+__device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+
+// Order-preserving 32-bit key of a float (larger float, larger key); -0 and +0
+// share one key, as they compare equal.
+__device__ __forceinline__ uint32_t order_key(float x) {
+    const uint32_t b = __float_as_uint(x == 0.0f ? 0.0f : x);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+
+// Eight lanes per 8-wide node, four nodes per warp: lane k of a group holds
+// candidate child k. Every choice is made exactly as one thread scanning the
+// candidates in order would make it (first largest on ties), so the node does
+// not depend on the lanes' arithmetic order. Loops run the same number of
+// times in every group, so each shuffle has the whole warp. Writes the node
+// (without its bases) and its 8 slot references when `have`; returns the
+// counts (inner | leaf << 32).
+__device__ unsigned long long collapse_group(const Node* __restrict__ nodes, bool have, uint32_t root_id,
+                                             Node8Q* __restrict__ out, int32_t* __restrict__ sref_out, uint32_t* err) {
+    constexpr uint32_t kAll = 0xFFFFFFFFu;
+    constexpr int W = kLanesPerNode;
+    const int k = threadIdx.x & (W - 1);
+    int32_t ref = kEmptySlot;
+    CBox box = {{0.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 0.0f}};
+    int cnt8 = 0;
+    if (have) {
+        const Node root = nodes[root_id];
+        box = child_box(root, k & 1);
+        if (k < 2) ref = k ? root.q3.y : root.q3.x;
+        cnt8 = 2;
+    }
+    // an inner candidate's node is fetched towards L2 as soon as it becomes a
+    // candidate, so opening it later waits on L2 rather than DRAM
+    if (ref >= 0) prefetch_l2(nodes + ref);
+    // open the inner candidate with the largest surface area (at most 6 times)
+    for (int step = 0; step < 6; ++step) {
+        const float area = half_area(box);
+        int best = -1;
+        float best_a = 0.0f;
+        for (int j = 0; j < W; ++j) {
+            const float aj = __shfl_sync(kAll, area, j, W);
+            const int32_t rj = __shfl_sync(kAll, ref, j, W);
+            if (j < cnt8 && rj >= 0 && (best < 0 || aj > best_a)) {
+                best = j;
+                best_a = aj;
+            }
+        }
+        const int32_t rb = __shfl_sync(kAll, ref, best < 0 ? 0 : best, W);
+        if (best >= 0 && cnt8 < 8) {
+            const Node cn = nodes[rb];
+            if (k == best) {
+                ref = cn.q3.x;
+                box = child_box(cn, 0);
+            }
+            if (k == cnt8) {
+                ref = cn.q3.y;
+                box = child_box(cn, 1);
+            }
+            if ((k == best || k == cnt8) && ref >= 0) prefetch_l2(nodes + ref);
+            ++cnt8;
+        }
+    }
+    // node box (folded in candidate order) and centre (lo + hi)
+    float lo[3], hi[3], nc[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        lo[a] = __shfl_sync(kAll, box.lo[a], 0, W);
+        hi[a] = __shfl_sync(kAll, box.hi[a], 0, W);
+    }
+#pragma unroll
+    for (int j = 1; j < W; ++j) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const float l = __shfl_sync(kAll, box.lo[a], j, W), h = __shfl_sync(kAll, box.hi[a], j, W);
+            if (j < cnt8) {
+                lo[a] = fminf(lo[a], l);
+                hi[a] = fmaxf(hi[a], h);
+            }
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) nc[a] = __fadd_rn(lo[a], hi[a]);
+    // this lane's child scored against every slot
+    const float dx = __fsub_rn(__fadd_rn(box.lo[0], box.hi[0]), nc[0]);
+    const float dy = __fsub_rn(__fadd_rn(box.lo[1], box.hi[1]), nc[1]);
+    const float dz = __fsub_rn(__fadd_rn(box.lo[2], box.hi[2]), nc[2]);
+    float sc[8];
+    bool nan_score = false;
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+        sc[s] = __fadd_rn(__fadd_rn((s & 1) ? dx : -dx, (s & 2) ? dy : -dy), (s & 4) ? dz : -dz);
+        nan_score |= isnan(sc[s]);
+    }
+    const bool slow = __any_sync(kAll, k < cnt8 && nan_score);
+    // greedy assignment: the best (score, then lowest child, then lowest slot) first
+    uint32_t used = 0;
+    bool taken = false;
+    int my_slot = -1;
+    for (int it = 0; it < 8; ++it) {
+        int win = -1;
+        if (!slow) {
+            // this lane's first largest free slot, then the group's largest
+            // score with the lowest pair 8 k + s on ties (-0 and +0 tie)
+            const bool cand = k < cnt8 && !taken;
+            int bs = -1;
+            float bsc = 0.0f;
+#pragma unroll
+            for (int s = 0; s < 8; ++s)
+                if (cand && !(used >> s & 1u) && (bs < 0 || sc[s] > bsc)) {
+                    bs = s;
+                    bsc = sc[s];
+                }
+            uint32_t key = bs >= 0 ? order_key(bsc) : 0u;
+            int p = bs >= 0 ? 8 * k + bs : 0xFF;
+#pragma unroll
+            for (int d = 1; d < W; d <<= 1) {
+                const uint32_t ok = __shfl_xor_sync(kAll, key, d, W);
+                const int op = __shfl_xor_sync(kAll, p, d, W);
+                if (ok > key || (ok == key && op < p)) {
+                    key = ok;
+                    p = op;
+                }
+            }
+            win = p;
+        } else {
+            // a NaN score in the warp: fold the group's pairs in order, as one thread would
+            float wsc = 0.0f;
+            for (int j = 0; j < W; ++j) {
+                const bool tj = __shfl_sync(kAll, (int)taken, j, W) != 0;
+#pragma unroll
+                for (int s = 0; s < 8; ++s) {
+                    const float x = __shfl_sync(kAll, sc[s], j, W);
+                    if (j < cnt8 && !tj && !(used >> s & 1u) && (win < 0 || x > wsc)) {
+                        win = 8 * j + s;
+                        wsc = x;
+                    }
+                }
+            }
+        }
+        if (it < cnt8) {
+            if (win < 0 || win >= 64) {  // no free pair: cannot happen while it < cnt8 <= 8
+                if (k == 0) atomicOr(err, ERR_RANGE);
+            } else {
+                used |= 1u << (win & 7);
+                if (k == (win >> 3)) {
+                    taken = true;
+                    my_slot = win & 7;
+                }
+            }
+        }
+    }
+    // quantise: per-axis exponents (lanes 0-2), then this lane's child's six planes
+    uint32_t my_be = 0;
+    if (have && k < 3) my_be = (uint32_t)(pick_exponent8(k == 0 ? lo[0] : (k == 1 ? lo[1] : lo[2]),
+                                                         k == 0 ? hi[0] : (k == 1 ? hi[1] : hi[2]), err) + 127);
+    uint32_t be[3];
+    float scale[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        be[a] = __shfl_sync(kAll, my_be, a, W);
+        scale[a] = __uint_as_float(be[a] << 23);
+    }
+    uint32_t wq[12];
+#pragma unroll
+    for (int w = 0; w < 12; ++w) wq[w] = 0;
+    if (k < cnt8 && my_slot >= 0) {
+        const int sh = 8 * (my_slot & 3), half = my_slot >> 2;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const uint32_t ql = quant_lo8(box.lo[a], scale[a], lo[a]) << sh;
+            const uint32_t qh = quant_hi8(box.hi[a], scale[a], lo[a]) << sh;
+            wq[4 * a + 0] = half ? 0u : ql;
+            wq[4 * a + 1] = half ? ql : 0u;
+            wq[4 * a + 2] = half ? 0u : qh;
+            wq[4 * a + 3] = half ? qh : 0u;
+        }
+    }
+    uint32_t imask = (k < cnt8 && ref >= 0 && my_slot >= 0) ? 1u << my_slot : 0u;
+#pragma unroll
+    for (int d = 1; d < W; d <<= 1) {
+        imask |= __shfl_xor_sync(kAll, imask, d, W);
+#pragma unroll
+        for (int w = 0; w < 12; ++w) wq[w] |= __shfl_xor_sync(kAll, wq[w], d, W);
+    }
+    if (!have) return 0ull;
+    // the node's 24 words: lane k writes words k, k + 8 and k + 16
+    uint32_t w0 = 0, w1 = 0, w2 = 0;
+    if (k < 3) w0 = __float_as_uint(k == 0 ? lo[0] : (k == 1 ? lo[1] : lo[2]));
+    if (k == 3) w0 = be[0] | (be[1] << 8) | (be[2] << 16) | (imask << 24);
+    if (k == 6) w0 = used;
+#pragma unroll
+    for (int w = 0; w < 8; ++w) {
+        if (k == w) w1 = wq[w];
+        if (k == w && w < 4) w2 = wq[8 + w];
+    }
+    uint32_t* o = reinterpret_cast<uint32_t*>(out);
+    o[k] = w0;
+    o[k + 8] = w1;
+    o[k + 16] = w2;
+    // slot references: each child at its slot, empty slots marked
+    if (k < cnt8 && my_slot >= 0) sref_out[my_slot] = ref;
+    if (!(used >> k & 1u)) sref_out[k] = kEmptySlot;
+    const uint32_t n_inner = __popc(imask);
+    return (unsigned long long)n_inner | ((unsigned long long)(cnt8 - n_inner) << 32);
+}
+
+// Nodes of the level, kNodesPerCollapseBlock per block, eight lanes each; one
+// count sum per block.
+__global__ void __launch_bounds__(kCollapseThreads) k8_collapse(const Node* __restrict__ nodes,
+                                                              const uint32_t* __restrict__ frontier, uint32_t level_n,
+                                                              uint32_t out_base, Node8Q* __restrict__ out,
+                                                              int32_t* __restrict__ slots,
+                                                              unsigned long long* __restrict__ cnt,
+                                                              unsigned long long* __restrict__ bsum, uint32_t* err) {
+    __shared__ unsigned long long s_cnt[kNodesPerCollapseBlock];
+    const int g = threadIdx.x / kLanesPerNode;
+    const uint32_t i = blockIdx.x * kNodesPerCollapseBlock + g;
+    const bool have = i < level_n;
+    const unsigned long long c =
+        collapse_group(nodes, have, have ? frontier[i] : 0u, out + out_base + i, slots + 8ull * i, err);
+    if ((threadIdx.x & (kLanesPerNode - 1)) == 0) {
+        s_cnt[g] = c;
+        if (have) cnt[i] = c;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long t = 0;
+        for (int j = 0; j < kNodesPerCollapseBlock; ++j) t += s_cnt[j];
+        bsum[blockIdx.x] = t;
+    }
+}
+
+// Exclusive scan of the block sums in place (one block); level totals to *total.
+__global__ void __launch_bounds__(kScanThreads) k8_scan_blocks(unsigned long long* bsum, uint32_t nblocks,
+                                                               unsigned long long* total) {
+    __shared__ unsigned long long s_warp[32];
+    const uint32_t per = (nblocks + kScanThreads - 1) / kScanThreads;
+    const uint32_t b0 = threadIdx.x * per, b1 = min(nblocks, b0 + per);
+    unsigned long long sum = 0;
+    for (uint32_t b = b0; b < b1; ++b) sum += bsum[b];
+    // exclusive scan of the threads' sums: within each warp, then over the warp totals
+    static_assert(kScanThreads == 1024, "32 warps of 32");
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    unsigned long long x = v;
+    unsigned long long x = sum;
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
         const unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, x, d);
@@ -108,166 +353,17 @@ __device__ unsigned long long block_exclusive(unsigned long long v, unsigned lon
     if (lane == 31) s_warp[warp] = x;
     __syncthreads();
     if (warp == 0) {
-        unsigned long long w = lane < kBlock8 / 32 ? s_warp[lane] : 0ull;
+        unsigned long long w = s_warp[lane];
 #pragma unroll
-        for (int d = 1; d < kBlock8 / 32; d <<= 1) {
+        for (int d = 1; d < 32; d <<= 1) {
             const unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, w, d);
             if (lane >= d) w += y;
         }
-        if (lane < kBlock8 / 32) s_warp[lane] = w;
+        s_warp[lane] = w;
     }
     __syncthreads();
-    const unsigned long long before = warp ? s_warp[warp - 1] : 0ull;
-    if (block_total) *block_total = s_warp[kBlock8 / 32 - 1];
-    return before + x - v;
-}
-
-__global__ void k8_init(const BvhMeta* __restrict__ meta, uint32_t* frontier) {
-    if (threadIdx.x == 0 && blockIdx.x == 0) frontier[0] = meta->root;
-}
-
-// One thread per 8-wide node of the level: collapse, assign slots, quantise.
-// Writes the node (without its bases), its 8 slot references and its counts
-// (inner | leaf << 32); one partial sum per block.
-__global__ void __launch_bounds__(kBlock8) k8_collapse(const Node* __restrict__ nodes,
-                                                       const uint32_t* __restrict__ frontier, uint32_t level_n,
-                                                       uint32_t out_base, Node8Q* __restrict__ out,
-                                                       int32_t* __restrict__ slots, unsigned long long* __restrict__ cnt,
-                                                       unsigned long long* __restrict__ bsum, uint32_t* err) {
-    const uint32_t i = blockIdx.x * kBlock8 + threadIdx.x;
-    unsigned long long c = 0;
-    if (i < level_n) {
-        const Node root = nodes[frontier[i]];
-        CBox box[8];
-        int32_t ref[8];
-        int cnt8 = 2;
-        ref[0] = root.q3.x;
-        box[0] = child_box(root, 0);
-        ref[1] = root.q3.y;
-        box[1] = child_box(root, 1);
-        while (cnt8 < 8) {
-            int best = -1;
-            float best_a = 0.0f;
-            for (int k = 0; k < cnt8; ++k)
-                if (ref[k] >= 0) {
-                    const float a = half_area(box[k]);
-                    if (best < 0 || a > best_a) {
-                        best = k;
-                        best_a = a;
-                    }
-                }
-            if (best < 0) break;
-            const Node cn = nodes[ref[best]];
-            ref[best] = cn.q3.x;
-            box[best] = child_box(cn, 0);
-            ref[cnt8] = cn.q3.y;
-            box[cnt8] = child_box(cn, 1);
-            ++cnt8;
-        }
-        // node box and centre (sums lo + hi, the factor 1/2 cancels)
-        float lo[3], hi[3], nc[3];
-        for (int a = 0; a < 3; ++a) {
-            lo[a] = box[0].lo[a];
-            hi[a] = box[0].hi[a];
-            for (int k = 1; k < cnt8; ++k) {
-                lo[a] = fminf(lo[a], box[k].lo[a]);
-                hi[a] = fmaxf(hi[a], box[k].hi[a]);
-            }
-            nc[a] = __fadd_rn(lo[a], hi[a]);
-        }
-        // greedy slot assignment: best (score, then lowest child, then lowest slot) first
-        int slot_of[8];
-        uint32_t used = 0;
-        for (int k = 0; k < 8; ++k) slot_of[k] = -1;
-        for (int it = 0; it < cnt8; ++it) {
-            int bk = -1, bs = -1;
-            float bsc = 0.0f;
-            for (int k = 0; k < cnt8; ++k) {
-                if (slot_of[k] >= 0) continue;
-                const float dx = __fsub_rn(__fadd_rn(box[k].lo[0], box[k].hi[0]), nc[0]);
-                const float dy = __fsub_rn(__fadd_rn(box[k].lo[1], box[k].hi[1]), nc[1]);
-                const float dz = __fsub_rn(__fadd_rn(box[k].lo[2], box[k].hi[2]), nc[2]);
-                for (int s = 0; s < 8; ++s) {
-                    if (used & (1u << s)) continue;
-                    const float sc = __fadd_rn(__fadd_rn((s & 1) ? dx : -dx, (s & 2) ? dy : -dy), (s & 4) ? dz : -dz);
-                    if (bk < 0 || sc > bsc) {
-                        bk = k;
-                        bs = s;
-                        bsc = sc;
-                    }
-                }
-            }
-            slot_of[bk] = bs;
-            used |= 1u << bs;
-        }
-        // quantise
-        float scale[3];
-        uint32_t be[3];
-        for (int a = 0; a < 3; ++a) {
-            const int e = pick_exponent8(lo[a], hi[a], err);
-            be[a] = (uint32_t)(e + 127);
-            scale[a] = __uint_as_float(be[a] << 23);
-        }
-        Node8Q o;
-        o.ox = lo[0];
-        o.oy = lo[1];
-        o.oz = lo[2];
-        for (int w = 0; w < 12; ++w) o.q[w] = 0;
-        uint32_t imask = 0;
-        int32_t sref[8];
-        for (int s = 0; s < 8; ++s) sref[s] = kEmptySlot;
-        uint32_t n_inner = 0, n_leaf = 0;
-        for (int k = 0; k < cnt8; ++k) {
-            const int s = slot_of[k];
-            sref[s] = ref[k];
-            if (ref[k] >= 0) {
-                imask |= 1u << s;
-                ++n_inner;
-            } else {
-                ++n_leaf;
-            }
-            for (int a = 0; a < 3; ++a) {
-                o.q[4 * a + (s >> 2)] |= quant_lo8(box[k].lo[a], scale[a], lo[a]) << (8 * (s & 3));
-                o.q[4 * a + 2 + (s >> 2)] |= quant_hi8(box[k].hi[a], scale[a], lo[a]) << (8 * (s & 3));
-            }
-        }
-        o.meta = be[0] | (be[1] << 8) | (be[2] << 16) | (imask << 24);
-        o.child_base = 0;
-        o.tri_base = 0;
-        o.valid = used;
-        o.pad0 = 0;
-        for (int w = 0; w < 4; ++w) o.pad1[w] = 0;
-        out[out_base + i] = o;
-        for (int s = 0; s < 8; ++s) slots[8ull * i + s] = sref[s];
-        c = (unsigned long long)n_inner | ((unsigned long long)n_leaf << 32);
-        cnt[i] = c;
-    }
-    unsigned long long total;
-    block_exclusive(c, &total);
-    if (threadIdx.x == 0) bsum[blockIdx.x] = total;
-}
-
-// Exclusive scan of the block sums in place (one block); level totals to *total.
-__global__ void __launch_bounds__(kScanThreads) k8_scan_blocks(unsigned long long* bsum, uint32_t nblocks,
-                                                               unsigned long long* total) {
-    __shared__ unsigned long long s_part[kScanThreads];
-    const uint32_t per = (nblocks + kScanThreads - 1) / kScanThreads;
-    const uint32_t b0 = threadIdx.x * per, b1 = min(nblocks, b0 + per);
-    unsigned long long sum = 0;
-    for (uint32_t b = b0; b < b1; ++b) sum += bsum[b];
-    s_part[threadIdx.x] = sum;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        unsigned long long run = 0;
-        for (int t = 0; t < kScanThreads; ++t) {
-            const unsigned long long v = s_part[t];
-            s_part[t] = run;
-            run += v;
-        }
-        *total = run;
-    }
-    __syncthreads();
-    unsigned long long run = s_part[threadIdx.x];
+    unsigned long long run = (warp ? s_warp[warp - 1] : 0ull) + x - sum;
+    if (threadIdx.x == kScanThreads - 1) *total = run + sum;
     for (uint32_t b = b0; b < b1; ++b) {
         const unsigned long long v = bsum[b];
         bsum[b] = run;
@@ -277,7 +373,9 @@ __global__ void __launch_bounds__(kScanThreads) k8_scan_blocks(unsigned long lon
 
 // Writes each node's bases, the next level's binary ids (inner children in
 // slot order) and the leaf triangles (in slot order) into the layout's
-// triangle array.
+// triangle array. A node's offsets are its collapse block's exclusive count
+// sum plus the counts of the nodes before it in that block, whose
+// kNodesPerCollapseBlock nodes are one warp here (a warp scan).
 __global__ void __launch_bounds__(kBlock8) k8_emit(uint32_t level_n, uint32_t out_base, uint32_t next_base,
                                                    uint32_t tri_cursor, Node8Q* __restrict__ out,
                                                    const int32_t* __restrict__ slots,
@@ -285,10 +383,18 @@ __global__ void __launch_bounds__(kBlock8) k8_emit(uint32_t level_n, uint32_t ou
                                                    const unsigned long long* __restrict__ bsum,
                                                    uint32_t* __restrict__ next_frontier, const Tri* __restrict__ tris,
                                                    Tri* __restrict__ tris8) {
+    static_assert(kNodesPerCollapseBlock == 32, "a collapse block's nodes are one emit warp");
     const uint32_t i = blockIdx.x * kBlock8 + threadIdx.x;
+    const int lane = threadIdx.x & 31;
     const unsigned long long c = i < level_n ? cnt[i] : 0ull;
-    const unsigned long long pre = block_exclusive(c, nullptr) + bsum[blockIdx.x];
+    unsigned long long x = c;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, x, d);
+        if (lane >= d) x += y;
+    }
     if (i >= level_n) return;
+    const unsigned long long pre = bsum[i / kNodesPerCollapseBlock] + (x - c);
     const uint32_t inner0 = (uint32_t)pre, leaf0 = (uint32_t)(pre >> 32);
     out[out_base + i].child_base = next_base + inner0;
     out[out_base + i].tri_base = tri_cursor + leaf0;
@@ -308,13 +414,13 @@ size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
 }  // namespace
 
-cudaError_t bvh8_build(BvhBuffers& b, uint32_t n, cudaStream_t s) {
+cudaError_t bvh8_build(BvhBuffers& b, uint32_t n, DevBuf& scratch, cudaStream_t s) {
     b.count8 = 0;
     b.tris8_count = 0;
     if (n == 0) return cudaSuccess;
     const size_t maxnodes = n > 1 ? n - 1 : 1;
     const size_t maxtris = std::max<size_t>(n, 2);  // a lone triangle fills both children of its node
-    const size_t maxblocks = (maxnodes + kBlock8 - 1) / kBlock8;
+    const size_t maxblocks = (maxnodes + kNodesPerCollapseBlock - 1) / kNodesPerCollapseBlock;
     // scratch: two frontiers, slot refs, counts, block sums, totals, and the nodes before compaction
     size_t off = 0;
     const size_t o_f0 = off; off += align256(4 * maxnodes);
@@ -325,9 +431,9 @@ cudaError_t bvh8_build(BvhBuffers& b, uint32_t n, cudaStream_t s) {
     const size_t o_tt = off; off += align256(16);
     const size_t o_nd = off; off += align256(sizeof(Node8Q) * maxnodes);
     cudaError_t e;
-    if ((e = b.scratch8.ensure(off)) != cudaSuccess) return e;
+    if ((e = scratch.ensure(off)) != cudaSuccess) return e;
     if ((e = b.tris8.ensure(sizeof(Tri) * maxtris)) != cudaSuccess) return e;
-    char* base = (char*)b.scratch8.p;
+    char* base = (char*)scratch.p;
     uint32_t* frontier[2] = {(uint32_t*)(base + o_f0), (uint32_t*)(base + o_f1)};
     int32_t* slots = (int32_t*)(base + o_sl);
     unsigned long long* cnt = (unsigned long long*)(base + o_cn);
@@ -339,11 +445,11 @@ cudaError_t bvh8_build(BvhBuffers& b, uint32_t n, cudaStream_t s) {
     int cur = 0;
     for (int level = 0; level_n > 0; ++level) {
         if (level >= kMaxLevels8 || out_base + (size_t)level_n > maxnodes) return cudaErrorInvalidValue;
-        const uint32_t nb = (level_n + kBlock8 - 1) / kBlock8;
-        k8_collapse<<<nb, kBlock8, 0, s>>>((const Node*)b.nodes.p, frontier[cur], level_n, out_base, staged, slots, cnt,
+        const uint32_t nb = (level_n + kNodesPerCollapseBlock - 1) / kNodesPerCollapseBlock;
+        k8_collapse<<<nb, kCollapseThreads, 0, s>>>((const Node*)b.nodes.p, frontier[cur], level_n, out_base, staged, slots, cnt,
                                            bsum, &((BvhMeta*)b.meta.p)->err);
         k8_scan_blocks<<<1, kScanThreads, 0, s>>>(bsum, nb, total);
-        k8_emit<<<nb, kBlock8, 0, s>>>(level_n, out_base, out_base + level_n, tri_cursor, staged, slots, cnt, bsum,
+        k8_emit<<<(level_n + kBlock8 - 1) / kBlock8, kBlock8, 0, s>>>(level_n, out_base, out_base + level_n, tri_cursor, staged, slots, cnt, bsum,
                                        frontier[cur ^ 1], (const Tri*)b.tris.p, (Tri*)b.tris8.p);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         unsigned long long h[1];
@@ -360,7 +466,6 @@ cudaError_t bvh8_build(BvhBuffers& b, uint32_t n, cudaStream_t s) {
         cudaSuccess)
         return e;
     if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
-    b.scratch8.release();
     b.count8 = out_base;
     b.tris8_count = tri_cursor;
     return cudaSuccess;

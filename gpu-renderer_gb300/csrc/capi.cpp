@@ -34,6 +34,7 @@ void context_free(gr_ctx* ctx) {
     if (ctx->batch_pool && ctx->batch_pool_free) ctx->batch_pool_free(ctx->batch_pool);
     ctx->batch_pool = nullptr;
     ctx->counter.release();
+    ctx->scratch8.release();
     ctx->stage_in.release();
     ctx->stage_out.release();
     if (ctx->stream2) cudaStreamSynchronize(ctx->stream2);
@@ -96,7 +97,8 @@ cudaError_t ensure_layout(gr_bvh* bvh, int layout, cudaStream_t s) {
     if (!bvh->built || layout == gr::kLayoutBvh2) return cudaSuccess;
     if (layout == gr::kLayoutBvh8Q8) {
         if (bvh->built8) return cudaSuccess;
-        const cudaError_t e = gr::bvh8_build(bvh->buf, bvh->n, s);
+        std::lock_guard<std::mutex> lock(bvh->ctx->scratch8_mu);
+        const cudaError_t e = gr::bvh8_build(bvh->buf, bvh->n, bvh->ctx->scratch8, s);
         if (e == cudaSuccess) bvh->built8 = true;
         return e;
     }

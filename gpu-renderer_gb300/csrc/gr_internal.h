@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <mutex>
 #include <string>
 
 #include "gr.h"
@@ -131,7 +132,6 @@ struct BvhBuffers {
     DevBuf nodes, tris, code, prim;  // outputs kept for traversal / export
     DevBuf nodes4, nodes4q;          // 4-wide layouts (built on request), indexed like `nodes`
     DevBuf nodes8, tris8;            // 8-wide layout (built on request): nodes from 0 (root), leaf-order triangles
-    DevBuf scratch8;                 // 8-wide build state
     uint32_t count8 = 0;             // 8-wide nodes
     uint32_t tris8_count = 0;        // triangles in tris8
     DevBuf scratch;                  // transient build state
@@ -164,7 +164,9 @@ cudaError_t lbvh_build_static(const float* d_verts, uint32_t n, Node* nodes, Tri
 // even depth becomes a 4-wide node at the same index)
 cudaError_t bvh4_build(BvhBuffers& b, uint32_t n, int layout, cudaStream_t s);
 // bvh8.cu: level by level, one host read of the level size per level (waits for `s`)
-cudaError_t bvh8_build(BvhBuffers& b, uint32_t n, cudaStream_t s);
+// `scratch` holds the build's level state (about 144 bytes per triangle); it
+// is the context's, kept between builds, and the caller holds its lock.
+cudaError_t bvh8_build(BvhBuffers& b, uint32_t n, DevBuf& scratch, cudaStream_t s);
 
 // trace.cu
 cudaError_t trace_launch(const BvhDevice& bvh, const void* nodes, const TraceTuning& tune, const gr_ray* d_rays,
@@ -188,6 +190,11 @@ struct gr_ctx {
     // of gr_trace_host's pipeline); error word at offset 64
     gr::DevBuf counter;
     gr::DevBuf stage_in, stage_out;  // device staging for the host-memory entry points
+    // 8-wide layout build state, reused by every BVH of the context (grown,
+    // never shrunk, until the context is destroyed); the render server's
+    // thread may build too, so it is taken under its lock
+    gr::DevBuf scratch8;
+    std::mutex scratch8_mu;
     void* batch_pool = nullptr;          // wave pool of gr_render_batch (owned; freed with the context)
     void (*batch_pool_free)(void*) = nullptr;
 };

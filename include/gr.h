@@ -55,7 +55,11 @@ typedef struct gr_bvh gr_bvh;
 
 /* ---- context ------------------------------------------------------------ */
 
-/* Binds `device` and creates a context (streams, memory pool). */
+/* Binds `device` and creates a context (streams, memory pool). The context
+ * keeps the 8-wide layout build's scratch (about 144 bytes per triangle of the
+ * largest BVH it has collapsed) between builds, so building a layout neither
+ * allocates nor frees device memory once it has grown; destroying the context
+ * frees it. */
 gr_status gr_context_create(int device, gr_ctx** out);
 gr_status gr_context_destroy(gr_ctx* ctx);
 /* Text of the last error recorded on `ctx` (never NULL). */

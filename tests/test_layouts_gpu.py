@@ -62,6 +62,30 @@ def test_bvh8_build_and_trace_match_oracle(ctx, oracle, n, scale):
     np.testing.assert_array_equal(_bits(ga)[:, 1] != 0xFFFFFFFF, occluded)
 
 
+def _tied_soups():
+    # a lattice of equal, axis-aligned triangles (equal areas and equal slot
+    # scores everywhere), the same lattice with every triangle repeated, and a
+    # mesh with mixed-sign zero coordinates: the collapse's ties and -0 / +0
+    g = np.stack(np.meshgrid(np.arange(12), np.arange(12), np.arange(12), indexing="ij"), -1).reshape(-1, 3)
+    base = np.array([[0, 0, 0], [0.5, 0, 0], [0, 0.5, 0]], np.float32)
+    lattice = (g[:, None, :].astype(np.float32) + base[None]).reshape(-1, 9)
+    doubled = np.repeat(lattice, 3, axis=0)
+    signed = lattice - 6.0
+    signed[signed == 0] = -0.0
+    return {"lattice": lattice, "repeated": doubled, "signed_zero": np.ascontiguousarray(signed, np.float32)}
+
+
+@pytest.mark.parametrize("name", ["lattice", "repeated", "signed_zero"])
+def test_bvh8_collapse_ties_match_oracle(ctx, oracle, name):
+    v = np.ascontiguousarray(_tied_soups()[name], np.float32)
+    b = gr.BVH(ctx)
+    b.build_host(v)
+    ob = oracle.lbvh(v)
+    want_nodes, want_tris = oracle.bvh8(ob)
+    np.testing.assert_array_equal(b.export_layout(gr.LAYOUT_BVH8_Q8), want_nodes)
+    np.testing.assert_array_equal(_bits(b.export_layout_tris(gr.LAYOUT_BVH8_Q8)), _bits(want_tris))
+
+
 def test_bvh8_rebuild_keeps_layout_current(ctx, oracle):
     b = gr.BVH(ctx)
     b.set_layout(gr.LAYOUT_BVH8_Q8)
