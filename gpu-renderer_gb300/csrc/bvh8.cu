@@ -36,6 +36,9 @@ constexpr int kCollapseThreads = kNodesPerCollapseBlock * kLanesPerNode;
 constexpr int kScanThreads = 1024;
 constexpr int32_t kEmptySlot = INT32_MIN;
 constexpr int kMaxLevels8 = 72;
+constexpr int kLevelsPerSync = 4;        // levels launched per host read-back of the level state
+constexpr int kCollapseBlocksPerSm = 4;  // grid of the collapse (its loop covers any level size)
+constexpr int kEmitBlocksPerSm = 4;
 
 // 8-wide planes: plane(q) = q * 2^e + lo, taken EXACTLY (the traversal
 // measures it as fma(q, 2^e / d, (lo - o) / d) with error margins, never
@@ -98,8 +101,22 @@ __device__ __forceinline__ float half_area(const CBox& b) {
     return __fadd_rn(__fadd_rn(__fmul_rn(dx, dy), __fmul_rn(dy, dz)), __fmul_rn(dz, dx));
 }
 
-__global__ void k8_init(const BvhMeta* __restrict__ meta, uint32_t* frontier) {
-    if (threadIdx.x == 0 && blockIdx.x == 0) frontier[0] = meta->root;
+// One level of the build as the device sees it: its node count, where its
+// nodes start in the output, where its leaf triangles start, and whether a
+// capacity was exceeded (the build then stops with no more writes). Level l's
+// scan writes level l + 1's state, so the host launches levels without reading
+// their sizes back.
+struct Level8 {
+    uint32_t n, out_base, tri_cursor, overflow;
+};
+
+__global__ void k8_init(const BvhMeta* __restrict__ meta, uint32_t* frontier, Level8* level,
+                        unsigned long long* bsum) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        frontier[0] = meta->root;
+        level[0] = Level8{1u, 0u, 0u, 0u};
+        bsum[0] = 0ull;
+    }
 }
 
 __device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
@@ -307,36 +324,41 @@ __device__ unsigned long long collapse_group(const Node* __restrict__ nodes, boo
     return (unsigned long long)n_inner | ((unsigned long long)(cnt8 - n_inner) << 32);
 }
 
-// Nodes of the level, kNodesPerCollapseBlock per block, eight lanes each; one
-// count sum per block.
+// The level's nodes, eight lanes each (four per warp), over a grid of any
+// size; each node's counts go to cnt[i] and are added into the sum of its
+// 32-node tile (bsum, zeroed by the previous level's scan).
 __global__ void __launch_bounds__(kCollapseThreads) k8_collapse(const Node* __restrict__ nodes,
-                                                              const uint32_t* __restrict__ frontier, uint32_t level_n,
-                                                              uint32_t out_base, Node8Q* __restrict__ out,
-                                                              int32_t* __restrict__ slots,
+                                                              const uint32_t* __restrict__ frontier,
+                                                              const Level8* __restrict__ level,
+                                                              Node8Q* __restrict__ out, int32_t* __restrict__ slots,
                                                               unsigned long long* __restrict__ cnt,
                                                               unsigned long long* __restrict__ bsum, uint32_t* err) {
-    __shared__ unsigned long long s_cnt[kNodesPerCollapseBlock];
-    const int g = threadIdx.x / kLanesPerNode;
-    const uint32_t i = blockIdx.x * kNodesPerCollapseBlock + g;
-    const bool have = i < level_n;
-    const unsigned long long c =
-        collapse_group(nodes, have, have ? frontier[i] : 0u, out + out_base + i, slots + 8ull * i, err);
-    if ((threadIdx.x & (kLanesPerNode - 1)) == 0) {
-        s_cnt[g] = c;
-        if (have) cnt[i] = c;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        unsigned long long t = 0;
-        for (int j = 0; j < kNodesPerCollapseBlock; ++j) t += s_cnt[j];
-        bsum[blockIdx.x] = t;
+    const Level8 L = *level;
+    constexpr uint32_t kPerWarp = 32 / kLanesPerNode;
+    const uint32_t warps = gridDim.x * (kCollapseThreads / 32);
+    const uint32_t g = (threadIdx.x & 31) / kLanesPerNode;
+    for (uint32_t w = blockIdx.x * (kCollapseThreads / 32) + threadIdx.x / 32; (uint64_t)w * kPerWarp < L.n;
+         w += warps) {  // the same trip count for the whole warp
+        const uint32_t i = w * kPerWarp + g;
+        const bool have = i < L.n;
+        const unsigned long long c =
+            collapse_group(nodes, have, have ? frontier[i] : 0u, out + L.out_base + i, slots + 8ull * i, err);
+        if (have && (threadIdx.x & (kLanesPerNode - 1)) == 0) {
+            cnt[i] = c;
+            atomicAdd(&bsum[i / kNodesPerCollapseBlock], c);
+        }
     }
 }
 
-// Exclusive scan of the block sums in place (one block); level totals to *total.
-__global__ void __launch_bounds__(kScanThreads) k8_scan_blocks(unsigned long long* bsum, uint32_t nblocks,
-                                                               unsigned long long* total) {
+// Exclusive scan of the level's tile sums in place (one block); writes the
+// next level's state and zeroes the next level's tile sums.
+__global__ void __launch_bounds__(kScanThreads) k8_scan_blocks(unsigned long long* bsum, const Level8* level,
+                                                               Level8* next, unsigned long long* next_bsum,
+                                                               uint32_t max_nodes, uint32_t max_tris) {
     __shared__ unsigned long long s_warp[32];
+    __shared__ uint32_t s_next_tiles;
+    const Level8 L = *level;
+    const uint32_t nblocks = (L.n + kNodesPerCollapseBlock - 1) / kNodesPerCollapseBlock;
     const uint32_t per = (nblocks + kScanThreads - 1) / kScanThreads;
     const uint32_t b0 = threadIdx.x * per, b1 = min(nblocks, b0 + per);
     unsigned long long sum = 0;
@@ -363,49 +385,68 @@ __global__ void __launch_bounds__(kScanThreads) k8_scan_blocks(unsigned long lon
     }
     __syncthreads();
     unsigned long long run = (warp ? s_warp[warp - 1] : 0ull) + x - sum;
-    if (threadIdx.x == kScanThreads - 1) *total = run + sum;
     for (uint32_t b = b0; b < b1; ++b) {
         const unsigned long long v = bsum[b];
         bsum[b] = run;
         run += v;
     }
+    if (threadIdx.x == 0) {
+        const unsigned long long total = s_warp[31];
+        Level8 nx;
+        nx.n = (uint32_t)total;
+        nx.out_base = L.out_base + L.n;
+        nx.tri_cursor = L.tri_cursor + (uint32_t)(total >> 32);
+        nx.overflow = L.overflow;
+        if ((uint64_t)nx.out_base + nx.n > max_nodes || nx.tri_cursor > max_tris) {
+            nx.overflow = 1u;
+            nx.n = 0u;
+        }
+        *next = nx;
+        s_next_tiles = (nx.n + kNodesPerCollapseBlock - 1) / kNodesPerCollapseBlock;
+    }
+    __syncthreads();
+    for (uint32_t b = threadIdx.x; b < s_next_tiles; b += kScanThreads) next_bsum[b] = 0ull;
 }
 
 // Writes each node's bases, the next level's binary ids (inner children in
 // slot order) and the leaf triangles (in slot order) into the layout's
-// triangle array. A node's offsets are its collapse block's exclusive count
-// sum plus the counts of the nodes before it in that block, whose
-// kNodesPerCollapseBlock nodes are one warp here (a warp scan).
-__global__ void __launch_bounds__(kBlock8) k8_emit(uint32_t level_n, uint32_t out_base, uint32_t next_base,
-                                                   uint32_t tri_cursor, Node8Q* __restrict__ out,
-                                                   const int32_t* __restrict__ slots,
+// triangle array. A node's offsets are its tile's exclusive count sum plus the
+// counts of the nodes before it in the tile, whose 32 nodes are one warp here
+// (a warp scan). Nothing is written once a capacity was exceeded.
+__global__ void __launch_bounds__(kBlock8) k8_emit(const Level8* __restrict__ level, const Level8* __restrict__ next,
+                                                   Node8Q* __restrict__ out, const int32_t* __restrict__ slots,
                                                    const unsigned long long* __restrict__ cnt,
                                                    const unsigned long long* __restrict__ bsum,
                                                    uint32_t* __restrict__ next_frontier, const Tri* __restrict__ tris,
                                                    Tri* __restrict__ tris8) {
-    static_assert(kNodesPerCollapseBlock == 32, "a collapse block's nodes are one emit warp");
-    const uint32_t i = blockIdx.x * kBlock8 + threadIdx.x;
+    static_assert(kNodesPerCollapseBlock == 32, "a tile's nodes are one emit warp");
+    const Level8 L = *level;
+    if (next->overflow) return;
+    const uint32_t next_base = L.out_base + L.n;
     const int lane = threadIdx.x & 31;
-    const unsigned long long c = i < level_n ? cnt[i] : 0ull;
-    unsigned long long x = c;
+    for (uint32_t base = blockIdx.x * kBlock8; base < L.n; base += gridDim.x * kBlock8) {  // block-uniform
+        const uint32_t i = base + threadIdx.x;
+        const unsigned long long c = i < L.n ? cnt[i] : 0ull;
+        unsigned long long x = c;
 #pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-        const unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, x, d);
-        if (lane >= d) x += y;
-    }
-    if (i >= level_n) return;
-    const unsigned long long pre = bsum[i / kNodesPerCollapseBlock] + (x - c);
-    const uint32_t inner0 = (uint32_t)pre, leaf0 = (uint32_t)(pre >> 32);
-    out[out_base + i].child_base = next_base + inner0;
-    out[out_base + i].tri_base = tri_cursor + leaf0;
-    uint32_t ri = 0, rl = 0;
-    for (int s = 0; s < 8; ++s) {
-        const int32_t r = slots[8ull * i + s];
-        if (r == kEmptySlot) continue;
-        if (r >= 0) {
-            next_frontier[inner0 + ri++] = (uint32_t)r;
-        } else {
-            tris8[tri_cursor + leaf0 + rl++] = tris[(uint32_t)(~r)];
+        for (int d = 1; d < 32; d <<= 1) {
+            const unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, x, d);
+            if (lane >= d) x += y;
+        }
+        if (i >= L.n) continue;
+        const unsigned long long pre = bsum[i / kNodesPerCollapseBlock] + (x - c);
+        const uint32_t inner0 = (uint32_t)pre, leaf0 = (uint32_t)(pre >> 32);
+        out[L.out_base + i].child_base = next_base + inner0;
+        out[L.out_base + i].tri_base = L.tri_cursor + leaf0;
+        uint32_t ri = 0, rl = 0;
+        for (int s = 0; s < 8; ++s) {
+            const int32_t r = slots[8ull * i + s];
+            if (r == kEmptySlot) continue;
+            if (r >= 0) {
+                next_frontier[inner0 + ri++] = (uint32_t)r;
+            } else {
+                tris8[L.tri_cursor + leaf0 + rl++] = tris[(uint32_t)(~r)];
+            }
         }
     }
 }
@@ -414,21 +455,23 @@ size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
 }  // namespace
 
-cudaError_t bvh8_build(BvhBuffers& b, uint32_t n, DevBuf& scratch, cudaStream_t s) {
+cudaError_t bvh8_build(BvhBuffers& b, uint32_t n, DevBuf& scratch, int num_sms, cudaStream_t s) {
     b.count8 = 0;
     b.tris8_count = 0;
     if (n == 0) return cudaSuccess;
     const size_t maxnodes = n > 1 ? n - 1 : 1;
     const size_t maxtris = std::max<size_t>(n, 2);  // a lone triangle fills both children of its node
-    const size_t maxblocks = (maxnodes + kNodesPerCollapseBlock - 1) / kNodesPerCollapseBlock;
-    // scratch: two frontiers, slot refs, counts, block sums, totals, and the nodes before compaction
+    const size_t maxtiles = (maxnodes + kNodesPerCollapseBlock - 1) / kNodesPerCollapseBlock;
+    // scratch: two frontiers, slot refs, counts, two sets of tile sums, the
+    // level states, and the nodes before compaction
     size_t off = 0;
     const size_t o_f0 = off; off += align256(4 * maxnodes);
     const size_t o_f1 = off; off += align256(4 * maxnodes);
     const size_t o_sl = off; off += align256(32 * maxnodes);
     const size_t o_cn = off; off += align256(8 * maxnodes);
-    const size_t o_bs = off; off += align256(8 * maxblocks);
-    const size_t o_tt = off; off += align256(16);
+    const size_t o_b0 = off; off += align256(8 * maxtiles);
+    const size_t o_b1 = off; off += align256(8 * maxtiles);
+    const size_t o_lv = off; off += align256(sizeof(Level8) * (kMaxLevels8 + 1));
     const size_t o_nd = off; off += align256(sizeof(Node8Q) * maxnodes);
     cudaError_t e;
     if ((e = scratch.ensure(off)) != cudaSuccess) return e;
@@ -437,30 +480,38 @@ cudaError_t bvh8_build(BvhBuffers& b, uint32_t n, DevBuf& scratch, cudaStream_t 
     uint32_t* frontier[2] = {(uint32_t*)(base + o_f0), (uint32_t*)(base + o_f1)};
     int32_t* slots = (int32_t*)(base + o_sl);
     unsigned long long* cnt = (unsigned long long*)(base + o_cn);
-    unsigned long long* bsum = (unsigned long long*)(base + o_bs);
-    unsigned long long* total = (unsigned long long*)(base + o_tt);
+    unsigned long long* tile_sums[2] = {(unsigned long long*)(base + o_b0), (unsigned long long*)(base + o_b1)};
+    Level8* level_state = (Level8*)(base + o_lv);
     Node8Q* staged = (Node8Q*)(base + o_nd);
-    k8_init<<<1, 32, 0, s>>>((const BvhMeta*)b.meta.p, frontier[0]);
-    uint32_t level_n = 1, out_base = 0, tri_cursor = 0;
-    int cur = 0;
-    for (int level = 0; level_n > 0; ++level) {
-        if (level >= kMaxLevels8 || out_base + (size_t)level_n > maxnodes) return cudaErrorInvalidValue;
-        const uint32_t nb = (level_n + kNodesPerCollapseBlock - 1) / kNodesPerCollapseBlock;
-        k8_collapse<<<nb, kCollapseThreads, 0, s>>>((const Node*)b.nodes.p, frontier[cur], level_n, out_base, staged, slots, cnt,
-                                           bsum, &((BvhMeta*)b.meta.p)->err);
-        k8_scan_blocks<<<1, kScanThreads, 0, s>>>(bsum, nb, total);
-        k8_emit<<<(level_n + kBlock8 - 1) / kBlock8, kBlock8, 0, s>>>(level_n, out_base, out_base + level_n, tri_cursor, staged, slots, cnt, bsum,
-                                       frontier[cur ^ 1], (const Tri*)b.tris.p, (Tri*)b.tris8.p);
+    const Node* nodes = (const Node*)b.nodes.p;
+    uint32_t* err = &((BvhMeta*)b.meta.p)->err;
+    const int sms = std::max(1, num_sms);
+    k8_init<<<1, 32, 0, s>>>((const BvhMeta*)b.meta.p, frontier[0], level_state, tile_sums[0]);
+    // levels are launched kLevelsPerSync at a time; the host reads the state
+    // after each batch and stops at the first empty level (launches past it do
+    // nothing)
+    Level8 h{};
+    int level = 0;
+    for (;;) {
+        for (int j = 0; j < kLevelsPerSync && level < kMaxLevels8; ++j, ++level) {
+            const int c = level & 1;
+            k8_collapse<<<sms * kCollapseBlocksPerSm, kCollapseThreads, 0, s>>>(
+                nodes, frontier[c], level_state + level, staged, slots, cnt, tile_sums[c], err);
+            k8_scan_blocks<<<1, kScanThreads, 0, s>>>(tile_sums[c], level_state + level, level_state + level + 1,
+                                                      tile_sums[c ^ 1], (uint32_t)maxnodes, (uint32_t)maxtris);
+            k8_emit<<<sms * kEmitBlocksPerSm, kBlock8, 0, s>>>(level_state + level, level_state + level + 1, staged,
+                                                              slots, cnt, tile_sums[c], frontier[c ^ 1],
+                                                              (const Tri*)b.tris.p, (Tri*)b.tris8.p);
+        }
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
-        unsigned long long h[1];
-        if ((e = cudaMemcpyAsync(h, total, sizeof(h), cudaMemcpyDeviceToHost, s)) != cudaSuccess) return e;
+        if ((e = cudaMemcpyAsync(&h, level_state + level, sizeof(h), cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+            return e;
         if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
-        out_base += level_n;
-        tri_cursor += (uint32_t)(h[0] >> 32);
-        level_n = (uint32_t)h[0];
-        cur ^= 1;
-        if (tri_cursor > maxtris) return cudaErrorInvalidValue;
+        if (h.overflow) return cudaErrorInvalidValue;
+        if (h.n == 0) break;
+        if (level >= kMaxLevels8) return cudaErrorInvalidValue;
     }
+    const uint32_t out_base = h.out_base, tri_cursor = h.tri_cursor;
     if ((e = b.nodes8.ensure(sizeof(Node8Q) * out_base)) != cudaSuccess) return e;
     if ((e = cudaMemcpyAsync(b.nodes8.p, staged, sizeof(Node8Q) * out_base, cudaMemcpyDeviceToDevice, s)) !=
         cudaSuccess)

@@ -98,7 +98,7 @@ cudaError_t ensure_layout(gr_bvh* bvh, int layout, cudaStream_t s) {
     if (layout == gr::kLayoutBvh8Q8) {
         if (bvh->built8) return cudaSuccess;
         std::lock_guard<std::mutex> lock(bvh->ctx->scratch8_mu);
-        const cudaError_t e = gr::bvh8_build(bvh->buf, bvh->n, bvh->ctx->scratch8, s);
+        const cudaError_t e = gr::bvh8_build(bvh->buf, bvh->n, bvh->ctx->scratch8, bvh->ctx->num_sms, s);
         if (e == cudaSuccess) bvh->built8 = true;
         return e;
     }

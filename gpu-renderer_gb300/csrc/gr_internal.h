@@ -166,7 +166,7 @@ cudaError_t bvh4_build(BvhBuffers& b, uint32_t n, int layout, cudaStream_t s);
 // bvh8.cu: level by level, one host read of the level size per level (waits for `s`)
 // `scratch` holds the build's level state (about 144 bytes per triangle); it
 // is the context's, kept between builds, and the caller holds its lock.
-cudaError_t bvh8_build(BvhBuffers& b, uint32_t n, DevBuf& scratch, cudaStream_t s);
+cudaError_t bvh8_build(BvhBuffers& b, uint32_t n, DevBuf& scratch, int num_sms, cudaStream_t s);
 
 // trace.cu
 cudaError_t trace_launch(const BvhDevice& bvh, const void* nodes, const TraceTuning& tune, const gr_ray* d_rays,
