@@ -124,11 +124,35 @@ __global__ void __launch_bounds__(kBlock) k_centroid_partials(const float* __res
     }
 }
 
-__global__ void k_centroid_final(const float* __restrict__ partial, int nparts, BvhMeta* meta) {
+// One block folds the partial boxes: strided over the partials, then across
+// the warp and the block (min / max do not depend on the order).
+__global__ void __launch_bounds__(kBlock) k_centroid_final(const float* __restrict__ partial, int nparts,
+                                                           BvhMeta* meta) {
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int p = threadIdx.x; p < nparts; p += kBlock) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = fminf(lo[k], partial[6 * p + k]);
+            hi[k] = fmaxf(hi[k], partial[6 * p + 3 + k]);
+        }
+    }
+    __shared__ float s[6][kBlock / 32];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        for (int o = 16; o > 0; o >>= 1) {
+            lo[k] = fminf(lo[k], __shfl_xor_sync(0xFFFFFFFFu, lo[k], o));
+            hi[k] = fmaxf(hi[k], __shfl_xor_sync(0xFFFFFFFFu, hi[k], o));
+        }
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) {
+        for (int k = 0; k < 3; ++k) { s[k][warp] = lo[k]; s[3 + k][warp] = hi[k]; }
+    }
+    __syncthreads();
     if (threadIdx.x < 6) {
         const int k = threadIdx.x;
-        float r = k < 3 ? INFINITY : -INFINITY;
-        for (int p = 0; p < nparts; ++p) r = k < 3 ? fminf(r, partial[6 * p + k]) : fmaxf(r, partial[6 * p + k]);
+        float r = s[k][0];
+        for (int w = 1; w < kBlock / 32; ++w) r = k < 3 ? fminf(r, s[k][w]) : fmaxf(r, s[k][w]);
         meta->cbox[k] = r;
     }
 }
@@ -705,7 +729,7 @@ cudaError_t lbvh_build(BvhBuffers& b, const float* d_verts, uint32_t n, int num_
     const int grid = (int)std::min<uint64_t>(((uint64_t)n + kBlock - 1) / kBlock, (uint64_t)num_sms * 8);
     const int parts = std::min(grid, kPartials);
     k_centroid_partials<<<parts, kBlock, 0, st>>>(d_verts, n, s.partial);
-    k_centroid_final<<<1, 32, 0, st>>>(s.partial, parts, meta);
+    k_centroid_final<<<1, kBlock, 0, st>>>(s.partial, parts, meta);
     k_morton_hist<<<std::min(grid, num_sms * 2), kBlock, 0, st>>>(d_verts, n, meta, code, prim, s.hist);
     k_hist_scan<<<4, 256, 0, st>>>(s.hist, s.offs);
 
@@ -768,13 +792,17 @@ namespace {
 
 constexpr uint32_t kStaticMaxTriangles = 1u << 17;  // 131,072 triangles
 
+constexpr size_t round256(size_t x) { return (x + 255) & ~size_t(255); }
+
 // Upper bound of scratch_layout(kStaticMaxTriangles): nine per-triangle word
-// arrays (+1 word), the centroid partials, histograms, look-back words, tile
-// counters and the error word, each rounded up to 256 bytes.
+// arrays (+1 word), the centroid partials, histograms, the sort's and the run
+// compaction's look-back words (per tile of each), tile counters and the error
+// word, each rounded up to 256 bytes as scratch_layout rounds them.
+constexpr size_t kStaticOsTiles = (kStaticMaxTriangles + kOsTile - 1) / kOsTile;
+constexpr size_t kStaticRunTiles = (kStaticMaxTriangles + kRunTile - 1) / kRunTile;
 constexpr size_t kStaticScratchBytes =
-    9 * (((size_t)kStaticMaxTriangles * 4 + 4 + 255) & ~size_t(255)) + ((6 * 1024 * 4 + 255) & ~size_t(255)) +
-    2 * 4096 + 4 * ((kStaticMaxTriangles + 4095) / 4096) * 256 * 4 + ((kStaticMaxTriangles + 4095) / 4096) * 4 +
-    16 * 256;
+    9 * round256((size_t)kStaticMaxTriangles * 4 + 4) + round256(sizeof(float) * 6 * kPartials) + 2 * 4096 +
+    round256(4 * kStaticOsTiles * 256 * 4) + round256(kStaticRunTiles * 4) + round256(16 * 4) + round256(4);
 
 static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
 
@@ -817,7 +845,7 @@ cudaError_t lbvh_build_static(const float* d_verts, uint32_t n, Node* nodes, Tri
     const int grid = (int)std::min<uint64_t>(((uint64_t)n + kBlock - 1) / kBlock, (uint64_t)num_sms * 8);
     const int parts = std::min(grid, kPartials);
     k_centroid_partials<<<parts, kBlock, 0, st>>>(d_verts, n, s.partial);
-    k_centroid_final<<<1, 32, 0, st>>>(s.partial, parts, meta);
+    k_centroid_final<<<1, kBlock, 0, st>>>(s.partial, parts, meta);
     k_morton_hist<<<std::min(grid, num_sms * 2), kBlock, 0, st>>>(d_verts, n, meta, code, prim, s.hist);
     k_hist_scan<<<4, 256, 0, st>>>(s.hist, s.offs);
     if ((e = cudaFuncSetAttribute(k_onesweep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kOsSmem)) !=
