@@ -143,3 +143,19 @@ def test_surface_rays_equal_brute_force(ctx, oracle, layout):
     rays = sc.surface_rays(v, 400000, seed_salt=12)
     np.testing.assert_array_equal(_bits(b.trace_host(rays)), _bits(oracle.trace_brute(v, rays)))
 
+
+
+def test_bvh8_builds_share_the_context_scratch(ctx, oracle):
+    # two BVHs of one context collapse alternately through the context's
+    # scratch (grown by the larger, reused by the smaller): each layout stays
+    # equal to the oracle's word for word
+    big, small = gr.BVH(ctx), gr.BVH(ctx)
+    for salt in (440, 441):
+        vb = sc.triangle_soup(60000, seed_salt=salt)
+        vs = sc.triangle_soup(3000, seed_salt=salt + 10)
+        for b, v in ((small, vs), (big, vb), (small, vs[::-1].copy())):
+            b.build_host(v)
+            b.set_layout(gr.LAYOUT_BVH8_Q8)
+            want_nodes, want_tris = oracle.bvh8(oracle.lbvh(v))
+            np.testing.assert_array_equal(b.export_layout(gr.LAYOUT_BVH8_Q8), want_nodes)
+            np.testing.assert_array_equal(_bits(b.export_layout_tris(gr.LAYOUT_BVH8_Q8)), _bits(want_tris))
