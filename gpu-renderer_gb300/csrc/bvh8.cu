@@ -37,7 +37,7 @@ constexpr int kScanThreads = 1024;
 constexpr int32_t kEmptySlot = INT32_MIN;
 constexpr int kMaxLevels8 = 72;
 constexpr int kLevelsPerSync = 4;        // levels launched per host read-back of the level state
-constexpr int kCollapseBlocksPerSm = 4;  // grid of the collapse (its loop covers any level size)
+constexpr int kCollapseBlocksPerSm = 5;  // grid of the collapse (its loop covers any level size)
 constexpr int kEmitBlocksPerSm = 4;
 
 // 8-wide planes: plane(q) = q * 2^e + lo, taken EXACTLY (the traversal
