@@ -646,7 +646,7 @@ __global__ void k_wave_end(Paths ps) {
 template <int LAYOUT, int SSTACK>
 cudaError_t issue_wave_l(const Paths& ps, uint32_t depth_steps, int tgrid, int tblock, int sgrid, bool bin,
                          cudaStream_t s) {
-    const size_t smem = sizeof(int2) * SSTACK * tblock;
+    const size_t smem = trav::traverse_smem(LAYOUT, SSTACK, tblock);
     cudaError_t e;
     const size_t cnt_bytes = sizeof(uint32_t) * (2 * kMaxDepth + 4);
     const size_t bin_bytes = sizeof(uint32_t) * (kCntWords - kBinBase);
@@ -690,7 +690,7 @@ cudaError_t issue_wave(const Paths& ps, uint32_t steps, int tgrid, int sgrid, bo
 
 // Resident blocks per SM of the closest-hit queue kernel for a configuration.
 cudaError_t trace_occupancy(const TraceTuning& t, int* occ) {
-    const size_t smem = sizeof(int2) * t.sstack * t.block;
+    const size_t smem = trav::traverse_smem(t.layout, t.sstack, t.block);
     const void* fn = nullptr;
 #define GR_PICK(L, S) \
     if (t.layout == L && t.sstack == S) fn = (const void*)k_trace_queue<L, S>;

@@ -59,7 +59,7 @@ cudaError_t launch(const BvhDevice& bvh, const void* nodes, int block, const flo
                    unsigned long long* counter, uint32_t* err, int num_sms, cudaStream_t s) {
     static int occ[3] = {0, 0, 0};  // per block size 64 / 128 / 256
     const int bi = block == 64 ? 0 : (block == 128 ? 1 : 2);
-    const size_t smem = sizeof(int2) * SSTACK * block;
+    const size_t smem = trav::traverse_smem(LAYOUT, SSTACK, block);
     if (occ[bi] == 0) {
         const cudaError_t e =
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[bi], k_trace<ANY, LAYOUT, SSTACK>, block, smem);

@@ -427,6 +427,14 @@ __device__ __forceinline__ uint32_t xor_permute8(uint32_t x, uint32_t oct) {
     return x;
 }
 
+constexpr uint32_t kPerm8Bytes = 8 * 256;
+
+// Dynamic shared memory of a traversal kernel: the short stacks, and for the
+// 8-wide layout the octant permutation table.
+inline size_t traverse_smem(int layout, int sstack, int block) {
+    return sizeof(int2) * (size_t)sstack * block + (layout == kLayoutBvh8Q8 ? kPerm8Bytes : 0);
+}
+
 template <int SSTACK>
 __device__ __forceinline__ int2 stack_at(int i, const int2* s_stack, const int2* l_stack) {
     return i < SSTACK ? s_stack[i * blockDim.x + threadIdx.x] : l_stack[i - SSTACK];
@@ -455,7 +463,8 @@ __device__ __forceinline__ bool leaf_at(Lane& L, uint32_t idx) { return leaf<ANY
 // stay on the stack as one group entry (child_base, inner mask | hits << 8),
 // taken one child at a time. Returns true when the ray is finished.
 template <bool ANY, int SSTACK>
-__device__ __forceinline__ bool trace_step8(Lane& L, int2* s_stack, int2* l_stack, uint32_t* err) {
+__device__ __forceinline__ bool trace_step8(Lane& L, int2* s_stack, int2* l_stack, uint32_t* err,
+                                            const unsigned char* perm8) {
     const float4* q = reinterpret_cast<const float4*>(static_cast<const Node8Q*>(L.nodes) + L.node);
     float4 h0, h1, b0, b1, c0, c1;
     ldg32B(q, h0, h1);
@@ -500,7 +509,7 @@ __device__ __forceinline__ bool trace_step8(Lane& L, int2* s_stack, int2* l_stac
     }
     hm &= valid;
     uint32_t thits = hm & ~imask;
-    const uint32_t ihits = xor_permute8(hm & imask, oct);
+    const uint32_t ihits = perm8[(oct << 8) | (hm & imask)];  // xor_permute8(hm & imask, oct)
     if (thits) {
         const uint32_t leafmask = valid & ~imask;
         do {
@@ -536,9 +545,10 @@ __device__ __forceinline__ bool trace_step8(Lane& L, int2* s_stack, int2* l_stac
 }
 
 template <bool ANY, int LAYOUT, int SSTACK>
-__device__ __forceinline__ bool trace_step(Lane& L, int2* s_stack, int2* l_stack, uint32_t* err) {
+__device__ __forceinline__ bool trace_step(Lane& L, int2* s_stack, int2* l_stack, uint32_t* err,
+                                           const unsigned char* perm8) {
     if (LAYOUT == kLayoutBvh2) return trace_step2<ANY, SSTACK>(L, s_stack, l_stack, err);
-    if (LAYOUT == kLayoutBvh8Q8) return trace_step8<ANY, SSTACK>(L, s_stack, l_stack, err);
+    if (LAYOUT == kLayoutBvh8Q8) return trace_step8<ANY, SSTACK>(L, s_stack, l_stack, err, perm8);
     return trace_step4<ANY, LAYOUT == kLayoutBvh4Q8, SSTACK>(L, s_stack, l_stack, err);
 }
 
@@ -557,10 +567,20 @@ constexpr int kRefillQueue = 8;
 //                                                     root (kNoNode when empty)
 //   void finish(uint64_t i, const Lane& L)            ray i is done (L.best_prim ==
 //                                                     0xFFFFFFFF means a miss)
-// The shared stack has SSTACK x blockDim.x int2 entries (dynamic shared memory).
+// The shared stack has SSTACK x blockDim.x int2 entries (dynamic shared memory),
+// followed for the 8-wide layout by the octant permutation table
+// (traverse_smem). Every thread of the block calls it (the table is filled
+// behind a block barrier).
 template <bool ANY, int LAYOUT, int SSTACK, int REFILL, class Src>
 __device__ __forceinline__ void traverse_loop(Src& src, unsigned long long* counter, uint32_t* err, int2* s_stack) {
     int2 l_stack[kStackMax - SSTACK];
+    // 8-wide layout: xor_permute8 as a table (octant x mask, 2 KB after the
+    // short stacks), filled once per block
+    unsigned char* perm8 = reinterpret_cast<unsigned char*>(s_stack + SSTACK * blockDim.x);
+    if (LAYOUT == kLayoutBvh8Q8) {
+        for (uint32_t i = threadIdx.x; i < kPerm8Bytes; i += blockDim.x) perm8[i] = (unsigned char)xor_permute8(i & 255u, i >> 8);
+        __syncthreads();
+    }
     const int lane = threadIdx.x & 31;
     const uint32_t ltmask = lanemask_lt();
     const uint64_t n = src.n;
@@ -600,7 +620,7 @@ __device__ __forceinline__ void traverse_loop(Src& src, unsigned long long* coun
             if (exhausted) break;
             continue;
         }
-        if (active && trace_step<ANY, LAYOUT, SSTACK>(L, s_stack, l_stack, err)) {
+        if (active && trace_step<ANY, LAYOUT, SSTACK>(L, s_stack, l_stack, err, perm8)) {
             src.finish(L.ray, L);
             active = false;
         }
