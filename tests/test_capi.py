@@ -43,3 +43,13 @@ def test_context_without_gpu_fails_cleanly(grlib):
     h = ctypes.c_void_p()
     st = grlib.gr_context_create(0, ctypes.byref(h))
     assert st != 0 and not h.value
+
+
+def test_bounded_wait_diagnostic_checks_its_context(grlib):
+    # host-side argument check only: no context, no device work
+    bits = ctypes.c_uint32(7)
+    fn = grlib.gr_diag_bounded_wait
+    fn.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32)]
+    fn.restype = ctypes.c_int
+    assert fn(None, 1000, ctypes.byref(bits)) == 1  # GR_ERR_INVALID
+    assert bits.value == 7
