@@ -350,41 +350,44 @@ __device__ __forceinline__ float min3(float a, float b, float c) {
     return r;
 }
 
-// Plane distances of slots b and b + 4 of one plane set: byte b of w0 and of
-// w1 as exact floats — the byte becomes the low mantissa bits of 2^23 (one
-// byte permute), then 2^23 is subtracted — times S plus C. The subtraction and
-// the FMA run as packed two-lane FP32 instructions (sub.rn.f32x2,
-// fma.rn.f32x2): each lane rounds exactly as the scalar __fsub_rn / __fmaf_rn
-// would, in half the instructions (measured: 7 % more rays per second on the
-// traversal microbenchmark, at the same 64 registers).
-__device__ __forceinline__ float2 plane_pair(uint32_t w0, uint32_t w1, int b, float S, float C) {
-    const float q0 = __uint_as_float(__byte_perm(w0, 0x4B000000u, 0x7540u | (uint32_t)b));
-    const float q1 = __uint_as_float(__byte_perm(w1, 0x4B000000u, 0x7540u | (uint32_t)b));
+// Plane distances of slots b and b + 4 of one plane set. Byte b of w0 and of
+// w1 becomes the mantissa byte of v = 1 + q * 2^-15 (one byte permute each:
+// 0x3F80qq00, exact), and the distance is one packed two-lane FMA,
+// fma(v, S', C') with S' = 2^15 * S and C' = C - S' from the node's terms
+// (axis_terms8): v * S' + C' = q * S + C up to the rounding of C', which the
+// node's margins cover. Each lane rounds exactly as a scalar __fmaf_rn would.
+__device__ __forceinline__ float2 plane_pair(uint32_t w0, uint32_t w1, int b, float Sp, float Cp) {
+    const float v0 = __uint_as_float(__byte_perm(w0, 0x3F800000u, 0x7604u | ((uint32_t)b << 4)));
+    const float v1 = __uint_as_float(__byte_perm(w1, 0x3F800000u, 0x7604u | ((uint32_t)b << 4)));
     float2 t;
     asm("{\n\t"
-        ".reg .b64 q, k, s, c, r;\n\t"
-        "mov.b64 q, {%2, %3};\n\t"
-        "mov.b64 k, {%4, %4};\n\t"
-        "sub.rn.f32x2 q, q, k;\n\t"
-        "mov.b64 s, {%5, %5};\n\t"
-        "mov.b64 c, {%6, %6};\n\t"
-        "fma.rn.f32x2 r, q, s, c;\n\t"
+        ".reg .b64 v, s, c, r;\n\t"
+        "mov.b64 v, {%2, %3};\n\t"
+        "mov.b64 s, {%4, %4};\n\t"
+        "mov.b64 c, {%5, %5};\n\t"
+        "fma.rn.f32x2 r, v, s, c;\n\t"
         "mov.b64 {%0, %1}, r;\n\t"
         "}"
         : "=f"(t.x), "=f"(t.y)
-        : "f"(q0), "f"(q1), "f"(8388608.0f), "f"(S), "f"(C));
+        : "f"(v0), "f"(v1), "f"(Sp), "f"(Cp));
     return t;
 }
 
-// Per node and axis: S = 2^e * (1/d), C = (lo - o) * (1/d), and the near /
-// far offsets C -+ m with m = |C| * 2^-21 + |S| * 2^-14.
-__device__ __forceinline__ void axis_terms8(uint32_t biased_e, float lo, float o, float inv, float& S, float& cn,
+// Per node and axis, with S = 2^e * (1/d) and C = (lo - o) * (1/d): the
+// plane scale S' = 2^15 * S (exact) and the near / far offsets C' -+ m with
+// C' = C - S' and m = |C| * 2^-20 + |S| * 2^-7. The roundings of C, C', the
+// offsets and the final FMA stay below 2.5 * 2^-23 * |C| + (2^-8 + 2^-16) * |S|
+// (C' = C - S' is rounded at the size of S', 2^15 |S|, and so is C' -+ m), so
+// the measured interval [near, far] always contains the quantised box's.
+__device__ __forceinline__ void axis_terms8(uint32_t biased_e, float lo, float o, float inv, float& Sp, float& cn,
                                             float& cf) {
-    S = __fmul_rn(__uint_as_float(biased_e << 23), inv);
+    const float S = __fmul_rn(__uint_as_float(biased_e << 23), inv);
     const float C = __fmul_rn(__fsub_rn(lo, o), inv);
-    const float m = __fmaf_rn(fabsf(C), 0x1p-21f, __fmul_rn(fabsf(S), 0x1p-14f));
-    cn = __fsub_rn(C, m);
-    cf = __fadd_rn(C, m);
+    Sp = __fmul_rn(S, 32768.0f);
+    const float Cp = __fsub_rn(C, Sp);
+    const float m = __fmaf_rn(fabsf(C), 0x1p-20f, __fmul_rn(fabsf(S), 0x1p-7f));
+    cn = __fsub_rn(Cp, m);
+    cf = __fadd_rn(Cp, m);
 }
 
 // axis_terms8 for the x and y axes at once, in packed two-lane FP32
@@ -394,7 +397,7 @@ __device__ __forceinline__ void axis_terms8_xy(uint32_t ex, uint32_t ey, float l
                                                float ix, float iy, float& Sx, float& Sy, float& cnx, float& cny,
                                                float& cfx, float& cfy) {
     asm("{\n\t"
-        ".reg .b64 e, inv, S, lo, o, C, aS, aC, k14, k21, t, m, cn, cf;\n\t"
+        ".reg .b64 e, inv, S, Sp, lo, o, C, Cp, aS, aC, k7, k15, k20, t, m, cn, cf;\n\t"
         "mov.b64 e, {%6, %7};\n\t"
         "mov.b64 inv, {%12, %13};\n\t"
         "mul.rn.f32x2 S, e, inv;\n\t"
@@ -402,15 +405,18 @@ __device__ __forceinline__ void axis_terms8_xy(uint32_t ex, uint32_t ey, float l
         "mov.b64 o, {%10, %11};\n\t"
         "sub.rn.f32x2 C, lo, o;\n\t"
         "mul.rn.f32x2 C, C, inv;\n\t"
+        "mov.b64 k15, 0x4700000047000000;\n\t"  // {2^15, 2^15}
+        "mul.rn.f32x2 Sp, S, k15;\n\t"
+        "sub.rn.f32x2 Cp, C, Sp;\n\t"
         "and.b64 aS, S, 0x7FFFFFFF7FFFFFFF;\n\t"
         "and.b64 aC, C, 0x7FFFFFFF7FFFFFFF;\n\t"
-        "mov.b64 k14, 0x3880000038800000;\n\t"  // {2^-14, 2^-14}
-        "mov.b64 k21, 0x3500000035000000;\n\t"  // {2^-21, 2^-21}
-        "mul.rn.f32x2 t, aS, k14;\n\t"
-        "fma.rn.f32x2 m, aC, k21, t;\n\t"
-        "sub.rn.f32x2 cn, C, m;\n\t"
-        "add.rn.f32x2 cf, C, m;\n\t"
-        "mov.b64 {%0, %1}, S;\n\t"
+        "mov.b64 k7, 0x3C0000003C000000;\n\t"   // {2^-7, 2^-7}
+        "mov.b64 k20, 0x3580000035800000;\n\t"  // {2^-20, 2^-20}
+        "mul.rn.f32x2 t, aS, k7;\n\t"
+        "fma.rn.f32x2 m, aC, k20, t;\n\t"
+        "sub.rn.f32x2 cn, Cp, m;\n\t"
+        "add.rn.f32x2 cf, Cp, m;\n\t"
+        "mov.b64 {%0, %1}, Sp;\n\t"
         "mov.b64 {%2, %3}, cn;\n\t"
         "mov.b64 {%4, %5}, cf;\n\t"
         "}"
@@ -451,12 +457,11 @@ template <bool ANY>
 __device__ __forceinline__ bool leaf_at(Lane& L, uint32_t idx) { return leaf<ANY>(L, ~(int32_t)idx); }
 
 // One 8-wide node. A child plane is q * 2^e + lo, taken exactly; its ray
-// distance is measured as fma(q, S, C) with S = 2^e / d (exact: a power-of-two
-// scaling) and C = (lo - o) / d, evaluated once per node and axis. The
-// rounding of C, of the offsets and of the final FMA stays below
-// |C| * 2^-22 + |S| * 2^-16, so near planes use C - m and far planes C + m
-// with m = |C| * 2^-21 + |S| * 2^-14: the measured interval always contains
-// the quantised box's. The near plane of an axis is lo when d >= 0, else hi.
+// distance q * S + C, with S = 2^e / d (exact: a power-of-two scaling) and
+// C = (lo - o) / d, is measured as one FMA from per-node terms
+// (axis_terms8, plane_pair), near planes with the offset C' - m and far
+// planes with C' + m, so the measured interval always contains the quantised
+// box's. The near plane of an axis is lo when d >= 0, else hi.
 // A child is hit when max(near, tmin) <= min(far, best_t * slack). Hit leaf
 // triangles are tested in slot order; hit inner children are ranked by
 // slot ^ octant and the lowest rank is visited next. The remaining inner hits
@@ -590,7 +595,9 @@ __device__ __forceinline__ void traverse_loop(Src& src, unsigned long long* coun
     for (;;) {
         const uint32_t idle = __ballot_sync(0xFFFFFFFFu, !active);
         const int nidle = __popc(idle);
-        if (!exhausted && (nidle >= REFILL || nidle == 32)) {
+        if (exhausted) {
+            if (nidle == 32) break;  // a refill that found no rays leaves every lane idle
+        } else if (nidle >= REFILL || nidle == 32) {
             unsigned long long base = 0;
             if (lane == 0) base = atomicAdd(counter, (unsigned long long)nidle);
             base = __shfl_sync(0xFFFFFFFFu, base, 0);
@@ -615,10 +622,6 @@ __device__ __forceinline__ void traverse_loop(Src& src, unsigned long long* coun
                     }
                 }
             }
-        }
-        if (__ballot_sync(0xFFFFFFFFu, active) == 0) {
-            if (exhausted) break;
-            continue;
         }
         if (active && trace_step<ANY, LAYOUT, SSTACK>(L, s_stack, l_stack, err, perm8)) {
             src.finish(L.ray, L);

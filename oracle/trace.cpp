@@ -627,11 +627,15 @@ void trace8_one(const uint32_t* nodes, const float* tris, uint32_t root, const f
         uint32_t nw[3][2], fw[3][2];
         const float bound = b.t * kCullSlack;
         for (int a = 0; a < 3; ++a) {
-            S[a] = f_of(((meta >> (8 * a)) & 0xFFu) << 23) * p.idir[a];
+            // plane distance q * S + C measured as fma(1 + q * 2^-15, S', C' -+ m)
+            // with S' = 2^15 S, C' = C - S' and m = |C| 2^-20 + |S| 2^-7
+            const float Sa = f_of(((meta >> (8 * a)) & 0xFFu) << 23) * p.idir[a];
             const float C = (f_of(o[a]) - p.o[a]) * p.idir[a];
-            const float m = std::fmaf(std::fabs(C), 0x1p-21f, std::fabs(S[a]) * 0x1p-14f);
-            cn[a] = C - m;
-            cf[a] = C + m;
+            S[a] = Sa * 32768.0f;
+            const float Cp = C - S[a];
+            const float m = std::fmaf(std::fabs(C), 0x1p-20f, std::fabs(Sa) * 0x1p-7f);
+            cn[a] = Cp - m;
+            cf[a] = Cp + m;
             for (int h = 0; h < 2; ++h) {
                 const uint32_t lo = o[8 + 4 * a + h], hi = o[8 + 4 * a + 2 + h];
                 nw[a][h] = sg[a] ? hi : lo;
@@ -642,8 +646,8 @@ void trace8_one(const uint32_t* nodes, const float* tris, uint32_t root, const f
         for (int k = 0; k < 8; ++k) {
             float tn[3], tf[3];
             for (int a = 0; a < 3; ++a) {
-                tn[a] = std::fmaf((float)byte_of(nw[a][k >> 2], k & 3), S[a], cn[a]);
-                tf[a] = std::fmaf((float)byte_of(fw[a][k >> 2], k & 3), S[a], cf[a]);
+                tn[a] = std::fmaf(f_of(0x3F800000u | (byte_of(nw[a][k >> 2], k & 3) << 8)), S[a], cn[a]);
+                tf[a] = std::fmaf(f_of(0x3F800000u | (byte_of(fw[a][k >> 2], k & 3) << 8)), S[a], cf[a]);
             }
             const float tnear = std::fmax(std::fmax(std::fmax(tn[0], tn[1]), tn[2]), p.tmin);
             const float tfar = std::fmin(std::fmin(std::fmin(tf[0], tf[1]), tf[2]), bound);
