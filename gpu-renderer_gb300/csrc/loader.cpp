@@ -25,6 +25,7 @@
 // image format leaves a texture at its 0.5 grey, an envmap skipped; recorded
 // as a warning); only the colour slots (reflectance, specularReflectance,
 // diffuseReflectance) take textures.
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -183,64 +184,106 @@ struct M4 {
     }
 };
 
-// General 4x4 inverse by Gauss-Jordan elimination with partial pivoting.
+// 4x4 inverse by Gauss-Jordan elimination with full pivoting in FP32, in the
+// operation order of the Numerical Recipes / pbrt routine the reference uses
+// (transform.cpp:30-90), so inverses (and the normals transformed by them) are
+// the same floats. False for a singular matrix.
 bool invert(const M4& a, M4& out) {
-    double w[4][8];
-    for (int i = 0; i < 4; ++i)
-        for (int j = 0; j < 8; ++j) w[i][j] = j < 4 ? a.m[i][j] : (j - 4 == i ? 1.0 : 0.0);
-    for (int c = 0; c < 4; ++c) {
-        int p = c;
-        for (int r = c + 1; r < 4; ++r)
-            if (std::fabs(w[r][c]) > std::fabs(w[p][c])) p = r;
-        if (w[p][c] == 0.0) return false;
-        if (p != c)
-            for (int j = 0; j < 8; ++j) std::swap(w[p][j], w[c][j]);
-        const double inv = 1.0 / w[c][c];
-        for (int j = 0; j < 8; ++j) w[c][j] *= inv;
-        for (int r = 0; r < 4; ++r) {
-            if (r == c) continue;
-            const double f = w[r][c];
-            for (int j = 0; j < 8; ++j) w[r][j] -= f * w[c][j];
+    int indxc[4], indxr[4];
+    int ipiv[4] = {0, 0, 0, 0};
+    float minv[4][4];
+    std::memcpy(minv, a.m, sizeof(minv));
+    for (int i = 0; i < 4; ++i) {
+        int irow = 0, icol = 0;
+        float big = 0.0f;
+        for (int j = 0; j < 4; ++j) {
+            if (ipiv[j] == 1) continue;
+            for (int k = 0; k < 4; ++k) {
+                if (ipiv[k] == 0) {
+                    if (std::fabs(minv[j][k]) >= big) {
+                        big = std::fabs(minv[j][k]);
+                        irow = j;
+                        icol = k;
+                    }
+                } else if (ipiv[k] > 1) {
+                    return false;
+                }
+            }
+        }
+        ++ipiv[icol];
+        if (irow != icol)
+            for (int k = 0; k < 4; ++k) std::swap(minv[irow][k], minv[icol][k]);
+        indxr[i] = irow;
+        indxc[i] = icol;
+        if (minv[icol][icol] == 0.0f) return false;
+        const float pivinv = 1.0f / minv[icol][icol];
+        minv[icol][icol] = 1.0f;
+        for (int j = 0; j < 4; ++j) minv[icol][j] *= pivinv;
+        for (int j = 0; j < 4; ++j) {
+            if (j == icol) continue;
+            const float save = minv[j][icol];
+            minv[j][icol] = 0.0f;
+            for (int k = 0; k < 4; ++k) minv[j][k] -= minv[icol][k] * save;
         }
     }
-    for (int i = 0; i < 4; ++i)
-        for (int j = 0; j < 4; ++j) out.m[i][j] = (float)w[i][j + 4];
+    for (int j = 3; j >= 0; --j)
+        if (indxr[j] != indxc[j])
+            for (int k = 0; k < 4; ++k) std::swap(minv[k][indxr[j]], minv[k][indxc[j]]);
+    std::memcpy(out.m, minv, sizeof(minv));
     return true;
 }
 
+M4 transpose(const M4& a) {
+    M4 r;
+    for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j) r.m[i][j] = a.m[j][i];
+    return r;
+}
+
+// A transform and its inverse, composed as the reference's Transform is
+// (transform.h:89-113): (A * B).inv = B.inv * A.inv, each elementary transform
+// carrying its own exact or computed inverse, so a normal is mapped by the same
+// inverse matrix the reference maps it by.
+struct XF {
+    M4 m = M4::identity(), inv = M4::identity();
+};
+XF compose(const XF& a, const XF& b) { return {a.m * b.m, b.inv * a.inv}; }
+
 float deg2rad(float d) { return d / 180.0f * 3.14159265358979323846f; }
 
-M4 translate(F3 d) {
-    M4 r = M4::identity();
-    r.m[0][3] = d.x;
-    r.m[1][3] = d.y;
-    r.m[2][3] = d.z;
+XF translate(F3 d) {
+    XF r;
+    r.m.m[0][3] = d.x; r.m.m[1][3] = d.y; r.m.m[2][3] = d.z;
+    r.inv.m[0][3] = -d.x; r.inv.m[1][3] = -d.y; r.inv.m[2][3] = -d.z;
     return r;
 }
-M4 scale(F3 s) {
-    M4 r = M4::identity();
-    r.m[0][0] = s.x;
-    r.m[1][1] = s.y;
-    r.m[2][2] = s.z;
+XF scale(F3 s) {
+    XF r;
+    r.m.m[0][0] = s.x; r.m.m[1][1] = s.y; r.m.m[2][2] = s.z;
+    // reciprocals taken in double and rounded to float, as the reference's do
+    r.inv.m[0][0] = (float)(1.0 / (double)s.x);
+    r.inv.m[1][1] = (float)(1.0 / (double)s.y);
+    r.inv.m[2][2] = (float)(1.0 / (double)s.z);
     return r;
 }
-M4 rotate(float deg, F3 axis) {  // rotation about an axis (Rodrigues)
+XF rotate(float deg, F3 axis) {  // rotation about an axis (Rodrigues); its inverse is the transpose
     const F3 a = normalize(axis);
     const float s = std::sin(deg2rad(deg)), c = std::cos(deg2rad(deg));
-    M4 r = M4::identity();
-    r.m[0][0] = a.x * a.x + (1 - a.x * a.x) * c;
-    r.m[0][1] = a.x * a.y * (1 - c) - a.z * s;
-    r.m[0][2] = a.x * a.z * (1 - c) + a.y * s;
-    r.m[1][0] = a.x * a.y * (1 - c) + a.z * s;
-    r.m[1][1] = a.y * a.y + (1 - a.y * a.y) * c;
-    r.m[1][2] = a.y * a.z * (1 - c) - a.x * s;
-    r.m[2][0] = a.x * a.z * (1 - c) - a.y * s;
-    r.m[2][1] = a.y * a.z * (1 - c) + a.x * s;
-    r.m[2][2] = a.z * a.z + (1 - a.z * a.z) * c;
+    XF r;
+    r.m.m[0][0] = a.x * a.x + (1 - a.x * a.x) * c;
+    r.m.m[0][1] = a.x * a.y * (1 - c) - a.z * s;
+    r.m.m[0][2] = a.x * a.z * (1 - c) + a.y * s;
+    r.m.m[1][0] = a.x * a.y * (1 - c) + a.z * s;
+    r.m.m[1][1] = a.y * a.y + (1 - a.y * a.y) * c;
+    r.m.m[1][2] = a.y * a.z * (1 - c) - a.x * s;
+    r.m.m[2][0] = a.x * a.z * (1 - c) - a.y * s;
+    r.m.m[2][1] = a.y * a.z * (1 - c) + a.x * s;
+    r.m.m[2][2] = a.z * a.z + (1 - a.z * a.z) * c;
+    r.inv = transpose(r.m);
     return r;
 }
 // camera-to-world with columns (left, up, forward, origin) (transform.cpp:220-249)
-M4 look_at(F3 target, F3 origin, F3 up) {
+bool look_at(F3 target, F3 origin, F3 up, XF& out) {
     const F3 f = normalize(target - origin);
     const F3 l = normalize(cross(up, f));
     const F3 u = cross(f, l);
@@ -249,7 +292,8 @@ M4 look_at(F3 target, F3 origin, F3 up) {
     r.m[0][1] = u.x; r.m[1][1] = u.y; r.m[2][1] = u.z;
     r.m[0][2] = f.x; r.m[1][2] = f.y; r.m[2][2] = f.z;
     r.m[0][3] = origin.x; r.m[1][3] = origin.y; r.m[2][3] = origin.z;
-    return r;
+    out.m = r;
+    return invert(r, out.inv);
 }
 
 bool parse_floats(const char* s, float* out, int n) {
@@ -273,7 +317,7 @@ struct Prop {
     float f = 0.0f;
     std::string s;
     F3 v{0, 0, 0};
-    M4 t = M4::identity();
+    M4 t = M4::identity(), tinv = M4::identity();  // transform and its inverse
     // texture: map index into the description's maps (-1: constant v), size, uv offset and scale
     int tex = -1;
     uint32_t tw = 0, th = 0;
@@ -436,33 +480,54 @@ bool load_obj(const std::string& path, MeshData& out, std::string& err) {
 
 // ---- procedural shapes (mitsubaloader.cpp:53-221) --------------------------------------------
 void make_rectangle(MeshData& m) {
+    // the unit square in z = 0 with texture coordinates at its corners and the
+    // +z normal; triangles (0, 1, 2) and (2, 3, 0) (mitsubaloader.cpp:119-151)
     const float p[] = {-1, -1, 0, 1, -1, 0, 1, 1, 0, -1, 1, 0};
     m.pos.assign(p, p + 12);
     m.nrm = {0, 0, 1, 0, 0, 1, 0, 0, 1, 0, 0, 1};
+    m.uv = {0, 0, 1, 0, 1, 1, 0, 1};
     m.has_normals = true;
+    m.has_uvs = true;
     m.idx = {0, 1, 2, 2, 3, 0};
 }
 
 void make_cube(MeshData& m) {
-    // six faces of [-1, 1]^3, four vertices each with the face normal
-    const int axes[6][3] = {{1, 0, 0}, {-1, 0, 0}, {0, 1, 0}, {0, -1, 0}, {0, 0, 1}, {0, 0, -1}};
+    // [-1, 1]^3 as the reference builds it (mitsubaloader.cpp:53-116): eight
+    // corners, six face normals and fourteen texture coordinates, each face a
+    // quad of (corner, texcoord, normal) triples split into (q0, q1, q2) and
+    // (q0, q2, q3). The triangle order (and so every hit's primitive id) and
+    // the corner order within each triangle are the reference's. A vertex here
+    // is one distinct triple, numbered in order of first use.
+    static const float corner[8][3] = {{1, 1, -1}, {1, -1, -1}, {1, 1, 1},   {1, -1, 1},
+                                       {-1, 1, -1}, {-1, -1, -1}, {-1, 1, 1}, {-1, -1, 1}};
+    static const float normal[6][3] = {{0, 1, 0}, {0, 0, 1}, {-1, 0, 0}, {0, -1, 0}, {1, 0, 0}, {0, 0, -1}};
+    static const float tex[14][2] = {{0.625f, 0.5f},  {0.875f, 0.5f},  {0.875f, 0.75f}, {0.625f, 0.75f},
+                                     {0.375f, 0.75f}, {0.625f, 1.0f},  {0.375f, 1.0f},  {0.375f, 0.0f},
+                                     {0.625f, 0.0f},  {0.625f, 0.25f}, {0.375f, 0.25f}, {0.125f, 0.5f},
+                                     {0.375f, 0.5f},  {0.125f, 0.75f}};
+    // per face: the quad's four (corner, texcoord) pairs; the face's normal is its index
+    static const int quad[6][4][2] = {{{0, 0}, {4, 1}, {6, 2}, {2, 3}},   {{3, 4}, {2, 3}, {6, 5}, {7, 6}},
+                                      {{7, 7}, {6, 8}, {4, 9}, {5, 10}},  {{5, 11}, {1, 12}, {3, 4}, {7, 13}},
+                                      {{1, 12}, {0, 0}, {2, 3}, {3, 4}},  {{5, 10}, {4, 9}, {0, 0}, {1, 12}}};
+    std::map<std::array<int, 3>, uint32_t> vertex_of;
+    auto vertex = [&](int c, int t, int n) {
+        const std::array<int, 3> key{c, t, n};
+        auto it = vertex_of.find(key);
+        if (it != vertex_of.end()) return it->second;
+        const uint32_t v = (uint32_t)vertex_of.size();
+        vertex_of.emplace(key, v);
+        m.pos.insert(m.pos.end(), {corner[c][0], corner[c][1], corner[c][2]});
+        m.nrm.insert(m.nrm.end(), {normal[n][0], normal[n][1], normal[n][2]});
+        m.uv.insert(m.uv.end(), {tex[t][0], tex[t][1]});
+        return v;
+    };
     for (int f = 0; f < 6; ++f) {
-        F3 n = f3((float)axes[f][0], (float)axes[f][1], (float)axes[f][2]);
-        // two tangents spanning the face, ordered so the winding faces outward
-        F3 t1 = std::fabs(n.x) > 0 ? f3(0, 1, 0) : f3(1, 0, 0);
-        F3 t2 = cross(n, t1);
-        const uint32_t base = (uint32_t)(m.pos.size() / 3);
-        const float sgn[4][2] = {{-1, -1}, {1, -1}, {1, 1}, {-1, 1}};
-        for (int k = 0; k < 4; ++k) {
-            m.pos.push_back(n.x + sgn[k][0] * t1.x + sgn[k][1] * t2.x);
-            m.pos.push_back(n.y + sgn[k][0] * t1.y + sgn[k][1] * t2.y);
-            m.pos.push_back(n.z + sgn[k][0] * t1.z + sgn[k][1] * t2.z);
-            m.nrm.insert(m.nrm.end(), {n.x, n.y, n.z});
-        }
-        const uint32_t q[6] = {0, 1, 2, 0, 2, 3};
-        for (uint32_t k : q) m.idx.push_back(base + k);
+        uint32_t q[4];
+        for (int k = 0; k < 4; ++k) q[k] = vertex(quad[f][k][0], quad[f][k][1], f);
+        m.idx.insert(m.idx.end(), {q[0], q[1], q[2], q[0], q[2], q[3]});
     }
     m.has_normals = true;
+    m.has_uvs = true;
 }
 
 void make_sphere(MeshData& m, float radius, int subdiv) {
@@ -588,7 +653,7 @@ bool read_float_image(const std::string& path, std::vector<float>& rgb, uint32_t
 struct Interp {
     gr_scene_desc* out;
     std::string dir;
-    M4 xf = M4::identity();
+    XF xf;
     gr_material cur{};
     bool have_cur = false;
     F3 cur_light{0, 0, 0};
@@ -711,11 +776,12 @@ struct Interp {
         } else {
             return fail("unsupported shape type '" + type + "'", n);
         }
-        M4 o2w = M4::identity();
+        M4 o2w = M4::identity(), inv = M4::identity();
         auto it = L.find("toWorld");
-        if (it != L.end() && it->second.kind == Prop::Transform) o2w = it->second.t;
-        M4 inv;
-        if (!invert(o2w, inv)) return fail("singular toWorld", n);
+        if (it != L.end() && it->second.kind == Prop::Transform) {
+            o2w = it->second.t;
+            inv = it->second.tinv;
+        }
         for (size_t v = 0; v < mesh.pos.size() / 3; ++v) {
             const float x = mesh.pos[3 * v], y = mesh.pos[3 * v + 1], z = mesh.pos[3 * v + 2];
             float r[4];
@@ -748,7 +814,7 @@ struct Interp {
     // Post-order walk (ParseTag, mitsubaloader.cpp:774-805).
     bool visit(const XNode& n, Props& parent) {
         const std::string& tag = n.name;
-        if (tag == "transform") xf = M4::identity();
+        if (tag == "transform") xf = XF();
         Props mine;
         for (auto& k : n.kids)
             if (!visit(*k, mine)) return false;
@@ -908,13 +974,16 @@ struct Interp {
             return fail("spectrum values are not supported", n);
         } else if (tag == "transform") {
             p.kind = Prop::Transform;
-            p.t = xf;
+            p.t = xf.m;
+            p.tinv = xf.inv;
         } else if (tag == "lookat" || tag == "lookAt") {
             F3 t, o, u;
             if (!parse_floats(n.attr("target"), &t.x, 3) || !parse_floats(n.attr("origin"), &o.x, 3) ||
                 !parse_floats(n.attr("up"), &u.x, 3))
                 return fail("bad lookat", n);
-            xf = xf * look_at(t, o, u);
+            XF la;
+            if (!look_at(t, o, u, la)) return fail("singular lookat", n);
+            xf = compose(xf, la);
             return true;
         } else if (tag == "translate") {
             F3 d;
@@ -924,7 +993,7 @@ struct Interp {
                 d = f3(n.attr("x") ? strtof(n.attr("x"), nullptr) : 0.0f, n.attr("y") ? strtof(n.attr("y"), nullptr) : 0.0f,
                        n.attr("z") ? strtof(n.attr("z"), nullptr) : 0.0f);
             }
-            xf = xf * translate(d);
+            xf = compose(xf, translate(d));
             return true;
         } else if (tag == "scale") {
             F3 d;
@@ -934,18 +1003,19 @@ struct Interp {
                 d = f3(n.attr("x") ? strtof(n.attr("x"), nullptr) : 1.0f, n.attr("y") ? strtof(n.attr("y"), nullptr) : 1.0f,
                        n.attr("z") ? strtof(n.attr("z"), nullptr) : 1.0f);
             }
-            xf = xf * scale(d);
+            xf = compose(xf, scale(d));
             return true;
         } else if (tag == "rotate") {
             const F3 a = f3(n.attr("x") ? strtof(n.attr("x"), nullptr) : 0.0f, n.attr("y") ? strtof(n.attr("y"), nullptr) : 0.0f,
                             n.attr("z") ? strtof(n.attr("z"), nullptr) : 0.0f);
             const float ang = n.attr("angle") ? strtof(n.attr("angle"), nullptr) : 0.0f;
-            xf = xf * rotate(ang, a);
+            xf = compose(xf, rotate(ang, a));
             return true;
         } else if (tag == "matrix") {
-            M4 m;
-            if (!parse_floats(value, &m.m[0][0], 16)) return fail("bad matrix", n);
-            xf = xf * m;
+            XF m;
+            if (!parse_floats(value, &m.m.m[0][0], 16)) return fail("bad matrix", n);
+            if (!invert(m.m, m.inv)) return fail("singular matrix", n);
+            xf = compose(xf, m);
             return true;
         } else {
             return fail("unexpected tag <" + tag + ">", n);
@@ -1049,6 +1119,14 @@ gr_status gr_scene_desc_mesh(const gr_scene_desc* d, uint32_t i, uint32_t* num_v
     if (h_positions && !m.pos.empty()) std::memcpy(h_positions, m.pos.data(), m.pos.size() * 4);
     if (h_normals && m.has_normals) std::memcpy(h_normals, m.nrm.data(), m.nrm.size() * 4);
     if (h_indices && !m.idx.empty()) std::memcpy(h_indices, m.idx.data(), m.idx.size() * 4);
+    return GR_OK;
+}
+
+gr_status gr_scene_desc_mesh_texcoords(const gr_scene_desc* d, uint32_t i, int* has_texcoords, float* h_texcoords) {
+    if (!d || i >= d->meshes.size()) return GR_ERR_INVALID;
+    const MeshData& m = d->meshes[i];
+    if (has_texcoords) *has_texcoords = m.has_uvs ? 1 : 0;
+    if (h_texcoords && m.has_uvs && !m.uv.empty()) std::memcpy(h_texcoords, m.uv.data(), m.uv.size() * 4);
     return GR_OK;
 }
 

@@ -687,6 +687,7 @@ _DESC_SIGS = {
     "gr_scene_desc_info": ([_P, _P, _P, _P, ctypes.POINTER(Camera), ctypes.POINTER(Environment)], ctypes.c_int),
     "gr_scene_desc_triangles": ([_P, _P, _P, _P], ctypes.c_int),
     "gr_scene_desc_mesh": ([_P, ctypes.c_uint32, _P, _P, _P, _P, _P, _P], ctypes.c_int),
+    "gr_scene_desc_mesh_texcoords": ([_P, ctypes.c_uint32, _P, _P], ctypes.c_int),
     "gr_scene_create_from_desc": ([_P, _P, ctypes.POINTER(_P)], ctypes.c_int),
     "gr_scene_load_xml": ([_P, ctypes.c_char_p, ctypes.POINTER(_P)], ctypes.c_int),
 }
@@ -722,6 +723,30 @@ class ParsedScene:
         mats = (Material * max(self.num_meshes, 1))()
         L.gr_scene_desc_triangles(self.h, _ptr(v), _ptr(mesh), mats)
         return v, mesh, [mats[i] for i in range(self.num_meshes)]
+
+    def triangle_attributes(self):
+        """Per triangle, in the flattened order of triangles(): shading
+        normals (n x 9 floats) and texture coordinates (n x 6 floats), NaN
+        where the triangle's mesh has none."""
+        L = _declare(_DESC_SIGS)
+        nrm = np.full((self.num_triangles, 9), np.nan, np.float32)
+        uvs = np.full((self.num_triangles, 6), np.nan, np.float32)
+        off = 0
+        for i in range(self.num_meshes):
+            nv, nt, hn, ht = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_int(), ctypes.c_int()
+            L.gr_scene_desc_mesh(self.h, i, ctypes.byref(nv), ctypes.byref(nt), ctypes.byref(hn), None, None, None)
+            L.gr_scene_desc_mesh_texcoords(self.h, i, ctypes.byref(ht), None)
+            idx = np.zeros((nt.value, 3), np.uint32)
+            n = np.zeros((nv.value, 3), np.float32) if hn.value else None
+            t = np.zeros((nv.value, 2), np.float32) if ht.value else None
+            L.gr_scene_desc_mesh(self.h, i, None, None, None, None, _ptr(n), _ptr(idx))
+            if t is not None:
+                L.gr_scene_desc_mesh_texcoords(self.h, i, None, _ptr(t))
+                uvs[off:off + nt.value] = t[idx].reshape(-1, 6)
+            if n is not None:
+                nrm[off:off + nt.value] = n[idx].reshape(-1, 9)
+            off += nt.value
+        return nrm, uvs
 
     def scene_desc(self):
         """The parsed scene as a gr.scenes.SceneDesc (one mesh per shape, each

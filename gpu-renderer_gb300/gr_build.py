@@ -86,22 +86,26 @@ def build_oracle():
     r = subprocess.run(["make", "-s", "-C", odir, "-j4"], capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("oracle build failed:\n%s\n%s" % (r.stdout, r.stderr))
+    sys.path.insert(0, odir)
+    import refsrc  # oracle/refsrc.py: where the reference tree is, if anywhere
     ref = os.path.join(odir, "ref", "build_ref.sh")
-    if os.path.isdir("/root/reference/src") and shutil.which("bash"):
-        r = subprocess.run(["bash", ref], capture_output=True, text=True)
+    if refsrc.root() and shutil.which("bash"):
+        r = subprocess.run(["bash", ref], capture_output=True, text=True,
+                           env=dict(os.environ, GR_REFERENCE_ROOT=refsrc.root()))
         if r.returncode != 0:
             raise RuntimeError("reference build failed:\n%s\n%s" % (r.stdout, r.stderr))
-    # the reference's Cornell-box fixture as this library's loader parses it
-    # (for rendering it with both integrators on the GPU, where the file is absent)
-    cbox = "/root/reference/scene/CBox/cbox.xml"
-    if os.path.exists(cbox):
-        sys.path.insert(0, odir)
+    # the reference's Cornell-box fixture as this library's loader parses it,
+    # and as the reference's own loader does (for rendering both on the GPU,
+    # where the file is absent)
+    cbox = refsrc.cbox_scenes().get("cbox.xml")
+    if cbox:
         import gr
         import ref_gpu
         os.makedirs(ref_gpu.REF_DIR, exist_ok=True)
         parsed = gr.ParsedScene(cbox)
         ref_gpu.save_desc(parsed.scene_desc(), ref_gpu.CBOX_SCENE)
         parsed.close()
+        ref_gpu.save_refloader_scene(cbox, ref_gpu.CBOX_REFLOADER_SCENE)
 
 
 if __name__ == "__main__":

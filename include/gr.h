@@ -429,6 +429,11 @@ gr_status gr_scene_desc_triangles(const gr_scene_desc* desc, float* h_verts, uin
  * triangle). Its material is h_mats[i] of gr_scene_desc_triangles. */
 gr_status gr_scene_desc_mesh(const gr_scene_desc* desc, uint32_t i, uint32_t* num_vertices, uint32_t* num_triangles,
                              int* has_normals, float* h_positions, float* h_normals, uint32_t* h_indices);
+/* Mesh i's texture coordinates as parsed (2 floats per vertex of
+ * gr_scene_desc_mesh), when it has them (Triangle::getTexcoords,
+ * triangle.h:71-76: OBJ "vt", and the rectangle and cube shapes). */
+gr_status gr_scene_desc_mesh_texcoords(const gr_scene_desc* desc, uint32_t i, int* has_texcoords,
+                                       float* h_texcoords);
 gr_status gr_scene_create_from_desc(gr_ctx* ctx, const gr_scene_desc* desc, gr_scene** out);
 /* Parse + create: the drop-in for PathTracer(filename) (pathtracer.cu:8-11). */
 gr_status gr_scene_load_xml(gr_ctx* ctx, const char* path, gr_scene** out);

@@ -24,6 +24,12 @@ template <BufferType TYPE, typename T>
 class Buffer {
 public:
     Buffer(size_t count = 0) : m_host(count) {}
+    // copies between buffer kinds (framebuffer.cpp:13-14 reads a device buffer
+    // back this way)
+    template <BufferType U>
+    Buffer(const Buffer<U, T>& other) : m_host(other.data(), other.data() + other.size()) {}
+    T operator[](size_t i) const { return m_host[i]; }
+    T& operator[](size_t i) { return m_host[i]; }
     // the reference's Buffer hands out a mutable pointer from a const object
     // (environment.cpp:5 relies on it)
     T* data() const { return const_cast<T*>(m_host.data()); }

@@ -72,6 +72,53 @@ def render_available(build="stock"):
 # where its tree is, travel to the GPU machine this way)
 # ---------------------------------------------------------------------------
 CBOX_SCENE = os.path.join(REF_DIR, "cbox_scene.npz")
+# the same fixture as the reference's own loader produces it (refloader.py)
+CBOX_REFLOADER_SCENE = os.path.join(REF_DIR, "cbox_refloader_scene.npz")
+
+
+def save_refloader_scene(xml_path, out_path):
+    """The scene the reference's own loader builds from `xml_path`, as a
+    SceneDesc file: one mesh per reference mesh with its triangles' corners as
+    separate vertices (m_cpu_triangles order), its shading normals, and the
+    material fields its type uses. The camera's field of view is kept in
+    degrees as this library parses it, after checking that the reference's
+    radians are exactly its degToRad."""
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(HERE), "gpu-renderer_gb300"))
+    import gr
+    import refloader
+    from gr.scenes import MeshDesc, SceneDesc
+    r = refloader.load(xml_path)
+    parsed = gr.ParsedScene(xml_path)
+    fov = parsed.camera["fov"]
+    parsed.close()
+    if refloader.deg_to_rad(fov).view(np.uint32) != r["camera"][16:17].view(np.uint32)[0]:
+        raise RuntimeError("field of view differs from the reference loader's")
+    meshes, mats = [], []
+    for i in range(r["materials"].shape[0]):
+        sel = r["mesh"] == i
+        k = int(sel.sum())
+        nrm = r["normals"][sel].reshape(-1, 3)
+        meshes.append(MeshDesc(r["verts"][sel].reshape(-1, 3), np.arange(3 * k, dtype=np.uint32).reshape(k, 3), i,
+                               normals=None if np.isnan(nrm).any() else nrm))
+        f = refloader.material_fields(r["materials"][i])
+        if "color_map_size" in f:
+            raise ValueError("textured materials have no record form here")
+        m = {"type": int(f["type"]), "color": tuple(map(float, f["color"])), "emission": tuple(map(float, f["emission"])),
+             "alpha_u": 0.0, "alpha_v": 0.0, "eta_i": (0.0, 0.0, 0.0), "eta_t": (0.0, 0.0, 0.0), "k": (0.0, 0.0, 0.0),
+             "ior": 0.0, "specular": (0.0, 0.0, 0.0)}
+        if "ior" in f:
+            m["ior"] = float(f["ior"][0])
+        for key in ("eta_i", "eta_t", "k", "specular"):
+            if key in f:
+                m[key] = tuple(map(float, f[key]))
+        if "alpha" in f:
+            m["alpha_u"], m["alpha_v"] = float(f["alpha"][0]), float(f["alpha"][1])
+        mats.append(m)
+    cam = {"to_world": r["camera"][:16].reshape(4, 4).copy(), "fov": fov, "width": int(r["camera"][17]),
+           "height": int(r["camera"][18])}
+    env = tuple(map(float, r["env"][1:4])) if r["env"][0] else None
+    save_desc(SceneDesc(meshes, mats, cam, env), out_path)
 
 
 def save_desc(desc, path):

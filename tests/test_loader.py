@@ -3,6 +3,7 @@ the reference's CBox fixtures where the reference tree is present, and
 malformed input."""
 import ctypes
 import os
+import sys
 
 import numpy as np
 import pytest
@@ -10,7 +11,8 @@ import pytest
 import gr
 from gr import mitsuba, scenes as sc
 
-REF_CBOX = "/root/reference/scene/CBox"
+sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle"))
+import refsrc  # noqa: E402
 
 
 def test_exported_cornell_box_round_trip(tmp_path):
@@ -43,8 +45,8 @@ def test_exported_glossy_scene_round_trip(tmp_path):
 
 @pytest.mark.parametrize("name,tris", [("cbox.xml", None), ("cbox(mesh).xml", None), ("cbox(sphere).xml", None)])
 def test_reference_cbox_fixtures_parse(name, tris):
-    path = os.path.join(REF_CBOX, name)
-    if not os.path.exists(path):
+    path = refsrc.cbox_scenes().get(name)
+    if not path:
         pytest.skip("reference scenes not present")
     p = gr.ParsedScene(path)
     assert p.num_triangles > 0 and p.num_light_triangles >= 2
@@ -183,9 +185,10 @@ def test_scene_desc_file_round_trip(tmp_path):
 
 
 def test_reference_cbox_parses():
-    if not os.path.exists(REF_CBOX):
+    path = refsrc.cbox_scenes().get("cbox.xml")
+    if not path:
         pytest.skip("reference tree absent")
-    d = gr.ParsedScene(os.path.join(REF_CBOX, "cbox.xml")).scene_desc()
+    d = gr.ParsedScene(path).scene_desc()
     assert len(d.meshes) == 6 and sum(m.normals is not None for m in d.meshes) == 2
     kinds = sorted((gr.material_record(m).type, round(gr.material_record(m).ior, 3)) for m in d.materials)
     assert kinds.count((gr.MAT_DIELECTRIC, 100.0)) == 1 and kinds.count((gr.MAT_DIELECTRIC, 1.5)) == 1
