@@ -151,6 +151,7 @@ const char* gr_status_string(int st) {
         case GR_ERR_TIMEOUT: return "device wait timed out";
         case GR_ERR_OVERFLOW: return "device capacity exceeded";
         case GR_ERR_IO: return "file could not be written";
+        case GR_ERR_BUSY: return "server busy: job refused";
         default: return "unknown status";
     }
 }

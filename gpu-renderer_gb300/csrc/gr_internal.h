@@ -25,6 +25,12 @@ constexpr uint32_t kSpinLimit = 1u << 22;
 
 // Largest triangle count a BVH accepts: look-back words pack a 30-bit count.
 constexpr uint32_t kMaxTriangles = (1u << 30) - 1;
+// Largest image (width x height, counted in 64 bits): pixel indices and the
+// 4-byte per-pixel arrays stay within 32-bit offsets.
+constexpr uint64_t kMaxPixels = 0xFFFFFFFFull / 4;
+inline bool pixels_ok(uint32_t width, uint32_t height) {
+    return width != 0 && height != 0 && (uint64_t)width * height <= kMaxPixels;
+}
 
 // Traversal-node layout, 64 bytes (four 16-byte words):
 //   q0 = (c0.lo.x, c0.hi.x, c0.lo.y, c0.hi.y)

@@ -112,7 +112,7 @@ gr_status gr_scene_create(gr_ctx* ctx, const gr_mesh* meshes, uint32_t num_meshe
     if (!ctx || !out || !camera || (num_meshes && !meshes) || (num_materials && !materials))
         return fail(ctx, GR_ERR_INVALID, "gr_scene_create: null argument");
     *out = nullptr;
-    if (camera->width == 0 || camera->height == 0 || !(camera->fov_deg > 0.0f && camera->fov_deg < 180.0f))
+    if (!gr::pixels_ok(camera->width, camera->height) || !(camera->fov_deg > 0.0f && camera->fov_deg < 180.0f))
         return fail(ctx, GR_ERR_INVALID, "gr_scene_create: bad camera");
     uint64_t ntri = 0;
     bool any_normals = false, any_uvs = false;

@@ -7,6 +7,7 @@
 // scene, pixel and sample, and each job's pixels are resolved in sample order,
 // a job's image is identical whatever else shares its waves.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -217,6 +218,8 @@ struct Job {
     void* h_res = nullptr;  // pinned: sums then counts
     size_t dev_bytes = 0, host_bytes = 0;
     cudaEvent_t done_ev = nullptr;
+    uint32_t waves = 0;
+    uint64_t first_wave = 0, last_wave = 0;
     bool scheduled_all = false;
     bool finished = false;
     std::vector<float> image;
@@ -241,6 +244,9 @@ struct gr_server {
     std::unordered_map<uint64_t, std::shared_ptr<Job>> all;
     std::unordered_map<gr_scene*, int> scene_refs;
     uint64_t bytes_in_use = 0;
+    double busy_since = -1.0;       // server clock when the current busy period began (-1: idle)
+    uint64_t paths_retired = 0;     // paths of completed jobs (throughput estimate)
+    std::atomic<uint32_t> inject_wave_failures{0};
     gr_server_stats stats{};
     std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
     std::string error;
@@ -249,10 +255,42 @@ struct gr_server {
 
     uint64_t job_bytes(const Job& j) const { return (uint64_t)j.hj.npix * (24 + 4); }
 
+    // Paths (pixels x samples) a job has not yet scheduled.
+    static uint64_t remaining(const Job& j) { return (uint64_t)(j.hj.spp_total - j.hj.spp_done) * j.hj.npix; }
+
+    // GR_SERVER_SHORTEST_FIRST order: jobs older than the age cap first (oldest
+    // first), then the least remaining work first (ties by arrival). Returns
+    // true when a goes before b.
+    bool before(const Job& a, const Job& b, double t) const {
+        const bool aged_a = opts.age_cap_s > 0 && t - a.st.submit_s > opts.age_cap_s;
+        const bool aged_b = opts.age_cap_s > 0 && t - b.st.submit_s > opts.age_cap_s;
+        if (aged_a != aged_b) return aged_a;
+        if (aged_a) return a.ticket < b.ticket;
+        const uint64_t ra = remaining(a), rb = remaining(b);
+        return ra != rb ? ra < rb : a.ticket < b.ticket;
+    }
+
+    // Measured throughput (paths per second of busy time) and the paths queued
+    // or running, for load shedding (with mu held).
+    double busy_seconds() const { return stats.busy_s + (busy_since >= 0 ? now() - busy_since : 0.0); }
+    uint64_t queued_paths() const {
+        uint64_t q = 0;
+        for (const auto& j : pending) q += remaining(*j);
+        for (const auto& j : active) q += remaining(*j);
+        return q;
+    }
+
     // Admission under the budget (called with mu held).
     void admit() {
         const uint32_t max_active = opts.max_active ? opts.max_active : gr::kMaxJobs;
         while (!pending.empty() && active.size() < max_active) {
+            if (opts.policy == GR_SERVER_SHORTEST_FIRST) {  // the next job to admit goes to the front
+                const double t = now();
+                auto best = pending.begin();
+                for (auto it = pending.begin() + 1; it != pending.end(); ++it)
+                    if (before(**it, **best, t)) best = it;
+                if (best != pending.begin()) std::iter_swap(pending.begin(), best);
+            }
             Job& j = *pending.front();
             uint64_t need = job_bytes(j);
             if (!scene_refs.count(j.scene)) need += gr_scene_device_bytes(j.scene);
@@ -274,10 +312,25 @@ struct gr_server {
             j.d_sum = (double*)d;
             j.d_cnt = (uint32_t*)(d + 24ull * j.hj.npix);
             j.h_res = h;
-            cudaMemsetAsync(d, 0, j.dev_bytes, stream);
             j.hj.fb = j.d_sum;
             j.hj.fbc = j.d_cnt;
-            cudaEventCreateWithFlags(&j.done_ev, cudaEventDisableTiming);
+            e = cudaMemsetAsync(d, 0, j.dev_bytes, stream);
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&j.done_ev, cudaEventDisableTiming);
+            if (e != cudaSuccess) {  // the job fails; nothing of it is in flight
+                cudaGetLastError();
+                cache.put_dev(j.dev_bytes, d);
+                cache.put_host(j.host_bytes, h);
+                j.d_sum = nullptr;
+                j.h_res = nullptr;
+                j.done_ev = nullptr;
+                error = cudaGetErrorString(e);
+                j.st.status = cuda_status(e);
+                j.finished = true;
+                j.st.done_s = now();
+                pending.pop_front();
+                cv_done.notify_all();
+                continue;
+            }
             j.st.admit_s = now();
             scene_refs[j.scene]++;
             bytes_in_use += need;
@@ -301,12 +354,28 @@ struct gr_server {
         j.done_ev = nullptr;
     }
 
+    // Ends an active job with an error status (with mu held): its buffers go
+    // back to the free lists (later work on the server's stream is ordered
+    // after anything still queued for it) and its waiters are woken.
+    void fail_active(const std::shared_ptr<Job>& j, gr_status st) {
+        if (j->finished) return;
+        j->st.status = st;
+        j->st.done_s = now();
+        j->finished = true;
+        release_job(*j);
+        auto it = std::find(active.begin(), active.end(), j);
+        if (it != active.end()) active.erase(it);
+        cv_done.notify_all();
+    }
+
     void run() {
         cudaSetDevice(ctx->device);
         std::vector<gr::JobDev> table;
-        double busy_since = -1.0;
         for (;;) {
             std::vector<std::shared_ptr<Job>> act;
+            std::vector<Job*> order;
+            std::vector<uint32_t> done_before;
+            uint32_t nj = 0, paths = 0, pix = 0, depth = 0;
             {
                 std::unique_lock<std::mutex> lk(mu);
                 admit();
@@ -321,38 +390,65 @@ struct gr_server {
                 }
                 if (busy_since < 0) busy_since = now();
                 act = active;
+                // pack one wave over the active jobs that still need samples, in
+                // the policy's order (under the lock: submit reads the progress)
+                for (auto& j : act)
+                    if (!j->scheduled_all) order.push_back(j.get());
+                if (opts.policy == GR_SERVER_SHORTEST_FIRST) {
+                    const double t = now();
+                    std::stable_sort(order.begin(), order.end(),
+                                     [&](const Job* a, const Job* b) { return before(*a, *b, t); });
+                }
+                std::vector<gr::HostJob*> hjs;
+                for (Job* j : order) {
+                    hjs.push_back(&j->hj);
+                    done_before.push_back(j->hj.spp_done);
+                }
+                if (!hjs.empty()) nj = gr::pack_wave(hjs, pool.capacity, table, &paths, &pix, &depth);
             }
-            // schedule one wave over the active jobs that still need samples
-            std::vector<gr::HostJob*> hjs;
-            for (auto& j : act)
-                if (!j->scheduled_all) hjs.push_back(&j->hj);
-            if (!hjs.empty()) {
-                uint32_t paths = 0, pix = 0, depth = 0;
-                const uint32_t nj = gr::pack_wave(hjs, pool.capacity, table, &paths, &pix, &depth);
+            if (!order.empty()) {
                 if (nj) {
                     gr::TraceTuning tune;
                     tune.layout = opts.layout;
                     tune.block = opts.block;
                     tune.sstack = opts.short_stack;
-                    const cudaError_t e = gr::run_wave(pool, table.data(), nj, paths, pix, depth, ctx->num_sms, stream,
-                                                       true, tune);
-                    if (e != cudaSuccess) {
-                        std::lock_guard<std::mutex> lk(mu);
-                        error = cudaGetErrorString(e);
-                        for (auto& j : act) {
-                            j->st.status = cuda_status(e);
-                        }
+                    cudaError_t e;
+                    if (inject_wave_failures.load() > 0) {  // host-side fault injection (gr_diag_server_fail_waves)
+                        inject_wave_failures.fetch_sub(1);
+                        e = cudaErrorLaunchFailure;
+                    } else {
+                        e = gr::run_wave(pool, table.data(), nj, paths, pix, depth, ctx->num_sms, stream, true, tune);
                     }
                     std::lock_guard<std::mutex> lk(mu);
+                    if (e != cudaSuccess) {
+                        // every job in flight fails: its samples cannot be completed
+                        cudaGetLastError();
+                        error = cudaGetErrorString(e);
+                        for (auto& j : act) fail_active(j, cuda_status(e));
+                        continue;
+                    }
                     stats.waves++;
+                    for (size_t k = 0; k < order.size(); ++k) {  // the jobs this wave carried
+                        if (order[k]->hj.spp_done == done_before[k]) continue;
+                        Job& j = *order[k];
+                        if (!j.first_wave) j.first_wave = stats.waves;
+                        j.last_wave = stats.waves;
+                        j.waves++;
+                    }
                 }
                 // jobs whose last samples went into this wave: copy out after it
                 for (auto& j : act) {
                     if (j->scheduled_all || j->hj.spp_done < j->hj.spp_total) continue;
                     j->scheduled_all = true;
                     const size_t npix = j->hj.npix;
-                    cudaMemcpyAsync(j->h_res, j->d_sum, 28 * npix, cudaMemcpyDeviceToHost, stream);
-                    cudaEventRecord(j->done_ev, stream);
+                    cudaError_t ce = cudaMemcpyAsync(j->h_res, j->d_sum, 28 * npix, cudaMemcpyDeviceToHost, stream);
+                    if (ce == cudaSuccess) ce = cudaEventRecord(j->done_ev, stream);
+                    if (ce != cudaSuccess) {
+                        cudaGetLastError();
+                        std::lock_guard<std::mutex> lk(mu);
+                        error = cudaGetErrorString(ce);
+                        fail_active(j, cuda_status(ce));
+                    }
                 }
             } else {
                 std::this_thread::sleep_for(std::chrono::microseconds(50));
@@ -360,7 +456,15 @@ struct gr_server {
             // retire finished jobs
             for (auto& j : act) {
                 if (!j->scheduled_all || j->finished) continue;
-                if (cudaEventQuery(j->done_ev) != cudaSuccess) continue;
+                const cudaError_t q = cudaEventQuery(j->done_ev);
+                if (q == cudaErrorNotReady) continue;
+                if (q != cudaSuccess) {  // an error, not completion: the job fails instead of waiting forever
+                    cudaGetLastError();
+                    std::lock_guard<std::mutex> lk(mu);
+                    error = cudaGetErrorString(q);
+                    fail_active(j, cuda_status(q));
+                    continue;
+                }
                 const uint32_t npix = j->hj.npix;
                 j->image.resize(3ull * npix);
                 const double* sum = (const double*)j->h_res;
@@ -369,6 +473,7 @@ struct gr_server {
                 std::lock_guard<std::mutex> lk(mu);
                 j->st.done_s = now();
                 j->st.samples = (uint64_t)j->hj.spp_total * npix;
+                paths_retired += j->st.samples;
                 j->finished = true;
                 release_job(*j);
                 active.erase(std::find(active.begin(), active.end(), j));
@@ -397,6 +502,12 @@ gr_status gr_server_create(gr_ctx* ctx, const gr_server_opts* opts, gr_server** 
     tt.sstack = sv->opts.short_stack;
     if (!gr::tuning_valid(tt)) {
         ctx->last_error = "gr_server_create: unsupported layout / block / short_stack";
+        delete sv;
+        return GR_ERR_INVALID;
+    }
+    if ((sv->opts.policy != GR_SERVER_FIFO && sv->opts.policy != GR_SERVER_SHORTEST_FIRST) ||
+        !(sv->opts.age_cap_s >= 0) || !(sv->opts.max_wait_s >= 0)) {
+        ctx->last_error = "gr_server_create: unknown policy or negative age cap / wait limit";
         delete sv;
         return GR_ERR_INVALID;
     }
@@ -442,6 +553,12 @@ gr_status gr_server_destroy(gr_server* sv) {
 
 double gr_server_now(const gr_server* sv) { return sv ? sv->now() : 0.0; }
 
+gr_status gr_diag_server_fail_waves(gr_server* sv, uint32_t count) {
+    if (!sv) return GR_ERR_INVALID;
+    sv->inject_wave_failures.store(count);
+    return GR_OK;
+}
+
 gr_status gr_server_submit(gr_server* sv, gr_scene* scene, const gr_camera* camera, const gr_render_opts* opts,
                            uint64_t* ticket) {
     if (!sv || !scene || !opts || !ticket || scene->ctx != sv->ctx) return GR_ERR_INVALID;
@@ -453,12 +570,13 @@ gr_status gr_server_submit(gr_server* sv, gr_scene* scene, const gr_camera* came
     }
     gr::SceneDev view = gr::scene_view(scene, sv->opts.layout);
     if (camera) {
-        if (camera->width == 0 || camera->height == 0 || !(camera->fov_deg > 0.0f && camera->fov_deg < 180.0f))
+        if (!gr::pixels_ok(camera->width, camera->height) || !(camera->fov_deg > 0.0f && camera->fov_deg < 180.0f))
             return GR_ERR_INVALID;
         view.cam = gr::make_camera(*camera);
     }
-    const uint32_t npix = view.cam.width * view.cam.height;
-    if (npix > sv->pool.capacity) return GR_ERR_INVALID;
+    const uint64_t npix64 = (uint64_t)view.cam.width * view.cam.height;
+    if (npix64 > sv->pool.capacity) return GR_ERR_INVALID;  // a job's pixels must fit one wave
+    const uint32_t npix = (uint32_t)npix64;
     auto j = std::make_shared<Job>();
     j->scene = scene;
     j->opts = *opts;
@@ -473,6 +591,17 @@ gr_status gr_server_submit(gr_server* sv, gr_scene* scene, const gr_camera* came
     j->hj.seed = opts->seed;
     {
         std::lock_guard<std::mutex> lk(sv->mu);
+        if (sv->opts.max_wait_s > 0) {  // load shedding at the measured throughput
+            const double busy = sv->busy_seconds();
+            if (sv->paths_retired > 0 && busy > 0) {
+                const double rate = (double)sv->paths_retired / busy;
+                const double wait = (double)(sv->queued_paths() + (uint64_t)npix * opts->spp) / rate;
+                if (wait > sv->opts.max_wait_s) {
+                    sv->stats.rejected++;
+                    return GR_ERR_BUSY;
+                }
+            }
+        }
         j->ticket = sv->next_ticket++;
         j->st.submit_s = sv->now();
         sv->pending.push_back(j);
@@ -495,6 +624,9 @@ gr_status gr_server_wait(gr_server* sv, uint64_t ticket, double timeout_s, int* 
     if (timeout_s < 0) sv->cv_done.wait(lk, pred);
     else sv->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), pred);
     if (done) *done = j->finished ? 1 : 0;
+    j->st.waves = j->waves;
+    j->st.first_wave = j->first_wave;
+    j->st.last_wave = j->last_wave;
     if (stats) *stats = j->st;
     if (j->finished && h_rgb && !j->image.empty()) std::memcpy(h_rgb, j->image.data(), j->image.size() * 4);
     if (j->finished) {

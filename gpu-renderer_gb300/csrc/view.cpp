@@ -75,7 +75,7 @@ gr_status gr_scene_get_camera(const gr_scene* sc, gr_camera* out) {
 gr_status gr_scene_set_camera(gr_scene* sc, const gr_camera* cam) {
     if (!sc || !cam) return GR_ERR_INVALID;
     gr_ctx* ctx = sc->ctx;
-    if (cam->width == 0 || cam->height == 0 || (uint64_t)cam->width * cam->height > 0xFFFFFFFFull / 4)
+    if (!gr::pixels_ok(cam->width, cam->height))
         return view_fail(ctx, GR_ERR_INVALID, "gr_scene_set_camera: bad resolution");
     if (!(cam->fov_deg > 0.0f && cam->fov_deg < 180.0f))
         return view_fail(ctx, GR_ERR_INVALID, "gr_scene_set_camera: field of view outside (0, 180) degrees");

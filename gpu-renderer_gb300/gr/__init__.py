@@ -18,8 +18,10 @@ LAYOUT_BVH2, LAYOUT_BVH4, LAYOUT_BVH4_Q8, LAYOUT_BVH8_Q8 = 0, 1, 2, 3
 LAYOUT_NAMES = {0: "bvh2", 1: "bvh4", 2: "bvh4_q8", 3: "bvh8_q8"}
 STATUS = {
     0: "GR_OK", 1: "GR_ERR_INVALID", 2: "GR_ERR_CUDA", 3: "GR_ERR_OOM_BUDGET",
-    4: "GR_ERR_PARSE", 5: "GR_ERR_TIMEOUT", 6: "GR_ERR_OVERFLOW", 7: "GR_ERR_IO",
+    4: "GR_ERR_PARSE", 5: "GR_ERR_TIMEOUT", 6: "GR_ERR_OVERFLOW", 7: "GR_ERR_IO", 8: "GR_ERR_BUSY",
 }
+GR_ERR_CUDA, GR_ERR_BUSY = 2, 8
+SERVER_FIFO, SERVER_SHORTEST_FIRST = 0, 1
 
 RAY_DTYPE = np.dtype([("o", "<f4", 3), ("d", "<f4", 3), ("tmin", "<f4"), ("tmax", "<f4")])
 HIT_DTYPE = np.dtype([("t", "<f4"), ("prim", "<i4"), ("u", "<f4"), ("v", "<f4")])
@@ -565,18 +567,21 @@ class PathTracer:
 
 class ServerOpts(ctypes.Structure):
     _fields_ = [("budget_bytes", ctypes.c_uint64), ("wave_paths", ctypes.c_uint32), ("max_active", ctypes.c_uint32),
-                ("layout", ctypes.c_int32), ("block", ctypes.c_int32), ("short_stack", ctypes.c_int32)]
+                ("layout", ctypes.c_int32), ("block", ctypes.c_int32), ("short_stack", ctypes.c_int32),
+                ("policy", ctypes.c_int32), ("age_cap_s", ctypes.c_double), ("max_wait_s", ctypes.c_double)]
 
 
 class JobStats(ctypes.Structure):
     _fields_ = [("submit_s", ctypes.c_double), ("admit_s", ctypes.c_double), ("done_s", ctypes.c_double),
-                ("samples", ctypes.c_uint64), ("status", ctypes.c_int32)]
+                ("samples", ctypes.c_uint64), ("status", ctypes.c_int32), ("waves", ctypes.c_uint32),
+                ("first_wave", ctypes.c_uint64), ("last_wave", ctypes.c_uint64)]
 
 
 class ServerStats(ctypes.Structure):
     _fields_ = [("submitted", ctypes.c_uint64), ("admitted", ctypes.c_uint64), ("completed", ctypes.c_uint64),
                 ("waves", ctypes.c_uint64), ("closest_rays", ctypes.c_uint64), ("shadow_rays", ctypes.c_uint64),
-                ("bytes_in_use", ctypes.c_uint64), ("peak_bytes", ctypes.c_uint64), ("busy_s", ctypes.c_double)]
+                ("bytes_in_use", ctypes.c_uint64), ("peak_bytes", ctypes.c_uint64), ("busy_s", ctypes.c_double),
+                ("rejected", ctypes.c_uint64)]
 
 
 _SERVER_SIGS = {
@@ -591,6 +596,7 @@ _SERVER_SIGS = {
                        ctypes.c_int),
     "gr_server_now": ([_P], ctypes.c_double),
     "gr_server_stats_get": ([_P, ctypes.POINTER(ServerStats)], ctypes.c_int),
+    "gr_diag_server_fail_waves": ([_P, ctypes.c_uint32], ctypes.c_int),
 }
 
 
@@ -621,10 +627,11 @@ def render_batch(ctx, scenes, opts, wave_paths=0):
 class Server:
     """Continuous-batching render server (gr_server)."""
 
-    def __init__(self, ctx, budget_bytes=0, wave_paths=0, max_active=0, layout=LAYOUT_BVH2, block=0, short_stack=0):
+    def __init__(self, ctx, budget_bytes=0, wave_paths=0, max_active=0, layout=LAYOUT_BVH2, block=0, short_stack=0,
+                 policy=SERVER_FIFO, age_cap_s=0.0, max_wait_s=0.0):
         L = _declare(_SERVER_SIGS)
         self.ctx = ctx
-        o = ServerOpts(budget_bytes, wave_paths, max_active, layout, block, short_stack)
+        o = ServerOpts(budget_bytes, wave_paths, max_active, layout, block, short_stack, policy, age_cap_s, max_wait_s)
         h = _P()
         ctx.check(L.gr_server_create(ctx.h, ctypes.byref(o), ctypes.byref(h)), "gr_server_create")
         self.h = h
@@ -659,6 +666,11 @@ class Server:
 
     def now(self):
         return _declare(_SERVER_SIGS).gr_server_now(self.h)
+
+    def fail_waves(self, count):
+        """Host-side fault injection: the next `count` waves report a failed
+        launch without running (gr_diag_server_fail_waves)."""
+        self.ctx.check(_declare(_SERVER_SIGS).gr_diag_server_fail_waves(self.h, count), "gr_diag_server_fail_waves")
 
     def stats(self):
         s = ServerStats()

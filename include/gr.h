@@ -33,7 +33,8 @@ typedef enum gr_status {
     GR_ERR_PARSE = 4,       /* scene file could not be parsed */
     GR_ERR_TIMEOUT = 5,     /* a bounded device-side wait gave up */
     GR_ERR_OVERFLOW = 6,    /* a device-side capacity (stack, queue) was exceeded */
-    GR_ERR_IO = 7           /* a file could not be written */
+    GR_ERR_IO = 7,          /* a file could not be written */
+    GR_ERR_BUSY = 8         /* the render server refused a job it could not start in time (load shedding) */
 } gr_status;
 
 /* Ray and hit records, byte-compatible with the reference's Ray and Hit
@@ -464,19 +465,33 @@ typedef struct gr_server_opts {
     int32_t layout;        /* node layout of every job (GR_LAYOUT_*); set on the scenes at submit */
     int32_t block;         /* traversal threads per block (0 = 128; see gr_trace_tuning) */
     int32_t short_stack;   /* shared-memory stack entries per thread (0 = 12) */
+    int32_t policy;        /* order in which jobs are admitted and packed into waves (GR_SERVER_*) */
+    double age_cap_s;      /* GR_SERVER_SHORTEST_FIRST: a job submitted longer ago than this goes ahead of
+                              shorter ones, oldest first (0 = no cap) */
+    double max_wait_s;     /* load shedding: gr_server_submit refuses a job with GR_ERR_BUSY when the work
+                              queued ahead of it plus its own, at the throughput measured so far, would take
+                              longer than this (0 = accept everything) */
 } gr_server_opts;
+
+/* Job order of a server: first come first served, or the job with the least
+ * remaining work (pixels x samples left) first, with the age cap above. */
+#define GR_SERVER_FIFO 0
+#define GR_SERVER_SHORTEST_FIRST 1
 
 typedef struct gr_job_stats {
     double submit_s, admit_s, done_s; /* seconds on the server's clock */
     uint64_t samples;
     int32_t status;                   /* gr_status of the job */
+    uint32_t waves;                   /* waves the job's samples ran in */
+    uint64_t first_wave, last_wave;   /* the server's wave numbers (1, 2, ...) of its first and last wave */
 } gr_job_stats;
 
 typedef struct gr_server_stats {
     uint64_t submitted, admitted, completed, waves;
     uint64_t closest_rays, shadow_rays;
     uint64_t bytes_in_use, peak_bytes;
-    double busy_s; /* time with at least one job in flight */
+    double busy_s;      /* time with at least one job in flight */
+    uint64_t rejected;  /* jobs refused with GR_ERR_BUSY */
 } gr_server_stats;
 
 gr_status gr_server_create(gr_ctx* ctx, const gr_server_opts* opts, gr_server** out);
@@ -500,6 +515,13 @@ gr_status gr_server_poll(gr_server* server, uint64_t ticket, int* done, float* h
 /* Seconds on the server's clock (the clock of gr_job_stats). */
 double gr_server_now(const gr_server* server);
 gr_status gr_server_stats_get(gr_server* server, gr_server_stats* out);
+
+/* Host-side fault injection for the render server (no counterpart in the
+ * reference): the server's next `count` waves report a failed launch instead
+ * of running (nothing reaches the GPU). Every job in flight then ends with
+ * GR_ERR_CUDA, as after a real launch failure; later jobs run normally. This
+ * exercises the server's error path: waiters and gr_server_destroy return. */
+gr_status gr_diag_server_fail_waves(gr_server* server, uint32_t count);
 
 #ifdef __cplusplus
 }
