@@ -5,7 +5,8 @@
 // src/renderer/sampling.h, bsdf.h, bsdfs/*.h, triangle.h), which itself follows
 // pbrt-v3; names and argument meaning are kept so the two can be read side by
 // side. Compiled with --fmad=false so each operation rounds as written, as the
-// host oracle does.
+// host oracle does (with contraction, chains of refractions turn last-bit
+// differences into different paths).
 #pragma once
 
 #include <stdint.h>

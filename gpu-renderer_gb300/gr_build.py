@@ -21,7 +21,11 @@ INCLUDES = ["-I", os.path.join(ROOT, "include"), "-I", CSRC]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"] + ARCH
 # The integrator's shading math rounds every operation as written (no FMA
 # contraction), like the host oracle it is compared with; traversal code uses
-# explicit round-to-nearest intrinsics everywhere and is unaffected.
+# explicit round-to-nearest intrinsics everywhere and is unaffected. Measured
+# on GB300: contraction made the glossy 1024x768 render 0.3 % faster, but
+# scenes of dielectrics then left the oracle's image by 4.5-7.6 % mean relative
+# error (a refraction chain turns a last-bit difference into another path),
+# against a 1e-3 bar.
 PER_FILE_FLAGS = {"render.cu": ["--fmad=false"]}
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-Wextra", "-Wno-unused-parameter",
              "-I", os.path.join(CUDA_HOME, "include")]
