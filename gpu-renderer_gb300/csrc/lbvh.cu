@@ -9,6 +9,8 @@
 #include <algorithm>
 #include <mutex>
 
+#include <cuda.h>  // CUcontext / CUresult: the driver entry points are reached through the runtime
+
 #include "gr_internal.h"
 
 namespace gr {
@@ -703,6 +705,53 @@ cudaError_t lookback_probe(uint32_t polls, uint32_t* h_err, cudaStream_t s) {
     return e;
 }
 
+namespace {
+
+// The build's launch sequence over laid-out scratch `s` (scratch_layout): the
+// one both the allocating build and the no-allocation build run. Zeroes the
+// scratch region that must start at zero, then centroid bounds, Morton codes
+// and histograms, four onesweep passes (the sorted codes and triangle ids end
+// in `code` / `prim`), equal-code runs, Karras splits, links, run subtrees and
+// the refit, and folds the build's error word into the header.
+cudaError_t launch_build(const float* d_verts, uint32_t n, const Scratch& s, Node* nodes, Tri* tris, uint32_t* code,
+                         uint32_t* prim, BvhMeta* meta, int num_sms, cudaStream_t st) {
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(s.zero_base, 0, s.zero_bytes, st)) != cudaSuccess) return e;
+    const int grid = (int)std::min<uint64_t>(((uint64_t)n + kBlock - 1) / kBlock, (uint64_t)num_sms * 8);
+    const int parts = std::min(grid, kPartials);
+    k_centroid_partials<<<parts, kBlock, 0, st>>>(d_verts, n, s.partial);
+    k_centroid_final<<<1, kBlock, 0, st>>>(s.partial, parts, meta);
+    k_morton_hist<<<std::min(grid, num_sms * 2), kBlock, 0, st>>>(d_verts, n, meta, code, prim, s.hist);
+    k_hist_scan<<<4, 256, 0, st>>>(s.hist, s.offs);
+    if ((e = cudaFuncSetAttribute(k_onesweep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kOsSmem)) !=
+        cudaSuccess)
+        return e;
+    const uint32_t os_tiles = (n + kOsTile - 1) / kOsTile;
+    uint32_t* kin = code;
+    uint32_t* vin = prim;
+    uint32_t* kout = s.keys_alt;
+    uint32_t* vout = s.vals_alt;
+    for (int pass = 0; pass < 4; ++pass) {
+        k_onesweep<<<os_tiles, kOsThreads, kOsSmem, st>>>(kin, vin, kout, vout, n, pass, s.offs,
+                                                          s.os_status + (size_t)pass * os_tiles * 256, s.tile_ctr, s.err);
+        std::swap(kin, kout);
+        std::swap(vin, vout);
+    }
+    // four passes: the sorted data is back in code/prim
+    const uint32_t run_tiles = (n + kRunTile - 1) / kRunTile;
+    k_runs<<<run_tiles, kRunThreads, 0, st>>>(code, n, s.ucode, s.run_start, s.uidx, s.run_status, s.tile_ctr + 4,
+                                              meta, s.err);
+    k_karras<<<grid, kBlock, 0, st>>>(s.ucode, s.run_start, meta, s.kgamma, s.gap_of);
+    k_link<<<grid, kBlock, 0, st>>>(s.kgamma, s.gap_of, s.run_start, meta, nodes, s.parent_leaf);
+    k_run_nodes<<<grid, kBlock, 0, st>>>(code, n, s.uidx, s.run_start, meta, nodes, s.parent_leaf, s.err);
+    k_refit<<<grid, kBlock, 0, st>>>(d_verts, n, prim, s.parent_leaf, nodes, tris, s.counters, s.err);
+    // fold the build's error word into the header the host reads
+    if ((e = cudaMemcpyAsync(&meta->err, s.err, 4, cudaMemcpyDeviceToDevice, st)) != cudaSuccess) return e;
+    return cudaGetLastError();
+}
+
+}  // namespace
+
 cudaError_t lbvh_build(BvhBuffers& b, const float* d_verts, uint32_t n, int num_sms, cudaStream_t st) {
     cudaError_t e;
     if ((e = b.meta.ensure(sizeof(BvhMeta))) != cudaSuccess) return e;
@@ -721,44 +770,8 @@ cudaError_t lbvh_build(BvhBuffers& b, const float* d_verts, uint32_t n, int num_
     const size_t need = scratch_layout(n, nullptr, &s);
     if ((e = b.scratch.ensure(need)) != cudaSuccess) return e;
     scratch_layout(n, (char*)b.scratch.p, &s);
-    if ((e = cudaMemsetAsync(s.zero_base, 0, s.zero_bytes, st)) != cudaSuccess) return e;
-    Node* nodes = (Node*)b.nodes.p;
-    uint32_t* code = (uint32_t*)b.code.p;
-    uint32_t* prim = (uint32_t*)b.prim.p;
-
-    const int grid = (int)std::min<uint64_t>(((uint64_t)n + kBlock - 1) / kBlock, (uint64_t)num_sms * 8);
-    const int parts = std::min(grid, kPartials);
-    k_centroid_partials<<<parts, kBlock, 0, st>>>(d_verts, n, s.partial);
-    k_centroid_final<<<1, kBlock, 0, st>>>(s.partial, parts, meta);
-    k_morton_hist<<<std::min(grid, num_sms * 2), kBlock, 0, st>>>(d_verts, n, meta, code, prim, s.hist);
-    k_hist_scan<<<4, 256, 0, st>>>(s.hist, s.offs);
-
-    if ((e = cudaFuncSetAttribute(k_onesweep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kOsSmem)) !=
-        cudaSuccess)
-        return e;
-    const uint32_t os_tiles = (n + kOsTile - 1) / kOsTile;
-    uint32_t* kin = code;
-    uint32_t* vin = prim;
-    uint32_t* kout = s.keys_alt;
-    uint32_t* vout = s.vals_alt;
-    for (int pass = 0; pass < 4; ++pass) {
-        k_onesweep<<<os_tiles, kOsThreads, kOsSmem, st>>>(kin, vin, kout, vout, n, pass, s.offs,
-                                                          s.os_status + (size_t)pass * os_tiles * 256, s.tile_ctr, s.err);
-        std::swap(kin, kout);
-        std::swap(vin, vout);
-    }
-    // four passes: the sorted data is back in code/prim
-
-    const uint32_t run_tiles = (n + kRunTile - 1) / kRunTile;
-    k_runs<<<run_tiles, kRunThreads, 0, st>>>(code, n, s.ucode, s.run_start, s.uidx, s.run_status, s.tile_ctr + 4,
-                                              meta, s.err);
-    k_karras<<<grid, kBlock, 0, st>>>(s.ucode, s.run_start, meta, s.kgamma, s.gap_of);
-    k_link<<<grid, kBlock, 0, st>>>(s.kgamma, s.gap_of, s.run_start, meta, nodes, s.parent_leaf);
-    k_run_nodes<<<grid, kBlock, 0, st>>>(code, n, s.uidx, s.run_start, meta, nodes, s.parent_leaf, s.err);
-    k_refit<<<grid, kBlock, 0, st>>>(d_verts, n, prim, s.parent_leaf, nodes, (Tri*)b.tris.p, s.counters, s.err);
-    // fold the build's error word into the header the host reads
-    if ((e = cudaMemcpyAsync(&meta->err, s.err, 4, cudaMemcpyDeviceToDevice, st)) != cudaSuccess) return e;
-    return cudaGetLastError();
+    return launch_build(d_verts, n, s, (Node*)b.nodes.p, (Tri*)b.tris.p, (uint32_t*)b.code.p, (uint32_t*)b.prim.p,
+                        meta, num_sms, st);
 }
 
 cudaError_t lbvh_export_ref(const BvhBuffers& b, uint32_t n, uint32_t* d_ref_nodes, cudaStream_t st) {
@@ -774,11 +787,11 @@ cudaError_t lbvh_export_ref(const BvhBuffers& b, uint32_t n, uint32_t* d_ref_nod
 }  // namespace gr
 
 // ---- build without allocation ------------------------------------------------------
-// Some callers cannot call cudaMalloc: code that runs while a stream is being
-// captured into a CUDA graph, plug-ins whose host application owns every byte
-// of device memory, and latency-critical loops where cudaMalloc / cudaFree
-// would synchronise the device. For them the build's scratch (sort buffers,
-// run arrays, parent links, refit counters, look-back words) lives in one
+// Some callers cannot call cudaMalloc: plug-ins whose host application owns
+// every byte of device memory (and hands the plug-in only the buffers of a
+// call), and latency-critical loops in which a cudaMalloc / cudaFree would
+// synchronise the device. For them the build's scratch (sort buffers, run
+// arrays, parent links, refit counters, look-back words) lives in one
 // file-scope device array, sized for kStaticMaxTriangles triangles; the caller
 // passes the input soup and every output buffer.
 //
@@ -806,23 +819,61 @@ constexpr size_t kStaticScratchBytes =
 
 static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
 
+// Identity of the calling thread's current CUDA context (cuCtxGetCurrent +
+// cuCtxGetId, reached through the runtime's driver entry points so the library
+// does not link the driver library). A context's id is unique for the life of
+// the process, so a device whose primary context was destroyed and created
+// again (cudaDeviceReset) shows a new id.
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+
+cudaError_t current_context_id(unsigned long long* id) {
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    if (!get_current || !get_id) {
+        void* a = nullptr;
+        void* b = nullptr;
+        cudaDriverEntryPointQueryResult qa = cudaDriverEntryPointSymbolNotFound, qb = qa;
+        cudaError_t e = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 12000, cudaEnableDefault, &qa);
+        if (e == cudaSuccess) e = cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &qb);
+        if (e != cudaSuccess) return e;
+        if (qa != cudaDriverEntryPointSuccess || qb != cudaDriverEntryPointSuccess || !a || !b)
+            return cudaErrorNotSupported;
+        get_current = reinterpret_cast<CtxGetCurrentFn>(a);
+        get_id = reinterpret_cast<CtxGetIdFn>(b);
+    }
+    CUcontext c = nullptr;
+    if (get_current(&c) != CUDA_SUCCESS || !c) return cudaErrorDeviceUninitialized;
+    if (get_id(c, id) != CUDA_SUCCESS) return cudaErrorDeviceUninitialized;
+    return cudaSuccess;
+}
+
 constexpr int kMaxDevices = 64;
 std::mutex g_static_mu;
-void* g_static_ptr[kMaxDevices] = {};
+struct StaticScratch {
+    unsigned long long ctx_id = 0;
+    void* ptr = nullptr;
+};
+StaticScratch g_static[kMaxDevices];
 
-// Device address of g_static_scratch on the current device. The array's name
-// in host code is only a host-side stand-in, so the address is looked up once
-// per device (with that device current) and cached.
+// Device address of g_static_scratch on the current device (the caller has
+// made `device` current). The array's name in host code is only a host-side
+// stand-in, so its address is looked up with cudaGetSymbolAddress once per
+// device at set-up, and again only if the device's context changed since.
 cudaError_t static_scratch(int device, void** out) {
     if (device < 0 || device >= kMaxDevices) return cudaErrorInvalidDevice;
     std::lock_guard<std::mutex> lock(g_static_mu);
-    if (!g_static_ptr[device]) {
+    unsigned long long id = 0;
+    cudaError_t e = current_context_id(&id);
+    if (e != cudaSuccess) return e;
+    StaticScratch& c = g_static[device];
+    if (!c.ptr || c.ctx_id != id) {
         void* p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
-        if (e != cudaSuccess) return e;
-        g_static_ptr[device] = p;
+        if ((e = cudaGetSymbolAddress(&p, g_static_scratch)) != cudaSuccess) return e;
+        c.ptr = p;
+        c.ctx_id = id;
     }
-    *out = g_static_ptr[device];
+    *out = c.ptr;
     return cudaSuccess;
 }
 
@@ -840,37 +891,7 @@ cudaError_t lbvh_build_static(const float* d_verts, uint32_t n, Node* nodes, Tri
     Scratch s;
     if (scratch_layout(n, nullptr, &s) > kStaticScratchBytes) return cudaErrorInvalidValue;
     scratch_layout(n, (char*)base, &s);
-    if ((e = cudaMemsetAsync(s.zero_base, 0, s.zero_bytes, st)) != cudaSuccess) return e;
-
-    const int grid = (int)std::min<uint64_t>(((uint64_t)n + kBlock - 1) / kBlock, (uint64_t)num_sms * 8);
-    const int parts = std::min(grid, kPartials);
-    k_centroid_partials<<<parts, kBlock, 0, st>>>(d_verts, n, s.partial);
-    k_centroid_final<<<1, kBlock, 0, st>>>(s.partial, parts, meta);
-    k_morton_hist<<<std::min(grid, num_sms * 2), kBlock, 0, st>>>(d_verts, n, meta, code, prim, s.hist);
-    k_hist_scan<<<4, 256, 0, st>>>(s.hist, s.offs);
-    if ((e = cudaFuncSetAttribute(k_onesweep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kOsSmem)) !=
-        cudaSuccess)
-        return e;
-    const uint32_t os_tiles = (n + kOsTile - 1) / kOsTile;
-    uint32_t* kin = code;
-    uint32_t* vin = prim;
-    uint32_t* kout = s.keys_alt;
-    uint32_t* vout = s.vals_alt;
-    for (int pass = 0; pass < 4; ++pass) {
-        k_onesweep<<<os_tiles, kOsThreads, kOsSmem, st>>>(kin, vin, kout, vout, n, pass, s.offs,
-                                                          s.os_status + (size_t)pass * os_tiles * 256, s.tile_ctr, s.err);
-        std::swap(kin, kout);
-        std::swap(vin, vout);
-    }
-    const uint32_t run_tiles = (n + kRunTile - 1) / kRunTile;
-    k_runs<<<run_tiles, kRunThreads, 0, st>>>(code, n, s.ucode, s.run_start, s.uidx, s.run_status, s.tile_ctr + 4,
-                                              meta, s.err);
-    k_karras<<<grid, kBlock, 0, st>>>(s.ucode, s.run_start, meta, s.kgamma, s.gap_of);
-    k_link<<<grid, kBlock, 0, st>>>(s.kgamma, s.gap_of, s.run_start, meta, nodes, s.parent_leaf);
-    k_run_nodes<<<grid, kBlock, 0, st>>>(code, n, s.uidx, s.run_start, meta, nodes, s.parent_leaf, s.err);
-    k_refit<<<grid, kBlock, 0, st>>>(d_verts, n, prim, s.parent_leaf, nodes, tris, s.counters, s.err);
-    if ((e = cudaMemcpyAsync(&meta->err, s.err, 4, cudaMemcpyDeviceToDevice, st)) != cudaSuccess) return e;
-    return cudaGetLastError();
+    return launch_build(d_verts, n, s, nodes, tris, code, prim, meta, num_sms, st);
 }
 
 }  // namespace gr

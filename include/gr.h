@@ -91,10 +91,10 @@ gr_status gr_bvh_build_host(gr_bvh* bvh, const float* h_verts, uint32_t n);
 uint32_t gr_bvh_size(const gr_bvh* bvh);
 
 /* Build without any device allocation. This entry point has no counterpart in
- * the reference. It is for callers that cannot call cudaMalloc: code running
- * while a stream is captured into a CUDA graph, plug-ins whose host
- * application owns all device memory, and latency-critical loops where
- * cudaMalloc / cudaFree would synchronise the device.
+ * the reference. It is for callers that cannot call cudaMalloc: plug-ins whose
+ * host application owns all device memory and hands them only the buffers of
+ * a call, and latency-critical loops where cudaMalloc / cudaFree would
+ * synchronise the device.
  *
  * The caller passes the input soup and every output buffer (device memory):
  *   d_nodes        64 bytes x max(n-1, 1)  traversal nodes (layout of gr_bvh_export's h_nodes)
@@ -108,7 +108,9 @@ uint32_t gr_bvh_size(const gr_bvh* bvh);
  * first call on a device looks up that array's device address, so make the
  * first call on each device before any stream capture. All calls share the
  * array: it is cleared where it must start at zero, and calls that overlap on
- * the GPU race on it. Stream-ordered; does not wait for the device. */
+ * the GPU race on it. If the device's context is destroyed and created again
+ * (cudaDeviceReset), the next call looks the array's address up again.
+ * Stream-ordered; does not wait for the device. */
 gr_status gr_bvh_build_noalloc(gr_ctx* ctx, const float* d_verts, uint32_t n, void* d_nodes, void* d_tris,
                                uint32_t* d_sorted_prim, uint32_t* d_sorted_code, void* d_header, void* stream);
 

@@ -1,11 +1,12 @@
 """The allocation-free LBVH build (gr_bvh_build_noalloc), called through the C
-ABI, gives the same BVH as gr_bvh_build on two calls in a row.
+ABI, gives the same BVH as gr_bvh_build, and as the oracle, on two calls in a
+row.
 
-It serves callers that cannot call cudaMalloc (stream capture, host-owned
-device memory, loops that must not synchronise): its scratch is a fixed array
-inside the library, so these tests also check that a second call does not see
-the first call's leftovers, and that an oversized request is refused.
-This file is collected last on purpose."""
+It serves callers that cannot call cudaMalloc (plug-ins whose host application
+owns all device memory, loops that must not synchronise the device): its
+scratch is a fixed array inside the library, so these tests also check that a
+second call does not see the first call's leftovers, and that an oversized
+request is refused. This file is collected last on purpose."""
 import ctypes
 
 import numpy as np
@@ -47,7 +48,7 @@ def _build_noalloc(ctx, verts):
             "root": int(h[0]), "err": int(h[2])}
 
 
-def test_noalloc_build_matches_gr_bvh_build_two_calls(ctx):
+def test_noalloc_build_matches_gr_bvh_build_two_calls(ctx, oracle):
     # a full-size call, then a smaller one over the same fixed scratch
     for n, salt in ((LIMIT, 301), (5000, 302)):
         v = sc.triangle_soup(n, seed_salt=salt)
@@ -62,6 +63,12 @@ def test_noalloc_build_matches_gr_bvh_build_two_calls(ctx):
             np.testing.assert_array_equal(got[k], want[k], err_msg=k)
         np.testing.assert_array_equal(got["tris"], want["tris"].view(np.uint32))
         b.close()
+        # and the oracle's restatement of the reference's LBVH, word for word
+        ref = oracle.lbvh(v)
+        assert got["root"] == ref["root"]
+        for k in ("sorted_prim", "sorted_code", "nodes"):
+            np.testing.assert_array_equal(got[k], ref[k], err_msg="oracle " + k)
+        np.testing.assert_array_equal(got["tris"], ref["tris"].view(np.uint32))
 
 
 def test_noalloc_build_refuses_oversize(ctx):
