@@ -17,6 +17,8 @@ namespace gr {
 namespace {
 
 constexpr int kBlock = 256;
+// sorted positions (and gaps) per block in the refit's first pass: one per thread
+constexpr int kRefitChunk = 256;
 
 // ---- small device helpers ---------------------------------------------------
 
@@ -523,55 +525,147 @@ __device__ __forceinline__ uint32_t atomic_add_acq_rel(uint32_t* p, uint32_t v) 
     return old;
 }
 
-__global__ void __launch_bounds__(kBlock) k_refit(const float* __restrict__ verts, uint32_t n,
-                                                  const uint32_t* __restrict__ prim, const uint32_t* __restrict__ parent_leaf,
-                                                  Node* nodes, Tri* __restrict__ tris, uint32_t* __restrict__ counters,
-                                                  uint32_t* __restrict__ err) {
-    for (uint32_t p = blockIdx.x * kBlock + threadIdx.x; p < n; p += gridDim.x * kBlock) {
-        const uint32_t id = prim[p];
-        const float* v = verts + 9ull * id;
-        float a[9];
+// Counter increment with acquire-release semantics at CTA scope on a
+// shared-memory word: orders this thread's global writes (its child box)
+// before the increment and the sibling's box, written by another thread of the
+// block before its increment, before this thread's later reads.
+__device__ __forceinline__ uint32_t atomic_add_acq_rel_cta(uint32_t* p, uint32_t v) {
+    uint32_t old;
+    const uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
+    asm volatile("atom.acq_rel.cta.shared.add.u32 %0, [%1], %2;" : "=r"(old) : "r"(a), "r"(v) : "memory");
+    return old;
+}
+
+// A child box written by another thread of the same block (plain load: the
+// shared-memory acquire above orders it).
+__device__ __forceinline__ Box3 get_child_box(const Node* nd, int slot) {
+    const float4 xy = reinterpret_cast<const float4*>(nd)[slot];
+    const float2 z = reinterpret_cast<const float2*>(&nd->q2)[slot];
+    Box3 b;
+    b.lo[0] = xy.x; b.hi[0] = xy.y; b.lo[1] = xy.z; b.hi[1] = xy.w; b.lo[2] = z.x; b.hi[2] = z.y;
+    return b;
+}
+
+__device__ __forceinline__ void box_union(Box3& a, const Box3& b) {
 #pragma unroll
-        for (int k = 0; k < 9; ++k) a[k] = __ldg(v + k);
-        Tri t;
-        t.a = make_float4(a[0], a[1], a[2], __uint_as_float(id));
-        t.b = make_float4(a[3], a[4], a[5], 0.0f);
-        t.c = make_float4(a[6], a[7], a[8], 0.0f);
-        tris[p] = t;
-        Box3 box;
+    for (int k = 0; k < 3; ++k) {
+        a.lo[k] = fminf(a.lo[k], b.lo[k]);
+        a.hi[k] = fmaxf(a.hi[k], b.hi[k]);
+    }
+}
+
+// Arrival at internal node `node` whose child box this thread has written into
+// slot `slot` (carrying that box): one GPU-scope ordered atomic on the node's
+// counter; the second arrival unions the two child boxes, writes the result
+// into its parent's slot and goes on up.
+__device__ __forceinline__ void climb_global(Node* nodes, uint32_t node, int slot, Box3 box,
+                                             uint32_t* __restrict__ counters, uint32_t* __restrict__ err) {
+    int guard = 0;
+    for (;;) {
+        Node* nd = nodes + node;
+        if (atomic_add_acq_rel(&counters[node], 1u) == 0) return;  // sibling not done yet
+        box_union(box, get_child_box_l2(nd, slot ^ 1));
+        const uint32_t parent = (uint32_t)__ldcg(&nd->q3.z);
+        if (parent == kNoNode) return;
+        Node* pn = nodes + parent;
+        slot = (__ldcg(&pn->q3.x) == (int32_t)node) ? 0 : 1;
+        put_child_box(pn, slot, box);
+        node = parent;
+        if (++guard > 128) {
+            atomicOr(err, ERR_RANGE);
+            return;
+        }
+    }
+}
+
+// Refit and leaf-order triangles. A block takes kRefitChunk sorted positions
+// (one block per chunk, so a block held up by a long climb delays no other
+// chunk), one per thread: the thread writes the position's triangle and
+// leaf box and walks up. Internal nodes are indexed by the gap they split, so
+// the chunk owns the nodes [base, base + kRefitChunk); arrivals at those are
+// counted in shared memory (an ordered atomic at block scope, not at GPU
+// scope), so every node whose subtree lies inside the chunk is finished
+// without a global atomic. An arrival at another chunk's node counts on that
+// node's global counter and goes on globally. After the chunk, a node of it
+// reached once adds its one arrival to the global counter: whichever of that
+// and the node's other (global) arrival comes second finishes the node, so
+// exactly one thread goes on. min / max are exact, so the boxes do not depend
+// on the order of arrivals.
+__global__ void __launch_bounds__(kRefitChunk) k_refit(const float* __restrict__ verts, uint32_t n,
+                                                       const uint32_t* __restrict__ prim,
+                                                       const uint32_t* __restrict__ parent_leaf, Node* nodes,
+                                                       Tri* __restrict__ tris, uint32_t* __restrict__ counters,
+                                                       uint32_t* __restrict__ err) {
+    __shared__ uint32_t s_cnt[kRefitChunk];
+    const uint32_t chunks = (n + kRefitChunk - 1) / kRefitChunk;
+    for (uint32_t c = blockIdx.x; c < chunks; c += gridDim.x) {  // block-uniform
+        const uint32_t base = c * kRefitChunk;
+        s_cnt[threadIdx.x] = 0;
+        __syncthreads();
+        const uint32_t p = base + threadIdx.x;  // one sorted position per thread
+        if (p < n) {
+            const uint32_t id = prim[p];
+            const float* v = verts + 9ull * id;
+            float a[9];
 #pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            box.lo[k] = fminf(fminf(a[k], a[3 + k]), a[6 + k]);
-            box.hi[k] = fmaxf(fmaxf(a[k], a[3 + k]), a[6 + k]);
-        }
-        if (n == 1) {
-            // one triangle: a single node whose two children are the same leaf
-            Node nd;
-            nd.q0 = make_float4(box.lo[0], box.hi[0], box.lo[1], box.hi[1]);
-            nd.q1 = nd.q0;
-            nd.q2 = make_float4(box.lo[2], box.hi[2], box.lo[2], box.hi[2]);
-            nd.q3 = make_int4(~0, ~0, (int32_t)kNoNode, 0);
-            nodes[0] = nd;
-            continue;
-        }
-        int32_t me = ~(int32_t)p;
-        uint32_t node = parent_leaf[p];
-        int guard = 0;
-        while (node != kNoNode) {
-            Node* nd = nodes + node;
-            const int slot = (nd->q3.x == me) ? 0 : 1;
-            put_child_box(nd, slot, box);
-            if (atomic_add_acq_rel(&counters[node], 1u) == 0) break;  // sibling not done yet
-            const Box3 sib = get_child_box_l2(nd, slot ^ 1);
+            for (int k = 0; k < 9; ++k) a[k] = __ldg(v + k);
+            Tri t;
+            t.a = make_float4(a[0], a[1], a[2], __uint_as_float(id));
+            t.b = make_float4(a[3], a[4], a[5], 0.0f);
+            t.c = make_float4(a[6], a[7], a[8], 0.0f);
+            tris[p] = t;
+            Box3 box;
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
-                box.lo[k] = fminf(box.lo[k], sib.lo[k]);
-                box.hi[k] = fmaxf(box.hi[k], sib.hi[k]);
+                box.lo[k] = fminf(fminf(a[k], a[3 + k]), a[6 + k]);
+                box.hi[k] = fmaxf(fmaxf(a[k], a[3 + k]), a[6 + k]);
             }
-            me = (int32_t)node;
-            node = (uint32_t)__ldcg(&nd->q3.z);
-            if (++guard > 128) { atomicOr(err, ERR_RANGE); break; }
+            if (n == 1) {
+                // one triangle: a single node whose two children are the same leaf
+                Node nd;
+                nd.q0 = make_float4(box.lo[0], box.hi[0], box.lo[1], box.hi[1]);
+                nd.q1 = nd.q0;
+                nd.q2 = make_float4(box.lo[2], box.hi[2], box.lo[2], box.hi[2]);
+                nd.q3 = make_int4(~0, ~0, (int32_t)kNoNode, 0);
+                nodes[0] = nd;
+            } else {
+                int32_t me = ~(int32_t)p;
+                uint32_t node = parent_leaf[p];
+                int guard = 0;
+                while (node != kNoNode) {
+                    Node* nd = nodes + node;
+                    const int slot = (nd->q3.x == me) ? 0 : 1;
+                    put_child_box(nd, slot, box);
+                    if (node - base >= (uint32_t)kRefitChunk) {  // another chunk's node
+                        climb_global(nodes, node, slot, box, counters, err);
+                        break;
+                    }
+                    if (atomic_add_acq_rel_cta(&s_cnt[node - base], 1u) == 0) break;  // sibling not done yet
+                    box_union(box, get_child_box(nd, slot ^ 1));
+                    me = (int32_t)node;
+                    node = (uint32_t)nd->q3.z;
+                    if (++guard > 128) {
+                        atomicOr(err, ERR_RANGE);
+                        break;
+                    }
+                }
+            }
         }
+        __syncthreads();
+        // this chunk's nodes reached once: their one arrival joins the global count
+        if (p + 1 < n && s_cnt[threadIdx.x] == 1 && atomic_add_acq_rel(&counters[p], 1u) == 1) {
+            Node* nd = nodes + p;  // node p: both children are done, their boxes are in its slots
+            Box3 box = get_child_box_l2(nd, 0);
+            box_union(box, get_child_box_l2(nd, 1));
+            const uint32_t parent = (uint32_t)__ldcg(&nd->q3.z);
+            if (parent != kNoNode) {
+                Node* pn = nodes + parent;
+                const int slot = (__ldcg(&pn->q3.x) == (int32_t)p) ? 0 : 1;
+                put_child_box(pn, slot, box);
+                climb_global(nodes, parent, slot, box, counters, err);
+            }
+        }
+        __syncthreads();
     }
 }
 
@@ -744,7 +838,9 @@ cudaError_t launch_build(const float* d_verts, uint32_t n, const Scratch& s, Nod
     k_karras<<<grid, kBlock, 0, st>>>(s.ucode, s.run_start, meta, s.kgamma, s.gap_of);
     k_link<<<grid, kBlock, 0, st>>>(s.kgamma, s.gap_of, s.run_start, meta, nodes, s.parent_leaf);
     k_run_nodes<<<grid, kBlock, 0, st>>>(code, n, s.uidx, s.run_start, meta, nodes, s.parent_leaf, s.err);
-    k_refit<<<grid, kBlock, 0, st>>>(d_verts, n, prim, s.parent_leaf, nodes, tris, s.counters, s.err);
+    const uint32_t chunks = (n + kRefitChunk - 1) / kRefitChunk;
+    k_refit<<<chunks, kRefitChunk, 0, st>>>(
+        d_verts, n, prim, s.parent_leaf, nodes, tris, s.counters, s.err);
     // fold the build's error word into the header the host reads
     if ((e = cudaMemcpyAsync(&meta->err, s.err, 4, cudaMemcpyDeviceToDevice, st)) != cudaSuccess) return e;
     return cudaGetLastError();
