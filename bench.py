@@ -293,6 +293,72 @@ def whole_job(local_seconds, units_per_rank, device):
     return ws * units_per_rank / t / 1e6, t
 
 
+# LBVH build, algorithmic bytes per triangle: 36 vertex read for the Morton
+# codes, 8 code / index write, 4 sort passes x 16, 36 vertex re-read for the
+# leaf boxes, 2 x 32 node writes, 8 parent links and counters.
+BUILD_BYTES_PER_TRI = 216
+
+
+def _binding(entry, event_ms, peak):
+    """What binds a kernel, from its committed ncu figures: DRAM bytes per
+    launch over the event-timed duration against the HBM peak, the L2 and
+    issue figures of the smaller capture of the same kernel."""
+    full, small = entry["full"], entry["small"]
+    traffic = full["dram_bytes_read"] + full["dram_bytes_write"]
+    dram_gbs = traffic / (event_ms / 1e3) / 1e9
+    return {"resource": "instruction issue",
+            "issue_active": small["issue_active_pct"] / 100,
+            "threads_per_warp_instruction": small["threads_per_warp_instruction"],
+            "dram_gbs": dram_gbs, "dram_frac_of_peak": dram_gbs / peak,
+            "l2_frac_of_peak": small["l2_throughput_pct_of_peak"] / 100,
+            "l2_hit_rate": small["l2_hit_rate_pct"] / 100,
+            "l2_bytes_per_ray": small["lts_bytes"] / small["rays"],
+            "warp_instructions_per_ray": small["warp_instructions"] / small["rays"],
+            "captured_rays": [full["rays"], small["rays"]]}, traffic
+
+
+def roofline_block(layout_name, achieved, peak, peak_kind, closest_ms, anyhit_ms, build_ms):
+    """The roofline entry of the JSON line. It leads with what binds the
+    headline kernel (measured: instruction issue at about half the lanes of a
+    warp, with DRAM and L2 far from their peaks), then gives the contract's
+    algorithmic-byte figure, whose bytes are the reference traversal's (its
+    348 node visits per ray on its binary tree): a fraction above 1 means L2
+    reuse and fewer visits, not HBM traffic. Any-hit and the LBVH build get
+    the same treatment."""
+    path = os.path.join(ROOT, "profiles", "roofline_inputs.json")
+    inputs = {}
+    if os.path.exists(path):
+        with open(path) as f:
+            inputs = json.load(f)
+    out = {}
+    traffic = None
+    captured = layout_name == "bvh8_q8"  # the captures are of the 8-wide kernels
+    if captured and "closest" in inputs:
+        out["binding"], traffic = _binding(inputs["closest"], closest_ms, peak)
+    out.update({"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "peak_kind": peak_kind, "traffic": traffic,
+                "kernel": "k_trace<closest, %s>" % layout_name, "bytes_per_ray": BYTES_PER_RAY,
+                "achieved_is": "reference-traversal bytes (11,364.8 B/ray: the reference's node and triangle "
+                               "fetches on its binary tree) per event-timed launch; above 1 of HBM = L2 reuse and "
+                               "fewer node visits, not DRAM traffic (see binding)"})
+    if captured and "anyhit" in inputs and anyhit_ms:
+        b, t = _binding(inputs["anyhit"], anyhit_ms, peak)
+        out["anyhit"] = {"kernel": "k_trace<any hit, %s>" % layout_name, "kernel_ms": anyhit_ms,
+                         "traffic": t, "binding": b}
+    if "build" in inputs and build_ms:
+        b = inputs["build"]
+        alg = BUILD_BYTES_PER_TRI * b["triangles"]
+        t = b["dram_bytes_read"] + b["dram_bytes_write"]
+        out["build"] = {"kernel": "LBVH build (13 launches), %d triangles" % b["triangles"], "ms": build_ms,
+                        "achieved": alg / (build_ms / 1e3) / 1e9, "frac": alg / (build_ms / 1e3) / 1e9 / peak,
+                        "unit": "GB/s", "algorithmic_bytes": alg, "traffic": t,
+                        "dram_frac_of_peak": t / (build_ms / 1e3) / 1e9 / peak,
+                        "binding": "latency: dependent launches, the sort's look-back and the refit's climbs "
+                                   "(longest: %s)" % ", ".join("%s %.0f us" % (k, v / 1e3)
+                                                             for k, v in b["longest"].items())}
+    return out
+
+
 def l2_flush(buf):
     buf.zero_()
 
@@ -310,7 +376,9 @@ def run_gpu(args):
     dev = torch.device("cuda", local)
     n_tris, n_rays = args.tris, args.rays
     verts = scenes.triangle_soup(n_tris)
-    rays = scenes.incoherent_rays(n_rays)
+    # --quick --any-hit times the shadow any-hit query instead (profiling)
+    quick_any = bool(args.quick and args.any_hit)
+    rays = scenes.shadow_rays(n_rays) if quick_any else scenes.incoherent_rays(n_rays)
     ctx = gr.Context(local)
     bvh = gr.BVH(ctx)
     stream = torch.cuda.current_stream()
@@ -353,7 +421,7 @@ def run_gpu(args):
     names = {v: k for k, v in gr.LAYOUT_NAMES.items()}
     torch.cuda.synchronize()
     if args.layout == "auto":
-        table = bvh.autotune(d_rays, n_rays, d_hits)
+        table = bvh.autotune(d_rays, n_rays, d_hits, any_hit=quick_any)
     else:
         bvh.set_tuning(names[args.layout], args.block, args.short_stack)
         table = []
@@ -364,7 +432,7 @@ def run_gpu(args):
                     for t, ms in table}
 
     for _ in range(max(args.warmup, 3)):
-        step(d_rays, d_hits, n_rays)
+        step(d_rays, d_hits, n_rays, quick_any)
     torch.cuda.synchronize()
 
     clocks = ClockSampler(local)
@@ -377,7 +445,7 @@ def run_gpu(args):
         l2_flush(flush)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        step(d_rays, d_hits, n_rays)
+        step(d_rays, d_hits, n_rays, quick_any)
         e1.record(stream)
         ev.append((e0, e1))
     torch.cuda.synchronize()
@@ -389,7 +457,8 @@ def run_gpu(args):
     if args.quick:
         clocks.stop()
         if rank == 0:
-            print(json.dumps({"quick": True, "tris": n_tris, "rays": n_rays, "tuning": tuning,
+            print(json.dumps({"quick": True, "query": "any hit" if quick_any else "closest hit", "tris": n_tris,
+                              "rays": n_rays, "tuning": tuning,
                               "autotune_mrays_s": layout_rates,
                               "kernel_ms_median": statistics.median(kernel_ms),
                               "mrays_s": n_rays / (statistics.median(kernel_ms) / 1e3) / 1e6}), flush=True)
@@ -413,6 +482,7 @@ def run_gpu(args):
             torch.cuda.synchronize()
             ms.append(e0.elapsed_time(e1))
         extras[name + "_mrays_s"] = r2.shape[0] / (statistics.median(ms) / 1e3) / 1e6
+        extras[name + "_kernel_ms"] = statistics.median(ms)
         del d_r2
     if rank == 0 and not args.no_reference_gpu:
         d_s = torch.from_numpy(scenes.shadow_rays(N_RAYS)).to(dev)
@@ -478,22 +548,10 @@ def run_gpu(args):
         peak, peak_kind = measured_peaks()
         avg_ms = sum(kernel_ms) / len(kernel_ms)
         achieved = BYTES_PER_RAY * N_RAYS / (avg_ms / 1e3) / 1e9
-        traffic, l2 = None, None
-        tp = os.path.join(ROOT, "profiles", "trace_closest_traffic.json")
-        if os.path.exists(tp):
-            with open(tp) as f:
-                tj = json.load(f)
-            # the capture is of one layout's kernel; other layouts report none
-            if tj.get("layout") == gr.LAYOUT_NAMES[layout]:
-                traffic = tj.get("bytes_per_launch")
-                c = tj.get("l2")
-                if c:
-                    # an HBM fraction above 1 means the working set sits in L2:
-                    # the L2 side of the same kernel (one ncu capture)
-                    l2 = {"hit_rate_pct": c["l2_hit_rate_pct"], "frac_of_l2_peak": c["l2_throughput_pct_of_peak"] / 100,
-                          "l2_bytes_per_ray": c["lts_bytes_per_ray"], "issue_active_pct": c["issue_active_pct"],
-                          "sample_rays": c["rays"],
-                          "reading": "issue bound: L2 and DRAM are far from their peaks"}
+        build_ms = statistics.median(build_ms)
+        roofline = roofline_block(layout_name=gr.LAYOUT_NAMES[layout], achieved=achieved, peak=peak,
+                                  peak_kind=peak_kind, closest_ms=avg_ms,
+                                  anyhit_ms=extras.get("shadow_anyhit_kernel_ms"), build_ms=build_ms)
         cb = cpu_reference(1, 0)
         out = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -502,18 +560,15 @@ def run_gpu(args):
             "config": {"workload": WORKLOAD, "triangles": N_TRIS, "rays": N_RAYS, "query": "closest hit",
                        "tuning": tuning, "autotune_mrays_s": layout_rates,
                        "l2": "flushed (256 MB write) before every timed step", "parallelism": "replicas"},
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
-                         "kernel": "k_trace<closest, %s>" % gr.LAYOUT_NAMES[layout], "bytes_per_ray": BYTES_PER_RAY,
-                         "l2": l2},
+            "roofline": roofline,
             "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": N_RAYS * 32,
                     "d2h_bytes_per_step": N_RAYS * 16, "api": "gr_trace_host with page-locked host rays and hits: the traversal reads the rays and "
                            "writes the hits in host memory over the host link inside the timed region"},
             "gpu_launches": args.steps,
             "clocks": clock_info,
-            "extra": dict(extras, bvh_build_ms=statistics.median(build_ms),
-                          bvh_build_mtris_s=N_TRIS / (statistics.median(build_ms) / 1e3) / 1e6,
+            "extra": dict(extras, bvh_build_ms=build_ms,
+                          bvh_build_mtris_s=N_TRIS / (build_ms / 1e3) / 1e6,
                           bvh8_collapse_ms=statistics.median(collapse_ms),
                           kernel_ms_median=statistics.median(kernel_ms)),
         }
@@ -539,6 +594,24 @@ def run_render_only(args):
     print(json.dumps(dict(out, workload=args.render_only)), flush=True)
 
 
+def run_serving_sweep(args):
+    """The serving configuration's full sweep (not part of the default run:
+    about six minutes): prints one JSON line of per-rate, per-policy latency
+    and throughput."""
+    import torch
+    import gr
+    from gr import workloads as wl
+    torch.cuda.set_device(0)
+    ctx = gr.Context(0)
+    names = {v: k for k, v in gr.LAYOUT_NAMES.items()}
+    tuning = (names[args.layout if args.layout != "auto" else "bvh8_q8"], args.block, args.short_stack,
+              args.wave_paths)
+    log = lambda m: print("[serving] " + m, file=sys.stderr, flush=True)  # noqa: E731
+    out = wl.config5_sweep(ctx, window_s=args.window, tuning=tuning, log=log)
+    print(json.dumps(dict(out, workload="serving sweep (Poisson arrivals, config-4 request distribution)")),
+          flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -554,6 +627,8 @@ def main():
                     help="node layout of the timed traversal (auto: autotune layout, block and short stack)")
     ap.add_argument("--block", type=int, default=128, choices=[64, 128, 256])
     ap.add_argument("--short-stack", type=int, default=12, choices=[8, 12, 16])
+    ap.add_argument("--any-hit", action="store_true",
+                    help="with --quick: time the shadow any-hit query (profiling the any-hit kernel)")
     ap.add_argument("--quick", action="store_true",
                     help="time the main query only (no extras, e2e or CPU baseline); for profiling")
     ap.add_argument("--render-only", default=None, choices=["config1", "config3"],
@@ -562,8 +637,13 @@ def main():
     ap.add_argument("--spp", type=int, default=0, help="samples per pixel of --render-only (0: the configuration's)")
     ap.add_argument("--wave-paths", type=int, default=0,
                     help="paths per wave of --render-only (0: the library's default)")
+    ap.add_argument("--serving-sweep", action="store_true",
+                    help="run the serving configuration's full sweep (rates 10-500/s, three server policies) and exit")
+    ap.add_argument("--window", type=float, default=20.0, help="seconds of arrivals per rate of --serving-sweep")
     args = ap.parse_args()
-    if args.render_only:
+    if args.serving_sweep:
+        run_serving_sweep(args)
+    elif args.render_only:
         run_render_only(args)
     elif args.impl == "reference":
         run_reference(args)

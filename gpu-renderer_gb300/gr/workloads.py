@@ -118,15 +118,19 @@ def config4(ctx, n_jobs=64, autotune=True):
     return out
 
 
-def _serve(ctx, scenes, requests, budget, max_active, rate, tuning):
+def _serve(ctx, scenes, requests, budget, max_active, rate, tuning, policy=gr.SERVER_FIFO, age_cap_s=0.0,
+           max_wait_s=0.0):
     """Submits `requests` (scene index, camera, spp, seed) at Poisson times of
-    `rate` per second; returns latency and throughput figures."""
+    `rate` per second; returns latency and throughput figures. With
+    max_wait_s > 0 the server refuses requests it cannot start in time
+    (GR_ERR_BUSY); those count as rejected and have no latency."""
     layout, block, sstack, wave = tuning
     srv = gr.Server(ctx, budget_bytes=budget, wave_paths=wave, max_active=max_active, layout=layout, block=block,
-                    short_stack=sstack)
+                    short_stack=sstack, policy=policy, age_cap_s=age_cap_s, max_wait_s=max_wait_s)
     r = np.random.default_rng(12345)
     gaps = r.exponential(1.0 / rate, size=len(requests))
     tickets = []
+    rejected = 0
     t0 = time.perf_counter()
     t_next = t0
     for (si, cam, spp, seed), gap in zip(requests, gaps):
@@ -134,21 +138,83 @@ def _serve(ctx, scenes, requests, budget, max_active, rate, tuning):
         delay = t_next - time.perf_counter()
         if delay > 0:
             time.sleep(delay)
-        tickets.append(srv.submit(scenes[si], spp, 8, seed, camera=cam))
+        try:
+            tickets.append(srv.submit(scenes[si], spp, 8, seed, camera=cam))
+        except gr.GrError as e:
+            if e.status != gr.GR_ERR_BUSY:
+                raise
+            rejected += 1
+    offered_s = time.perf_counter() - t0
     lat, done_s, sub_s = [], [], []
+    samples = 0
     for t in tickets:
-        ok, _, js = srv.wait(t, timeout=600.0)
+        ok, _, js = srv.wait(t, timeout=900.0)
         if ok:
             lat.append(js.done_s - js.submit_s)
             done_s.append(js.done_s)
             sub_s.append(js.submit_s)
+            samples += js.samples
     st = srv.stats()
     srv.close()
     span = max(done_s) - min(sub_s) if done_s else float("nan")
-    lat = np.asarray(lat)
-    return {"rate": rate, "requests": len(requests), "completed": len(lat),
-            "p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
-            "renders_s": len(lat) / span, "waves": int(st.waves), "peak_bytes": int(st.peak_bytes)}
+    lat = np.asarray(lat) if lat else np.asarray([float("nan")])
+    return {"rate": rate, "requests": len(requests), "completed": len(done_s), "rejected": rejected,
+            "offered_s": offered_s, "p50_ms": float(np.percentile(lat, 50) * 1e3),
+            "p99_ms": float(np.percentile(lat, 99) * 1e3), "max_ms": float(np.max(lat) * 1e3),
+            "renders_s": len(done_s) / span, "msamples_s": samples / span / 1e6, "waves": int(st.waves),
+            "peak_bytes": int(st.peak_bytes)}
+
+
+def config5_sweep(ctx, rates=(10, 20, 50, 100, 200, 500), window_s=20.0, fifo_overload_window_s=5.0,
+                  overload_rate=100, pool=8, budget=150 * 10**9, tuning=(gr.LAYOUT_BVH2, 128, 12, 0),
+                  age_cap_s=2.0, max_wait_s=0.5, log=None):
+    """The serving configuration as specified: Poisson arrivals swept over
+    `rates` per second, `window_s` seconds of arrivals each, requests drawn from
+    the batch configuration's scene, resolution and spp distribution over a
+    pool of resident scenes, under an HBM budget. Three server policies:
+      fifo       first come first served, every request accepted;
+      srf        shortest remaining work first, with an age cap;
+      srf_shed   srf plus load shedding: a request the server cannot start
+                 within max_wait_s at its measured throughput is refused.
+    Without shedding a rate above the server's capacity grows the queue for as
+    long as arrivals last, so fifo and srf run their overload rates
+    (> overload_rate) for fifo_overload_window_s only; their p99 there is the
+    queue's growth over that window."""
+    descs = [sc.batch_job(i)[0] for i in range(pool)]
+    scenes = [gr.Scene(ctx, d) for d in descs]
+    r = np.random.default_rng(0x5EED0005)
+    out = {"scene_pool": pool, "budget_bytes": budget, "window_s": window_s,
+           "fifo_overload_window_s": fifo_overload_window_s, "age_cap_s": age_cap_s, "max_wait_s": max_wait_s,
+           "tuning": {"layout": gr.LAYOUT_NAMES[tuning[0]], "block": tuning[1], "short_stack": tuning[2],
+                      "wave_paths": tuning[3] or (1 << 22)}, "runs": []}
+
+    def make_requests(n):
+        reqs = []
+        for k in range(n):
+            si = int(r.integers(0, pool))
+            res = int(r.choice(sc.RESOLUTIONS))
+            spp = int(r.choice(sc.SPPS))
+            reqs.append((si, dict(descs[si].camera, width=res, height=res), spp, k))
+        return reqs
+
+    # warm-up: every scene once (graphs captured, pool grown)
+    _serve(ctx, scenes, make_requests(2 * pool), budget, 0, 1000.0, tuning)
+    for rate in rates:
+        for name, policy, cap, wait in (("fifo", gr.SERVER_FIFO, 0.0, 0.0),
+                                        ("srf", gr.SERVER_SHORTEST_FIRST, age_cap_s, 0.0),
+                                        ("srf_shed", gr.SERVER_SHORTEST_FIRST, age_cap_s, max_wait_s)):
+            win = window_s if (wait > 0 or rate <= overload_rate) else fifo_overload_window_s
+            reqs = make_requests(max(4, int(rate * win)))
+            res = _serve(ctx, scenes, reqs, budget, 0, rate, tuning, policy=policy, age_cap_s=cap, max_wait_s=wait)
+            res.update(policy=name, window_s=win)
+            out["runs"].append(res)
+            if log:
+                log("lambda %g %s: %d requests, %d done, %d refused, p50 %.0f ms, p99 %.0f ms, %.1f renders/s, "
+                    "%.0f M samples/s" % (rate, name, res["requests"], res["completed"], res["rejected"], res["p50_ms"],
+                                          res["p99_ms"], res["renders_s"], res["msamples_s"]))
+    for s in scenes:
+        s.close()
+    return out
 
 
 def config5(ctx, rates=(10, 20, 50, 100, 200), window_s=3.0, overload_window_s=2.0, overload_rate=50,
