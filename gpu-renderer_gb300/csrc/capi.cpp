@@ -6,6 +6,7 @@
 #include <vector>
 
 #include "gr_internal.h"
+#include "render.h"
 
 namespace gr {
 
@@ -156,9 +157,10 @@ const char* gr_status_string(int st) {
     }
 }
 
-gr_status gr_context_create(int device, gr_ctx** out) {
+gr_status gr_context_create(int device, const gr_opts* opts, gr_ctx** out) {
     if (!out) return GR_ERR_INVALID;
     *out = nullptr;
+    if (opts && opts->flags != 0) return GR_ERR_INVALID;
     int count = 0;
     if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count) {
         cudaGetLastError();
@@ -167,6 +169,7 @@ gr_status gr_context_create(int device, gr_ctx** out) {
     gr_ctx* ctx = new (std::nothrow) gr_ctx();
     if (!ctx) return GR_ERR_OOM_BUDGET;
     ctx->device = device;
+    ctx->default_wave_paths = opts && opts->default_wave_paths ? opts->default_wave_paths : gr::kDefaultWavePaths;
     cudaError_t e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);

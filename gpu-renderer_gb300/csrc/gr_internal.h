@@ -201,6 +201,7 @@ struct gr_ctx {
     // thread may build too, so it is taken under its lock
     gr::DevBuf scratch8;
     std::mutex scratch8_mu;
+    uint32_t default_wave_paths = 0;     // wave size when neither a call nor its scene sets one (gr_opts)
     void* batch_pool = nullptr;          // wave pool of gr_render_batch (owned; freed with the context)
     void (*batch_pool_free)(void*) = nullptr;
 };

@@ -631,6 +631,19 @@ __global__ void __launch_bounds__(kShadeThreads) k_filter(const double* __restri
     }
 }
 
+// Mean linear radiance per pixel (3 floats), the same arithmetic as the host
+// read-back of gr_render: sum * (1 / count) in double, rounded to float.
+__global__ void __launch_bounds__(kShadeThreads) k_mean_rgb(const double* __restrict__ fb,
+                                                            const uint32_t* __restrict__ fbc, uint32_t npix,
+                                                            float* __restrict__ out) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < npix; i += gridDim.x * blockDim.x) {
+        const uint32_t n = fbc[i];
+        const double inv = n ? 1.0 / (double)n : 0.0;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) out[3ull * i + c] = (float)(fb[3ull * i + c] * inv);
+    }
+}
+
 __global__ void k_wave_end(Paths ps) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     WaveHeader* h = ps.hdr;
@@ -838,6 +851,13 @@ cudaError_t filter_rgba8(const double* fb, const uint32_t* fbc, uint32_t npix, u
     if (npix == 0) return cudaSuccess;
     const int grid = (int)std::min<uint32_t>((npix + kShadeThreads - 1) / kShadeThreads, 4096u);
     k_filter<<<grid, kShadeThreads, 0, s>>>(fb, fbc, npix, out);
+    return cudaGetLastError();
+}
+
+cudaError_t mean_rgb(const double* fb, const uint32_t* fbc, uint32_t npix, float* out, cudaStream_t s) {
+    if (npix == 0) return cudaSuccess;
+    const int grid = (int)std::min<uint32_t>((npix + kShadeThreads - 1) / kShadeThreads, 4096u);
+    k_mean_rgb<<<grid, kShadeThreads, 0, s>>>(fb, fbc, npix, out);
     return cudaGetLastError();
 }
 

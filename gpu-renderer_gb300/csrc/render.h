@@ -208,6 +208,8 @@ uint32_t pack_wave(std::vector<HostJob*>& jobs, uint32_t capacity, std::vector<J
 // Mean radiance -> sRGB-encoded RGBA8 (R in the low byte), the reference's
 // filter_kernel (pathtracer_kernel.h:792-810); pixels without samples are black.
 cudaError_t filter_rgba8(const double* fb, const uint32_t* fbc, uint32_t npix, uint32_t* out, cudaStream_t s);
+// Mean radiance of an accumulation into 3 floats per pixel in device memory.
+cudaError_t mean_rgb(const double* fb, const uint32_t* fbc, uint32_t npix, float* out, cudaStream_t s);
 
 }  // namespace gr
 

@@ -305,7 +305,7 @@ gr_status gr_scene_info(const gr_scene* sc, uint32_t* width, uint32_t* height, u
     return GR_OK;
 }
 
-gr_status gr_render(gr_scene* sc, const gr_render_opts* opts, float* h_rgb, gr_render_stats* stats) {
+gr_status gr_render(gr_scene* sc, const gr_render_opts* opts, float* rgb, gr_render_stats* stats) {
     if (!sc || !opts) return GR_ERR_INVALID;
     gr_ctx* ctx = sc->ctx;
     if (opts->max_depth > (uint32_t)gr::kMaxDepth)
@@ -316,7 +316,7 @@ gr_status gr_render(gr_scene* sc, const gr_render_opts* opts, float* h_rgb, gr_r
     const uint32_t npix = sc->cam.width * sc->cam.height;
     const bool asked = opts->wave_paths || sc->default_wave_paths;
     const uint64_t want_paths = opts->wave_paths ? opts->wave_paths
-                                : (sc->default_wave_paths ? sc->default_wave_paths : gr::kDefaultWavePaths);
+                                : (sc->default_wave_paths ? sc->default_wave_paths : ctx->default_wave_paths);
     uint32_t per_wave = (uint32_t)std::max<uint64_t>(1, want_paths / npix);
     if (opts->spp) per_wave = std::min(per_wave, opts->spp);
     uint64_t cap64 = (uint64_t)per_wave * npix;
@@ -362,9 +362,20 @@ gr_status gr_render(gr_scene* sc, const gr_render_opts* opts, float* h_rgb, gr_r
     uint32_t err = 0;
     SC_CUDA(ctx, cudaMemcpyAsync(&after, pool->ps.hdr, sizeof(after), cudaMemcpyDeviceToHost, s));
     SC_CUDA(ctx, cudaMemcpyAsync(&err, pool->error_word(), 4, cudaMemcpyDeviceToHost, s));
+    // the image goes to device memory by a kernel, or to host memory below
+    bool on_device = false;
+    if (rgb) {
+        cudaPointerAttributes pa{};
+        SC_CUDA(ctx, cudaPointerGetAttributes(&pa, rgb));
+        on_device = pa.type == cudaMemoryTypeDevice || pa.type == cudaMemoryTypeManaged;
+        if (on_device && pa.device != ctx->device)
+            return fail(ctx, GR_ERR_INVALID, "gr_render: output buffer on another device");
+        if (on_device) SC_CUDA(ctx, gr::mean_rgb((const double*)sc->fb.p, (const uint32_t*)sc->fb_count.p, npix, rgb, s));
+    }
     SC_CUDA(ctx, cudaStreamSynchronize(s));
     sc->samples_done += opts->spp;
-    if (h_rgb) {
+    if (rgb && !on_device) {
+        float* h_rgb = rgb;
         std::vector<double> sum(3ull * npix);
         std::vector<uint32_t> cnt(npix);
         SC_CUDA(ctx, cudaMemcpy(sum.data(), sc->fb.p, 24ull * npix, cudaMemcpyDeviceToHost));

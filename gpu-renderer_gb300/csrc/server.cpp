@@ -105,7 +105,7 @@ extern "C" gr_status gr_render_batch(gr_ctx* ctx, gr_scene* const* scenes, const
     }
     cudaError_t e = cudaSetDevice(ctx->device);
     if (e != cudaSuccess) return cuda_status(e);
-    uint64_t want = wave_paths ? wave_paths : gr::kDefaultWavePaths;
+    uint64_t want = wave_paths ? wave_paths : ctx->default_wave_paths;
     uint64_t work = 0;
     for (uint32_t i = 0; i < n; ++i) work += (uint64_t)opts[i].spp * jobs[i].npix;
     want = std::min<uint64_t>(want, std::max<uint64_t>(work, 1));  // no larger than the batch

@@ -47,7 +47,7 @@ def load():
     sig = {
         "gr_version": ([], ctypes.c_int),
         "gr_status_string": ([ctypes.c_int], ctypes.c_char_p),
-        "gr_context_create": ([ctypes.c_int, ctypes.POINTER(_P)], ctypes.c_int),
+        "gr_context_create": ([ctypes.c_int, _P, ctypes.POINTER(_P)], ctypes.c_int),
         "gr_context_destroy": ([_P], ctypes.c_int),
         "gr_last_error": ([_P], ctypes.c_char_p),
         "gr_bvh_create": ([_P, ctypes.POINTER(_P)], ctypes.c_int),
@@ -105,13 +105,20 @@ class TuningResult(ctypes.Structure):
     _fields_ = [("tuning", Tuning), ("ms", ctypes.c_float)]
 
 
-class Context:
-    """A gr context bound to one CUDA device."""
+class Opts(ctypes.Structure):
+    """Context options (gr_opts)."""
+    _fields_ = [("default_wave_paths", ctypes.c_uint32), ("flags", ctypes.c_uint32)]
 
-    def __init__(self, device=0):
+
+class Context:
+    """A gr context bound to one CUDA device. default_wave_paths: the wave
+    size of renders that set none (0 = the library's)."""
+
+    def __init__(self, device=0, default_wave_paths=0):
         L = load()
         h = _P()
-        st = L.gr_context_create(device, ctypes.byref(h))
+        opts = Opts(default_wave_paths, 0)
+        st = L.gr_context_create(device, ctypes.byref(opts), ctypes.byref(h))
         if st != GR_OK:
             raise GrError(st, "gr_context_create(%d)" % device)
         self.h = h
@@ -452,11 +459,14 @@ class Scene:
         self.ctx.check(_declare(_SCENE_SIGS).gr_scene_rgba8(self.h, _ptr(d_out), _P(stream) if stream else None),
                        "gr_scene_rgba8")
 
-    def render(self, spp, max_depth=8, seed=0, rr_depth=3, flags=0, wave_paths=0, want_image=True):
+    def render(self, spp, max_depth=8, seed=0, rr_depth=3, flags=0, wave_paths=0, want_image=True, out=None):
+        """Adds spp samples per pixel; returns (mean image, RenderStats). `out`
+        may be a device tensor of height x width x 3 floats that gr_render
+        fills on the GPU (then it is returned in place of a host image)."""
         L = _declare(_SCENE_SIGS)
         o = RenderOpts(spp, max_depth, seed, rr_depth, flags, wave_paths)
         st = RenderStats()
-        img = np.zeros((self.height, self.width, 3), np.float32) if want_image else None
+        img = out if out is not None else (np.zeros((self.height, self.width, 3), np.float32) if want_image else None)
         self.ctx.check(L.gr_render(self.h, ctypes.byref(o), _ptr(img), ctypes.byref(st)), "gr_render")
         return img, st
 

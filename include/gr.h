@@ -56,12 +56,22 @@ typedef struct gr_bvh gr_bvh;
 
 /* ---- context ------------------------------------------------------------ */
 
-/* Binds `device` and creates a context (streams, memory pool). The context
- * keeps the 8-wide layout build's scratch (about 144 bytes per triangle of the
- * largest BVH it has collapsed) between builds, so building a layout neither
- * allocates nor frees device memory once it has grown; destroying the context
- * frees it. */
-gr_status gr_context_create(int device, gr_ctx** out);
+/* Context options (the reference has none: its frame size and queues follow
+ * the scene, pathtracer.cu:41-150). */
+typedef struct gr_opts {
+    uint32_t default_wave_paths; /* paths in flight per render wave when neither the call nor its scene sets the
+                                    wave size (0 = the whole call as one wave up to 64 Mi paths); the context's
+                                    pool of path state, about 172 bytes per path, grows to the largest wave used */
+    uint32_t flags;              /* reserved, 0 */
+} gr_opts;
+
+/* Binds `device` and creates a context (streams, memory pool); `opts` may be
+ * NULL for the defaults. The context keeps the 8-wide layout build's scratch
+ * (about 144 bytes per triangle of the largest BVH it has collapsed) between
+ * builds, so building a layout neither allocates nor frees device memory once
+ * it has grown; destroying the context frees it. Replaces the process-global
+ * CUDA state the reference sets up implicitly. */
+gr_status gr_context_create(int device, const gr_opts* opts, gr_ctx** out);
 gr_status gr_context_destroy(gr_ctx* ctx);
 /* Text of the last error recorded on `ctx` (never NULL). */
 const char* gr_last_error(const gr_ctx* ctx);
@@ -319,10 +329,13 @@ gr_status gr_scene_info(const gr_scene* scene, uint32_t* width, uint32_t* height
 /* Replaces PathTracer::render(uint32 num) (pathtracer.cu:152-170): adds
  * opts->spp samples per pixel to the scene's accumulation buffer with the
  * wavefront integrator (camera rays, closest hit, NEE + MIS shading, shadow
- * any-hit, Russian roulette) and, when h_rgb is not NULL, writes the running
- * mean radiance (width x height x 3 floats, row 0 first) to host memory.
- * Successive calls continue the sample sequence, as repeated render() calls do. */
-gr_status gr_render(gr_scene* scene, const gr_render_opts* opts, float* h_rgb, gr_render_stats* stats);
+ * any-hit, Russian roulette) and, when rgb is not NULL, writes the running
+ * mean radiance (width x height x 3 floats, row 0 first) to it. rgb may be
+ * host memory or device memory of the scene's device (told apart with
+ * cudaPointerGetAttributes; a device buffer is written by a kernel, with the
+ * same floats as the host read-back). Waits for the device. Successive calls
+ * continue the sample sequence, as repeated render() calls do. */
+gr_status gr_render(gr_scene* scene, const gr_render_opts* opts, float* rgb, gr_render_stats* stats);
 
 /* The raw accumulation: per-pixel radiance sums (3 doubles) and sample counts.
  * Either pointer may be NULL. Replaces FrameBuffer's m_buffer / m_sample_num. */

@@ -41,7 +41,7 @@ def test_context_without_gpu_fails_cleanly(grlib):
     if torch.cuda.is_available():
         pytest.skip("a GPU is present")
     h = ctypes.c_void_p()
-    st = grlib.gr_context_create(0, ctypes.byref(h))
+    st = grlib.gr_context_create(0, None, ctypes.byref(h))
     assert st != 0 and not h.value
 
 
