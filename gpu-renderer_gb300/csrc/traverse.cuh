@@ -568,10 +568,12 @@ __device__ __forceinline__ bool trace_step(Lane& L, int2* s_stack, int2* l_stack
 }
 
 // A warp refills its idle lanes once at least REFILL of them are idle. The
-// ray-query kernels use 4 (a ray loads in two 16-byte reads); the render's
-// queue kernels use 8 (a queued path also looks up its job and scene).
+// ray-query kernels use 4 (a ray loads in two 16-byte reads; 2, 6 and 8
+// measured slower); the render's queue kernels use 12 (a queued path also looks
+// up its job and scene; 4, 6, 8, 16 and 20 measured slower on the Cornell and
+// glossy renders).
 constexpr int kRefillRays = 4;
-constexpr int kRefillQueue = 8;
+constexpr int kRefillQueue = 12;
 
 // Persistent dynamic-fetch loop. `Src` supplies the work:
 //   uint64_t n                                        number of rays
