@@ -141,13 +141,13 @@ struct BvhBuffers {
     uint32_t count8 = 0;             // 8-wide nodes
     uint32_t tris8_count = 0;        // triangles in tris8
     DevBuf scratch;                  // transient build state
-    DevBuf meta;                     // small device header (root, unique count, error word)
+    DevBuf meta;                     // small device header (root, error word, centroid bounds)
 };
 
 // Host-visible layout of the small per-BVH device header.
 struct BvhMeta {
     uint32_t root;
-    uint32_t unique;
+    uint32_t pad0;
     uint32_t err;
     uint32_t pad;
     float cbox[6];  // centroid bounds used for the Morton codes

@@ -1,6 +1,7 @@
-// GPU LBVH build: Morton codes -> onesweep radix sort -> equal-code runs ->
-// Karras radix tree over unique codes + midpoint subtrees inside runs ->
-// bottom-up atomic refit. Produces the same tree as the reference's host
+// GPU LBVH build: Morton codes -> onesweep radix sort -> the split level of
+// each gap between sorted codes (the radix tree's over unique codes, midpoint
+// subtrees inside runs of equal codes) -> one bottom-up pass that links the
+// nodes and fits their boxes. Produces the same tree as the reference's host
 // LBVH_build (src/renderer/bvh.h:186-221) with ties kept in input order.
 //
 // Every float operation that feeds a Morton code is written with an explicit
@@ -341,164 +342,74 @@ __global__ void __launch_bounds__(kOsThreads) k_onesweep(const uint32_t* __restr
     }
 }
 
-// ---- 4. equal-code runs (single-pass scan with decoupled look-back) ------------
+// ---- 4. split levels of the gaps -----------------------------------------------------
+// Gap g lies between sorted positions g and g + 1; internal nodes are stored at
+// the gap they split. Its level orders the gaps by depth in the tree:
+//   - codes differ: the length of their common prefix, clz(code[g] ^ code[g + 1])
+//     (2..31: the codes have 30 bits), the radix tree's split level (Karras,
+//     HPG 2012; the reference's split search, bvh.h:125-160);
+//   - codes equal (a run of equal codes, split at its midpoint recursively,
+//     bvh.h:162-165): 32 + the depth of g's node in the run's midpoint subtree,
+//     so every gap inside a run ranks below the run's outer gaps.
+// A node covering positions [lo, hi] is a child of the node at one of its two
+// outer gaps, lo - 1 or hi: in a binary tree over ordered leaves both outer gaps
+// belong to ancestors, the parent is the deeper one, and two outer gaps never
+// tie (for distinct codes the shared prefix of lo - 1 and hi + 1 with the
+// range would have to differ at the same bit in opposite directions). So the
+// level of the two outer gaps alone picks every node's parent (the bottom-up
+// form of the same radix tree: Apetrei, EG 2014).
 
-constexpr int kRunThreads = 256;
-constexpr int kRunItems = 16;
-constexpr int kRunTile = kRunThreads * kRunItems;
-
-__global__ void __launch_bounds__(kRunThreads) k_runs(const uint32_t* __restrict__ code, uint32_t n,
-                                                      uint32_t* __restrict__ ucode, uint32_t* __restrict__ run_start,
-                                                      uint32_t* __restrict__ uidx, uint32_t* __restrict__ status,
-                                                      uint32_t* __restrict__ tile_ctr, BvhMeta* meta,
-                                                      uint32_t* __restrict__ err) {
-    __shared__ uint32_t s_warp[kRunThreads / 32];
-    __shared__ uint32_t s_tile, s_excl;
-    if (threadIdx.x == 0) s_tile = atomicAdd(tile_ctr, 1u);
-    __syncthreads();
-    const uint32_t tile = s_tile;
-    const uint64_t first = (uint64_t)tile * kRunTile + (uint64_t)threadIdx.x * kRunItems;
-    uint32_t heads = 0;
-    bool head[kRunItems];
-#pragma unroll
-    for (int j = 0; j < kRunItems; ++j) {
-        const uint64_t i = first + j;
-        head[j] = i < n && (i == 0 || code[i] != code[i - 1]);
-        heads += head[j];
+// Depth of gap g (codes g and g + 1 equal) in the midpoint subtree of its run:
+// the run's ends by exponential then binary search over the sorted codes, then
+// a descent from the run's root split.
+__device__ __forceinline__ uint32_t run_depth(const uint32_t* __restrict__ code, uint32_t n, uint32_t g,
+                                              uint32_t* __restrict__ err) {
+    const uint32_t c = code[g];
+    int64_t good = g, bad = -1;  // code[good] == c; code[bad] < c (or bad = -1)
+    for (int64_t step = 1;; step <<= 1) {
+        const int64_t t = good - step;
+        if (t < 0) break;
+        if (code[t] != c) { bad = t; break; }
+        good = t;
     }
-    uint32_t tot;
-    const uint32_t off = block_exclusive_scan<kRunThreads>(heads, s_warp, &tot);
-    if (threadIdx.x == 0) {
-        uint32_t* st = status + tile;
-        uint32_t excl = 0;
-        if (tile == 0) {
-            st_release(st, kFlagInc | tot);
-        } else {
-            st_release(st, kFlagAgg | tot);
-            excl = lookback(status, 1, (int64_t)tile, kSpinLimit, err);
-            st_release(st, kFlagInc | ((excl + tot) & kCountMask));
-        }
-        s_excl = excl;
-        const uint64_t tiles = ((uint64_t)n + kRunTile - 1) / kRunTile;
-        if (tile + 1 == tiles) {
-            meta->unique = excl + tot;
-            run_start[excl + tot] = n;  // sentinel: run u spans [run_start[u], run_start[u+1])
-        }
+    while (good - bad > 1) {
+        const int64_t mid = bad + ((good - bad) >> 1);
+        if (code[mid] == c) good = mid; else bad = mid;
     }
-    __syncthreads();
-    uint32_t u = s_excl + off;  // number of heads before this thread's first item
-#pragma unroll
-    for (int j = 0; j < kRunItems; ++j) {
-        const uint64_t i = first + j;
-        if (i < n) {
-            if (head[j]) {
-                ucode[u] = code[i];
-                run_start[u] = (uint32_t)i;
-                ++u;
-            }
-            uidx[i] = u - 1;
+    const uint32_t s = (uint32_t)good;
+    int64_t good_r = (int64_t)g + 1, bad_r = n;  // code[good_r] == c; code[bad_r] > c (or n)
+    for (int64_t step = 1;; step <<= 1) {
+        const int64_t t = good_r + step;
+        if (t >= (int64_t)n) break;
+        if (code[t] != c) { bad_r = t; break; }
+        good_r = t;
+    }
+    while (bad_r - good_r > 1) {
+        const int64_t mid = good_r + ((bad_r - good_r) >> 1);
+        if (code[mid] == c) good_r = mid; else bad_r = mid;
+    }
+    uint32_t a = s, b = (uint32_t)good_r;  // the run, inclusive
+    uint32_t G = a + ((b - a + 1) >> 1) - 1, depth = 0;
+    while (G != g) {
+        if (g < G) b = G; else a = G + 1;
+        G = a + ((b - a + 1) >> 1) - 1;
+        if (++depth > 32) {
+            atomicOr(err, ERR_RANGE);
+            break;
         }
     }
+    return depth;
 }
 
-// ---- 5. hierarchy ------------------------------------------------------------------
-
-__device__ __forceinline__ int delta(const uint32_t* __restrict__ uc, int i, int j, int m) {
-    if (j < 0 || j >= m) return -1;
-    return __clz(uc[i] ^ uc[j]);  // unique codes: never equal for i != j
-}
-
-// Root (or leaf) code of the midpoint subtree of run u.
-__device__ __forceinline__ int32_t run_root(const uint32_t* __restrict__ run_start, uint32_t u) {
-    const uint32_t s = run_start[u], len = run_start[u + 1] - s;
-    return len == 1 ? ~(int32_t)s : (int32_t)(s + (len >> 1) - 1);
-}
-
-// Karras (HPG 2012) split finding over the unique codes. Each unique internal
-// node k records its split gamma and whether its children are unique leaves.
-__global__ void __launch_bounds__(kBlock) k_karras(const uint32_t* __restrict__ ucode,
-                                                   const uint32_t* __restrict__ run_start, const BvhMeta* __restrict__ meta,
-                                                   uint32_t* __restrict__ kgamma, uint32_t* __restrict__ gap_of) {
-    const int m = (int)meta->unique;
-    for (int i = blockIdx.x * kBlock + threadIdx.x; i < m - 1; i += gridDim.x * kBlock) {
-        const int d = (delta(ucode, i, i + 1, m) - delta(ucode, i, i - 1, m)) >= 0 ? 1 : -1;
-        const int dmin = delta(ucode, i, i - d, m);
-        int lmax = 2;
-        while (delta(ucode, i, i + lmax * d, m) > dmin) lmax <<= 1;
-        int l = 0;
-        for (int t = lmax >> 1; t >= 1; t >>= 1)
-            if (delta(ucode, i, i + (l + t) * d, m) > dmin) l += t;
-        const int j = i + l * d;
-        const int dnode = delta(ucode, i, j, m);
-        int s = 0;
-        for (int div = 2;; div <<= 1) {
-            const int t = (l + div - 1) / div;
-            if (delta(ucode, i, i + (s + t) * d, m) > dnode) s += t;
-            if (t == 1) break;
-        }
-        const int gamma = i + s * d + min(d, 0);
-        const int lo = min(i, j), hi = max(i, j);
-        // bit 31: left child is a unique leaf; bit 30: right child is a unique leaf
-        kgamma[i] = (uint32_t)gamma | (lo == gamma ? 0x80000000u : 0u) | (hi == gamma + 1 ? 0x40000000u : 0u);
-        gap_of[i] = run_start[gamma + 1] - 1;
-    }
-}
-
-__global__ void __launch_bounds__(kBlock) k_link(const uint32_t* __restrict__ kgamma, const uint32_t* __restrict__ gap_of,
-                                                 const uint32_t* __restrict__ run_start, BvhMeta* meta, Node* nodes,
-                                                 uint32_t* __restrict__ parent_leaf) {
-    const int m = (int)meta->unique;
-    for (int k = blockIdx.x * kBlock + threadIdx.x; k < m - 1; k += gridDim.x * kBlock) {
-        const uint32_t g = kgamma[k];
-        const uint32_t gamma = g & 0x3FFFFFFFu;
-        const uint32_t G = gap_of[k];
-        const int32_t left = (g & 0x80000000u) ? run_root(run_start, gamma) : (int32_t)gap_of[gamma];
-        const int32_t right = (g & 0x40000000u) ? run_root(run_start, gamma + 1) : (int32_t)gap_of[gamma + 1];
-        nodes[G].q3.x = left;
-        nodes[G].q3.y = right;
-        nodes[G].q3.w = 0;
-        if (left >= 0) nodes[left].q3.z = (int32_t)G; else parent_leaf[~left] = G;
-        if (right >= 0) nodes[right].q3.z = (int32_t)G; else parent_leaf[~right] = G;
-        if (k == 0) {
-            nodes[G].q3.z = (int32_t)kNoNode;
-            meta->root = G;
-        }
-    }
-}
-
-// Internal nodes inside equal-code runs: the run [s, e) is split at its
-// midpoint recursively (bvh.h:162-165). Each gap g inside a run finds its node
-// by descending from the run's root.
-__global__ void __launch_bounds__(kBlock) k_run_nodes(const uint32_t* __restrict__ code, uint32_t n,
-                                                      const uint32_t* __restrict__ uidx,
-                                                      const uint32_t* __restrict__ run_start, BvhMeta* meta, Node* nodes,
-                                                      uint32_t* __restrict__ parent_leaf, uint32_t* __restrict__ err) {
+__global__ void __launch_bounds__(kBlock) k_gaps(const uint32_t* __restrict__ code, uint32_t n,
+                                                 uint8_t* __restrict__ level, uint32_t* __restrict__ err) {
     for (uint32_t g = blockIdx.x * kBlock + threadIdx.x; g + 1 < n; g += gridDim.x * kBlock) {
-        if (code[g] != code[g + 1]) continue;
-        const uint32_t u = uidx[g];
-        uint32_t a = run_start[u], b = run_start[u + 1] - 1;  // inclusive leaf range
-        uint32_t G = a + ((b - a + 1) >> 1) - 1;
-        if (G == g && meta->unique == 1) {
-            nodes[G].q3.z = (int32_t)kNoNode;
-            meta->root = G;
-        }
-        int guard = 0;
-        while (G != g) {
-            if (g < G) b = G; else a = G + 1;
-            G = a + ((b - a + 1) >> 1) - 1;
-            if (++guard > 64) { atomicOr(err, ERR_RANGE); break; }
-        }
-        const int32_t left = (a == G) ? ~(int32_t)a : (int32_t)(a + ((G - a + 1) >> 1) - 1);
-        const int32_t right = (G + 1 == b) ? ~(int32_t)b : (int32_t)(G + 1 + ((b - G) >> 1) - 1);
-        nodes[G].q3.x = left;
-        nodes[G].q3.y = right;
-        nodes[G].q3.w = 0;
-        if (left >= 0) nodes[left].q3.z = (int32_t)G; else parent_leaf[~left] = G;
-        if (right >= 0) nodes[right].q3.z = (int32_t)G; else parent_leaf[~right] = G;
+        const uint32_t c0 = code[g], c1 = code[g + 1];
+        level[g] = (uint8_t)(c0 != c1 ? (uint32_t)__clz(c0 ^ c1) : 32u + run_depth(code, n, g, err));
     }
 }
 
-// ---- 6. refit + leaf-order triangles ---------------------------------------------
+// ---- 5. hierarchy, boxes and leaf-order triangles in one bottom-up pass ------------
 
 __device__ __forceinline__ void put_child_box(Node* nd, int slot, const Box3& b) {
     float4* q = reinterpret_cast<float4*>(nd);
@@ -515,9 +426,9 @@ __device__ __forceinline__ Box3 get_child_box_l2(const Node* nd, int slot) {
 }
 
 // Counter increment with acquire-release semantics at GPU scope: this thread's
-// earlier writes (its child box) are visible to the thread that sees the
-// incremented count, and the sibling's box, written before its own increment,
-// is visible to this thread's later reads. One ordered atomic in place of two
+// earlier writes (its child box and link) are visible to the thread that sees
+// the incremented count, and the sibling's, written before its own increment,
+// are visible to this thread's later reads. One ordered atomic in place of two
 // full fences around a relaxed one.
 __device__ __forceinline__ uint32_t atomic_add_acq_rel(uint32_t* p, uint32_t v) {
     uint32_t old;
@@ -526,9 +437,9 @@ __device__ __forceinline__ uint32_t atomic_add_acq_rel(uint32_t* p, uint32_t v) 
 }
 
 // Counter increment with acquire-release semantics at CTA scope on a
-// shared-memory word: orders this thread's global writes (its child box)
-// before the increment and the sibling's box, written by another thread of the
-// block before its increment, before this thread's later reads.
+// shared-memory word: orders this thread's global writes (its child box and
+// link) before the increment and the sibling's, written by another thread of
+// the block before its increment, before this thread's later reads.
 __device__ __forceinline__ uint32_t atomic_add_acq_rel_cta(uint32_t* p, uint32_t v) {
     uint32_t old;
     const uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
@@ -554,48 +465,95 @@ __device__ __forceinline__ void box_union(Box3& a, const Box3& b) {
     }
 }
 
-// Arrival at internal node `node` whose child box this thread has written into
-// slot `slot` (carrying that box): one GPU-scope ordered atomic on the node's
-// counter; the second arrival unions the two child boxes, writes the result
-// into its parent's slot and goes on up.
-__device__ __forceinline__ void climb_global(Node* nodes, uint32_t node, int slot, Box3 box,
-                                             uint32_t* __restrict__ counters, uint32_t* __restrict__ err) {
-    int guard = 0;
-    for (;;) {
-        Node* nd = nodes + node;
-        if (atomic_add_acq_rel(&counters[node], 1u) == 0) return;  // sibling not done yet
-        box_union(box, get_child_box_l2(nd, slot ^ 1));
-        const uint32_t parent = (uint32_t)__ldcg(&nd->q3.z);
-        if (parent == kNoNode) return;
-        Node* pn = nodes + parent;
-        slot = (__ldcg(&pn->q3.x) == (int32_t)node) ? 0 : 1;
-        put_child_box(pn, slot, box);
-        node = parent;
-        if (++guard > 128) {
-            atomicOr(err, ERR_RANGE);
+// A finished subtree on its way up: its id (~position for a leaf, else its
+// gap), the sorted positions it covers and its box.
+struct Sub {
+    int32_t me;
+    uint32_t lo, hi;
+    Box3 box;
+};
+
+// Where the climb writes: the node array, the parent of each leaf, and per
+// internal node the outer end of each child's range (far[2G] = the left
+// child's first position, far[2G + 1] = the right child's last).
+struct ClimbOut {
+    Node* nodes;
+    uint32_t* parent_leaf;
+    uint32_t* far;
+    BvhMeta* meta;
+    uint32_t* counters;
+    uint32_t* err;
+};
+
+// The finished subtree `s` (not the whole range) hangs below gap `G` in slot
+// `slot` (0 = left): its box and id go into the parent's slot, its outer end
+// into far, and the parent's index into its own record.
+__device__ __forceinline__ void attach(const ClimbOut& o, const Sub& s, uint32_t G, int slot) {
+    Node* pn = o.nodes + G;
+    put_child_box(pn, slot, s.box);
+    reinterpret_cast<int32_t*>(&pn->q3)[slot] = s.me;
+    o.far[2 * G + slot] = slot == 0 ? s.lo : s.hi;
+    if (s.me >= 0) *reinterpret_cast<int2*>(&o.nodes[s.me].q3.z) = make_int2((int32_t)G, 0);
+    else o.parent_leaf[~s.me] = G;
+}
+
+// Parent gap of a subtree covering [lo, hi] (not the whole range) and the slot
+// the subtree takes there.
+__device__ __forceinline__ uint32_t parent_gap(const uint8_t* __restrict__ level, uint32_t lo, uint32_t hi,
+                                               uint32_t n, int& slot) {
+    if (lo == 0 || (hi + 1 < n && __ldg(level + hi) > __ldg(level + lo - 1))) {
+        slot = 0;
+        return hi;
+    }
+    slot = 1;
+    return lo - 1;
+}
+
+// The whole range is finished: `s` is the root.
+__device__ __forceinline__ void set_root(const ClimbOut& o, const Sub& s) {
+    *reinterpret_cast<int2*>(&o.nodes[s.me].q3.z) = make_int2((int32_t)kNoNode, 0);
+    o.meta->root = (uint32_t)s.me;
+}
+
+// Climb from finished subtree `s` with GPU-scope counters: at each parent the
+// first arrival stops, the second unions its sibling's box and range and goes
+// on up.
+__device__ __forceinline__ void climb_global(const ClimbOut& o, const uint8_t* __restrict__ level, uint32_t n, Sub s) {
+    for (int guard = 0;; ++guard) {
+        if (s.lo == 0 && s.hi + 1 == n) {
+            set_root(o, s);
             return;
         }
+        if (guard > 128) {
+            atomicOr(o.err, ERR_RANGE);
+            return;
+        }
+        int slot;
+        const uint32_t G = parent_gap(level, s.lo, s.hi, n, slot);
+        attach(o, s, G, slot);
+        if (atomic_add_acq_rel(&o.counters[G], 1u) == 0) return;  // sibling not done yet
+        box_union(s.box, get_child_box_l2(o.nodes + G, slot ^ 1));
+        if (slot == 0) s.hi = __ldcg(&o.far[2 * G + 1]); else s.lo = __ldcg(&o.far[2 * G]);
+        s.me = (int32_t)G;
     }
 }
 
-// Refit and leaf-order triangles. A block takes kRefitChunk sorted positions
-// (one block per chunk, so a block held up by a long climb delays no other
-// chunk), one per thread: the thread writes the position's triangle and
-// leaf box and walks up. Internal nodes are indexed by the gap they split, so
-// the chunk owns the nodes [base, base + kRefitChunk); arrivals at those are
-// counted in shared memory (an ordered atomic at block scope, not at GPU
-// scope), so every node whose subtree lies inside the chunk is finished
-// without a global atomic. An arrival at another chunk's node counts on that
-// node's global counter and goes on globally. After the chunk, a node of it
-// reached once adds its one arrival to the global counter: whichever of that
-// and the node's other (global) arrival comes second finishes the node, so
-// exactly one thread goes on. min / max are exact, so the boxes do not depend
-// on the order of arrivals.
-__global__ void __launch_bounds__(kRefitChunk) k_refit(const float* __restrict__ verts, uint32_t n,
+// One bottom-up pass builds the tree: a block takes kRefitChunk sorted
+// positions (one block per chunk, so a block held up by a long climb delays no
+// other chunk), one per thread; the thread writes the position's triangle and
+// leaf box and climbs, writing each node's links, parent and child boxes as it
+// goes. The chunk owns the gaps [base, base + kRefitChunk); arrivals there are
+// counted in shared memory (an ordered atomic at block scope), so every node
+// whose subtree lies inside the chunk is finished without a global atomic. An
+// arrival at another chunk's node counts on that node's global counter and
+// goes on globally. After the chunk, a node of it reached once adds its one
+// arrival to the global counter: whichever of that and the node's other
+// (global) arrival comes second finishes the node, so exactly one thread goes
+// on. min / max are exact, so the boxes do not depend on the order of arrivals.
+__global__ void __launch_bounds__(kRefitChunk) k_climb(const float* __restrict__ verts, uint32_t n,
                                                        const uint32_t* __restrict__ prim,
-                                                       const uint32_t* __restrict__ parent_leaf, Node* nodes,
-                                                       Tri* __restrict__ tris, uint32_t* __restrict__ counters,
-                                                       uint32_t* __restrict__ err) {
+                                                       const uint8_t* __restrict__ level, ClimbOut o,
+                                                       Tri* __restrict__ tris) {
     __shared__ uint32_t s_cnt[kRefitChunk];
     const uint32_t chunks = (n + kRefitChunk - 1) / kRefitChunk;
     for (uint32_t c = blockIdx.x; c < chunks; c += gridDim.x) {  // block-uniform
@@ -614,62 +572,67 @@ __global__ void __launch_bounds__(kRefitChunk) k_refit(const float* __restrict__
             t.b = make_float4(a[3], a[4], a[5], 0.0f);
             t.c = make_float4(a[6], a[7], a[8], 0.0f);
             tris[p] = t;
-            Box3 box;
+            Sub s;
+            s.me = ~(int32_t)p;
+            s.lo = s.hi = p;
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
-                box.lo[k] = fminf(fminf(a[k], a[3 + k]), a[6 + k]);
-                box.hi[k] = fmaxf(fmaxf(a[k], a[3 + k]), a[6 + k]);
+                s.box.lo[k] = fminf(fminf(a[k], a[3 + k]), a[6 + k]);
+                s.box.hi[k] = fmaxf(fmaxf(a[k], a[3 + k]), a[6 + k]);
             }
             if (n == 1) {
                 // one triangle: a single node whose two children are the same leaf
                 Node nd;
-                nd.q0 = make_float4(box.lo[0], box.hi[0], box.lo[1], box.hi[1]);
+                nd.q0 = make_float4(s.box.lo[0], s.box.hi[0], s.box.lo[1], s.box.hi[1]);
                 nd.q1 = nd.q0;
-                nd.q2 = make_float4(box.lo[2], box.hi[2], box.lo[2], box.hi[2]);
+                nd.q2 = make_float4(s.box.lo[2], s.box.hi[2], s.box.lo[2], s.box.hi[2]);
                 nd.q3 = make_int4(~0, ~0, (int32_t)kNoNode, 0);
-                nodes[0] = nd;
+                o.nodes[0] = nd;
+                o.meta->root = 0;
             } else {
-                int32_t me = ~(int32_t)p;
-                uint32_t node = parent_leaf[p];
-                int guard = 0;
-                while (node != kNoNode) {
-                    Node* nd = nodes + node;
-                    const int slot = (nd->q3.x == me) ? 0 : 1;
-                    put_child_box(nd, slot, box);
-                    if (node - base >= (uint32_t)kRefitChunk) {  // another chunk's node
-                        climb_global(nodes, node, slot, box, counters, err);
+                for (int guard = 0;; ++guard) {
+                    if (s.lo == 0 && s.hi + 1 == n) {
+                        set_root(o, s);
                         break;
                     }
-                    if (atomic_add_acq_rel_cta(&s_cnt[node - base], 1u) == 0) break;  // sibling not done yet
-                    box_union(box, get_child_box(nd, slot ^ 1));
-                    me = (int32_t)node;
-                    node = (uint32_t)nd->q3.z;
-                    if (++guard > 128) {
-                        atomicOr(err, ERR_RANGE);
+                    if (guard > 128) {
+                        atomicOr(o.err, ERR_RANGE);
                         break;
                     }
+                    int slot;
+                    const uint32_t G = parent_gap(level, s.lo, s.hi, n, slot);
+                    attach(o, s, G, slot);
+                    if (G - base >= (uint32_t)kRefitChunk) {  // another chunk's node
+                        if (atomic_add_acq_rel(&o.counters[G], 1u) == 0) break;
+                        box_union(s.box, get_child_box_l2(o.nodes + G, slot ^ 1));
+                        if (slot == 0) s.hi = __ldcg(&o.far[2 * G + 1]); else s.lo = __ldcg(&o.far[2 * G]);
+                        s.me = (int32_t)G;
+                        climb_global(o, level, n, s);
+                        break;
+                    }
+                    if (atomic_add_acq_rel_cta(&s_cnt[G - base], 1u) == 0) break;  // sibling not done yet
+                    box_union(s.box, get_child_box(o.nodes + G, slot ^ 1));
+                    if (slot == 0) s.hi = o.far[2 * G + 1]; else s.lo = o.far[2 * G];
+                    s.me = (int32_t)G;
                 }
             }
         }
         __syncthreads();
         // this chunk's nodes reached once: their one arrival joins the global count
-        if (p + 1 < n && s_cnt[threadIdx.x] == 1 && atomic_add_acq_rel(&counters[p], 1u) == 1) {
-            Node* nd = nodes + p;  // node p: both children are done, their boxes are in its slots
-            Box3 box = get_child_box_l2(nd, 0);
-            box_union(box, get_child_box_l2(nd, 1));
-            const uint32_t parent = (uint32_t)__ldcg(&nd->q3.z);
-            if (parent != kNoNode) {
-                Node* pn = nodes + parent;
-                const int slot = (__ldcg(&pn->q3.x) == (int32_t)p) ? 0 : 1;
-                put_child_box(pn, slot, box);
-                climb_global(nodes, parent, slot, box, counters, err);
-            }
+        if (p + 1 < n && s_cnt[threadIdx.x] == 1 && atomic_add_acq_rel(&o.counters[p], 1u) == 1) {
+            Sub s;  // node p: both children are done, their boxes and ends are in its record
+            s.me = (int32_t)p;
+            s.box = get_child_box_l2(o.nodes + p, 0);
+            box_union(s.box, get_child_box_l2(o.nodes + p, 1));
+            s.lo = __ldcg(&o.far[2 * p]);
+            s.hi = __ldcg(&o.far[2 * p + 1]);
+            climb_global(o, level, n, s);
         }
         __syncthreads();
     }
 }
 
-// ---- 7. reference-layout export (parity only) -------------------------------------
+// ---- 6. reference-layout export (parity only) -------------------------------------
 // Preorder index of a node covering leaves [first, ...] = 2*first + number of
 // left turns on the path from the root.
 
@@ -734,10 +697,11 @@ __global__ void __launch_bounds__(kBlock) k_export_ref(const Node* __restrict__ 
 size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
 struct Scratch {
-    uint32_t *keys_alt, *vals_alt, *uidx, *ucode, *run_start, *kgamma, *gap_of, *parent_leaf, *counters;
-    uint32_t *hist, *offs, *os_status, *run_status, *tile_ctr, *err;
+    uint32_t *keys_alt, *vals_alt, *parent_leaf, *far, *counters;
+    uint8_t* level;
+    uint32_t *hist, *offs, *os_status, *tile_ctr, *err;
     float* partial;
-    size_t zero_bytes;  // bytes from hist up to the end of the zeroed region
+    size_t zero_bytes;  // bytes from the counters up to the end of the zeroed region
     void* zero_base;
 };
 
@@ -745,7 +709,6 @@ constexpr int kPartials = 1024;
 
 size_t scratch_layout(uint32_t n, char* base, Scratch* s) {
     const uint64_t os_tiles = ((uint64_t)n + kOsTile - 1) / kOsTile;
-    const uint64_t run_tiles = ((uint64_t)n + kRunTile - 1) / kRunTile;
     size_t off = 0;
     auto take = [&](size_t bytes) {
         char* p = base ? base + off : nullptr;
@@ -755,12 +718,9 @@ size_t scratch_layout(uint32_t n, char* base, Scratch* s) {
     const size_t w = 4ull * n;
     s->keys_alt = (uint32_t*)take(w);
     s->vals_alt = (uint32_t*)take(w);
-    s->uidx = (uint32_t*)take(w);
-    s->ucode = (uint32_t*)take(w);
-    s->run_start = (uint32_t*)take(w + 4);
-    s->kgamma = (uint32_t*)take(w);
-    s->gap_of = (uint32_t*)take(w);
     s->parent_leaf = (uint32_t*)take(w);
+    s->far = (uint32_t*)take(2 * w);
+    s->level = (uint8_t*)take(n);
     s->partial = (float*)take(sizeof(float) * 6 * kPartials);
     // everything from here on is zeroed before each build
     const size_t zstart = off;
@@ -768,7 +728,6 @@ size_t scratch_layout(uint32_t n, char* base, Scratch* s) {
     s->hist = (uint32_t*)take(4 * 256 * 4);
     s->offs = (uint32_t*)take(4 * 256 * 4);
     s->os_status = (uint32_t*)take(4ull * os_tiles * 256 * 4);
-    s->run_status = (uint32_t*)take(run_tiles * 4);
     s->tile_ctr = (uint32_t*)take(16 * 4);
     s->err = (uint32_t*)take(4);
     s->zero_base = base ? base + zstart : nullptr;
@@ -805,8 +764,9 @@ namespace {
 // one both the allocating build and the no-allocation build run. Zeroes the
 // scratch region that must start at zero, then centroid bounds, Morton codes
 // and histograms, four onesweep passes (the sorted codes and triangle ids end
-// in `code` / `prim`), equal-code runs, Karras splits, links, run subtrees and
-// the refit, and folds the build's error word into the header.
+// in `code` / `prim`), the gaps' split levels and the bottom-up pass that links
+// the nodes and fits their boxes, and folds the build's error word into the
+// header.
 cudaError_t launch_build(const float* d_verts, uint32_t n, const Scratch& s, Node* nodes, Tri* tris, uint32_t* code,
                          uint32_t* prim, BvhMeta* meta, int num_sms, cudaStream_t st) {
     cudaError_t e;
@@ -832,15 +792,10 @@ cudaError_t launch_build(const float* d_verts, uint32_t n, const Scratch& s, Nod
         std::swap(vin, vout);
     }
     // four passes: the sorted data is back in code/prim
-    const uint32_t run_tiles = (n + kRunTile - 1) / kRunTile;
-    k_runs<<<run_tiles, kRunThreads, 0, st>>>(code, n, s.ucode, s.run_start, s.uidx, s.run_status, s.tile_ctr + 4,
-                                              meta, s.err);
-    k_karras<<<grid, kBlock, 0, st>>>(s.ucode, s.run_start, meta, s.kgamma, s.gap_of);
-    k_link<<<grid, kBlock, 0, st>>>(s.kgamma, s.gap_of, s.run_start, meta, nodes, s.parent_leaf);
-    k_run_nodes<<<grid, kBlock, 0, st>>>(code, n, s.uidx, s.run_start, meta, nodes, s.parent_leaf, s.err);
+    k_gaps<<<grid, kBlock, 0, st>>>(code, n, s.level, s.err);
     const uint32_t chunks = (n + kRefitChunk - 1) / kRefitChunk;
-    k_refit<<<chunks, kRefitChunk, 0, st>>>(
-        d_verts, n, prim, s.parent_leaf, nodes, tris, s.counters, s.err);
+    const ClimbOut out{nodes, s.parent_leaf, s.far, meta, s.counters, s.err};
+    k_climb<<<chunks, kRefitChunk, 0, st>>>(d_verts, n, prim, s.level, out, tris);
     // fold the build's error word into the header the host reads
     if ((e = cudaMemcpyAsync(&meta->err, s.err, 4, cudaMemcpyDeviceToDevice, st)) != cudaSuccess) return e;
     return cudaGetLastError();
@@ -886,8 +841,8 @@ cudaError_t lbvh_export_ref(const BvhBuffers& b, uint32_t n, uint32_t* d_ref_nod
 // Some callers cannot call cudaMalloc: plug-ins whose host application owns
 // every byte of device memory (and hands the plug-in only the buffers of a
 // call), and latency-critical loops in which a cudaMalloc / cudaFree would
-// synchronise the device. For them the build's scratch (sort buffers, run
-// arrays, parent links, refit counters, look-back words) lives in one
+// synchronise the device. For them the build's scratch (sort buffers, split
+// levels, parent links, node counters, look-back words) lives in one
 // file-scope device array, sized for kStaticMaxTriangles triangles; the caller
 // passes the input soup and every output buffer.
 //
@@ -903,15 +858,16 @@ constexpr uint32_t kStaticMaxTriangles = 1u << 17;  // 131,072 triangles
 
 constexpr size_t round256(size_t x) { return (x + 255) & ~size_t(255); }
 
-// Upper bound of scratch_layout(kStaticMaxTriangles): nine per-triangle word
-// arrays (+1 word), the centroid partials, histograms, the sort's and the run
-// compaction's look-back words (per tile of each), tile counters and the error
-// word, each rounded up to 256 bytes as scratch_layout rounds them.
+// Upper bound of scratch_layout(kStaticMaxTriangles): four per-triangle word
+// arrays (sort buffers, leaf parents, node counters), the two range ends per
+// node, one level byte per gap, the centroid partials, histograms, the sort's
+// look-back words (per tile of each pass), tile counters and the error word,
+// each rounded up to 256 bytes as scratch_layout rounds them.
 constexpr size_t kStaticOsTiles = (kStaticMaxTriangles + kOsTile - 1) / kOsTile;
-constexpr size_t kStaticRunTiles = (kStaticMaxTriangles + kRunTile - 1) / kRunTile;
 constexpr size_t kStaticScratchBytes =
-    9 * round256((size_t)kStaticMaxTriangles * 4 + 4) + round256(sizeof(float) * 6 * kPartials) + 2 * 4096 +
-    round256(4 * kStaticOsTiles * 256 * 4) + round256(kStaticRunTiles * 4) + round256(16 * 4) + round256(4);
+    4 * round256((size_t)kStaticMaxTriangles * 4) + round256((size_t)kStaticMaxTriangles * 8) +
+    round256(kStaticMaxTriangles) + round256(sizeof(float) * 6 * kPartials) + 2 * 4096 +
+    round256(4 * kStaticOsTiles * 256 * 4) + round256(16 * 4) + round256(4);
 
 static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
 
