@@ -65,30 +65,31 @@ __device__ __forceinline__ uint32_t spread10(uint32_t x) {
     return x;
 }
 
-// Block-wide exclusive scan of one uint32 per thread (blockDim.x <= 1024).
-template <int THREADS>
-__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* s_warp, uint32_t* total) {
+// Block-wide exclusive scan of one value per thread (blockDim.x <= 1024);
+// `s_warp` holds THREADS / 32 values.
+template <int THREADS, class T>
+__device__ __forceinline__ T block_exclusive_scan(T v, T* s_warp, T* total) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint32_t x = v;
+    T x = v;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-        uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+        T y = __shfl_up_sync(0xFFFFFFFFu, x, o);
         if (lane >= o) x += y;
     }
     if (lane == 31) s_warp[warp] = x;
     __syncthreads();
     if (warp == 0) {
         constexpr int W = THREADS / 32;
-        uint32_t w = lane < W ? s_warp[lane] : 0;
+        T w = lane < W ? s_warp[lane] : T(0);
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            uint32_t y = __shfl_up_sync(0xFFFFFFFFu, w, o);
+            T y = __shfl_up_sync(0xFFFFFFFFu, w, o);
             if (lane >= o) w += y;
         }
         if (lane < W) s_warp[lane] = w;  // inclusive warp totals
     }
     __syncthreads();
-    uint32_t base = warp > 0 ? s_warp[warp - 1] : 0;
+    T base = warp > 0 ? s_warp[warp - 1] : T(0);
     *total = s_warp[THREADS / 32 - 1];
     __syncthreads();
     return base + x - v;
@@ -96,8 +97,37 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* s
 
 // ---- 1. centroid bounds -------------------------------------------------------
 
-__global__ void __launch_bounds__(kBlock) k_centroid_partials(const float* __restrict__ verts, uint32_t n,
-                                                              float* __restrict__ partial) {
+// Min / max of the six bound values over the block (lo in 0-2, hi in 3-5);
+// threads 0-5 return them.
+__device__ __forceinline__ float block_bounds(float lo[3], float hi[3]) {
+    __shared__ float s[6][kBlock / 32];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        for (int o = 16; o > 0; o >>= 1) {
+            lo[k] = fminf(lo[k], __shfl_xor_sync(0xFFFFFFFFu, lo[k], o));
+            hi[k] = fmaxf(hi[k], __shfl_xor_sync(0xFFFFFFFFu, hi[k], o));
+        }
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) {
+        for (int k = 0; k < 3; ++k) { s[k][warp] = lo[k]; s[3 + k][warp] = hi[k]; }
+    }
+    __syncthreads();
+    float r = 0.0f;
+    if (threadIdx.x < 6) {
+        const int k = threadIdx.x;
+        r = s[k][0];
+        for (int w = 1; w < kBlock / 32; ++w) r = k < 3 ? fminf(r, s[k][w]) : fmaxf(r, s[k][w]);
+    }
+    return r;
+}
+
+// Centroid bounds: each block reduces its share of the triangles to a partial
+// box; the last block to finish (counted on `done`) folds the partials into
+// the header (min / max do not depend on the order).
+__global__ void __launch_bounds__(kBlock) k_centroid(const float* __restrict__ verts, uint32_t n,
+                                                     float* __restrict__ partial, uint32_t* __restrict__ done,
+                                                     BvhMeta* meta) {
     float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
     for (uint32_t i = blockIdx.x * kBlock + threadIdx.x; i < n; i += gridDim.x * kBlock) {
         Box3 b = tri_box(verts, i);
@@ -108,67 +138,41 @@ __global__ void __launch_bounds__(kBlock) k_centroid_partials(const float* __res
             hi[k] = fmaxf(hi[k], c);
         }
     }
-    __shared__ float s[6][kBlock / 32];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        for (int o = 16; o > 0; o >>= 1) {
-            lo[k] = fminf(lo[k], __shfl_xor_sync(0xFFFFFFFFu, lo[k], o));
-            hi[k] = fmaxf(hi[k], __shfl_xor_sync(0xFFFFFFFFu, hi[k], o));
-        }
-    }
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (lane == 0) {
-        for (int k = 0; k < 3; ++k) { s[k][warp] = lo[k]; s[3 + k][warp] = hi[k]; }
+    const float r = block_bounds(lo, hi);
+    __shared__ bool s_last;
+    if (threadIdx.x < 6) {
+        partial[6 * blockIdx.x + threadIdx.x] = r;
+        __threadfence();
     }
     __syncthreads();
-    if (threadIdx.x < 6) {
-        const int k = threadIdx.x;
-        float r = s[k][0];
-        for (int w = 1; w < kBlock / 32; ++w) r = k < 3 ? fminf(r, s[k][w]) : fmaxf(r, s[k][w]);
-        partial[6 * blockIdx.x + k] = r;
-    }
-}
-
-// One block folds the partial boxes: strided over the partials, then across
-// the warp and the block (min / max do not depend on the order).
-__global__ void __launch_bounds__(kBlock) k_centroid_final(const float* __restrict__ partial, int nparts,
-                                                           BvhMeta* meta) {
-    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
-    for (int p = threadIdx.x; p < nparts; p += kBlock) {
+    if (threadIdx.x == 0) s_last = atomicAdd(done, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    for (int k = 0; k < 3; ++k) { lo[k] = INFINITY; hi[k] = -INFINITY; }
+    for (uint32_t p = threadIdx.x; p < gridDim.x; p += kBlock) {
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-            lo[k] = fminf(lo[k], partial[6 * p + k]);
-            hi[k] = fmaxf(hi[k], partial[6 * p + 3 + k]);
+            lo[k] = fminf(lo[k], __ldcg(partial + 6 * p + k));
+            hi[k] = fmaxf(hi[k], __ldcg(partial + 6 * p + 3 + k));
         }
     }
-    __shared__ float s[6][kBlock / 32];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        for (int o = 16; o > 0; o >>= 1) {
-            lo[k] = fminf(lo[k], __shfl_xor_sync(0xFFFFFFFFu, lo[k], o));
-            hi[k] = fmaxf(hi[k], __shfl_xor_sync(0xFFFFFFFFu, hi[k], o));
-        }
-    }
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (lane == 0) {
-        for (int k = 0; k < 3; ++k) { s[k][warp] = lo[k]; s[3 + k][warp] = hi[k]; }
-    }
-    __syncthreads();
-    if (threadIdx.x < 6) {
-        const int k = threadIdx.x;
-        float r = s[k][0];
-        for (int w = 1; w < kBlock / 32; ++w) r = k < 3 ? fminf(r, s[k][w]) : fmaxf(r, s[k][w]);
-        meta->cbox[k] = r;
-    }
+    __syncthreads();  // block_bounds' shared words are reused
+    const float f = block_bounds(lo, hi);
+    if (threadIdx.x < 6) meta->cbox[threadIdx.x] = f;
 }
 
 // ---- 2. Morton codes + the four digit histograms ------------------------------
 
+// Also clears the sort's look-back words (`status`, `nstatus` words) for the
+// passes that follow.
 __global__ void __launch_bounds__(kBlock) k_morton_hist(const float* __restrict__ verts, uint32_t n,
                                                         const BvhMeta* __restrict__ meta, uint32_t* __restrict__ keys,
-                                                        uint32_t* __restrict__ vals, uint32_t* __restrict__ hist) {
+                                                        uint32_t* __restrict__ vals, uint32_t* __restrict__ hist,
+                                                        uint32_t* __restrict__ status, uint32_t nstatus) {
     __shared__ uint32_t s_hist[4 * 256];
     for (int i = threadIdx.x; i < 4 * 256; i += kBlock) s_hist[i] = 0;
+    for (uint32_t i = blockIdx.x * kBlock + threadIdx.x; i < nstatus; i += gridDim.x * kBlock) status[i] = 0;
     __syncthreads();
     float blo[3], bhi[3];
 #pragma unroll
@@ -194,13 +198,6 @@ __global__ void __launch_bounds__(kBlock) k_morton_hist(const float* __restrict_
     __syncthreads();
     for (int i = threadIdx.x; i < 4 * 256; i += kBlock)
         if (s_hist[i]) atomicAdd(&hist[i], s_hist[i]);
-}
-
-__global__ void __launch_bounds__(256) k_hist_scan(const uint32_t* __restrict__ hist, uint32_t* __restrict__ offs) {
-    __shared__ uint32_t s_warp[8];
-    uint32_t total;
-    const uint32_t v = hist[256 * blockIdx.x + threadIdx.x];
-    offs[256 * blockIdx.x + threadIdx.x] = block_exclusive_scan<256>(v, s_warp, &total);
 }
 
 // ---- 3. onesweep radix pass ------------------------------------------------------
@@ -240,11 +237,11 @@ __device__ __forceinline__ uint32_t lookback(const uint32_t* status, size_t stri
     }
     return excl;
 }
-constexpr size_t kOsSmem = sizeof(uint32_t) * (kOsWarps * 256 + 256 + 256 + 2 * kOsTile + 8 + 1);
+constexpr size_t kOsSmem = sizeof(uint32_t) * (kOsWarps * 256 + 256 + 256 + 2 * kOsTile + 2 * kOsWarps + 1);
 
 __global__ void __launch_bounds__(kOsThreads) k_onesweep(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
                                                          uint32_t* __restrict__ kout, uint32_t* __restrict__ vout,
-                                                         uint32_t n, int pass, const uint32_t* __restrict__ offs,
+                                                         uint32_t n, int pass, const uint32_t* __restrict__ hist,
                                                          uint32_t* __restrict__ status, uint32_t* __restrict__ tile_ctr,
                                                          uint32_t* __restrict__ err) {
     extern __shared__ uint32_t smem[];
@@ -253,8 +250,8 @@ __global__ void __launch_bounds__(kOsThreads) k_onesweep(const uint32_t* __restr
     uint32_t* s_gbase = s_dstart + 256;            // [256] global digit bases
     uint32_t* s_keys = s_gbase + 256;              // [tile]
     uint32_t* s_vals = s_keys + kOsTile;           // [tile]
-    uint32_t* s_warp = s_vals + kOsTile;           // [8] scan scratch
-    uint32_t* s_tile = s_warp + 8;
+    unsigned long long* s_warp = reinterpret_cast<unsigned long long*>(s_vals + kOsTile);  // [warps] scan scratch
+    uint32_t* s_tile = reinterpret_cast<uint32_t*>(s_warp + kOsWarps);
 
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int shift = 8 * pass;
@@ -300,8 +297,13 @@ __global__ void __launch_bounds__(kOsThreads) k_onesweep(const uint32_t* __restr
         cnt = run;
     }
     __syncthreads();
-    uint32_t tot;
-    const uint32_t dstart = block_exclusive_scan<kOsThreads>(threadIdx.x < 256 ? cnt : 0u, s_warp, &tot);
+    // one scan gives the tile-local digit starts (low word) and the pass's
+    // global digit starts from the histogram (high word; the tile's counts sum
+    // to at most kOsTile, so the low word never carries)
+    unsigned long long tot;
+    const unsigned long long both = block_exclusive_scan<kOsThreads>(
+        threadIdx.x < 256 ? ((unsigned long long)hist[256 * pass + threadIdx.x] << 32) | cnt : 0ull, s_warp, &tot);
+    const uint32_t dstart = (uint32_t)both;
     if (threadIdx.x < 256) {
         const int d = threadIdx.x;
         s_dstart[d] = dstart;
@@ -314,7 +316,7 @@ __global__ void __launch_bounds__(kOsThreads) k_onesweep(const uint32_t* __restr
             excl = lookback(status + d, 256, (int64_t)tile, kSpinLimit, err);
             st_release(st, kFlagInc | ((excl + cnt) & kCountMask));
         }
-        s_gbase[d] = offs[256 * pass + d] + excl;
+        s_gbase[d] = (uint32_t)(both >> 32) + excl;
     }
     __syncthreads();
 #pragma unroll
@@ -401,11 +403,14 @@ __device__ __forceinline__ uint32_t run_depth(const uint32_t* __restrict__ code,
     return depth;
 }
 
+// Also clears the node counters of the bottom-up pass.
 __global__ void __launch_bounds__(kBlock) k_gaps(const uint32_t* __restrict__ code, uint32_t n,
-                                                 uint8_t* __restrict__ level, uint32_t* __restrict__ err) {
+                                                 uint8_t* __restrict__ level, uint32_t* __restrict__ counters,
+                                                 uint32_t* __restrict__ err) {
     for (uint32_t g = blockIdx.x * kBlock + threadIdx.x; g + 1 < n; g += gridDim.x * kBlock) {
         const uint32_t c0 = code[g], c1 = code[g + 1];
         level[g] = (uint8_t)(c0 != c1 ? (uint32_t)__clz(c0 ^ c1) : 32u + run_depth(code, n, g, err));
+        counters[g] = 0;
     }
 }
 
@@ -447,16 +452,6 @@ __device__ __forceinline__ uint32_t atomic_add_acq_rel_cta(uint32_t* p, uint32_t
     return old;
 }
 
-// A child box written by another thread of the same block (plain load: the
-// shared-memory acquire above orders it).
-__device__ __forceinline__ Box3 get_child_box(const Node* nd, int slot) {
-    const float4 xy = reinterpret_cast<const float4*>(nd)[slot];
-    const float2 z = reinterpret_cast<const float2*>(&nd->q2)[slot];
-    Box3 b;
-    b.lo[0] = xy.x; b.hi[0] = xy.y; b.lo[1] = xy.z; b.hi[1] = xy.w; b.lo[2] = z.x; b.hi[2] = z.y;
-    return b;
-}
-
 __device__ __forceinline__ void box_union(Box3& a, const Box3& b) {
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
@@ -466,47 +461,60 @@ __device__ __forceinline__ void box_union(Box3& a, const Box3& b) {
 }
 
 // A finished subtree on its way up: its id (~position for a leaf, else its
-// gap), the sorted positions it covers and its box.
+// gap), the sorted positions it covers, the levels of its two outer gaps
+// lo - 1 and hi (-1 where the range ends the sequence) and its box.
 struct Sub {
     int32_t me;
     uint32_t lo, hi;
+    int32_t llo, lhi;
     Box3 box;
 };
 
-// Where the climb writes: the node array, the parent of each leaf, and per
-// internal node the outer end of each child's range (far[2G] = the left
-// child's first position, far[2G + 1] = the right child's last).
+// Where the climb writes: the node array, the parent of each leaf, per
+// internal node and child slot the child's outer end and that end's outer-gap
+// level (far[2G] = the left child's first position and the level of the gap
+// before it, far[2G + 1] = the right child's last position and the level of
+// the gap after it), the node counters, and per chunk the subtree left to
+// attach across the chunk's left border.
 struct ClimbOut {
     Node* nodes;
     uint32_t* parent_leaf;
-    uint32_t* far;
+    unsigned long long* far;
     BvhMeta* meta;
     uint32_t* counters;
+    Sub* pend;
     uint32_t* err;
 };
 
-// The finished subtree `s` (not the whole range) hangs below gap `G` in slot
-// `slot` (0 = left): its box and id go into the parent's slot, its outer end
-// into far, and the parent's index into its own record.
+// Slot of the parent of a subtree that is not the whole range: the outer gap
+// with the higher level (0: the gap after it, the subtree is a left child).
+__device__ __forceinline__ int parent_slot(const Sub& s) { return s.lhi > s.llo ? 0 : 1; }
+
+__device__ __forceinline__ unsigned long long far_word(const Sub& s, int slot) {
+    const uint32_t end = slot == 0 ? s.lo : s.hi;
+    const int32_t lv = slot == 0 ? s.llo : s.lhi;
+    return ((unsigned long long)(uint32_t)(lv & 0xFF) << 32) | end;
+}
+
+// Takes the sibling's outer end (and its gap level) from its far word: the
+// subtree becomes its parent's range.
+__device__ __forceinline__ void widen(Sub& s, int slot, unsigned long long w) {
+    const uint32_t end = (uint32_t)w;
+    const uint32_t lb = (uint32_t)(w >> 32) & 0xFFu;
+    const int32_t lv = lb == 0xFFu ? -1 : (int32_t)lb;
+    if (slot == 0) { s.hi = end; s.lhi = lv; } else { s.lo = end; s.llo = lv; }
+}
+
+// The finished subtree `s` hangs below gap `G` in slot `slot` (0 = left): its
+// box and id go into the parent's record, its far word into far, and the
+// parent's index into its own record.
 __device__ __forceinline__ void attach(const ClimbOut& o, const Sub& s, uint32_t G, int slot) {
     Node* pn = o.nodes + G;
     put_child_box(pn, slot, s.box);
     reinterpret_cast<int32_t*>(&pn->q3)[slot] = s.me;
-    o.far[2 * G + slot] = slot == 0 ? s.lo : s.hi;
+    o.far[2 * G + slot] = far_word(s, slot);
     if (s.me >= 0) *reinterpret_cast<int2*>(&o.nodes[s.me].q3.z) = make_int2((int32_t)G, 0);
     else o.parent_leaf[~s.me] = G;
-}
-
-// Parent gap of a subtree covering [lo, hi] (not the whole range) and the slot
-// the subtree takes there.
-__device__ __forceinline__ uint32_t parent_gap(const uint8_t* __restrict__ level, uint32_t lo, uint32_t hi,
-                                               uint32_t n, int& slot) {
-    if (lo == 0 || (hi + 1 < n && __ldg(level + hi) > __ldg(level + lo - 1))) {
-        slot = 0;
-        return hi;
-    }
-    slot = 1;
-    return lo - 1;
 }
 
 // The whole range is finished: `s` is the root.
@@ -517,10 +525,11 @@ __device__ __forceinline__ void set_root(const ClimbOut& o, const Sub& s) {
 
 // Climb from finished subtree `s` with GPU-scope counters: at each parent the
 // first arrival stops, the second unions its sibling's box and range and goes
-// on up.
-__device__ __forceinline__ void climb_global(const ClimbOut& o, const uint8_t* __restrict__ level, uint32_t n, Sub s) {
+// on up. Two round trips a level: the counter, then the sibling's box and far
+// word (which carries the level the next step needs).
+__device__ __forceinline__ void climb_global(const ClimbOut& o, Sub s) {
     for (int guard = 0;; ++guard) {
-        if (s.lo == 0 && s.hi + 1 == n) {
+        if (s.llo < 0 && s.lhi < 0) {
             set_root(o, s);
             return;
         }
@@ -528,37 +537,38 @@ __device__ __forceinline__ void climb_global(const ClimbOut& o, const uint8_t* _
             atomicOr(o.err, ERR_RANGE);
             return;
         }
-        int slot;
-        const uint32_t G = parent_gap(level, s.lo, s.hi, n, slot);
+        const int slot = parent_slot(s);
+        const uint32_t G = slot == 0 ? s.hi : s.lo - 1;
         attach(o, s, G, slot);
         if (atomic_add_acq_rel(&o.counters[G], 1u) == 0) return;  // sibling not done yet
         box_union(s.box, get_child_box_l2(o.nodes + G, slot ^ 1));
-        if (slot == 0) s.hi = __ldcg(&o.far[2 * G + 1]); else s.lo = __ldcg(&o.far[2 * G]);
+        widen(s, slot, __ldcg(&o.far[2 * G + (slot ^ 1)]));
         s.me = (int32_t)G;
     }
 }
 
-// One bottom-up pass builds the tree: a block takes kRefitChunk sorted
-// positions (one block per chunk, so a block held up by a long climb delays no
-// other chunk), one per thread; the thread writes the position's triangle and
-// leaf box and climbs, writing each node's links, parent and child boxes as it
-// goes. The chunk owns the gaps [base, base + kRefitChunk); arrivals there are
-// counted in shared memory (an ordered atomic at block scope), so every node
-// whose subtree lies inside the chunk is finished without a global atomic. An
-// arrival at another chunk's node counts on that node's global counter and
-// goes on globally. After the chunk, a node of it reached once adds its one
-// arrival to the global counter: whichever of that and the node's other
-// (global) arrival comes second finishes the node, so exactly one thread goes
-// on. min / max are exact, so the boxes do not depend on the order of arrivals.
-__global__ void __launch_bounds__(kRefitChunk) k_climb(const float* __restrict__ verts, uint32_t n,
-                                                       const uint32_t* __restrict__ prim,
-                                                       const uint8_t* __restrict__ level, ClimbOut o,
-                                                       Tri* __restrict__ tris) {
+// Bottom-up pass, part 1: a block takes kRefitChunk sorted positions, one per
+// thread; the thread writes the position's triangle and climbs while its
+// subtree's parent is one of the chunk's gaps [base, base + kRefitChunk).
+// Arrivals are counted in shared memory (an ordered atomic at block scope)
+// and the sibling's box and far word are read from shared memory (global
+// copies are written for part 2 and for the output). A subtree inside the
+// chunk can have its parent outside only at gap base - 1 (its range starts at
+// base), so at most one subtree per chunk is left over: it goes to `pend`.
+// A node of the chunk reached once records that arrival in its global counter.
+__global__ void __launch_bounds__(kRefitChunk) k_climb_chunk(const float* __restrict__ verts, uint32_t n,
+                                                             const uint32_t* __restrict__ prim,
+                                                             const uint8_t* __restrict__ level, ClimbOut o,
+                                                             Tri* __restrict__ tris) {
     __shared__ uint32_t s_cnt[kRefitChunk];
+    __shared__ float s_box[kRefitChunk][2][6];
+    __shared__ unsigned long long s_far[kRefitChunk][2];
+    __shared__ Sub s_pend;
     const uint32_t chunks = (n + kRefitChunk - 1) / kRefitChunk;
     for (uint32_t c = blockIdx.x; c < chunks; c += gridDim.x) {  // block-uniform
         const uint32_t base = c * kRefitChunk;
         s_cnt[threadIdx.x] = 0;
+        if (threadIdx.x == 0) s_pend.lo = 0;  // no subtree left over (a left-over range starts at base > 0)
         __syncthreads();
         const uint32_t p = base + threadIdx.x;  // one sorted position per thread
         if (p < n) {
@@ -575,6 +585,8 @@ __global__ void __launch_bounds__(kRefitChunk) k_climb(const float* __restrict__
             Sub s;
             s.me = ~(int32_t)p;
             s.lo = s.hi = p;
+            s.llo = p > 0 ? (int32_t)__ldg(level + p - 1) : -1;
+            s.lhi = p + 1 < n ? (int32_t)__ldg(level + p) : -1;
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
                 s.box.lo[k] = fminf(fminf(a[k], a[3 + k]), a[6 + k]);
@@ -591,7 +603,7 @@ __global__ void __launch_bounds__(kRefitChunk) k_climb(const float* __restrict__
                 o.meta->root = 0;
             } else {
                 for (int guard = 0;; ++guard) {
-                    if (s.lo == 0 && s.hi + 1 == n) {
+                    if (s.llo < 0 && s.lhi < 0) {
                         set_root(o, s);
                         break;
                     }
@@ -599,36 +611,63 @@ __global__ void __launch_bounds__(kRefitChunk) k_climb(const float* __restrict__
                         atomicOr(o.err, ERR_RANGE);
                         break;
                     }
-                    int slot;
-                    const uint32_t G = parent_gap(level, s.lo, s.hi, n, slot);
-                    attach(o, s, G, slot);
-                    if (G - base >= (uint32_t)kRefitChunk) {  // another chunk's node
-                        if (atomic_add_acq_rel(&o.counters[G], 1u) == 0) break;
-                        box_union(s.box, get_child_box_l2(o.nodes + G, slot ^ 1));
-                        if (slot == 0) s.hi = __ldcg(&o.far[2 * G + 1]); else s.lo = __ldcg(&o.far[2 * G]);
-                        s.me = (int32_t)G;
-                        climb_global(o, level, n, s);
+                    const int slot = parent_slot(s);
+                    if (slot == 1 && s.lo == base) {  // parent at gap base - 1, another chunk's
+                        s_pend = s;
                         break;
                     }
-                    if (atomic_add_acq_rel_cta(&s_cnt[G - base], 1u) == 0) break;  // sibling not done yet
-                    box_union(s.box, get_child_box(o.nodes + G, slot ^ 1));
-                    if (slot == 0) s.hi = o.far[2 * G + 1]; else s.lo = o.far[2 * G];
+                    const uint32_t G = slot == 0 ? s.hi : s.lo - 1;
+                    const uint32_t g = G - base;
+                    attach(o, s, G, slot);
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) {
+                        s_box[g][slot][k] = s.box.lo[k];
+                        s_box[g][slot][3 + k] = s.box.hi[k];
+                    }
+                    s_far[g][slot] = far_word(s, slot);
+                    if (atomic_add_acq_rel_cta(&s_cnt[g], 1u) == 0) break;  // sibling not done yet
+                    Box3 sb;
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) {
+                        sb.lo[k] = s_box[g][slot ^ 1][k];
+                        sb.hi[k] = s_box[g][slot ^ 1][3 + k];
+                    }
+                    box_union(s.box, sb);
+                    widen(s, slot, s_far[g][slot ^ 1]);
                     s.me = (int32_t)G;
                 }
             }
         }
         __syncthreads();
-        // this chunk's nodes reached once: their one arrival joins the global count
-        if (p + 1 < n && s_cnt[threadIdx.x] == 1 && atomic_add_acq_rel(&o.counters[p], 1u) == 1) {
-            Sub s;  // node p: both children are done, their boxes and ends are in its record
-            s.me = (int32_t)p;
-            s.box = get_child_box_l2(o.nodes + p, 0);
-            box_union(s.box, get_child_box_l2(o.nodes + p, 1));
-            s.lo = __ldcg(&o.far[2 * p]);
-            s.hi = __ldcg(&o.far[2 * p + 1]);
-            climb_global(o, level, n, s);
-        }
+        // this chunk's nodes reached once: the arrival goes into the global count
+        if (p + 1 < n && s_cnt[threadIdx.x] == 1) o.counters[p] = 1;
+        if (threadIdx.x == 0) o.pend[c] = s_pend;
         __syncthreads();
+    }
+}
+
+// Bottom-up pass, part 2: one thread per chunk attaches the chunk's left-over
+// subtree (if any) across the chunk's left border and climbs with GPU-scope
+// counters. Part 1's writes are complete and visible (kernel boundary); every
+// node still open has exactly its missing arrivals left.
+constexpr int kUpThreads = 64;  // small blocks: the climbs spread over many SMs
+
+__global__ void __launch_bounds__(kUpThreads) k_climb_up(uint32_t chunks, ClimbOut o) {
+    for (uint32_t c = blockIdx.x * kUpThreads + threadIdx.x; c < chunks; c += gridDim.x * kUpThreads) {
+        const Sub* ps = o.pend + c;
+        Sub s;
+        s.lo = ps->lo;
+        if (s.lo == 0) continue;
+        s.me = ps->me;
+        s.hi = ps->hi;
+        s.llo = ps->llo;
+        s.lhi = ps->lhi;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            s.box.lo[k] = ps->box.lo[k];
+            s.box.hi[k] = ps->box.hi[k];
+        }
+        climb_global(o, s);
     }
 }
 
@@ -697,11 +736,13 @@ __global__ void __launch_bounds__(kBlock) k_export_ref(const Node* __restrict__ 
 size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
 struct Scratch {
-    uint32_t *keys_alt, *vals_alt, *parent_leaf, *far, *counters;
+    uint32_t *keys_alt, *vals_alt, *parent_leaf, *counters;
+    unsigned long long* far;
+    Sub* pend;
     uint8_t* level;
-    uint32_t *hist, *offs, *os_status, *tile_ctr, *err;
+    uint32_t *hist, *os_status, *tile_ctr, *err;
     float* partial;
-    size_t zero_bytes;  // bytes from the counters up to the end of the zeroed region
+    size_t zero_bytes;  // bytes from the histograms up to the end of the zeroed region
     void* zero_base;
 };
 
@@ -719,15 +760,15 @@ size_t scratch_layout(uint32_t n, char* base, Scratch* s) {
     s->keys_alt = (uint32_t*)take(w);
     s->vals_alt = (uint32_t*)take(w);
     s->parent_leaf = (uint32_t*)take(w);
-    s->far = (uint32_t*)take(2 * w);
+    s->far = (unsigned long long*)take(16ull * n);
+    s->pend = (Sub*)take(sizeof(Sub) * (((uint64_t)n + kRefitChunk - 1) / kRefitChunk));
     s->level = (uint8_t*)take(n);
     s->partial = (float*)take(sizeof(float) * 6 * kPartials);
+    s->counters = (uint32_t*)take(w);                            // cleared by k_gaps
+    s->os_status = (uint32_t*)take(4ull * os_tiles * 256 * 4);  // cleared by k_morton_hist
     // everything from here on is zeroed before each build
     const size_t zstart = off;
-    s->counters = (uint32_t*)take(w);
     s->hist = (uint32_t*)take(4 * 256 * 4);
-    s->offs = (uint32_t*)take(4 * 256 * 4);
-    s->os_status = (uint32_t*)take(4ull * os_tiles * 256 * 4);
     s->tile_ctr = (uint32_t*)take(16 * 4);
     s->err = (uint32_t*)take(4);
     s->zero_base = base ? base + zstart : nullptr;
@@ -773,29 +814,29 @@ cudaError_t launch_build(const float* d_verts, uint32_t n, const Scratch& s, Nod
     if ((e = cudaMemsetAsync(s.zero_base, 0, s.zero_bytes, st)) != cudaSuccess) return e;
     const int grid = (int)std::min<uint64_t>(((uint64_t)n + kBlock - 1) / kBlock, (uint64_t)num_sms * 8);
     const int parts = std::min(grid, kPartials);
-    k_centroid_partials<<<parts, kBlock, 0, st>>>(d_verts, n, s.partial);
-    k_centroid_final<<<1, kBlock, 0, st>>>(s.partial, parts, meta);
-    k_morton_hist<<<std::min(grid, num_sms * 2), kBlock, 0, st>>>(d_verts, n, meta, code, prim, s.hist);
-    k_hist_scan<<<4, 256, 0, st>>>(s.hist, s.offs);
+    k_centroid<<<parts, kBlock, 0, st>>>(d_verts, n, s.partial, s.tile_ctr + 4, meta);
+    const uint32_t os_tiles = (n + kOsTile - 1) / kOsTile;
+    k_morton_hist<<<std::min(grid, num_sms * 2), kBlock, 0, st>>>(d_verts, n, meta, code, prim, s.hist, s.os_status,
+                                                                  4 * os_tiles * 256);
     if ((e = cudaFuncSetAttribute(k_onesweep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kOsSmem)) !=
         cudaSuccess)
         return e;
-    const uint32_t os_tiles = (n + kOsTile - 1) / kOsTile;
     uint32_t* kin = code;
     uint32_t* vin = prim;
     uint32_t* kout = s.keys_alt;
     uint32_t* vout = s.vals_alt;
     for (int pass = 0; pass < 4; ++pass) {
-        k_onesweep<<<os_tiles, kOsThreads, kOsSmem, st>>>(kin, vin, kout, vout, n, pass, s.offs,
+        k_onesweep<<<os_tiles, kOsThreads, kOsSmem, st>>>(kin, vin, kout, vout, n, pass, s.hist,
                                                           s.os_status + (size_t)pass * os_tiles * 256, s.tile_ctr, s.err);
         std::swap(kin, kout);
         std::swap(vin, vout);
     }
     // four passes: the sorted data is back in code/prim
-    k_gaps<<<grid, kBlock, 0, st>>>(code, n, s.level, s.err);
+    k_gaps<<<grid, kBlock, 0, st>>>(code, n, s.level, s.counters, s.err);
     const uint32_t chunks = (n + kRefitChunk - 1) / kRefitChunk;
-    const ClimbOut out{nodes, s.parent_leaf, s.far, meta, s.counters, s.err};
-    k_climb<<<chunks, kRefitChunk, 0, st>>>(d_verts, n, prim, s.level, out, tris);
+    const ClimbOut out{nodes, s.parent_leaf, s.far, meta, s.counters, s.pend, s.err};
+    k_climb_chunk<<<chunks, kRefitChunk, 0, st>>>(d_verts, n, prim, s.level, out, tris);
+    k_climb_up<<<(chunks + kUpThreads - 1) / kUpThreads, kUpThreads, 0, st>>>(chunks, out);
     // fold the build's error word into the header the host reads
     if ((e = cudaMemcpyAsync(&meta->err, s.err, 4, cudaMemcpyDeviceToDevice, st)) != cudaSuccess) return e;
     return cudaGetLastError();
@@ -859,15 +900,18 @@ constexpr uint32_t kStaticMaxTriangles = 1u << 17;  // 131,072 triangles
 constexpr size_t round256(size_t x) { return (x + 255) & ~size_t(255); }
 
 // Upper bound of scratch_layout(kStaticMaxTriangles): four per-triangle word
-// arrays (sort buffers, leaf parents, node counters), the two range ends per
-// node, one level byte per gap, the centroid partials, histograms, the sort's
-// look-back words (per tile of each pass), tile counters and the error word,
-// each rounded up to 256 bytes as scratch_layout rounds them.
+// arrays (sort buffers, leaf parents, node counters), the two far words per
+// node, the left-over subtree per chunk, one level byte per gap, the centroid
+// partials, the histograms, the sort's look-back words (per tile of each
+// pass), tile counters and the error word, each rounded up to 256 bytes as
+// scratch_layout rounds them.
 constexpr size_t kStaticOsTiles = (kStaticMaxTriangles + kOsTile - 1) / kOsTile;
+constexpr size_t kStaticChunks = (kStaticMaxTriangles + kRefitChunk - 1) / kRefitChunk;
 constexpr size_t kStaticScratchBytes =
-    4 * round256((size_t)kStaticMaxTriangles * 4) + round256((size_t)kStaticMaxTriangles * 8) +
-    round256(kStaticMaxTriangles) + round256(sizeof(float) * 6 * kPartials) + 2 * 4096 +
-    round256(4 * kStaticOsTiles * 256 * 4) + round256(16 * 4) + round256(4);
+    4 * round256((size_t)kStaticMaxTriangles * 4) + round256((size_t)kStaticMaxTriangles * 16) +
+    round256(sizeof(Sub) * kStaticChunks) + round256(kStaticMaxTriangles) +
+    round256(sizeof(float) * 6 * kPartials) + 4096 + round256(4 * kStaticOsTiles * 256 * 4) + round256(16 * 4) +
+    round256(4);
 
 static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
 
