@@ -441,17 +441,6 @@ __device__ __forceinline__ uint32_t atomic_add_acq_rel(uint32_t* p, uint32_t v) 
     return old;
 }
 
-// Counter increment with acquire-release semantics at CTA scope on a
-// shared-memory word: orders this thread's global writes (its child box and
-// link) before the increment and the sibling's, written by another thread of
-// the block before its increment, before this thread's later reads.
-__device__ __forceinline__ uint32_t atomic_add_acq_rel_cta(uint32_t* p, uint32_t v) {
-    uint32_t old;
-    const uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
-    asm volatile("atom.acq_rel.cta.shared.add.u32 %0, [%1], %2;" : "=r"(old) : "r"(a), "r"(v) : "memory");
-    return old;
-}
-
 __device__ __forceinline__ void box_union(Box3& a, const Box3& b) {
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
@@ -547,27 +536,53 @@ __device__ __forceinline__ void climb_global(const ClimbOut& o, Sub s) {
     }
 }
 
+// Writes a finished node's whole 64-byte record (two 32-byte stores): the
+// children's boxes, their ids, the parent's index.
+__device__ __forceinline__ void write_node(Node* nd, const Box3& b0, const Box3& b1, int32_t l0, int32_t l1,
+                                           uint32_t parent) {
+    float* q = reinterpret_cast<float*>(nd);
+    asm volatile("st.global.v8.f32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(q), "f"(b0.lo[0]), "f"(b0.hi[0]),
+                 "f"(b0.lo[1]), "f"(b0.hi[1]), "f"(b1.lo[0]), "f"(b1.hi[0]), "f"(b1.lo[1]), "f"(b1.hi[1])
+                 : "memory");
+    asm volatile("st.global.v8.f32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(q + 8), "f"(b0.lo[2]),
+                 "f"(b0.hi[2]), "f"(b1.lo[2]), "f"(b1.hi[2]), "f"(__int_as_float(l0)), "f"(__int_as_float(l1)),
+                 "f"(__uint_as_float(parent)), "f"(0.0f)
+                 : "memory");
+}
+
+// Bit-or with acquire-release semantics at CTA scope on a shared-memory word
+// (the arrival mask of a node: bit = child slot).
+__device__ __forceinline__ uint32_t atomic_or_acq_rel_cta(uint32_t* p, uint32_t v) {
+    uint32_t old;
+    const uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
+    asm volatile("atom.acq_rel.cta.shared.or.b32 %0, [%1], %2;" : "=r"(old) : "r"(a), "r"(v) : "memory");
+    return old;
+}
+
 // Bottom-up pass, part 1: a block takes kRefitChunk sorted positions, one per
 // thread; the thread writes the position's triangle and climbs while its
 // subtree's parent is one of the chunk's gaps [base, base + kRefitChunk).
-// Arrivals are counted in shared memory (an ordered atomic at block scope)
-// and the sibling's box and far word are read from shared memory (global
-// copies are written for part 2 and for the output). A subtree inside the
-// chunk can have its parent outside only at gap base - 1 (its range starts at
-// base), so at most one subtree per chunk is left over: it goes to `pend`.
-// A node of the chunk reached once records that arrival in its global counter.
+// Arrivals are marked in shared memory (an ordered bit-or at block scope,
+// bit = child slot) and each child's box, id and far word wait there for the
+// sibling; the second arrival writes the node's whole record once it knows
+// the node's parent. A subtree inside the chunk can have its parent outside
+// only at gap base - 1 (its range starts at base), so at most one subtree per
+// chunk is left over: it goes to `pend`. A node of the chunk reached once gets
+// that child's slot written to its record and the arrival to its global
+// counter.
 __global__ void __launch_bounds__(kRefitChunk) k_climb_chunk(const float* __restrict__ verts, uint32_t n,
                                                              const uint32_t* __restrict__ prim,
                                                              const uint8_t* __restrict__ level, ClimbOut o,
                                                              Tri* __restrict__ tris) {
-    __shared__ uint32_t s_cnt[kRefitChunk];
+    __shared__ uint32_t s_mask[kRefitChunk];
     __shared__ float s_box[kRefitChunk][2][6];
     __shared__ unsigned long long s_far[kRefitChunk][2];
+    __shared__ int32_t s_link[kRefitChunk][2];
     __shared__ Sub s_pend;
     const uint32_t chunks = (n + kRefitChunk - 1) / kRefitChunk;
     for (uint32_t c = blockIdx.x; c < chunks; c += gridDim.x) {  // block-uniform
         const uint32_t base = c * kRefitChunk;
-        s_cnt[threadIdx.x] = 0;
+        s_mask[threadIdx.x] = 0;
         if (threadIdx.x == 0) s_pend.lo = 0;  // no subtree left over (a left-over range starts at base > 0)
         __syncthreads();
         const uint32_t p = base + threadIdx.x;  // one sorted position per thread
@@ -594,53 +609,76 @@ __global__ void __launch_bounds__(kRefitChunk) k_climb_chunk(const float* __rest
             }
             if (n == 1) {
                 // one triangle: a single node whose two children are the same leaf
-                Node nd;
-                nd.q0 = make_float4(s.box.lo[0], s.box.hi[0], s.box.lo[1], s.box.hi[1]);
-                nd.q1 = nd.q0;
-                nd.q2 = make_float4(s.box.lo[2], s.box.hi[2], s.box.lo[2], s.box.hi[2]);
-                nd.q3 = make_int4(~0, ~0, (int32_t)kNoNode, 0);
-                o.nodes[0] = nd;
+                write_node(o.nodes, s.box, s.box, ~0, ~0, kNoNode);
                 o.meta->root = 0;
             } else {
+                // s is finished and is not the root; a node's record is written
                 for (int guard = 0;; ++guard) {
-                    if (s.llo < 0 && s.lhi < 0) {
-                        set_root(o, s);
-                        break;
-                    }
                     if (guard > 128) {
                         atomicOr(o.err, ERR_RANGE);
                         break;
                     }
                     const int slot = parent_slot(s);
+                    const uint32_t P = slot == 0 ? s.hi : s.lo - 1;
+                    if (s.me < 0) o.parent_leaf[~s.me] = P;
                     if (slot == 1 && s.lo == base) {  // parent at gap base - 1, another chunk's
                         s_pend = s;
                         break;
                     }
-                    const uint32_t G = slot == 0 ? s.hi : s.lo - 1;
-                    const uint32_t g = G - base;
-                    attach(o, s, G, slot);
+                    const uint32_t g = P - base;
 #pragma unroll
                     for (int k = 0; k < 3; ++k) {
                         s_box[g][slot][k] = s.box.lo[k];
                         s_box[g][slot][3 + k] = s.box.hi[k];
                     }
                     s_far[g][slot] = far_word(s, slot);
-                    if (atomic_add_acq_rel_cta(&s_cnt[g], 1u) == 0) break;  // sibling not done yet
-                    Box3 sb;
+                    s_link[g][slot] = s.me;
+                    if (atomic_or_acq_rel_cta(&s_mask[g], 1u << slot) == 0) break;  // sibling not done yet
+                    // second arrival: the node's range and parent, then its record
+                    // (both child slots from shared memory) and its box
+                    const int32_t me = s.me;
+                    widen(s, slot, s_far[g][slot ^ 1]);
+                    s.me = (int32_t)P;
+                    const bool root = s.llo < 0 && s.lhi < 0;
+                    Box3 b0, b1;
 #pragma unroll
                     for (int k = 0; k < 3; ++k) {
-                        sb.lo[k] = s_box[g][slot ^ 1][k];
-                        sb.hi[k] = s_box[g][slot ^ 1][3 + k];
+                        b0.lo[k] = s_box[g][0][k];
+                        b0.hi[k] = s_box[g][0][3 + k];
+                        b1.lo[k] = s_box[g][1][k];
+                        b1.hi[k] = s_box[g][1][3 + k];
                     }
-                    box_union(s.box, sb);
-                    widen(s, slot, s_far[g][slot ^ 1]);
-                    s.me = (int32_t)G;
+                    write_node(o.nodes + P, b0, b1, slot == 0 ? me : s_link[g][0], slot == 0 ? s_link[g][1] : me,
+                               root ? kNoNode : (parent_slot(s) == 0 ? s.hi : s.lo - 1));
+                    box_union(b0, b1);
+                    s.box = b0;
+                    if (root) {
+                        o.meta->root = P;
+                        break;
+                    }
                 }
             }
         }
         __syncthreads();
-        // this chunk's nodes reached once: the arrival goes into the global count
-        if (p + 1 < n && s_cnt[threadIdx.x] == 1) o.counters[p] = 1;
+        // this chunk's nodes reached once: the child's slot goes into the record
+        // and the arrival into the global count
+        if (p + 1 < n) {
+            const uint32_t m = s_mask[threadIdx.x];
+            if (m == 1u || m == 2u) {
+                const int slot = m == 1u ? 0 : 1;
+                Box3 b;
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    b.lo[k] = s_box[threadIdx.x][slot][k];
+                    b.hi[k] = s_box[threadIdx.x][slot][3 + k];
+                }
+                Node* nd = o.nodes + p;
+                put_child_box(nd, slot, b);
+                reinterpret_cast<int32_t*>(&nd->q3)[slot] = s_link[threadIdx.x][slot];
+                o.far[2 * p + slot] = s_far[threadIdx.x][slot];
+                o.counters[p] = 1;
+            }
+        }
         if (threadIdx.x == 0) o.pend[c] = s_pend;
         __syncthreads();
     }
