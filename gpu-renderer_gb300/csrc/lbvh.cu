@@ -560,21 +560,22 @@ __device__ __forceinline__ uint32_t atomic_or_acq_rel_cta(uint32_t* p, uint32_t 
 }
 
 // Bottom-up pass, part 1: a block takes kRefitChunk sorted positions, one per
-// thread; the thread writes the position's triangle and climbs while its
-// subtree's parent is one of the chunk's gaps [base, base + kRefitChunk).
-// Arrivals are marked in shared memory (an ordered bit-or at block scope,
-// bit = child slot) and each child's box, id and far word wait there for the
-// sibling; the second arrival writes the node's whole record once it knows
-// the node's parent. A subtree inside the chunk can have its parent outside
-// only at gap base - 1 (its range starts at base), so at most one subtree per
-// chunk is left over: it goes to `pend`. A node of the chunk reached once gets
-// that child's slot written to its record and the arrival to its global
-// counter.
+// thread; the thread climbs while its subtree's parent is one of the chunk's
+// gaps [base, base + kRefitChunk). The climb touches shared memory only:
+// arrivals are marked with an ordered bit-or at block scope (bit = child
+// slot), each child's box, id and far word wait there for the sibling, and
+// the second arrival records the node's parent. A subtree inside the chunk can
+// have its parent outside only at gap base - 1 (its range starts at base), so
+// at most one subtree per chunk is left over: it goes to `pend`. After the
+// block barrier each thread writes, coalesced, its position's triangle and
+// leaf parent and its gap's node: the whole record if both children arrived,
+// else the one child's slot, far word and arrival count for part 2.
 __global__ void __launch_bounds__(kRefitChunk) k_climb_chunk(const float* __restrict__ verts, uint32_t n,
                                                              const uint32_t* __restrict__ prim,
                                                              const uint8_t* __restrict__ level, ClimbOut o,
                                                              Tri* __restrict__ tris) {
     __shared__ uint32_t s_mask[kRefitChunk];
+    __shared__ uint32_t s_parent[kRefitChunk];
     __shared__ float s_box[kRefitChunk][2][6];
     __shared__ unsigned long long s_far[kRefitChunk][2];
     __shared__ int32_t s_link[kRefitChunk][2];
@@ -586,17 +587,17 @@ __global__ void __launch_bounds__(kRefitChunk) k_climb_chunk(const float* __rest
         if (threadIdx.x == 0) s_pend.lo = 0;  // no subtree left over (a left-over range starts at base > 0)
         __syncthreads();
         const uint32_t p = base + threadIdx.x;  // one sorted position per thread
+        Tri t;
+        uint32_t leaf_parent = kNoNode;
         if (p < n) {
             const uint32_t id = prim[p];
             const float* v = verts + 9ull * id;
             float a[9];
 #pragma unroll
             for (int k = 0; k < 9; ++k) a[k] = __ldg(v + k);
-            Tri t;
             t.a = make_float4(a[0], a[1], a[2], __uint_as_float(id));
             t.b = make_float4(a[3], a[4], a[5], 0.0f);
             t.c = make_float4(a[6], a[7], a[8], 0.0f);
-            tris[p] = t;
             Sub s;
             s.me = ~(int32_t)p;
             s.lo = s.hi = p;
@@ -612,7 +613,7 @@ __global__ void __launch_bounds__(kRefitChunk) k_climb_chunk(const float* __rest
                 write_node(o.nodes, s.box, s.box, ~0, ~0, kNoNode);
                 o.meta->root = 0;
             } else {
-                // s is finished and is not the root; a node's record is written
+                // s is finished and is not the root
                 for (int guard = 0;; ++guard) {
                     if (guard > 128) {
                         atomicOr(o.err, ERR_RANGE);
@@ -620,7 +621,7 @@ __global__ void __launch_bounds__(kRefitChunk) k_climb_chunk(const float* __rest
                     }
                     const int slot = parent_slot(s);
                     const uint32_t P = slot == 0 ? s.hi : s.lo - 1;
-                    if (s.me < 0) o.parent_leaf[~s.me] = P;
+                    if (s.me < 0) leaf_parent = P;
                     if (slot == 1 && s.lo == base) {  // parent at gap base - 1, another chunk's
                         s_pend = s;
                         break;
@@ -634,48 +635,48 @@ __global__ void __launch_bounds__(kRefitChunk) k_climb_chunk(const float* __rest
                     s_far[g][slot] = far_word(s, slot);
                     s_link[g][slot] = s.me;
                     if (atomic_or_acq_rel_cta(&s_mask[g], 1u << slot) == 0) break;  // sibling not done yet
-                    // second arrival: the node's range and parent, then its record
-                    // (both child slots from shared memory) and its box
-                    const int32_t me = s.me;
-                    widen(s, slot, s_far[g][slot ^ 1]);
-                    s.me = (int32_t)P;
-                    const bool root = s.llo < 0 && s.lhi < 0;
-                    Box3 b0, b1;
+                    Box3 sb;
 #pragma unroll
                     for (int k = 0; k < 3; ++k) {
-                        b0.lo[k] = s_box[g][0][k];
-                        b0.hi[k] = s_box[g][0][3 + k];
-                        b1.lo[k] = s_box[g][1][k];
-                        b1.hi[k] = s_box[g][1][3 + k];
+                        sb.lo[k] = s_box[g][slot ^ 1][k];
+                        sb.hi[k] = s_box[g][slot ^ 1][3 + k];
                     }
-                    write_node(o.nodes + P, b0, b1, slot == 0 ? me : s_link[g][0], slot == 0 ? s_link[g][1] : me,
-                               root ? kNoNode : (parent_slot(s) == 0 ? s.hi : s.lo - 1));
-                    box_union(b0, b1);
-                    s.box = b0;
-                    if (root) {
+                    box_union(s.box, sb);
+                    widen(s, slot, s_far[g][slot ^ 1]);
+                    s.me = (int32_t)P;
+                    if (s.llo < 0 && s.lhi < 0) {  // the root
+                        s_parent[g] = kNoNode;
                         o.meta->root = P;
                         break;
                     }
+                    s_parent[g] = parent_slot(s) == 0 ? s.hi : s.lo - 1;
                 }
             }
         }
         __syncthreads();
-        // this chunk's nodes reached once: the child's slot goes into the record
-        // and the arrival into the global count
+        if (p < n) {
+            tris[p] = t;
+            if (n > 1) o.parent_leaf[p] = leaf_parent;
+        }
         if (p + 1 < n) {
             const uint32_t m = s_mask[threadIdx.x];
-            if (m == 1u || m == 2u) {
-                const int slot = m == 1u ? 0 : 1;
-                Box3 b;
+            const int j = threadIdx.x;
+            Box3 b0, b1;
 #pragma unroll
-                for (int k = 0; k < 3; ++k) {
-                    b.lo[k] = s_box[threadIdx.x][slot][k];
-                    b.hi[k] = s_box[threadIdx.x][slot][3 + k];
-                }
+            for (int k = 0; k < 3; ++k) {
+                b0.lo[k] = s_box[j][0][k];
+                b0.hi[k] = s_box[j][0][3 + k];
+                b1.lo[k] = s_box[j][1][k];
+                b1.hi[k] = s_box[j][1][3 + k];
+            }
+            if (m == 3u) {  // finished here: the whole record
+                write_node(o.nodes + p, b0, b1, s_link[j][0], s_link[j][1], s_parent[j]);
+            } else if (m != 0u) {  // one child arrived: its slot, far word and count for part 2
+                const int slot = m == 1u ? 0 : 1;
                 Node* nd = o.nodes + p;
-                put_child_box(nd, slot, b);
-                reinterpret_cast<int32_t*>(&nd->q3)[slot] = s_link[threadIdx.x][slot];
-                o.far[2 * p + slot] = s_far[threadIdx.x][slot];
+                put_child_box(nd, slot, slot == 0 ? b0 : b1);
+                reinterpret_cast<int32_t*>(&nd->q3)[slot] = s_link[j][slot];
+                o.far[2 * p + slot] = s_far[j][slot];
                 o.counters[p] = 1;
             }
         }
