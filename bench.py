@@ -349,12 +349,13 @@ def roofline_block(layout_name, achieved, peak, peak_kind, closest_ms, anyhit_ms
         b = inputs["build"]
         alg = BUILD_BYTES_PER_TRI * b["triangles"]
         t = b["dram_bytes_read"] + b["dram_bytes_write"]
-        out["build"] = {"kernel": "LBVH build (13 launches), %d triangles" % b["triangles"], "ms": build_ms,
+        out["build"] = {"kernel": "LBVH build (%d launches), %d triangles" % (b["launches"], b["triangles"]),
+                        "ms": build_ms,
                         "achieved": alg / (build_ms / 1e3) / 1e9, "frac": alg / (build_ms / 1e3) / 1e9 / peak,
                         "unit": "GB/s", "algorithmic_bytes": alg, "traffic": t,
                         "dram_frac_of_peak": t / (build_ms / 1e3) / 1e9 / peak,
-                        "binding": "latency: dependent launches, the sort's look-back and the refit's climbs "
-                                   "(longest: %s)" % ", ".join("%s %.0f us" % (k, v / 1e3)
+                        "binding": "latency: dependent launches, the sort's look-back and the bottom-up "
+                                   "climbs (longest: %s)" % ", ".join("%s %.0f us" % (k, v / 1e3)
                                                              for k, v in b["longest"].items())}
     return out
 

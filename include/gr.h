@@ -113,7 +113,7 @@ uint32_t gr_bvh_size(const gr_bvh* bvh);
  *   d_sorted_code  4 bytes x n             Morton codes in sorted order
  *   d_header       64 bytes                uint32 root index at byte 0, device error bits at byte 8
  * The build's scratch is one fixed device array inside the library, sized for
- * at most 131,072 triangles (about 4.8 MB, held on every GPU that loads the
+ * at most 131,072 triangles (about 4.5 MB, held on every GPU that loads the
  * library until the process exits); a larger n returns GR_ERR_INVALID. The
  * first call on a device looks up that array's device address, so make the
  * first call on each device before any stream capture. All calls share the
