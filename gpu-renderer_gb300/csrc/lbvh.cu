@@ -202,7 +202,7 @@ __global__ void __launch_bounds__(kBlock) k_morton_hist(const float* __restrict_
 
 // ---- 3. onesweep radix pass ------------------------------------------------------
 // One pass sorts by one 8-bit digit. Tiles of 4096 keys are ranked in shared
-// memory (warp multi-split with match_any, stable in input order), the tile's
+// memory (warp multi-split by ballots, stable in input order), the tile's
 // per-digit counts are published and prefixed with decoupled look-back, and
 // keys are written out grouped by digit.
 
@@ -237,6 +237,22 @@ __device__ __forceinline__ uint32_t lookback(const uint32_t* status, size_t stri
     }
     return excl;
 }
+// Lanes of the warp holding the same 8-bit digit as this lane (digit 256 marks
+// a key past the end: those lanes match only each other). Nine ballots at full
+// issue rate in place of one match instruction, whose throughput made the
+// ranking the longest phase of a pass.
+__device__ __forceinline__ uint32_t match_digit(uint32_t d) {
+    uint32_t peers = __ballot_sync(0xFFFFFFFFu, d < 256u);
+    if (d >= 256u) peers = ~peers;
+#pragma unroll
+    for (int b = 0; b < 8; ++b) {
+        const bool bit = (d >> b) & 1u;
+        const uint32_t m = __ballot_sync(0xFFFFFFFFu, bit);
+        peers &= bit ? m : ~m;
+    }
+    return peers;
+}
+
 constexpr size_t kOsSmem = sizeof(uint32_t) * (kOsWarps * 256 + 256 + 256 + 2 * kOsTile + 2 * kOsWarps + 1);
 
 __global__ void __launch_bounds__(kOsThreads) k_onesweep(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
@@ -275,7 +291,7 @@ __global__ void __launch_bounds__(kOsThreads) k_onesweep(const uint32_t* __restr
 #pragma unroll
     for (int j = 0; j < kOsItems; ++j) {
         const uint32_t d = dig[j];
-        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
+        const uint32_t peers = match_digit(d);
         const uint32_t lt = __popc(peers & ltmask);
         const uint32_t before = d < 256u ? wc[d] : 0u;
         __syncwarp();
