@@ -253,28 +253,61 @@ __device__ __forceinline__ uint32_t match_digit(uint32_t d) {
     return peers;
 }
 
+// Cooperative sort: up to this many tiles each tile sums the earlier tiles'
+// digit counts itself (one grid barrier); more tiles scan the counts first.
+constexpr uint32_t kSumTiles = 64;
+
 constexpr size_t kOsSmem = sizeof(uint32_t) * (kOsWarps * 256 + 256 + 256 + 2 * kOsTile + 2 * kOsWarps + 1);
 
-__global__ void __launch_bounds__(kOsThreads) k_onesweep(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
-                                                         uint32_t* __restrict__ kout, uint32_t* __restrict__ vout,
-                                                         uint32_t n, int pass, const uint32_t* __restrict__ hist,
-                                                         uint32_t* __restrict__ status, uint32_t* __restrict__ tile_ctr,
-                                                         uint32_t* __restrict__ err) {
-    extern __shared__ uint32_t smem[];
+// Grid-wide barrier of a cooperative launch (every block resident): block
+// arrivals are counted on `ctr`, and the k-th barrier of the launch waits for
+// (k + 1) * gridDim.x arrivals, at most kSpinLimit polls (then ERR_TIMEOUT).
+// The block barrier before the fence puts every thread's writes ahead of the
+// arrival; the block barrier after it puts the other blocks' writes ahead of
+// every thread's later reads (which go to L2: __ldcg).
+__device__ __forceinline__ void grid_barrier(uint32_t* ctr, uint32_t target, uint32_t* err) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(ctr, 1u);
+        uint32_t spins = 0;
+        while (ld_acquire(ctr) < target) {
+            if (++spins > kSpinLimit) {
+                atomicOr(err, ERR_TIMEOUT);
+                break;
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+}
+
+// One tile of one sort pass: ranks the tile's keys by the pass's digit, finds
+// where each digit's run of the tile starts in the output, and writes the
+// tile out grouped by digit. The runs' output starts come from the pass's
+// digit histogram plus the counts of the tiles before this one, by decoupled
+// look-back over `status` (COOP false) or, in a cooperative launch (COOP
+// true), from the counts every tile publishes in `status` (digit-major) before
+// a grid barrier (`barrier` is its index in the launch): up to kSumTiles tiles
+// each tile sums the columns itself; beyond, the blocks scan the columns over
+// the tiles and a second grid barrier follows.
+template <bool COOP>
+__device__ __forceinline__ void sort_tile(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
+                                          uint32_t* __restrict__ kout, uint32_t* __restrict__ vout, uint32_t n,
+                                          int pass, const uint32_t* __restrict__ hist, uint32_t tile,
+                                          uint32_t* __restrict__ status, uint32_t* sync_ctr, uint32_t barrier,
+                                          uint32_t* __restrict__ err, uint32_t* smem) {
     uint32_t* s_wcnt = smem;                       // [warps][256]
     uint32_t* s_dstart = s_wcnt + kOsWarps * 256;  // [256] tile-local digit starts
     uint32_t* s_gbase = s_dstart + 256;            // [256] global digit bases
     uint32_t* s_keys = s_gbase + 256;              // [tile]
     uint32_t* s_vals = s_keys + kOsTile;           // [tile]
     unsigned long long* s_warp = reinterpret_cast<unsigned long long*>(s_vals + kOsTile);  // [warps] scan scratch
-    uint32_t* s_tile = reinterpret_cast<uint32_t*>(s_warp + kOsWarps);
 
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int shift = 8 * pass;
-    if (threadIdx.x == 0) *s_tile = atomicAdd(tile_ctr + pass, 1u);
     for (int i = threadIdx.x; i < kOsWarps * 256; i += kOsThreads) s_wcnt[i] = 0;
     __syncthreads();
-    const uint32_t tile = *s_tile;
     const uint64_t base = (uint64_t)tile * kOsTile;
 
     uint32_t key[kOsItems], val[kOsItems], rank[kOsItems], dig[kOsItems];
@@ -282,8 +315,8 @@ __global__ void __launch_bounds__(kOsThreads) k_onesweep(const uint32_t* __restr
     for (int j = 0; j < kOsItems; ++j) {
         const uint64_t idx = base + warp * (32 * kOsItems) + j * 32 + lane;
         const bool ok = idx < n;
-        key[j] = ok ? kin[idx] : 0u;
-        val[j] = ok ? vin[idx] : 0u;
+        key[j] = ok ? (COOP ? __ldcg(kin + idx) : kin[idx]) : 0u;
+        val[j] = ok ? (COOP ? __ldcg(vin + idx) : vin[idx]) : 0u;
         dig[j] = ok ? ((key[j] >> shift) & 0xFFu) : 256u;
     }
     const uint32_t ltmask = lanemask_lt();
@@ -320,7 +353,60 @@ __global__ void __launch_bounds__(kOsThreads) k_onesweep(const uint32_t* __restr
     const unsigned long long both = block_exclusive_scan<kOsThreads>(
         threadIdx.x < 256 ? ((unsigned long long)hist[256 * pass + threadIdx.x] << 32) | cnt : 0ull, s_warp, &tot);
     const uint32_t dstart = (uint32_t)both;
-    if (threadIdx.x < 256) {
+    if (COOP) {
+        // counts digit-major: column d holds digit d's count of every tile
+        const uint32_t tiles = gridDim.x;
+        if (threadIdx.x < 256) status[(size_t)threadIdx.x * tiles + tile] = cnt;
+        grid_barrier(sync_ctr, (barrier + 1) * gridDim.x, err);
+        if (tiles <= kSumTiles) {
+            // few tiles: each warp sums 16 digits' columns up to this tile,
+            // 32 tiles per coalesced load
+            constexpr int kDigitsPerWarp = 256 / kOsWarps, kRound = 8;
+#pragma unroll
+            for (int r = 0; r < kDigitsPerWarp; r += kRound) {
+                uint32_t acc[kRound];
+#pragma unroll
+                for (int k = 0; k < kRound; ++k) acc[k] = 0;
+                for (uint32_t t = lane; t < tile; t += 32) {
+#pragma unroll
+                    for (int k = 0; k < kRound; ++k)
+                        acc[k] += __ldcg(status + (size_t)(warp * kDigitsPerWarp + r + k) * tiles + t);
+                }
+#pragma unroll
+                for (int k = 0; k < kRound; ++k) {
+                    const uint32_t sum = __reduce_add_sync(0xFFFFFFFFu, acc[k]);
+                    if (lane == 0) s_gbase[warp * kDigitsPerWarp + r + k] = sum;
+                }
+            }
+            __syncthreads();
+            if (threadIdx.x < 256) {
+                s_dstart[threadIdx.x] = dstart;
+                s_gbase[threadIdx.x] += (uint32_t)(both >> 32);
+            }
+        } else {
+            // many tiles: each block turns some columns into exclusive prefixes
+            // over the tiles, then every tile reads its own (summing every
+            // column in every tile moved tens of MB through L2 per pass)
+            for (uint32_t d = blockIdx.x; d < 256; d += gridDim.x) {
+                uint32_t* col = status + (size_t)d * tiles;
+                uint32_t carry = 0;
+                for (uint32_t t0 = 0; t0 < tiles; t0 += kOsThreads) {
+                    const uint32_t t = t0 + threadIdx.x;
+                    const uint32_t v = t < tiles ? __ldcg(col + t) : 0u;
+                    unsigned long long sum;
+                    const uint32_t ex =
+                        (uint32_t)block_exclusive_scan<kOsThreads>((unsigned long long)v, s_warp, &sum);
+                    if (t < tiles) col[t] = carry + ex;
+                    carry += (uint32_t)sum;
+                }
+            }
+            grid_barrier(sync_ctr, (barrier + 2) * gridDim.x, err);
+            if (threadIdx.x < 256) {
+                s_dstart[threadIdx.x] = dstart;
+                s_gbase[threadIdx.x] = (uint32_t)(both >> 32) + __ldcg(status + (size_t)threadIdx.x * tiles + tile);
+            }
+        }
+    } else if (threadIdx.x < 256) {
         const int d = threadIdx.x;
         s_dstart[d] = dstart;
         uint32_t* st = status + (size_t)tile * 256 + d;
@@ -357,6 +443,40 @@ __global__ void __launch_bounds__(kOsThreads) k_onesweep(const uint32_t* __restr
         } else {
             atomicOr(err, ERR_RANGE);
         }
+    }
+}
+
+// One sort pass, tiles taken in launch order from `tile_ctr` (so a tile's
+// predecessors have started: the look-back's waits end).
+__global__ void __launch_bounds__(kOsThreads, 2) k_onesweep(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
+                                                         uint32_t* __restrict__ kout, uint32_t* __restrict__ vout,
+                                                         uint32_t n, int pass, const uint32_t* __restrict__ hist,
+                                                         uint32_t* __restrict__ status, uint32_t* __restrict__ tile_ctr,
+                                                         uint32_t* __restrict__ err) {
+    extern __shared__ uint32_t smem[];
+    __shared__ uint32_t s_tile;
+    if (threadIdx.x == 0) s_tile = atomicAdd(tile_ctr + pass, 1u);
+    __syncthreads();
+    sort_tile<false>(kin, vin, kout, vout, n, pass, hist, s_tile, status, nullptr, 0, err, smem);
+}
+
+// All four sort passes in one cooperative launch, one block per tile (every
+// tile resident): keys and values go from (key_a, val_a) to (key_b, val_b)
+// and back, twice. Grid barriers a pass: after the tiles publish their counts,
+// after the counts are scanned (more than kSumTiles tiles), and after the
+// tiles are written (before the next pass reads them and overwrites the
+// counts).
+__global__ void __launch_bounds__(kOsThreads, 2) k_sort_coop(uint32_t* key_a, uint32_t* val_a, uint32_t* key_b,
+                                                          uint32_t* val_b, uint32_t n,
+                                                          const uint32_t* __restrict__ hist, uint32_t* counts,
+                                                          uint32_t* sync_ctr, uint32_t* err) {
+    extern __shared__ uint32_t smem[];
+    const uint32_t per_pass = gridDim.x <= kSumTiles ? 2 : 3;  // grid barriers a pass
+    for (int pass = 0; pass < 4; ++pass) {
+        const bool even = (pass & 1) == 0;
+        sort_tile<true>(even ? key_a : key_b, even ? val_a : val_b, even ? key_b : key_a, even ? val_b : val_a, n,
+                        pass, hist, blockIdx.x, counts, sync_ctr, per_pass * pass, err, smem);
+        if (pass < 3) grid_barrier(sync_ctr, per_pass * (pass + 1) * gridDim.x, err);
     }
 }
 
@@ -856,6 +976,38 @@ cudaError_t lookback_probe(uint32_t polls, uint32_t* h_err, cudaStream_t s) {
 
 namespace {
 
+// How many sort tiles one cooperative launch can hold on the current device
+// (resident blocks of k_sort_coop per SM times the SMs; 0 without cooperative
+// launch), looked up once per device.
+cudaError_t sort_coop_capacity(int num_sms, int* tiles) {
+    static std::mutex mu;
+    static int cached[64];
+    static bool known[64];
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lock(mu);
+    if (dev < 0 || dev >= 64 || !known[dev]) {
+        int coop = 0, per_sm = 0;
+        if ((e = cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev)) != cudaSuccess) return e;
+        if ((e = cudaFuncSetAttribute(k_sort_coop, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kOsSmem)) !=
+            cudaSuccess)
+            return e;
+        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sort_coop, kOsThreads, kOsSmem)) !=
+            cudaSuccess)
+            return e;
+        const int cap = coop ? per_sm * num_sms : 0;
+        if (dev < 0 || dev >= 64) {
+            *tiles = cap;
+            return cudaSuccess;
+        }
+        cached[dev] = cap;
+        known[dev] = true;
+    }
+    *tiles = cached[dev];
+    return cudaSuccess;
+}
+
 // The build's launch sequence over laid-out scratch `s` (scratch_layout): the
 // one both the allocating build and the no-allocation build run. Zeroes the
 // scratch region that must start at zero, then centroid bounds, Morton codes
@@ -876,15 +1028,28 @@ cudaError_t launch_build(const float* d_verts, uint32_t n, const Scratch& s, Nod
     if ((e = cudaFuncSetAttribute(k_onesweep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kOsSmem)) !=
         cudaSuccess)
         return e;
-    uint32_t* kin = code;
-    uint32_t* vin = prim;
-    uint32_t* kout = s.keys_alt;
-    uint32_t* vout = s.vals_alt;
-    for (int pass = 0; pass < 4; ++pass) {
-        k_onesweep<<<os_tiles, kOsThreads, kOsSmem, st>>>(kin, vin, kout, vout, n, pass, s.hist,
-                                                          s.os_status + (size_t)pass * os_tiles * 256, s.tile_ctr, s.err);
-        std::swap(kin, kout);
-        std::swap(vin, vout);
+    int coop_tiles = 0;
+    if ((e = sort_coop_capacity(num_sms, &coop_tiles)) != cudaSuccess) return e;
+    if (os_tiles <= (uint32_t)coop_tiles) {
+        // every tile resident: the four passes in one cooperative launch
+        uint32_t* sync_ctr = s.tile_ctr + 8;
+        void* args[] = {&code, &prim, (void*)&s.keys_alt, (void*)&s.vals_alt, &n, (void*)&s.hist,
+                        (void*)&s.os_status, &sync_ctr, (void*)&s.err};
+        if ((e = cudaLaunchCooperativeKernel((const void*)k_sort_coop, dim3(os_tiles), dim3(kOsThreads), args, kOsSmem,
+                                             st)) != cudaSuccess)
+            return e;
+    } else {
+        uint32_t* kin = code;
+        uint32_t* vin = prim;
+        uint32_t* kout = s.keys_alt;
+        uint32_t* vout = s.vals_alt;
+        for (int pass = 0; pass < 4; ++pass) {
+            k_onesweep<<<os_tiles, kOsThreads, kOsSmem, st>>>(kin, vin, kout, vout, n, pass, s.hist,
+                                                              s.os_status + (size_t)pass * os_tiles * 256,
+                                                              s.tile_ctr, s.err);
+            std::swap(kin, kout);
+            std::swap(vin, vout);
+        }
     }
     // four passes: the sorted data is back in code/prim
     k_gaps<<<grid, kBlock, 0, st>>>(code, n, s.level, s.counters, s.err);

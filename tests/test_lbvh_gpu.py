@@ -36,7 +36,10 @@ def test_gpu_lbvh_matches_reference_golden(ctx, oracle, case):
     _compare(got, oracle.lbvh(verts))
 
 
-@pytest.mark.parametrize("n", [2, 3, 4095, 4096, 4097, 65537, 1000000])
+# 1,000,000 triangles sort in one cooperative launch (245 tiles of 4,096 keys,
+# all resident); 2,000,000 need more tiles than a GB300 holds at once (two per
+# SM) and take the four look-back passes.
+@pytest.mark.parametrize("n", [2, 3, 4095, 4096, 4097, 65537, 1000000, 2000000])
 def test_gpu_lbvh_matches_oracle(ctx, oracle, n):
     v = sc.triangle_soup(n, seed_salt=90 + n % 11)
     if n > 100:
