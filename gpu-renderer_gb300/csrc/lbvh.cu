@@ -261,18 +261,19 @@ constexpr size_t kOsSmem = sizeof(uint32_t) * (kOsWarps * 256 + 256 + 256 + 2 * 
 
 // Grid-wide barrier of a cooperative launch (every block resident): block
 // arrivals are counted on `ctr`, and the k-th barrier of the launch waits for
-// (k + 1) * gridDim.x arrivals, at most kSpinLimit polls (then ERR_TIMEOUT).
+// (k + 1) * gridDim.x arrivals, at most `limit` polls (then ERR_TIMEOUT).
 // The block barrier before the fence puts every thread's writes ahead of the
 // arrival; the block barrier after it puts the other blocks' writes ahead of
 // every thread's later reads (which go to L2: __ldcg).
-__device__ __forceinline__ void grid_barrier(uint32_t* ctr, uint32_t target, uint32_t* err) {
+__device__ __forceinline__ void grid_barrier(uint32_t* ctr, uint32_t target, uint32_t* err,
+                                             uint32_t limit = kSpinLimit) {
     __syncthreads();
     if (threadIdx.x == 0) {
         __threadfence();
         atomicAdd(ctr, 1u);
         uint32_t spins = 0;
         while (ld_acquire(ctr) < target) {
-            if (++spins > kSpinLimit) {
+            if (++spins > limit) {
                 atomicOr(err, ERR_TIMEOUT);
                 break;
             }
@@ -951,21 +952,24 @@ size_t scratch_layout(uint32_t n, char* base, Scratch* s) {
     return off;
 }
 
-// The look-back's bounded wait on its own: tile 1 looks back at tile 0, whose
-// status word nothing publishes, so the wait runs out after `limit` polls.
-__global__ void k_lookback_probe(const uint32_t* status, uint32_t limit, uint32_t* err, uint32_t* out) {
+// The build's bounded waits on their own: tile 1 looks back at tile 0, whose
+// status word nothing publishes, and a one-block grid barrier waits for a
+// second block that does not exist, so both waits run out after `limit` polls.
+__global__ void k_lookback_probe(const uint32_t* status, uint32_t limit, uint32_t* err, uint32_t* out,
+                                 uint32_t* ctr) {
     if (threadIdx.x == 0 && blockIdx.x == 0) *out = lookback(status, 1, 1, limit, err);
+    grid_barrier(ctr, 2, err, limit);
 }
 
 }  // namespace
 
 cudaError_t lookback_probe(uint32_t polls, uint32_t* h_err, cudaStream_t s) {
     uint32_t* d = nullptr;
-    cudaError_t e = cudaMalloc(&d, 3 * sizeof(uint32_t));  // status word, error word, result
+    cudaError_t e = cudaMalloc(&d, 4 * sizeof(uint32_t));  // status word, error word, result, barrier counter
     if (e != cudaSuccess) return e;
-    e = cudaMemsetAsync(d, 0, 3 * sizeof(uint32_t), s);
+    e = cudaMemsetAsync(d, 0, 4 * sizeof(uint32_t), s);
     if (e == cudaSuccess) {
-        k_lookback_probe<<<1, 32, 0, s>>>(d, std::min(polls, kSpinLimit), d + 1, d + 2);
+        k_lookback_probe<<<1, 32, 0, s>>>(d, std::min(polls, kSpinLimit), d + 1, d + 2, d + 3);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaMemcpyAsync(h_err, d + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);

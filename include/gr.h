@@ -376,9 +376,11 @@ gr_status gr_scene_rgba8_host(gr_scene* scene, uint32_t* h_rgba);
 /* ---- diagnostics -------------------------------------------------------------
  * Every device-side wait of the library is bounded: a wait that runs out sets an
  * error bit and returns, the call reports GR_ERR_TIMEOUT, and the context stays
- * usable. This runs the LBVH build's look-back wait on a status word nothing
- * publishes, for `polls` polls, and so returns GR_ERR_TIMEOUT with the device
- * error bits (ERR_TIMEOUT = 1) in *err_bits. */
+ * usable. This runs the LBVH build's two kinds of wait, each for `polls` polls:
+ * the sort's look-back on a status word nothing publishes, and the cooperative
+ * sort's grid barrier in a one-block launch waiting for a second block; both run
+ * out, so it returns GR_ERR_TIMEOUT with the device error bits (ERR_TIMEOUT = 1)
+ * in *err_bits. */
 gr_status gr_diag_bounded_wait(gr_ctx* ctx, uint32_t polls, uint32_t* err_bits);
 
 /* ---- image files: FrameBuffer::output / WriteImage (framebuffer.cpp:11-26, imageio.cpp:59-82) ----

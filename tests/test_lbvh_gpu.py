@@ -79,9 +79,10 @@ def test_gpu_lbvh_empty(ctx):
 
 @pytest.mark.parametrize("polls", [1, 1000, 1 << 16])
 def test_bounded_wait_gives_up_and_context_stays_usable(ctx, oracle, polls):
-    # the build's look-back wait on a status word that nothing publishes: it gives
-    # up after its poll limit, the call reports GR_ERR_TIMEOUT with the device bit,
-    # and the same context then builds and traces as before
+    # the build's look-back wait on a status word that nothing publishes and its
+    # grid barrier waiting for a block that does not exist: both give up after
+    # their poll limit, the call reports GR_ERR_TIMEOUT with the device bit, and
+    # the same context then builds and traces as before
     st, bits = ctx.bounded_wait(polls)
     assert st == 5 and bits == 1
     v = sc.triangle_soup(5000, seed_salt=95)
