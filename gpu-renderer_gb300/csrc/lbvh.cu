@@ -1034,15 +1034,24 @@ cudaError_t launch_build(const float* d_verts, uint32_t n, const Scratch& s, Nod
         return e;
     int coop_tiles = 0;
     if ((e = sort_coop_capacity(num_sms, &coop_tiles)) != cudaSuccess) return e;
+    bool sorted = false;
     if (os_tiles <= (uint32_t)coop_tiles) {
-        // every tile resident: the four passes in one cooperative launch
+        // every tile resident: the four passes in one cooperative launch (a
+        // launch the device refuses as too large, e.g. a client held to part of
+        // the SMs, falls back to the look-back passes)
         uint32_t* sync_ctr = s.tile_ctr + 8;
         void* args[] = {&code, &prim, (void*)&s.keys_alt, (void*)&s.vals_alt, &n, (void*)&s.hist,
                         (void*)&s.os_status, &sync_ctr, (void*)&s.err};
-        if ((e = cudaLaunchCooperativeKernel((const void*)k_sort_coop, dim3(os_tiles), dim3(kOsThreads), args, kOsSmem,
-                                             st)) != cudaSuccess)
+        e = cudaLaunchCooperativeKernel((const void*)k_sort_coop, dim3(os_tiles), dim3(kOsThreads), args, kOsSmem, st);
+        if (e == cudaSuccess) {
+            sorted = true;
+        } else if (e == cudaErrorCooperativeLaunchTooLarge) {
+            (void)cudaGetLastError();
+        } else {
             return e;
-    } else {
+        }
+    }
+    if (!sorted) {
         uint32_t* kin = code;
         uint32_t* vin = prim;
         uint32_t* kout = s.keys_alt;
