@@ -18,7 +18,7 @@ namespace gr {
 namespace {
 
 constexpr int kBlock = 256;
-// sorted positions (and gaps) per block in the refit's first pass: one per thread
+// sorted positions (and gaps) per block in the bottom-up pass's first part: one per thread
 constexpr int kRefitChunk = 256;
 
 // ---- small device helpers ---------------------------------------------------

@@ -83,9 +83,10 @@ int gr_version(void);
 /* ---- acceleration structure ----------------------------------------------
  * Replaces LBVH_build (src/renderer/bvh.h:186-221), which runs single-threaded
  * on the host. The GPU build computes 30-bit Morton codes of triangle
- * centroids, sorts them with a stable onesweep radix sort, builds the Karras
- * radix tree over unique codes with midpoint splits inside equal-code runs
- * (the reference's rule, bvh.h:161-176) and refits boxes bottom-up. */
+ * centroids, sorts them with a stable LSD radix sort, and builds the radix tree
+ * over unique codes with midpoint splits inside equal-code runs (the
+ * reference's rule, bvh.h:161-176) in one bottom-up pass that links the nodes
+ * and fits their boxes. */
 
 gr_status gr_bvh_create(gr_ctx* ctx, gr_bvh** out);
 gr_status gr_bvh_destroy(gr_bvh* bvh);

@@ -49,6 +49,16 @@ def test_gpu_lbvh_matches_oracle(ctx, oracle, n):
     _compare(b.export(), oracle.lbvh(v))
 
 
+def test_gpu_lbvh_long_equal_run(ctx, oracle):
+    # 200,000 triangles with one centroid inside a 1M soup: a 200,000-long run of
+    # equal codes, whose gaps find their depth in the run's midpoint subtree
+    v = sc.triangle_soup(1000000, seed_salt=96)
+    v[300000:500000] = v[300000]
+    b = gr.BVH(ctx)
+    b.build_host(v)
+    _compare(b.export(), oracle.lbvh(v))
+
+
 def test_gpu_lbvh_all_identical(ctx, oracle):
     v = np.repeat(sc.triangle_soup(1, seed_salt=92), 100000, axis=0)
     b = gr.BVH(ctx)
