@@ -713,7 +713,7 @@ __global__ void __launch_bounds__(kRefitChunk) k_climb_chunk(const float* __rest
                                                              Tri* __restrict__ tris) {
     __shared__ uint32_t s_mask[kRefitChunk];
     __shared__ uint32_t s_parent[kRefitChunk];
-    __shared__ float s_box[kRefitChunk][2][6];
+    __shared__ __align__(16) float s_box[kRefitChunk][2][6];  // per gap and slot: lo.xyz, hi.xyz
     __shared__ unsigned long long s_far[kRefitChunk][2];
     __shared__ int32_t s_link[kRefitChunk][2];
     __shared__ Sub s_pend;
@@ -764,20 +764,17 @@ __global__ void __launch_bounds__(kRefitChunk) k_climb_chunk(const float* __rest
                         break;
                     }
                     const uint32_t g = P - base;
-#pragma unroll
-                    for (int k = 0; k < 3; ++k) {
-                        s_box[g][slot][k] = s.box.lo[k];
-                        s_box[g][slot][3 + k] = s.box.hi[k];
-                    }
+                    float2* sb2 = reinterpret_cast<float2*>(s_box[g][slot]);
+                    sb2[0] = make_float2(s.box.lo[0], s.box.lo[1]);
+                    sb2[1] = make_float2(s.box.lo[2], s.box.hi[0]);
+                    sb2[2] = make_float2(s.box.hi[1], s.box.hi[2]);
                     s_far[g][slot] = far_word(s, slot);
                     s_link[g][slot] = s.me;
                     if (atomic_or_acq_rel_cta(&s_mask[g], 1u << slot) == 0) break;  // sibling not done yet
+                    const float2* ob2 = reinterpret_cast<const float2*>(s_box[g][slot ^ 1]);
+                    const float2 u0 = ob2[0], u1 = ob2[1], u2 = ob2[2];
                     Box3 sb;
-#pragma unroll
-                    for (int k = 0; k < 3; ++k) {
-                        sb.lo[k] = s_box[g][slot ^ 1][k];
-                        sb.hi[k] = s_box[g][slot ^ 1][3 + k];
-                    }
+                    sb.lo[0] = u0.x; sb.lo[1] = u0.y; sb.lo[2] = u1.x; sb.hi[0] = u1.y; sb.hi[1] = u2.x; sb.hi[2] = u2.y;
                     box_union(s.box, sb);
                     widen(s, slot, s_far[g][slot ^ 1]);
                     s.me = (int32_t)P;
@@ -798,14 +795,11 @@ __global__ void __launch_bounds__(kRefitChunk) k_climb_chunk(const float* __rest
         if (p + 1 < n) {
             const uint32_t m = s_mask[threadIdx.x];
             const int j = threadIdx.x;
+            const float4* sb4 = reinterpret_cast<const float4*>(s_box[j]);
+            const float4 u = sb4[0], w = sb4[1], z = sb4[2];
             Box3 b0, b1;
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                b0.lo[k] = s_box[j][0][k];
-                b0.hi[k] = s_box[j][0][3 + k];
-                b1.lo[k] = s_box[j][1][k];
-                b1.hi[k] = s_box[j][1][3 + k];
-            }
+            b0.lo[0] = u.x; b0.lo[1] = u.y; b0.lo[2] = u.z; b0.hi[0] = u.w; b0.hi[1] = w.x; b0.hi[2] = w.y;
+            b1.lo[0] = w.z; b1.lo[1] = w.w; b1.lo[2] = z.x; b1.hi[0] = z.y; b1.hi[1] = z.z; b1.hi[2] = z.w;
             if (m == 3u) {  // finished here: the whole record
                 write_node(o.nodes + p, b0, b1, s_link[j][0], s_link[j][1], s_parent[j]);
             } else if (m != 0u) {  // one child arrived: its slot, far word and count for part 2
