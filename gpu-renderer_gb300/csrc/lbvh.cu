@@ -1,4 +1,4 @@
-// GPU LBVH build: Morton codes -> onesweep radix sort -> the split level of
+// GPU LBVH build: Morton codes -> LSD radix sort -> the split level of
 // each gap between sorted codes (the radix tree's over unique codes, midpoint
 // subtrees inside runs of equal codes) -> one bottom-up pass that links the
 // nodes and fits their boxes. Produces the same tree as the reference's host
@@ -164,8 +164,8 @@ __global__ void __launch_bounds__(kBlock) k_centroid(const float* __restrict__ v
 
 // ---- 2. Morton codes + the four digit histograms ------------------------------
 
-// Also clears the sort's look-back words (`status`, `nstatus` words) for the
-// passes that follow.
+// Also clears the sort's status words (`status`, `nstatus` words), which the
+// look-back passes need at zero.
 __global__ void __launch_bounds__(kBlock) k_morton_hist(const float* __restrict__ verts, uint32_t n,
                                                         const BvhMeta* __restrict__ meta, uint32_t* __restrict__ keys,
                                                         uint32_t* __restrict__ vals, uint32_t* __restrict__ hist,
@@ -200,11 +200,13 @@ __global__ void __launch_bounds__(kBlock) k_morton_hist(const float* __restrict_
         if (s_hist[i]) atomicAdd(&hist[i], s_hist[i]);
 }
 
-// ---- 3. onesweep radix pass ------------------------------------------------------
-// One pass sorts by one 8-bit digit. Tiles of 4096 keys are ranked in shared
+// ---- 3. radix sort ----------------------------------------------------------------
+// Four passes of one 8-bit digit each. Tiles of 4096 keys are ranked in shared
 // memory (warp multi-split by ballots, stable in input order), the tile's
-// per-digit counts are published and prefixed with decoupled look-back, and
-// keys are written out grouped by digit.
+// per-digit counts are prefixed over the tiles before it, and keys are written
+// out grouped by digit. The prefix comes from a grid barrier and a scan of every
+// tile's counts when all tiles fit on the GPU at once (all four passes in one
+// cooperative launch), else from decoupled look-back (one launch per pass).
 
 constexpr int kOsThreads = 512;
 constexpr int kOsItems = 8;
